@@ -1,0 +1,167 @@
+/*
+ * spacecharge_gb300.h — C ABI of the GB300 space-charge kick library
+ * (libspacecharge_gb300.so).
+ *
+ * The library replaces the hot path of SpaceCharge.jl v1.2.0:
+ *   Mesh3D (src/mesh.jl:122-265) -> deposit! (src/deposition.jl:218)
+ *   -> solve! (src/solvers/free_space.jl:14) -> interpolate_field
+ *   (src/interpolation.jl:100).
+ * A Julia host binds these functions with `ccall`; the Python host in
+ * spacecharge.jl_gb300/python binds them with ctypes.
+ *
+ * Conventions
+ *  - Every function returns an int status (SC_OK = 0).  On failure
+ *    sc_last_error() returns a message for the calling thread.  Argument
+ *    errors that the reference raises with `error("...")` return
+ *    SC_ERR_INVALID with the reference's message text.
+ *  - Particle arrays and field outputs are DEVICE pointers (CuArray /
+ *    torch CUDA storage) of `dtype` (SC_F32 or SC_F64); outputs have the
+ *    particle dtype, as `similar(particles_x)` does (interpolation.jl:110).
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Work is
+ *    enqueued asynchronously; nothing synchronises unless stated.
+ *  - Arrays are column-major as in Julia: rho is (nx,ny,nz) with x fastest.
+ *    efield is (nx,ny,nz,3) component-planar for SC_PREC_PLAIN64 meshes and
+ *    packed (4,nx,ny,nz) = (Ex,Ey,Ez,0) per node for the hand-written
+ *    pipelines (sc_mesh_info.efield_layout says which).
+ */
+#ifndef SPACECHARGE_GB300_H
+#define SPACECHARGE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SC_OK               0
+#define SC_ERR_INVALID      1  /* bad argument (the reference's ErrorException) */
+#define SC_ERR_CUDA         2  /* CUDA runtime / cuFFT failure */
+#define SC_ERR_OOM          3  /* device allocation failed */
+#define SC_ERR_OUT_OF_RANGE 4  /* particles outside the mesh were skipped */
+#define SC_ERR_TIMEOUT      5  /* a bounded device-side wait gave up */
+#define SC_ERR_UNSUPPORTED  6  /* size or option this build does not handle */
+
+/* particle / output element types */
+#define SC_F32 0
+#define SC_F64 1
+
+/* mesh precision (the Julia wrapper maps T=Float64 -> SC_PREC_FP64,
+ * T=Float32 -> SC_PREC_MIXED) */
+#define SC_PREC_PLAIN64 0 /* the reference algorithm, FP64, cuFFT Z2Z, 7 FFTs */
+#define SC_PREC_FP64    1 /* hand-written pruned pipeline in FP64 */
+#define SC_PREC_MIXED   2 /* hand-written pipeline: FP32 deposit/FFT/gather,
+                             FP64 IGF differences, origin offsets, charge sum */
+
+/* deposit modes */
+#define SC_DEPOSIT_ATOMIC        0 /* one thread per particle, 8 atomics */
+#define SC_DEPOSIT_SORTED        1 /* bin by cell, warp-segmented sums, few atomics */
+#define SC_DEPOSIT_DETERMINISTIC 2 /* sorted, fixed reduction order, no float atomics */
+
+/* efield layouts */
+#define SC_LAYOUT_PLANAR 0
+#define SC_LAYOUT_PACKED 1
+
+typedef struct sc_mesh sc_mesh;
+
+typedef struct sc_mesh_info {
+    int32_t grid_size[3];
+    int32_t precision;
+    double  min_bounds[3];
+    double  max_bounds[3];
+    double  delta[3];
+    double  gamma;
+    double  total_charge;
+    int32_t efield_layout;  /* SC_LAYOUT_* */
+    int32_t elem_bytes;     /* sizeof element of rho / efield */
+    int32_t fft_shape[3];   /* transform length per axis */
+    int32_t device;
+} sc_mesh_info;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int sc_version(void);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* sc_last_error(void);
+
+/* Manual-bounds constructor: Mesh3D(grid_size, min_bounds, max_bounds;
+ * T, gamma, total_charge), src/mesh.jl:223-265.  Validates grid >= 2 and
+ * max > min (mesh.jl:233-238); delta = (max-min)/(n-1) (mesh.jl:247).
+ * Allocates rho and efield (zeroed) on the current CUDA device. */
+int sc_mesh_create(const int32_t grid_size[3], const double min_bounds[3],
+                   const double max_bounds[3], double gamma, double total_charge,
+                   int precision, sc_mesh** out);
+
+/* The bounds arithmetic of the particle-bounds constructor, src/mesh.jl:
+ * 133-177: validation, extrema (one device reduction + a 48-byte copy to
+ * the host, which synchronises `stream`), 1e-6*delta padding, delta
+ * recomputation and the delta == 0 -> 1e-6 patch, all in FP64. */
+int sc_auto_bounds(const int32_t grid_size[3], const void* x, const void* y,
+                   const void* z, int64_t n, int dtype, double min_bounds[3],
+                   double max_bounds[3], double delta[3], void* stream);
+
+/* Particle-bounds constructor: Mesh3D(grid_size, px, py, pz; T, gamma,
+ * total_charge), src/mesh.jl:122-201.  Synchronises `stream`. */
+int sc_mesh_create_from_particles(const int32_t grid_size[3], const void* x,
+                                  const void* y, const void* z, int64_t n, int dtype,
+                                  double gamma, double total_charge, int precision,
+                                  void* stream, sc_mesh** out);
+
+/* Frees the mesh, its fields and its workspace. */
+int sc_mesh_destroy(sc_mesh* mesh);
+
+/* Mesh properties (the fields of Mesh3D, src/mesh.jl:19-34). */
+int sc_mesh_get_info(const sc_mesh* mesh, sc_mesh_info* info);
+
+/* Device pointers to mesh.rho and mesh.efield (owned by the mesh). */
+int sc_mesh_rho(sc_mesh* mesh, void** dptr);
+int sc_mesh_efield(sc_mesh* mesh, void** dptr);
+
+/* Enable (1, default) or disable (0) reuse of the Green-function spectrum
+ * between solves while delta, gamma and the cathode offset are unchanged.
+ * The reference rebuilds it on every solve! (free_space.jl:77-96). */
+int sc_mesh_set_green_cache(sc_mesh* mesh, int enabled);
+
+/* clear_mesh!(mesh), src/deposition.jl:10-12. */
+int sc_clear_mesh(sc_mesh* mesh, void* stream);
+
+/* deposit!(mesh, px, py, pz, pq; clear), src/deposition.jl:218-247.
+ * Cell indices are floor((x - min)/delta) in FP64 exactly as the
+ * reference computes them (deposition.jl:39-46).  Particles whose cell is
+ * outside the mesh are skipped and counted (the reference has no check,
+ * deposition.jl:64); read the count with sc_mesh_out_of_range. */
+int sc_deposit(sc_mesh* mesh, const void* x, const void* y, const void* z,
+               const void* q, int64_t n, int dtype, int clear, int mode, void* stream);
+
+/* solve!(mesh; at_cathode), src/solvers/free_space.jl:14-101. */
+int sc_solve(sc_mesh* mesh, int at_cathode, void* stream);
+
+/* interpolate_field(mesh, px, py, pz) -> (Ex, Ey, Ez),
+ * src/interpolation.jl:100-128, into caller-owned device outputs. */
+int sc_interpolate_field(sc_mesh* mesh, const void* x, const void* y, const void* z,
+                         int64_t n, int dtype, void* ex, void* ey, void* ez,
+                         void* stream);
+
+/* deposit! + solve! + interpolate_field in one call: the unit timed by
+ * benchmark/full_pipeline_benchmark.jl:43-48. */
+int sc_kick(sc_mesh* mesh, const void* x, const void* y, const void* z, const void* q,
+            int64_t n, int dtype, int at_cathode, void* ex, void* ey, void* ez,
+            void* stream);
+
+/* The binning step of deposit!/interpolate_field on its own: for each
+ * particle, the 0-based lower-corner node (ix, iy, iz) = floor((x-min)/delta)
+ * (deposition.jl:39-46) into idx[3*p .. 3*p+2], or -1s when outside the
+ * mesh, and the in-cell fractions (deposition.jl:49-51) into frac[3*p ..]
+ * as FP64.  Uses the same device arithmetic as the mesh's deposit kernel. */
+int sc_cell_index(sc_mesh* mesh, const void* x, const void* y, const void* z, int64_t n, int dtype,
+                  int32_t* idx, double* frac, void* stream);
+
+/* Number of particles skipped as out of range since the last call
+ * (deposit and interpolate); resets the counter.  Synchronises `stream`. */
+int sc_mesh_out_of_range(sc_mesh* mesh, int64_t* count, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPACECHARGE_GB300_H */

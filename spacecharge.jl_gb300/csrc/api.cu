@@ -1,0 +1,357 @@
+// C-ABI entry points: argument validation with the reference's error
+// messages, mesh lifecycle and dispatch to the kernels of each precision.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <vector>
+
+#include "sc_internal.cuh"
+
+namespace sc {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    set_error("CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
+    return e == cudaErrorMemoryAllocation ? SC_ERR_OOM : SC_ERR_CUDA;
+}
+
+// ------------------------------------------------------- per-device state
+static std::mutex g_ctx_mu;
+static std::vector<DeviceCtx*> g_ctx;
+
+int device_ctx(DeviceCtx** out) {
+    int dev = 0;
+    SC_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    if ((int)g_ctx.size() <= dev) g_ctx.resize(dev + 1, nullptr);
+    if (g_ctx[dev]) {
+        *out = g_ctx[dev];
+        return SC_OK;
+    }
+    DeviceCtx* c = new DeviceCtx();
+    c->device = dev;
+    SC_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, dev));
+    // Twiddle table exp(-2 pi i k / kMaxL) built in FP64 from sin/cos of
+    // exactly representable multiples of pi/2^kMaxLog: each FP32 entry is the
+    // correctly rounded FP64 value.
+    std::vector<float2> t32(kMaxL);
+    std::vector<double2> t64(kMaxL);
+    for (int k = 0; k < kMaxL; ++k) {
+        long double a = -2.0L * 3.141592653589793238462643383279502884L * (long double)k / (long double)kMaxL;
+        double c = (double)cosl(a), s = (double)sinl(a);
+        t64[k] = make_double2(c, s);
+        t32[k] = make_float2((float)c, (float)s);
+    }
+    SC_CUDA(cudaMalloc(&c->tw32, sizeof(float2) * kMaxL));
+    SC_CUDA(cudaMalloc(&c->tw64, sizeof(double2) * kMaxL));
+    SC_CUDA(cudaMemcpy(c->tw32, t32.data(), sizeof(float2) * kMaxL, cudaMemcpyHostToDevice));
+    SC_CUDA(cudaMemcpy(c->tw64, t64.data(), sizeof(double2) * kMaxL, cudaMemcpyHostToDevice));
+    c->partial_blocks = 2 * c->sm_count;
+    SC_CUDA(cudaMalloc(&c->partials, sizeof(double) * 6 * (c->partial_blocks + 1)));
+    g_ctx[dev] = c;
+    *out = c;
+    return SC_OK;
+}
+
+Geom make_geom(const sc_mesh* m) {
+    Geom g;
+    for (int d = 0; d < 3; ++d) {
+        g.n[d] = m->n[d];
+        g.lo[d] = m->lo[d];
+        g.delta[d] = m->delta[d];
+        g.inv[d] = 1.0 / m->delta[d];
+    }
+    return g;
+}
+
+static int check_grid(const int32_t* g) {
+    if (!g) return fail(SC_ERR_INVALID, "grid_size is NULL");
+    // src/mesh.jl:133-135
+    for (int d = 0; d < 3; ++d)
+        if (g[d] <= 1) return fail(SC_ERR_INVALID, "All elements of grid_size must be at least 2.");
+    return SC_OK;
+}
+
+static int check_dtype(int dtype) {
+    if (dtype != SC_F32 && dtype != SC_F64)
+        return fail(SC_ERR_INVALID, "dtype must be SC_F32 or SC_F64");
+    return SC_OK;
+}
+
+static int mesh_alloc(const int32_t* g, const double* lo, const double* hi, const double* delta,
+                      double gamma, double total_charge, int precision, sc_mesh** out) {
+    if (!out) return fail(SC_ERR_INVALID, "out is NULL");
+    if (precision != SC_PREC_PLAIN64 && precision != SC_PREC_FP64 && precision != SC_PREC_MIXED)
+        return fail(SC_ERR_INVALID, "unknown precision %d", precision);
+    if (!(gamma > 0) || !isfinite(gamma)) return fail(SC_ERR_INVALID, "gamma must be a positive finite number");
+    sc_mesh* m = new sc_mesh();
+    for (int d = 0; d < 3; ++d) {
+        m->n[d] = g[d];
+        m->lo[d] = lo[d];
+        m->hi[d] = hi[d];
+        m->delta[d] = delta[d];
+    }
+    m->N = (int64_t)g[0] * g[1] * g[2];
+    m->gamma = gamma;
+    m->total_charge = total_charge;
+    m->precision = precision;
+    cudaError_t e = cudaGetDevice(&m->device);
+    if (e != cudaSuccess) {
+        delete m;
+        return cuda_fail(e, "cudaGetDevice");
+    }
+    DeviceCtx* ctx = nullptr;
+    int st = device_ctx(&ctx);
+    if (st != SC_OK) {
+        delete m;
+        return st;
+    }
+    if (precision != SC_PREC_PLAIN64) {
+        st = native_prepare(m);
+        if (st != SC_OK) {
+            delete m;
+            return st;
+        }
+    }
+    const size_t eb = field_elem_bytes(precision);
+    const size_t ncomp = precision == SC_PREC_PLAIN64 ? 3 : 4;
+    e = cudaMalloc(&m->rho, eb * m->N);
+    if (e == cudaSuccess) e = cudaMalloc(&m->efield, eb * ncomp * m->N);
+    if (e == cudaSuccess) e = cudaMalloc(&m->oob, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(m->rho, 0, eb * m->N);
+    if (e == cudaSuccess) e = cudaMemset(m->efield, 0, eb * ncomp * m->N);
+    if (e == cudaSuccess) e = cudaMemset(m->oob, 0, sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        cudaFree(m->rho);
+        cudaFree(m->efield);
+        cudaFree(m->oob);
+        delete m;
+        return cuda_fail(e, "mesh allocation");
+    }
+    *out = m;
+    return SC_OK;
+}
+
+static int check_mesh(const sc_mesh* m) {
+    if (!m) return fail(SC_ERR_INVALID, "mesh is NULL");
+    return SC_OK;
+}
+
+// Make the mesh's device current for the duration of a call.
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+}  // namespace sc
+
+using namespace sc;
+
+extern "C" {
+
+int sc_version(void) { return 10000; }
+
+const char* sc_last_error(void) { return g_err; }
+
+int sc_mesh_create(const int32_t grid_size[3], const double min_bounds[3], const double max_bounds[3],
+                   double gamma, double total_charge, int precision, sc_mesh** out) {
+    SC_TRY(check_grid(grid_size));
+    if (!min_bounds || !max_bounds) return fail(SC_ERR_INVALID, "bounds are NULL");
+    // src/mesh.jl:236-238
+    for (int d = 0; d < 3; ++d)
+        if (!(max_bounds[d] > min_bounds[d]))
+            return fail(SC_ERR_INVALID, "max_bounds must be strictly greater than min_bounds for all dimensions.");
+    double delta[3];
+    for (int d = 0; d < 3; ++d) delta[d] = (max_bounds[d] - min_bounds[d]) / (double)(grid_size[d] - 1);  // :247
+    return mesh_alloc(grid_size, min_bounds, max_bounds, delta, gamma, total_charge, precision, out);
+}
+
+int sc_auto_bounds(const int32_t grid_size[3], const void* x, const void* y, const void* z, int64_t n,
+                   int dtype, double min_bounds[3], double max_bounds[3], double delta[3], void* stream) {
+    SC_TRY(check_grid(grid_size));
+    SC_TRY(check_dtype(dtype));
+    if (n <= 0 || !x || !y || !z) return fail(SC_ERR_INVALID, "Particle arrays cannot be empty.");  // :137-139
+    double mins[3], maxs[3];
+    SC_TRY(bounds_reduce(x, y, z, n, dtype, mins, maxs, (cudaStream_t)stream));
+    for (int d = 0; d < 3; ++d)
+        if (!isfinite(mins[d]) || !isfinite(maxs[d]))
+            return fail(SC_ERR_INVALID, "particle coordinates must be finite");
+    // src/mesh.jl:152-177, Float64 throughout
+    double dl[3], lo[3], hi[3];
+    for (int d = 0; d < 3; ++d) dl[d] = (maxs[d] - mins[d]) / (double)(grid_size[d] - 1);
+    for (int d = 0; d < 3; ++d) {
+        lo[d] = mins[d] - 1e-6 * dl[d];
+        hi[d] = maxs[d] + 1e-6 * dl[d];
+    }
+    for (int d = 0; d < 3; ++d) dl[d] = (hi[d] - lo[d]) / (double)(grid_size[d] - 1);
+    for (int d = 0; d < 3; ++d) dl[d] = dl[d] == 0 ? 1e-6 : dl[d];
+    for (int d = 0; d < 3; ++d) {
+        if (min_bounds) min_bounds[d] = lo[d];
+        if (max_bounds) max_bounds[d] = hi[d];
+        if (delta) delta[d] = dl[d];
+    }
+    return SC_OK;
+}
+
+int sc_mesh_create_from_particles(const int32_t grid_size[3], const void* x, const void* y, const void* z,
+                                  int64_t n, int dtype, double gamma, double total_charge, int precision,
+                                  void* stream, sc_mesh** out) {
+    double lo[3], hi[3], dl[3];
+    SC_TRY(sc_auto_bounds(grid_size, x, y, z, n, dtype, lo, hi, dl, stream));
+    return mesh_alloc(grid_size, lo, hi, dl, gamma, total_charge, precision, out);
+}
+
+int sc_mesh_destroy(sc_mesh* m) {
+    if (!m) return SC_OK;
+    DeviceGuard g(m->device);
+    if (m->precision == SC_PREC_PLAIN64)
+        plain_release(m);
+    else
+        native_release(m);
+    cudaFree(m->rho);
+    cudaFree(m->efield);
+    cudaFree(m->oob);
+    delete m;
+    return SC_OK;
+}
+
+int sc_mesh_get_info(const sc_mesh* m, sc_mesh_info* info) {
+    SC_TRY(check_mesh(m));
+    if (!info) return fail(SC_ERR_INVALID, "info is NULL");
+    memset(info, 0, sizeof(*info));
+    for (int d = 0; d < 3; ++d) {
+        info->grid_size[d] = m->n[d];
+        info->min_bounds[d] = m->lo[d];
+        info->max_bounds[d] = m->hi[d];
+        info->delta[d] = m->delta[d];
+        info->fft_shape[d] = m->precision == SC_PREC_PLAIN64 ? 2 * m->n[d] : m->nw.L[d];
+    }
+    info->precision = m->precision;
+    info->gamma = m->gamma;
+    info->total_charge = m->total_charge;
+    info->efield_layout = m->precision == SC_PREC_PLAIN64 ? SC_LAYOUT_PLANAR : SC_LAYOUT_PACKED;
+    info->elem_bytes = (int32_t)field_elem_bytes(m->precision);
+    info->device = m->device;
+    return SC_OK;
+}
+
+int sc_mesh_rho(sc_mesh* m, void** p) {
+    SC_TRY(check_mesh(m));
+    if (!p) return fail(SC_ERR_INVALID, "dptr is NULL");
+    *p = m->rho;
+    return SC_OK;
+}
+
+int sc_mesh_efield(sc_mesh* m, void** p) {
+    SC_TRY(check_mesh(m));
+    if (!p) return fail(SC_ERR_INVALID, "dptr is NULL");
+    *p = m->efield;
+    return SC_OK;
+}
+
+int sc_mesh_set_green_cache(sc_mesh* m, int enabled) {
+    SC_TRY(check_mesh(m));
+    m->green_cache = enabled != 0;
+    if (!m->green_cache) {
+        m->nw.key_free.valid = false;
+        m->nw.key_img.valid = false;
+    }
+    return SC_OK;
+}
+
+int sc_clear_mesh(sc_mesh* m, void* stream) {
+    SC_TRY(check_mesh(m));
+    DeviceGuard g(m->device);
+    SC_CUDA(cudaMemsetAsync(m->rho, 0, field_elem_bytes(m->precision) * m->N, (cudaStream_t)stream));
+    return SC_OK;
+}
+
+int sc_deposit(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n,
+               int dtype, int clear, int mode, void* stream) {
+    SC_TRY(check_mesh(m));
+    SC_TRY(check_dtype(dtype));
+    if (n < 0) return fail(SC_ERR_INVALID, "Particle coordinate and charge arrays must have the same length.");
+    if (n > 0 && (!x || !y || !z || !q)) return fail(SC_ERR_INVALID, "particle pointer is NULL");
+    if (mode != SC_DEPOSIT_ATOMIC && mode != SC_DEPOSIT_SORTED && mode != SC_DEPOSIT_DETERMINISTIC)
+        return fail(SC_ERR_INVALID, "unknown deposit mode %d", mode);
+    DeviceGuard g(m->device);
+    if (clear) SC_TRY(sc_clear_mesh(m, stream));
+    if (n == 0) return SC_OK;
+    return deposit_launch(m, x, y, z, q, n, dtype, mode, (cudaStream_t)stream);
+}
+
+int sc_solve(sc_mesh* m, int at_cathode, void* stream) {
+    SC_TRY(check_mesh(m));
+    DeviceGuard g(m->device);
+    if (m->precision == SC_PREC_PLAIN64) return plain_solve(m, at_cathode, (cudaStream_t)stream);
+    return native_solve(m, at_cathode, (cudaStream_t)stream);
+}
+
+int sc_interpolate_field(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n, int dtype,
+                         void* ex, void* ey, void* ez, void* stream) {
+    SC_TRY(check_mesh(m));
+    SC_TRY(check_dtype(dtype));
+    if (n < 0) return fail(SC_ERR_INVALID, "negative particle count");
+    if (n == 0) return SC_OK;
+    if (!x || !y || !z || !ex || !ey || !ez) return fail(SC_ERR_INVALID, "particle or output pointer is NULL");
+    DeviceGuard g(m->device);
+    return gather_launch(m, x, y, z, n, dtype, ex, ey, ez, (cudaStream_t)stream);
+}
+
+int sc_kick(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
+            int at_cathode, void* ex, void* ey, void* ez, void* stream) {
+    SC_TRY(sc_deposit(m, x, y, z, q, n, dtype, 1, SC_DEPOSIT_ATOMIC, stream));
+    SC_TRY(sc_solve(m, at_cathode, stream));
+    return sc_interpolate_field(m, x, y, z, n, dtype, ex, ey, ez, stream);
+}
+
+int sc_cell_index(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n, int dtype, int32_t* idx,
+                  double* frac, void* stream) {
+    SC_TRY(check_mesh(m));
+    SC_TRY(check_dtype(dtype));
+    if (n < 0) return fail(SC_ERR_INVALID, "negative particle count");
+    if (n == 0) return SC_OK;
+    if (!x || !y || !z || !idx || !frac) return fail(SC_ERR_INVALID, "NULL pointer");
+    DeviceGuard g(m->device);
+    return cell_index_launch(m, x, y, z, n, dtype, idx, frac, (cudaStream_t)stream);
+}
+
+int sc_mesh_out_of_range(sc_mesh* m, int64_t* count, void* stream) {
+    SC_TRY(check_mesh(m));
+    DeviceGuard g(m->device);
+    unsigned long long h = 0;
+    SC_CUDA(cudaMemcpyAsync(&h, m->oob, sizeof(h), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    SC_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    SC_CUDA(cudaMemsetAsync(m->oob, 0, sizeof(h), (cudaStream_t)stream));
+    if (count) *count = (int64_t)h;
+    return SC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,191 @@
+// Trilinear field interpolation, src/interpolation.jl:17-128.
+//
+// gather_plain: the reference's kernel restated: FP64 IEEE-division cell
+//   index, 8 weights (:46-53), 24 scalar loads from the component-planar
+//   efield (:56-85), same summation order; output in the particle type.
+// gather_packed: the hand-written pipelines read the packed (Ex,Ey,Ez,0)
+//   node as one 16-byte (FP32) or 32-byte (FP64) load, 8 loads per particle.
+// Out-of-range particles get E = 0 and are counted (the reference reads out
+// of bounds there).
+#include "cells.cuh"
+#include "sc_internal.cuh"
+
+namespace sc {
+
+Axes make_axes(const sc_mesh* m);
+
+template <typename P>
+__global__ void __launch_bounds__(256) gather_plain(const P* __restrict__ px, const P* __restrict__ py,
+                                                    const P* __restrict__ pz, int64_t n, Axes ax,
+                                                    const double* __restrict__ ef, P* __restrict__ ex,
+                                                    P* __restrict__ ey, P* __restrict__ ez,
+                                                    unsigned long long* __restrict__ oob) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int ix, iy, iz;
+    double dx, dy, dz;
+    const bool ok = cell_exact(px[p], ax.a[0], ix, dx) & cell_exact(py[p], ax.a[1], iy, dy) &
+                    cell_exact(pz[p], ax.a[2], iz, dz);
+    if (!ok) {
+        atomicAdd(oob, 1ull);
+        ex[p] = P(0);
+        ey[p] = P(0);
+        ez[p] = P(0);
+        return;
+    }
+    const double w000 = (1 - dx) * (1 - dy) * (1 - dz);
+    const double w100 = dx * (1 - dy) * (1 - dz);
+    const double w010 = (1 - dx) * dy * (1 - dz);
+    const double w110 = dx * dy * (1 - dz);
+    const double w001 = (1 - dx) * (1 - dy) * dz;
+    const double w101 = dx * (1 - dy) * dz;
+    const double w011 = (1 - dx) * dy * dz;
+    const double w111 = dx * dy * dz;
+    const int nx = ax.a[0].n, ny = ax.a[1].n, nz = ax.a[2].n;
+    const int64_t sy = nx, sz = (int64_t)nx * ny, N = sz * nz;
+    const int64_t b = ix + sy * iy + sz * iz;
+    double out[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const double* e = ef + c * N + b;
+        // left-to-right sum without FMA contraction, as Julia evaluates it
+        double acc = __dmul_rn(e[0], w000);
+        acc = __dadd_rn(acc, __dmul_rn(e[1], w100));
+        acc = __dadd_rn(acc, __dmul_rn(e[sy], w010));
+        acc = __dadd_rn(acc, __dmul_rn(e[1 + sy], w110));
+        acc = __dadd_rn(acc, __dmul_rn(e[sz], w001));
+        acc = __dadd_rn(acc, __dmul_rn(e[1 + sz], w101));
+        acc = __dadd_rn(acc, __dmul_rn(e[sy + sz], w011));
+        out[c] = __dadd_rn(acc, __dmul_rn(e[1 + sy + sz], w111));
+    }
+    ex[p] = (P)out[0];
+    ey[p] = (P)out[1];
+    ez[p] = (P)out[2];
+}
+
+template <typename T>
+struct Packed;
+template <>
+struct Packed<float> {
+    using V = float4;
+};
+template <>
+struct Packed<double> {
+    using V = dnode4;
+};
+
+__device__ __forceinline__ dnode4 ldg4(const dnode4* p) {
+    // two 16-byte loads (sm_100+ also has 32-byte loads; keep it portable)
+    const double2* q = reinterpret_cast<const double2*>(p);
+    const double2 a = __ldg(q), b = __ldg(q + 1);
+    return dnode4{a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
+
+template <typename P, typename A>
+__device__ __forceinline__ P to_out(A v);
+template <>
+__device__ __forceinline__ float to_out<float, float>(float v) { return v; }
+template <>
+__device__ __forceinline__ double to_out<double, float>(float v) { return f32_to_f64(v); }
+template <>
+__device__ __forceinline__ float to_out<float, double>(double v) { return (float)v; }
+template <>
+__device__ __forceinline__ double to_out<double, double>(double v) { return v; }
+
+template <typename A>
+struct GCell;
+template <>
+struct GCell<float> {
+    template <typename P>
+    __device__ __forceinline__ static bool run(P x, const AxisP& a, int& i, float& f) {
+        return cell_df32(x, a, i, f);
+    }
+};
+template <>
+struct GCell<double> {
+    template <typename P>
+    __device__ __forceinline__ static bool run(P x, const AxisP& a, int& i, double& f) {
+        return cell_dp(x, a, i, f);
+    }
+};
+
+template <typename P, typename A>
+__global__ void __launch_bounds__(256) gather_packed(const P* __restrict__ px, const P* __restrict__ py,
+                                                     const P* __restrict__ pz, int64_t n, Axes ax,
+                                                     const typename Packed<A>::V* __restrict__ ef,
+                                                     P* __restrict__ ex, P* __restrict__ ey, P* __restrict__ ez,
+                                                     unsigned long long* __restrict__ oob) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int ix, iy, iz;
+    A dx, dy, dz;
+    const bool ok = GCell<A>::run(px[p], ax.a[0], ix, dx) & GCell<A>::run(py[p], ax.a[1], iy, dy) &
+                    GCell<A>::run(pz[p], ax.a[2], iz, dz);
+    if (!ok) {
+        atomicAdd(oob, 1ull);
+        ex[p] = P(0);
+        ey[p] = P(0);
+        ez[p] = P(0);
+        return;
+    }
+    const int nx = ax.a[0].n, ny = ax.a[1].n;
+    const int64_t sy = nx, sz = (int64_t)nx * ny;
+    const typename Packed<A>::V* e = ef + (ix + sy * iy + sz * iz);
+    const A ux = A(1) - dx, uy = A(1) - dy, uz = A(1) - dz;
+    const A w[8] = {ux * uy * uz, dx * uy * uz, ux * dy * uz, dx * dy * uz,
+                    ux * uy * dz, dx * uy * dz, ux * dy * dz, dx * dy * dz};
+    const int64_t off[8] = {0, 1, sy, 1 + sy, sz, 1 + sz, sy + sz, 1 + sy + sz};
+    A sx = 0, sy_ = 0, sz_ = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const typename Packed<A>::V v = ldg4(e + off[k]);
+        sx += v.x * w[k];
+        sy_ += v.y * w[k];
+        sz_ += v.z * w[k];
+    }
+    ex[p] = to_out<P, A>(sx);
+    ey[p] = to_out<P, A>(sy_);
+    ez[p] = to_out<P, A>(sz_);
+}
+
+int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n, int dtype, void* ex,
+                  void* ey, void* ez, cudaStream_t s) {
+    const Axes ax = make_axes(m);
+    const int64_t blocks = (n + 255) / 256;
+    if (m->precision == SC_PREC_PLAIN64) {
+        if (dtype == SC_F64)
+            gather_plain<double><<<blocks, 256, 0, s>>>((const double*)x, (const double*)y, (const double*)z, n, ax,
+                                                       (const double*)m->efield, (double*)ex, (double*)ey,
+                                                       (double*)ez, m->oob);
+        else
+            gather_plain<float><<<blocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z, n, ax,
+                                                      (const double*)m->efield, (float*)ex, (float*)ey, (float*)ez,
+                                                      m->oob);
+        SC_LAUNCH_CHECK("gather_plain");
+        return SC_OK;
+    }
+    if (m->precision == SC_PREC_MIXED) {
+        if (dtype == SC_F64)
+            gather_packed<double, float><<<blocks, 256, 0, s>>>((const double*)x, (const double*)y,
+                                                               (const double*)z, n, ax, (const float4*)m->efield,
+                                                               (double*)ex, (double*)ey, (double*)ez, m->oob);
+        else
+            gather_packed<float, float><<<blocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z, n,
+                                                              ax, (const float4*)m->efield, (float*)ex, (float*)ey,
+                                                              (float*)ez, m->oob);
+    } else {
+        if (dtype == SC_F64)
+            gather_packed<double, double><<<blocks, 256, 0, s>>>((const double*)x, (const double*)y,
+                                                                (const double*)z, n, ax, (const dnode4*)m->efield,
+                                                                (double*)ex, (double*)ey, (double*)ez, m->oob);
+        else
+            gather_packed<float, double><<<blocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z,
+                                                               n, ax, (const dnode4*)m->efield, (float*)ex,
+                                                               (float*)ey, (float*)ez, m->oob);
+    }
+    SC_LAUNCH_CHECK("gather_packed");
+    return SC_OK;
+}
+
+}  // namespace sc

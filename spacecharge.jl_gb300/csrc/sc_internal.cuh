@@ -1,0 +1,149 @@
+// Internal declarations shared by the CUDA translation units of
+// libspacecharge_gb300.so.  Nothing here is part of the public C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/spacecharge_gb300.h"
+
+namespace sc {
+
+// src/utils.jl:7-8
+constexpr double kClight = 299792458.0;
+constexpr double kFpei = kClight * kClight * 1.0e-7;
+
+// Packed FP64 field node (Ex, Ey, Ez, 0); 32-byte aligned.
+struct __align__(32) dnode4 {
+    double x, y, z, w;
+};
+
+// Longest transform per axis of the hand-written FFT (power of two).
+constexpr int kMaxL = 1024;
+constexpr int kMaxLog = 10;
+
+// ---------------------------------------------------------------- errors
+void set_error(const char* fmt, ...);
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define SC_CUDA(call)                                            \
+    do {                                                         \
+        cudaError_t _e = (call);                                 \
+        if (_e != cudaSuccess) return ::sc::cuda_fail(_e, #call); \
+    } while (0)
+
+#define SC_LAUNCH_CHECK(what)                                    \
+    do {                                                         \
+        cudaError_t _e = cudaGetLastError();                     \
+        if (_e != cudaSuccess) return ::sc::cuda_fail(_e, what); \
+    } while (0)
+
+#define SC_TRY(...)                       \
+    do {                                  \
+        int _s = (__VA_ARGS__);           \
+        if (_s != SC_OK) return _s;       \
+    } while (0)
+
+// ------------------------------------------------------- per-device state
+struct DeviceCtx {
+    int device = -1;
+    float2* tw32 = nullptr;   // exp(-2 pi i k / kMaxL), k < kMaxL, FP32
+    double2* tw64 = nullptr;  // the same in FP64
+    double* partials = nullptr;  // bounds reduction partials
+    int partial_blocks = 0;
+    int sm_count = 0;
+};
+int device_ctx(DeviceCtx** out);  // for the current device
+
+// ----------------------------------------------------------- Green cache
+struct GreenKey {
+    double delta[3];
+    double gamma;
+    double offset_z;
+    bool valid = false;
+};
+
+// ------------------------------------------------------------------ mesh
+struct NativeWork {
+    // transform lengths and half-spectrum width
+    int L[3] = {0, 0, 0};
+    int log2L[3] = {0, 0, 0};
+    int Hx = 0;
+    size_t elem = 0;        // sizeof(T2) of the pipeline
+    void* A = nullptr;      // Hx x ny x nz            (after x pass)
+    void* B = nullptr;      // Hx x Ly x nz            (after y pass)
+    void* C = nullptr;      // 3 x Hx x Ly x nz        (after z pass)
+    void* D = nullptr;      // 3 x Hx x ny x nz        (after inverse y)
+    // Green function construction
+    double* fcorner = nullptr;  // FP64 antiderivative on corner lattice
+    void* kgrid = nullptr;      // real kernel on the L grid (T)
+    void* kspec = nullptr;      // its half spectrum (T2), Hx x Ly x Lz
+    void* gfree = nullptr;      // compressed free-space spectra, 3 comps (T)
+    void* gimg = nullptr;       // compressed image spectra, 3 comps (T2)
+    GreenKey key_free, key_img;
+};
+
+struct PlainWork {
+    cufftHandle plan = 0;
+    bool plan_ok = false;
+    double2* crho = nullptr;
+    double2* cgrn = nullptr;
+    double2* tmp = nullptr;
+};
+
+}  // namespace sc
+
+struct sc_mesh {
+    int n[3];
+    int64_t N;
+    double lo[3], hi[3], delta[3];
+    double gamma, total_charge;
+    int precision;
+    int device;
+    bool green_cache = true;
+    void* rho = nullptr;     // T[N]
+    void* efield = nullptr;  // planar T[3N] or packed T[4N]
+    unsigned long long* oob = nullptr;  // device counter of skipped particles
+    sc::NativeWork nw;
+    sc::PlainWork pw;
+};
+
+namespace sc {
+
+inline size_t field_elem_bytes(int precision) {
+    return precision == SC_PREC_MIXED ? 4 : 8;
+}
+
+// Kernel-side mesh geometry, passed by value.
+struct Geom {
+    int n[3];
+    double lo[3];
+    double delta[3];
+    double inv[3];  // 1/delta rounded to FP64
+};
+Geom make_geom(const sc_mesh* m);
+
+// entry points implemented per translation unit -------------------------
+int bounds_reduce(const void* x, const void* y, const void* z, int64_t n, int dtype,
+                  double mins[3], double maxs[3], cudaStream_t s);
+
+int deposit_launch(sc_mesh* m, const void* x, const void* y, const void* z, const void* q,
+                   int64_t n, int dtype, int mode, cudaStream_t s);
+int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n,
+                  int dtype, void* ex, void* ey, void* ez, cudaStream_t s);
+
+int cell_index_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n, int dtype,
+                      int32_t* idx, double* frac, cudaStream_t s);
+
+int plain_solve(sc_mesh* m, int at_cathode, cudaStream_t s);
+int plain_release(sc_mesh* m);
+
+int native_prepare(sc_mesh* m);  // sizes only (no allocation)
+int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s);
+int native_release(sc_mesh* m);
+
+}  // namespace sc

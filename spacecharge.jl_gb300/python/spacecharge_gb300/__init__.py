@@ -1,0 +1,11 @@
+"""GB300 space-charge kick: Python host of libspacecharge_gb300.so.
+
+Mirrors SpaceCharge.jl's exports (src/SpaceCharge.jl:17): Mesh3D, deposit
+(deposit!), clear_mesh (clear_mesh!), interpolate_field, solve (solve!), plus
+kick (the three in one library call).
+"""
+from ._lib import SpaceChargeError, load  # noqa: F401
+from .mesh import CLIGHT, FPEI, Mesh3D, clear_mesh, deposit, interpolate_field, kick, solve  # noqa: F401
+
+__all__ = ["Mesh3D", "deposit", "clear_mesh", "interpolate_field", "solve", "kick", "SpaceChargeError",
+           "CLIGHT", "FPEI", "load"]

@@ -1,0 +1,259 @@
+"""Python host of the GB300 space-charge kick, mirroring SpaceCharge.jl's
+public API (src/SpaceCharge.jl:17): Mesh3D, deposit (deposit!), clear_mesh
+(clear_mesh!), solve (solve!) and interpolate_field, with the same argument
+meaning and error behaviour.  All compute runs in libspacecharge_gb300.so;
+torch supplies device memory and the current CUDA stream."""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import SpaceChargeError
+
+CLIGHT = 299792458.0  # src/utils.jl:7
+FPEI = CLIGHT ** 2 * 1.0e-7  # src/utils.jl:8
+
+_PRECISIONS = {"plain64": L.SC_PREC_PLAIN64, "fp64": L.SC_PREC_FP64, "mixed": L.SC_PREC_MIXED}
+_MODES = {"atomic": L.SC_DEPOSIT_ATOMIC, "sorted": L.SC_DEPOSIT_SORTED,
+          "deterministic": L.SC_DEPOSIT_DETERMINISTIC}
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream():
+    torch = _torch()
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _length(a) -> int:
+    return int(a.numel()) if hasattr(a, "numel") else int(np.asarray(a).size)
+
+
+def _is_device_tensor(a) -> bool:
+    return hasattr(a, "is_cuda") and bool(a.is_cuda)
+
+
+def _as_device(arrays, dtype=None):
+    """Particle arrays -> contiguous CUDA tensors of one float dtype (the
+    promoted type, as Julia promotes mixed element types)."""
+    torch = _torch()
+    ts = []
+    for a in arrays:
+        if isinstance(a, torch.Tensor):
+            t = a
+        else:
+            t = torch.from_numpy(np.ascontiguousarray(np.asarray(a)))
+        ts.append(t)
+    if dtype is None:
+        dtype = torch.float64 if any(t.dtype == torch.float64 for t in ts) else torch.float32
+        if any(not t.is_floating_point() for t in ts):
+            dtype = torch.float64
+    out = []
+    for t in ts:
+        if t.dtype != dtype:
+            t = t.to(dtype)
+        if not t.is_cuda:
+            t = t.pin_memory().cuda(non_blocking=True) if t.numel() else t.cuda()
+        out.append(t.contiguous())
+    return out, (L.SC_F64 if dtype == torch.float64 else L.SC_F32)
+
+
+class _CudaView:
+    """__cuda_array_interface__ over mesh-owned memory; keeps the mesh alive."""
+
+    def __init__(self, handle, ptr, shape, typestr):
+        self._handle = handle
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (ptr, False),
+                                         "version": 2, "strides": None}
+
+
+class _Handle:
+    def __init__(self, ptr: C.c_void_p):
+        self.ptr = ptr
+
+    def __del__(self):
+        if self.ptr and self.ptr.value and L._lib is not None:
+            L._lib.sc_mesh_destroy(self.ptr)
+            self.ptr = None
+
+
+class Mesh3D:
+    """Mesh3D(grid_size, particles_x, particles_y, particles_z; ...) or
+    Mesh3D(grid_size, min_bounds, max_bounds; ...), src/mesh.jl:122-265.
+
+    Keywords: T (np.float64 -> precision "fp64", np.float32 -> "mixed"),
+    precision ("plain64" = the reference algorithm in FP64 with cuFFT,
+    "fp64", "mixed"), gamma, total_charge.
+    """
+
+    def __init__(self, grid_size: Sequence[int], *args, T=np.float64, precision: str | None = None,
+                 gamma: float = 1.0, total_charge: float = 0.0):
+        if len(grid_size) != 3:
+            raise SpaceChargeError("grid_size must have 3 elements")
+        if precision is None:
+            precision = "fp64" if np.dtype(T) == np.float64 else "mixed"
+        if precision not in _PRECISIONS:
+            raise SpaceChargeError(f"unknown precision {precision!r}")
+        self.precision = precision
+        g = (C.c_int32 * 3)(*[int(v) for v in grid_size])
+        out = C.c_void_p()
+        prec = _PRECISIONS[precision]
+        if len(args) == 2:  # manual bounds, mesh.jl:223-265
+            lo = (C.c_double * 3)(*[float(v) for v in args[0]])
+            hi = (C.c_double * 3)(*[float(v) for v in args[1]])
+            L.call("sc_mesh_create", g, lo, hi, float(gamma), float(total_charge), prec, C.byref(out))
+        elif len(args) == 3:  # particle bounds, mesh.jl:122-201
+            if any(int(v) <= 1 for v in grid_size):  # :133-135
+                raise SpaceChargeError("All elements of grid_size must be at least 2.")
+            lens = [_length(a) for a in args]
+            if min(lens) == 0:  # :137-139
+                raise SpaceChargeError("Particle arrays cannot be empty.")
+            if not (lens[0] == lens[1] == lens[2]):  # :141-143
+                raise SpaceChargeError("Particle coordinate arrays must have the same length.")
+            (x, y, z), dt = _as_device(args)
+            L.call("sc_mesh_create_from_particles", g, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
+                   C.c_void_p(z.data_ptr()), lens[0], dt, float(gamma), float(total_charge), prec, _stream(),
+                   C.byref(out))
+        else:
+            raise SpaceChargeError("Mesh3D(grid_size, px, py, pz) or Mesh3D(grid_size, min_bounds, max_bounds)")
+        self._h = _Handle(out)
+        info = L.MeshInfo()
+        L.call("sc_mesh_get_info", self._h.ptr, C.byref(info))
+        self.grid_size = tuple(int(v) for v in info.grid_size)
+        self.min_bounds = tuple(float(v) for v in info.min_bounds)
+        self.max_bounds = tuple(float(v) for v in info.max_bounds)
+        self.delta = tuple(float(v) for v in info.delta)
+        self.gamma = float(info.gamma)
+        self.total_charge = float(info.total_charge)
+        self.fft_shape = tuple(int(v) for v in info.fft_shape)
+        self.efield_layout = int(info.efield_layout)
+        self.T = np.float32 if info.elem_bytes == 4 else np.float64
+        self._rho = None
+        self._efield = None
+
+    # --- field access (mesh.rho / mesh.efield in the reference) -----------
+    @property
+    def ptr(self):
+        return self._h.ptr
+
+    @property
+    def rho(self):
+        """Device view of rho with shape (nx, ny, nz) (x fastest, as Julia)."""
+        if self._rho is None:
+            torch = _torch()
+            p = C.c_void_p()
+            L.call("sc_mesh_rho", self._h.ptr, C.byref(p))
+            nx, ny, nz = self.grid_size
+            ts = "<f4" if self.T == np.float32 else "<f8"
+            base = torch.as_tensor(_CudaView(self._h, p.value, (nz, ny, nx), ts), device="cuda")
+            self._rho = base.permute(2, 1, 0)
+        return self._rho
+
+    @property
+    def efield(self):
+        """Device view of efield with shape (nx, ny, nz, 3)."""
+        if self._efield is None:
+            torch = _torch()
+            p = C.c_void_p()
+            L.call("sc_mesh_efield", self._h.ptr, C.byref(p))
+            nx, ny, nz = self.grid_size
+            ts = "<f4" if self.T == np.float32 else "<f8"
+            if self.efield_layout == L.SC_LAYOUT_PACKED:
+                base = torch.as_tensor(_CudaView(self._h, p.value, (nz, ny, nx, 4), ts), device="cuda")
+                self._efield = base.permute(2, 1, 0, 3)[..., :3]
+            else:
+                base = torch.as_tensor(_CudaView(self._h, p.value, (3, nz, ny, nx), ts), device="cuda")
+                self._efield = base.permute(3, 2, 1, 0)
+        return self._efield
+
+    def set_green_cache(self, enabled: bool) -> None:
+        L.call("sc_mesh_set_green_cache", self._h.ptr, 1 if enabled else 0)
+
+    def out_of_range(self) -> int:
+        """Particles skipped as outside the mesh since the last query."""
+        n = C.c_int64()
+        L.call("sc_mesh_out_of_range", self._h.ptr, C.byref(n), _stream())
+        return int(n.value)
+
+    def __repr__(self):  # mesh.jl:267-273
+        nx, ny, nz = self.grid_size
+        lo, hi = self.min_bounds, self.max_bounds
+        T = "Float32" if self.T == np.float32 else "Float64"
+        return (f"Mesh3D{{{T}, {self.precision}}} ({nx}x{ny}x{nz}) bounds=[({lo[0]},{lo[1]},{lo[2]}), "
+                f"({hi[0]},{hi[1]},{hi[2]})] gamma={self.gamma}")
+
+
+def clear_mesh(mesh: Mesh3D) -> None:
+    """clear_mesh!(mesh), src/deposition.jl:10-12."""
+    L.call("sc_clear_mesh", mesh.ptr, _stream())
+
+
+def deposit(mesh: Mesh3D, particles_x, particles_y, particles_z, particles_q, clear: bool = True,
+            mode: str = "atomic") -> None:
+    """deposit!(mesh, px, py, pz, pq; clear=true), src/deposition.jl:218-247."""
+    lens = [_length(a) for a in (particles_x, particles_y, particles_z, particles_q)]
+    if not (lens[0] == lens[1] == lens[2] == lens[3]):  # :226-228
+        raise SpaceChargeError("Particle coordinate and charge arrays must have the same length.")
+    if mode not in _MODES:
+        raise SpaceChargeError(f"unknown deposit mode {mode!r}")
+    if lens[0] == 0:
+        if clear:
+            clear_mesh(mesh)
+        return
+    (x, y, z, q), dt = _as_device((particles_x, particles_y, particles_z, particles_q))
+    L.call("sc_deposit", mesh.ptr, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), C.c_void_p(z.data_ptr()),
+           C.c_void_p(q.data_ptr()), lens[0], dt, 1 if clear else 0, _MODES[mode], _stream())
+
+
+def solve(mesh: Mesh3D, at_cathode: bool = False) -> None:
+    """solve!(mesh; at_cathode=false), src/solvers/free_space.jl:14-47."""
+    L.call("sc_solve", mesh.ptr, 1 if at_cathode else 0, _stream())
+
+
+def _similar_out(template, xs):
+    """Outputs of the particle type and array kind (similar(particles_x))."""
+    torch = _torch()
+    return [torch.empty_like(xs[0]) for _ in range(3)]
+
+
+def _return_like(template, outs):
+    torch = _torch()
+    if isinstance(template, torch.Tensor):
+        return tuple(o if template.is_cuda else o.cpu() for o in outs)
+    return tuple(o.cpu().numpy() for o in outs)
+
+
+def interpolate_field(mesh: Mesh3D, particles_x, particles_y, particles_z):
+    """interpolate_field(mesh, px, py, pz) -> (Ex, Ey, Ez),
+    src/interpolation.jl:100-128: outputs have the particle element type and
+    array kind (device tensors stay on the device, host arrays come back to
+    the host)."""
+    lens = [_length(a) for a in (particles_x, particles_y, particles_z)]
+    if not (lens[0] == lens[1] == lens[2]):
+        raise SpaceChargeError("Particle coordinate arrays must have the same length.")
+    (x, y, z), dt = _as_device((particles_x, particles_y, particles_z))
+    ex, ey, ez = _similar_out(particles_x, (x, y, z))
+    if lens[0]:
+        L.call("sc_interpolate_field", mesh.ptr, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
+               C.c_void_p(z.data_ptr()), lens[0], dt, C.c_void_p(ex.data_ptr()), C.c_void_p(ey.data_ptr()),
+               C.c_void_p(ez.data_ptr()), _stream())
+    return _return_like(particles_x, (ex, ey, ez))
+
+
+def kick(mesh: Mesh3D, particles_x, particles_y, particles_z, particles_q, at_cathode: bool = False):
+    """deposit! -> solve! -> interpolate_field in one library call."""
+    lens = [_length(a) for a in (particles_x, particles_y, particles_z, particles_q)]
+    if not (lens[0] == lens[1] == lens[2] == lens[3]):
+        raise SpaceChargeError("Particle coordinate and charge arrays must have the same length.")
+    (x, y, z, q), dt = _as_device((particles_x, particles_y, particles_z, particles_q))
+    ex, ey, ez = _similar_out(particles_x, (x, y, z))
+    L.call("sc_kick", mesh.ptr, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), C.c_void_p(z.data_ptr()),
+           C.c_void_p(q.data_ptr()), lens[0], dt, 1 if at_cathode else 0, C.c_void_p(ex.data_ptr()),
+           C.c_void_p(ey.data_ptr()), C.c_void_p(ez.data_ptr()), _stream())
+    return _return_like(particles_x, (ex, ey, ez))

@@ -1,0 +1,271 @@
+"""Parity of the CUDA library (through the C ABI / Python host) with the CPU
+oracle on the same seeded inputs, for every precision, plus the reference's
+own GPU test assertions (test/test_gpu.jl).
+
+Tolerances (max |a-b| / max |b| over the compared arrays):
+  plain64, fp64 : 1e-11 (FP64 throughout; only FFT rounding differs)
+  mixed         : 1e-5  (FP32 deposit/FFT/gather vs the FP64 oracle)
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+PRECS = ["plain64", "fp64", "mixed"]
+TOL = {"plain64": 1e-11, "fp64": 1e-11, "mixed": 1e-5}
+RHO_TOL = {"plain64": 1e-13, "fp64": 1e-13, "mixed": 1e-6}
+
+
+def relerr(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    s = np.abs(b).max()
+    return np.abs(a - b).max() / (s if s > 0 else 1.0)
+
+
+def host(t):
+    return t.detach().cpu().numpy().astype(np.float64)
+
+
+def bunch(n, seed, sig=(1e-3, 1e-3, 1e-3), cut=5.0):
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in sig:
+        v = rng.standard_normal(n)
+        bad = np.abs(v) > cut
+        while bad.any():  # resample beyond +-cut sigma
+            v[bad] = rng.standard_normal(bad.sum())
+            bad = np.abs(v) > cut
+        out.append(v * s)
+    return out
+
+
+def run_both(sc, grid, xyzq, prec, gamma=1.0, at_cathode=False, bounds=None):
+    x, y, z, q = xyzq
+    if bounds is None:
+        om = O.mesh_auto(grid, x, y, z, gamma=gamma)
+        m = sc.Mesh3D(grid, x, y, z, precision=prec, gamma=gamma)
+    else:
+        om = O.mesh_manual(grid, *bounds, gamma=gamma)
+        m = sc.Mesh3D(grid, *bounds, precision=prec, gamma=gamma)
+    O.deposit(om, x, y, z, q)
+    O.solve(om, at_cathode=at_cathode)
+    oe = O.interpolate_field(om, x, y, z)
+    sc.deposit(m, x, y, z, q)
+    rho = host(m.rho)
+    sc.solve(m, at_cathode=at_cathode)
+    e = sc.interpolate_field(m, x, y, z)
+    return om, m, rho, oe, e
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_auto_bounds_match_oracle(sc, cuda, prec):
+    x, y, z = bunch(5000, 1)
+    m = sc.Mesh3D((10, 20, 30), x, y, z, precision=prec)
+    om = O.mesh_auto((10, 20, 30), x, y, z)
+    assert m.min_bounds == tuple(float(v) for v in om.min_bounds)
+    assert m.max_bounds == tuple(float(v) for v in om.max_bounds)
+    assert m.delta == tuple(float(v) for v in om.delta)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("grid,gamma", [((16, 16, 24), 2.0), ((10, 12, 7), 1.0), ((8, 8, 8), 10.0)])
+def test_kick_parity(sc, cuda, prec, grid, gamma):
+    n = 6000
+    x, y, z = bunch(n, 11, sig=(1e-3, 0.7e-3, 1.5e-3))
+    q = np.full(n, 1e-9 / n)
+    om, m, rho, oe, e = run_both(sc, grid, (x, y, z, q), prec, gamma=gamma)
+    assert relerr(rho, om.rho) < RHO_TOL[prec]
+    assert relerr(host(m.efield), om.efield) < TOL[prec]
+    for a, b in zip(e, oe):
+        assert relerr(a, b) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_cathode_parity(sc, cuda, prec):
+    n = 5000
+    x, y, z = bunch(n, 3, sig=(1e-3, 1e-3, 0.5e-3))
+    z = np.abs(z) + 0.2e-3
+    q = np.full(n, 1e-10 / n)
+    om, m, rho, oe, e = run_both(sc, (12, 12, 16), (x, y, z, q), prec, gamma=1.5, at_cathode=True)
+    assert relerr(host(m.efield), om.efield) < TOL[prec]
+    for a, b in zip(e, oe):
+        assert relerr(a, b) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_manual_bounds_and_float32_particles(sc, cuda, prec):
+    import torch
+
+    n = 4000
+    x, y, z = bunch(n, 5)
+    q = np.full(n, 1e-9 / n)
+    b = ((-5e-3,) * 3, (5e-3,) * 3)
+    x32, y32, z32, q32 = (np.asarray(v, np.float32) for v in (x, y, z, q))
+    om = O.mesh_manual((16, 16, 16), *b)
+    O.deposit(om, x32, y32, z32, q32)
+    O.solve(om)
+    oe = O.interpolate_field(om, x32, y32, z32)
+    m = sc.Mesh3D((16, 16, 16), *b, precision=prec)
+    dev = [torch.from_numpy(v).cuda() for v in (x32, y32, z32, q32)]
+    sc.deposit(m, *dev)
+    sc.solve(m)
+    e = sc.interpolate_field(m, *dev[:3])
+    assert all(t.dtype == torch.float32 and t.is_cuda for t in e)  # similar(particles_x)
+    tol = max(TOL[prec], 2e-6)  # outputs are FP32
+    for a, b_ in zip(e, oe):
+        assert relerr(host(a), b_) < tol
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_cell_index_bit_exact(sc, cuda, prec):
+    """The binning step against the reference's floor((x-min)/delta) on
+    adversarial positions: exactly on faces, one ulp either side, and a bunch
+    far from the origin."""
+    import ctypes as C
+
+    import torch
+
+    from spacecharge_gb300 import _lib as L
+
+    rng = np.random.default_rng(2)
+    lo, hi, n = (-0.37e-3, 1000.0 - 2e-3, -7e-3), (0.41e-3, 1000.0 + 3e-3, 9e-3), (33, 64, 129)
+    m = sc.Mesh3D(n, lo, hi, precision=prec)
+    om = O.mesh_manual(n, lo, hi)
+    pts = []
+    for d in range(3):
+        k = rng.integers(0, n[d] - 1, 3000)
+        face = om.min_bounds[d] + k * om.delta[d]
+        v = np.concatenate([face, np.nextafter(face, np.inf), np.nextafter(face, -np.inf),
+                            rng.uniform(om.min_bounds[d], om.max_bounds[d], 3000)])
+        pts.append(v)
+    cnt = min(len(p) for p in pts)
+    px, py, pz = (np.ascontiguousarray(p[:cnt]) for p in pts)
+    (oi, of) = O.cic_cells(om, px, py, pz)
+    nmax = np.array(n)[:, None] - 2
+    valid = ((oi >= 0) & (oi <= nmax)).all(axis=0)
+    dev = [torch.from_numpy(v).cuda() for v in (px, py, pz)]
+    idx = torch.empty(cnt * 3, dtype=torch.int32, device="cuda")
+    frac = torch.empty(cnt * 3, dtype=torch.float64, device="cuda")
+    L.call("sc_cell_index", m.ptr, *[C.c_void_p(t.data_ptr()) for t in dev], cnt, L.SC_F64,
+           C.c_void_p(idx.data_ptr()), C.c_void_p(frac.data_ptr()), None)
+    torch.cuda.synchronize()
+    gi = idx.cpu().numpy().reshape(cnt, 3).T
+    gf = frac.cpu().numpy().reshape(cnt, 3).T
+    assert np.array_equal(gi[:, valid], oi[:, valid])
+    assert (gi[:, ~valid] == -1).all()
+    ftol = 0.0 if prec == "plain64" else (1e-12 if prec == "fp64" else 2e-7)
+    assert np.abs(gf[:, valid] - of[:, valid]).max() <= ftol
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_out_of_range_counted(sc, cuda, prec):
+    m = sc.Mesh3D((8, 8, 8), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), precision=prec)
+    x = np.array([0.5, 1.0, -0.1, 0.3, 7.0])
+    sc.deposit(m, x, x, x, np.ones(5))
+    e = sc.interpolate_field(m, x, x, x)
+    # x = 1.0 is the max bound: floor gives n-1, outside [0, n-2]
+    assert m.out_of_range() == 6
+    assert abs(float(m.rho.sum()) - 2.0) < 1e-6
+    assert all(v[1] == 0 and v[2] == 0 and v[4] == 0 for v in e)
+
+
+# ----------------------------------------------- test/test_gpu.jl restated
+@pytest.mark.parametrize("prec", PRECS)
+def test_reference_gpu_suite(sc, cuda, prec):
+    import torch
+
+    # GPU Deposition (test_gpu.jl:24-43)
+    m = sc.Mesh3D((8, 8, 8), [0.5], [0.5], [0.5], precision=prec)
+    one = torch.tensor([0.5], dtype=torch.float32, device="cuda")
+    sc.deposit(m, one, one, one, torch.tensor([1.0], dtype=torch.float32, device="cuda"))
+    assert abs(float(m.rho.sum()) - 1.0) < 1e-6 and bool((m.rho > 0).any())
+    # GPU Solver (:75-95)
+    m = sc.Mesh3D((8, 8, 8), [0.0], [0.0], [0.0], precision=prec, gamma=2.0)
+    sc.deposit(m, [0.0], [0.0], [0.0], [1.0])
+    sc.solve(m)
+    assert bool((m.efield != 0).any())
+    # Multiple particles (:97-123)
+    px, py, pz, pq = [0.2, 0.8], [0.3, 0.7], [0.4, 0.6], [1.0, -1.0]
+    m = sc.Mesh3D((6, 6, 6), px, py, pz, precision=prec)
+    sc.deposit(m, px, py, pz, pq)
+    sc.solve(m)
+    e = sc.interpolate_field(m, px, py, pz)
+    assert all(np.isfinite(v).all() and len(v) == 2 for v in e)
+    assert abs(float(m.rho.sum())) < 1e-6
+    # Clear (:187-203)
+    sc.clear_mesh(m)
+    assert bool((m.rho == 0).all())
+    # Interpolation with a set field (:45-73): efield view is writable
+    m = sc.Mesh3D((6, 6, 6), [0.5], [0.5], [0.5], precision=prec)
+    m.efield[0, 0, 0, 0] = 1.0
+    m.efield[1, 0, 0, 0] = 2.0
+    e = sc.interpolate_field(m, [0.5], [0.5], [0.5])
+    assert np.isfinite(e[0][0]) and e[1][0] == 0 and e[2][0] == 0
+    # Constant field interpolates exactly (test_interpolation.jl:115-133)
+    m = sc.Mesh3D((4, 4, 4), [0.0, 1.0], [0.0, 1.0], [0.0, 1.0], precision=prec)
+    m.efield[...] = 1.0
+    e = sc.interpolate_field(m, [0.0, 1.0], [0.0, 1.0], [0.0, 1.0])
+    assert all(np.allclose(v, 1.0, rtol=1e-6) for v in e)
+    # Point charge field at the centre (test_interpolation.jl:87-112)
+    m = sc.Mesh3D((8, 8, 8), [0.0], [0.0], [0.0], precision=prec)
+    sc.deposit(m, [0.0], [0.0], [0.0], [1.0])
+    sc.solve(m)
+    e = sc.interpolate_field(m, [0.0], [0.0], [0.0])
+    assert all(abs(v[0]) > 1e7 for v in e)
+    # Cathode and gamma change the field (test_solvers.jl:33-78)
+    a = sc.Mesh3D((16, 16, 16), [0.0], [0.0], [0.01], precision=prec, gamma=2.0)
+    b = sc.Mesh3D((16, 16, 16), [0.0], [0.0], [0.01], precision=prec, gamma=2.0)
+    for mm in (a, b):
+        sc.deposit(mm, [0.0], [0.0], [0.01], [1.0])
+    sc.solve(a, at_cathode=True)
+    sc.solve(b)
+    assert not np.allclose(host(a.efield), host(b.efield))
+    assert np.isfinite(host(a.efield)).all()
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_accumulate(sc, cuda, prec):  # test_deposition.jl:67-86
+    m = sc.Mesh3D((4, 4, 4), [0.5], [0.5], [0.5], precision=prec)
+    sc.deposit(m, [0.5], [0.5], [0.5], [1.0])
+    first = float(m.rho.sum())
+    sc.deposit(m, [0.5], [0.5], [0.5], [1.0], clear=False)
+    assert abs(float(m.rho.sum()) - 2 * first) < 1e-6
+
+
+def test_plain_gather_bitwise(sc, cuda):
+    """With the same efield, the plain gather reproduces the reference's
+    arithmetic exactly (interpolation.jl:30-85)."""
+    import torch
+
+    rng = np.random.default_rng(9)
+    om = O.mesh_manual((9, 7, 11), (-1.0, -2.0, 0.5), (1.0, 0.3, 2.0))
+    om.efield[...] = rng.standard_normal(om.efield.shape)
+    m = sc.Mesh3D((9, 7, 11), (-1.0, -2.0, 0.5), (1.0, 0.3, 2.0), precision="plain64")
+    m.efield.copy_(torch.from_numpy(om.efield).cuda())
+    px = rng.uniform(-1.0, 1.0 - 1e-9, 5000)
+    py = rng.uniform(-2.0, 0.3 - 1e-9, 5000)
+    pz = rng.uniform(0.5, 2.0 - 1e-9, 5000)
+    e = sc.interpolate_field(m, px, py, pz)
+    oe = O.interpolate_field(om, px, py, pz)
+    for a, b in zip(e, oe):
+        assert np.array_equal(a, b)
+
+
+def test_mixed_vs_fp64_tolerance(sc, cuda):
+    """Mixed precision against the all-FP64 path on a boosted anisotropic
+    Gaussian (the 1M-particle 64x64x128 gamma=10 case at reduced size):
+    max relative field error <= 1e-5."""
+    n = 200_000
+    x, y, z = bunch(n, 21, sig=(1e-3, 1e-3, 1e-4))
+    q = np.full(n, 1e-9 / n)
+    b = ((-5e-3, -5e-3, -5e-4), (5e-3, 5e-3, 5e-4))
+    res = {}
+    for prec in ("plain64", "mixed"):
+        m = sc.Mesh3D((32, 32, 64), *b, precision=prec, gamma=10.0)
+        e = sc.kick(m, x, y, z, q)
+        res[prec] = (host(m.efield), e)
+    assert relerr(res["mixed"][0], res["plain64"][0]) < 1e-5
+    for a, b_ in zip(res["mixed"][1], res["plain64"][1]):
+        assert relerr(a, b_) < 1e-5
