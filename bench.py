@@ -1,0 +1,369 @@
+"""Benchmark of the full space-charge kick (deposit + solve + interpolate).
+
+Workload (one "step" = one full kick): a Lorentz-boosted anisotropic Gaussian
+bunch of 1,000,000 macro-particles, sigma_x = sigma_y = 1 mm, sigma_z = 0.1 mm
+(lab frame, draws beyond 5 sigma resampled, seed 42), gamma = 10, 1 nC in
+equal weights, FP64 SoA positions and charges, on a 64 x 64 x 128 mesh
+spanning +-5 sigma.  The mixed-precision kick (FP32 deposit/FFT/gather, FP64
+IGF and origin offsets) is timed with the Green function rebuilt on every
+kick (the reference rebuilds it in every solve!), inputs resident in HBM and
+L2 flushed (256 MB write) between kicks.  The plain FP64 path (the
+reference's algorithm with cuFFT Z2Z) is timed on the same inputs and the
+mixed fields are compared with it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun (N > 1) every rank runs the same kick on its own GPU
+(replicas; the kick has no data-parallel exchange), the timed region is
+bracketed by barriers and the max over ranks is reported.
+
+--impl reference times the CPU restatement of the reference (oracle/, FP64
+NumPy/SciPy, all host cores for the FFTs) on the same workload; rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "spacecharge.jl_gb300", "python"))
+
+METRIC = "full kick ms (deposit+solve+interp), mixed vs FP64 at rel-err<=1e-5; grad ms"
+GRID = (64, 64, 128)
+NP = 1_000_000
+SIGMA = (1e-3, 1e-3, 1e-4)
+GAMMA = 10.0
+QTOT = 1e-9
+SEED = 42
+BOUNDS = tuple((-5 * s for s in SIGMA)), tuple((5 * s for s in SIGMA))
+WORKLOAD = "boosted Gaussian 1M particles, 64x64x128 mesh, gamma=10, +-5 sigma, FP64 particles"
+
+
+def make_bunch(n=NP, seed=SEED, sigma=SIGMA):
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in sigma:
+        v = rng.standard_normal(n)
+        bad = np.abs(v) > 5.0
+        while bad.any():
+            v[bad] = rng.standard_normal(int(bad.sum()))
+            bad = np.abs(v) > 5.0
+        out.append(v * s)
+    out.append(np.full(n, QTOT / n))
+    return out
+
+
+def algorithmic_bytes(np_, n, s_g, s_out=8):
+    """Compulsory bytes of one kick: particles read by deposit (x,y,z,q) and
+    gather (x,y,z) and written by the gather (Ex,Ey,Ez), rho written and read,
+    E written and read (FFT intermediates and the Green spectrum excluded)."""
+    return np_ * (32 + 24 + 3 * s_out) + n * 8 * s_g
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------ distributed
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def max_over_ranks(v, ws):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ---------------------------------------------------------- CPU reference
+def cpu_kick_time(steps, warmup, bunch, max_seconds=None):
+    """Time the oracle (FP64 NumPy/SciPy restatement of the reference) on the
+    full workload; returns (ms per kick, kicks timed)."""
+    import oracle as O
+
+    x, y, z, q = bunch
+    times = []
+    for i in range(warmup + steps):
+        t0 = time.perf_counter()
+        m = O.mesh_manual(GRID, *BOUNDS, gamma=GAMMA, total_charge=QTOT)
+        O.kick(m, x, y, z, q)
+        dt = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(dt)
+        if max_seconds is not None and sum(times) > max_seconds and times:
+            break
+    return 1e3 * float(np.mean(times)), len(times)
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    bunch = make_bunch()
+    ms, k = cpu_kick_time(args.steps, args.warmup, bunch)
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(ms, 3), "unit": "ms", "n_gpus": args.gpus,
+        "steps": k, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Gaussian bunch)",
+        "config": {"workload": WORKLOAD, "grid": list(GRID), "particles": NP, "gamma": GAMMA},
+        "cpu_baseline": {"value": round(ms, 3), "unit": "ms", "cores": cores, "kind": "port",
+                         "sample": f"{k} full kicks of the workload (FP64 oracle: serial deposit, "
+                                   f"scipy.fft workers={cores})"},
+        "e2e": {"value": round(ms, 3), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# -------------------------------------------------------------- GPU arm
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import __graft_entry__ as g
+
+    g.build()
+    import spacecharge_gb300 as sc
+    from spacecharge_gb300 import _lib as L
+    import ctypes as C
+
+    bunch = make_bunch()
+    dev = [torch.from_numpy(v).cuda() for v in bunch]
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+
+    def timed(fn, steps, warmup, per_step_flush=True):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        barrier(ws)
+        torch.cuda.synchronize()
+        for a, b in evs:
+            if per_step_flush:
+                flush.zero_()
+            a.record(stream)
+            fn()
+            b.record(stream)
+        torch.cuda.synchronize()
+        barrier(ws)
+        return float(np.mean([a.elapsed_time(b) for a, b in evs]))
+
+    ex, ey, ez = (torch.empty_like(dev[0]) for _ in range(3))
+
+    def kick(m):
+        return lambda: L.call("sc_kick", m.ptr, *[C.c_void_p(t.data_ptr()) for t in dev[:4]], NP, L.SC_F64, 0,
+                              C.c_void_p(ex.data_ptr()), C.c_void_p(ey.data_ptr()), C.c_void_p(ez.data_ptr()),
+                              C.c_void_p(stream.cuda_stream))
+
+    # ---- mixed kick, Green function rebuilt each kick (headline value)
+    mm = sc.Mesh3D(GRID, *BOUNDS, precision="mixed", gamma=GAMMA, total_charge=QTOT)
+    mm.set_green_cache(False)
+    kick(mm)()
+    l0 = C.c_int64()
+    L.call("sc_mesh_launch_count", mm.ptr, C.byref(l0))
+    L.call("sc_mesh_set_profiling", mm.ptr, 1)
+    L.call("sc_mesh_stage_times", mm.ptr, None, None, C.c_void_p(stream.cuda_stream))  # reset
+    sampler = ClockSampler(local)
+    sampler.start()
+    ms_mixed = timed(kick(mm), args.steps, args.warmup)
+    stage_ms = (C.c_double * L.SC_NUM_STAGES)()
+    stage_n = (C.c_int64 * L.SC_NUM_STAGES)()
+    L.call("sc_mesh_stage_times", mm.ptr, stage_ms, stage_n, C.c_void_p(stream.cuda_stream))
+    L.call("sc_mesh_set_profiling", mm.ptr, 0)
+    l1 = C.c_int64()
+    L.call("sc_mesh_launch_count", mm.ptr, C.byref(l1))
+    launches_per_kick = (l1.value - l0.value) / (args.steps + args.warmup)
+    mixed_e = [t.double().cpu().numpy() for t in (ex, ey, ez)]
+    mixed_grid = mm.efield.double().cpu().numpy()
+    ms_mixed = max_over_ranks(ms_mixed, ws)
+
+    # ---- mixed kick with the Green spectrum reused (same geometry)
+    mm.set_green_cache(True)
+    ms_cached = max_over_ranks(timed(kick(mm), args.steps, args.warmup), ws)
+
+    # ---- plain FP64 path (reference algorithm, cuFFT Z2Z)
+    mp = sc.Mesh3D(GRID, *BOUNDS, precision="plain64", gamma=GAMMA, total_charge=QTOT)
+    ms_plain = max_over_ranks(timed(kick(mp), max(3, args.steps // 4), 3), ws)
+    plain_e = [t.double().cpu().numpy() for t in (ex, ey, ez)]
+    plain_grid = mp.efield.double().cpu().numpy()
+
+    def rel(a, b):
+        return float(np.abs(a - b).max() / np.abs(b).max()), float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    err_grid = rel(mixed_grid, plain_grid)
+    errs_p = [rel(a, b) for a, b in zip(mixed_e, plain_e)]
+    err_part = (max(e[0] for e in errs_p), max(e[1] for e in errs_p))
+
+    # ---- end to end through the public API with host buffers
+    host_in = [torch.from_numpy(v).pin_memory() for v in bunch]
+    host_out = [torch.empty(NP, dtype=torch.float64).pin_memory() for _ in range(3)]
+    mm.set_green_cache(False)
+
+    def e2e_step():
+        for h, d in zip(host_in, dev):
+            d.copy_(h, non_blocking=True)
+        kick(mm)()
+        for h, d in zip(host_out, (ex, ey, ez)):
+            h.copy_(d, non_blocking=True)
+
+    ms_e2e = max_over_ranks(timed(e2e_step, args.steps, args.warmup), ws)
+    clocks = sampler.stop()
+
+    # ---- roofline of the dominant stage (CUDA events inside the timed loop)
+    names = L.STAGES
+    per = {names[k]: stage_ms[k] / max(1, stage_n[k]) for k in range(L.SC_NUM_STAGES) if stage_n[k]}
+    nx, ny, nz = GRID
+    N = nx * ny * nz
+    Hx, Ly, Lz = 65, 128, 256
+    stage_bytes = {
+        "deposit": NP * 32 + N * 4,
+        "gather": NP * (24 + 24) + N * 16,
+        "fwd_x": N * 4 + Hx * ny * nz * 8,
+        "fwd_y": Hx * ny * nz * 8 + Hx * Ly * nz * 8,
+        "zpass": Hx * Ly * nz * 8 + 3 * Hx * Ly * nz * 8,
+        "inv_y": 3 * Hx * Ly * nz * 8 + 3 * Hx * ny * nz * 8,
+        "inv_x": 3 * Hx * ny * nz * 8 + N * 16,
+    }
+    dom = max((k for k in per if k in stage_bytes), key=lambda k: per[k])
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+    ach = stage_bytes[dom] / (per[dom] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(ach / peak, 4), "peak_source": peak_src, "traffic": None,
+                "algorithmic_bytes": stage_bytes[dom], "ms_per_launch": round(per[dom], 5)}
+
+    # ---- CPU baseline: the oracle on a bounded sample (rank 0, N = 1)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu_ms, k = cpu_kick_time(2, 0, bunch, max_seconds=30)
+        cpu = {"value": round(cpu_ms, 2), "unit": "ms", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{k} full kicks of the same workload with the FP64 oracle (serial deposit, "
+                         f"scipy.fft workers={os.cpu_count()})"}
+
+    kick_bytes = algorithmic_bytes(NP, N, 4)
+    line = {
+        "metric": METRIC, "value": round(ms_mixed, 4), "unit": "ms", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_mixed, 4), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 IGF, offsets)",
+        "data": "synthetic (seeded Gaussian bunch)",
+        "config": {"workload": WORKLOAD, "grid": list(GRID), "particles": NP, "gamma": GAMMA,
+                   "precision": "mixed", "green": "rebuilt every kick", "l2": "flushed (256 MB) between kicks",
+                   "parallelism": f"replicas x{ws}"},
+        "ms_fp64_plain": round(ms_plain, 4),
+        "speedup_vs_fp64_plain": round(ms_plain / ms_mixed, 3),
+        "ms_green_cached": round(ms_cached, 4),
+        "max_rel_err_vs_fp64": {"mesh": err_grid[0], "particles": err_part[0]},
+        "rms_rel_err_vs_fp64": {"mesh": err_grid[1], "particles": err_part[1]},
+        "grad_ms": None,
+        "particles_per_s": round(ws * NP / (ms_mixed * 1e-3), 1),
+        "kick_algorithmic_bytes": kick_bytes,
+        "kick_GBps": round(kick_bytes / (ms_mixed * 1e-3) / 1e9, 1),
+        "stage_ms": {k: round(v, 5) for k, v in per.items()},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(ms_e2e, 4), "unit": "ms", "h2d_bytes_per_step": 4 * NP * 8,
+                "d2h_bytes_per_step": 3 * NP * 8},
+        "gpu_launches": int(round(launches_per_kick * args.steps)),
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

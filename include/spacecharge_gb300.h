@@ -58,6 +58,18 @@ extern "C" {
 #define SC_DEPOSIT_SORTED        1 /* bin by cell, warp-segmented sums, few atomics */
 #define SC_DEPOSIT_DETERMINISTIC 2 /* sorted, fixed reduction order, no float atomics */
 
+/* pipeline stages timed by sc_mesh_stage_times */
+#define SC_STAGE_DEPOSIT   0 /* clear + deposit kernels */
+#define SC_STAGE_GREEN     1 /* Green-function build (IGF + its transform) */
+#define SC_STAGE_FWD_X     2 /* hand-written: real rows -> half spectra */
+#define SC_STAGE_FWD_Y     3 /* hand-written: y transform */
+#define SC_STAGE_ZPASS     4 /* hand-written: z transform x Green x inverse z */
+#define SC_STAGE_INV_Y     5 /* hand-written: inverse y */
+#define SC_STAGE_INV_X     6 /* hand-written: inverse x -> packed efield */
+#define SC_STAGE_GATHER    7 /* interpolation */
+#define SC_STAGE_PLAIN_FFT 8 /* plain path: pad, cuFFT Z2Z, product, extract */
+#define SC_NUM_STAGES      9
+
 /* efield layouts */
 #define SC_LAYOUT_PLANAR 0
 #define SC_LAYOUT_PACKED 1
@@ -155,6 +167,34 @@ int sc_kick(sc_mesh* mesh, const void* x, const void* y, const void* z, const vo
  * as FP64.  Uses the same device arithmetic as the mesh's deposit kernel. */
 int sc_cell_index(sc_mesh* mesh, const void* x, const void* y, const void* z, int64_t n, int dtype,
                   int32_t* idx, double* frac, void* stream);
+
+/* Stage timing: while enabled, every stage of deposit/solve/interpolate is
+ * bracketed by CUDA events recorded on the caller's stream.
+ * sc_mesh_stage_times synchronises `stream`, writes the milliseconds and the
+ * number of timed executions per stage accumulated since the previous query
+ * (arrays of SC_NUM_STAGES), and resets them. */
+int sc_mesh_set_profiling(sc_mesh* mesh, int enabled);
+int sc_mesh_stage_times(sc_mesh* mesh, double* ms, int64_t* calls, void* stream);
+
+/* Number of kernels this mesh has launched since it was created (cuFFT's
+ * internal kernels count as one per transform). */
+int sc_mesh_launch_count(const sc_mesh* mesh, int64_t* count);
+
+/* Hand-written adjoint of sc_kick (the pullback of the ChainRulesCore.rrule
+ * of `kick` in the Julia host; the reference itself is not differentiable:
+ * src/mesh.jl:100 restricts T to AbstractFloat).  Recomputes the forward
+ * deposit and solve for these particles (mesh.rho / mesh.efield are left as
+ * after sc_kick, except efield's unused fourth lane), then returns
+ * d(loss)/d(x, y, z, q) into dx, dy, dz, dq (particle dtype) given
+ *   gex, gey, gez : d(loss)/d(Ex, Ey, Ez) at the particles (NULL = zero),
+ *   ggrid         : d(loss)/d(mesh.efield) in the mesh's packed layout
+ *                   (4, nx, ny, nz) of its element type, or NULL.
+ * The mesh geometry is held fixed; gradients are those of the piecewise
+ * smooth map inside each particle's cell.  Needs an SC_PREC_FP64 or
+ * SC_PREC_MIXED mesh (SC_ERR_UNSUPPORTED otherwise). */
+int sc_kick_adjoint(sc_mesh* mesh, const void* x, const void* y, const void* z, const void* q, int64_t n,
+                    int dtype, int at_cathode, const void* gex, const void* gey, const void* gez,
+                    const void* ggrid, void* dx, void* dy, void* dz, void* dq, void* stream);
 
 /* Number of particles skipped as out of range since the last call
  * (deposit and interpolate); resets the counter.  Synchronises `stream`. */

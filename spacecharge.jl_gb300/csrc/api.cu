@@ -83,6 +83,35 @@ Geom make_geom(const sc_mesh* m) {
     return g;
 }
 
+void StageTimer::begin(int stage, cudaStream_t s) {
+    if (open_stage >= 0) end(s);
+    if (used[stage] == ev[stage].size()) {
+        Pair p;
+        if (cudaEventCreate(&p.a) != cudaSuccess || cudaEventCreate(&p.b) != cudaSuccess) return;
+        ev[stage].push_back(p);
+    }
+    cudaEventRecord(ev[stage][used[stage]].a, s);
+    open_stage = stage;
+}
+
+void StageTimer::end(cudaStream_t s) {
+    if (open_stage < 0) return;
+    cudaEventRecord(ev[open_stage][used[open_stage]].b, s);
+    used[open_stage]++;
+    open_stage = -1;
+}
+
+void StageTimer::release() {
+    for (int k = 0; k < SC_NUM_STAGES; ++k) {
+        for (auto& p : ev[k]) {
+            cudaEventDestroy(p.a);
+            cudaEventDestroy(p.b);
+        }
+        ev[k].clear();
+        used[k] = 0;
+    }
+}
+
 static int check_grid(const int32_t* g) {
     if (!g) return fail(SC_ERR_INVALID, "grid_size is NULL");
     // src/mesh.jl:133-135
@@ -235,10 +264,41 @@ int sc_mesh_destroy(sc_mesh* m) {
         plain_release(m);
     else
         native_release(m);
+    m->timer.release();
     cudaFree(m->rho);
     cudaFree(m->efield);
     cudaFree(m->oob);
     delete m;
+    return SC_OK;
+}
+
+int sc_mesh_set_profiling(sc_mesh* m, int enabled) {
+    SC_TRY(check_mesh(m));
+    m->timer.enabled = enabled != 0;
+    return SC_OK;
+}
+
+int sc_mesh_stage_times(sc_mesh* m, double* ms, int64_t* calls, void* stream) {
+    SC_TRY(check_mesh(m));
+    DeviceGuard g(m->device);
+    SC_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    for (int k = 0; k < SC_NUM_STAGES; ++k) {
+        double tot = 0;
+        for (size_t i = 0; i < m->timer.used[k]; ++i) {
+            float t = 0;
+            SC_CUDA(cudaEventElapsedTime(&t, m->timer.ev[k][i].a, m->timer.ev[k][i].b));
+            tot += t;
+        }
+        if (ms) ms[k] = tot;
+        if (calls) calls[k] = (int64_t)m->timer.used[k];
+        m->timer.used[k] = 0;
+    }
+    return SC_OK;
+}
+
+int sc_mesh_launch_count(const sc_mesh* m, int64_t* count) {
+    SC_TRY(check_mesh(m));
+    if (count) *count = m->launches;
     return SC_OK;
 }
 
@@ -302,6 +362,7 @@ int sc_deposit(sc_mesh* m, const void* x, const void* y, const void* z, const vo
     if (mode != SC_DEPOSIT_ATOMIC && mode != SC_DEPOSIT_SORTED && mode != SC_DEPOSIT_DETERMINISTIC)
         return fail(SC_ERR_INVALID, "unknown deposit mode %d", mode);
     DeviceGuard g(m->device);
+    StageScope st(m->timer, SC_STAGE_DEPOSIT, (cudaStream_t)stream);
     if (clear) SC_TRY(sc_clear_mesh(m, stream));
     if (n == 0) return SC_OK;
     return deposit_launch(m, x, y, z, q, n, dtype, mode, (cudaStream_t)stream);
@@ -322,6 +383,7 @@ int sc_interpolate_field(sc_mesh* m, const void* x, const void* y, const void* z
     if (n == 0) return SC_OK;
     if (!x || !y || !z || !ex || !ey || !ez) return fail(SC_ERR_INVALID, "particle or output pointer is NULL");
     DeviceGuard g(m->device);
+    StageScope st(m->timer, SC_STAGE_GATHER, (cudaStream_t)stream);
     return gather_launch(m, x, y, z, n, dtype, ex, ey, ez, (cudaStream_t)stream);
 }
 
@@ -330,6 +392,20 @@ int sc_kick(sc_mesh* m, const void* x, const void* y, const void* z, const void*
     SC_TRY(sc_deposit(m, x, y, z, q, n, dtype, 1, SC_DEPOSIT_ATOMIC, stream));
     SC_TRY(sc_solve(m, at_cathode, stream));
     return sc_interpolate_field(m, x, y, z, n, dtype, ex, ey, ez, stream);
+}
+
+int sc_kick_adjoint(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
+                    int at_cathode, const void* gex, const void* gey, const void* gez, const void* ggrid, void* dx,
+                    void* dy, void* dz, void* dq, void* stream) {
+    SC_TRY(check_mesh(m));
+    SC_TRY(check_dtype(dtype));
+    if (n < 0) return fail(SC_ERR_INVALID, "negative particle count");
+    if (n > 0 && (!x || !y || !z || !q || !dx || !dy || !dz || !dq))
+        return fail(SC_ERR_INVALID, "particle or gradient pointer is NULL");
+    DeviceGuard g(m->device);
+    if (n == 0) return SC_OK;
+    return adjoint_launch(m, x, y, z, q, n, dtype, at_cathode, gex, gey, gez, ggrid, dx, dy, dz, dq,
+                          (cudaStream_t)stream);
 }
 
 int sc_cell_index(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n, int dtype, int32_t* idx,

@@ -3,10 +3,9 @@
 // deposit_plain: the reference's GPU kernel restated (one thread per
 //   particle, FP64 IEEE-division cell index, 8 FP64 atomics with the
 //   reference's weight products), plus a bounds check.
-// deposit_atomic: the hand-written pipelines.  Same cell index (bit-exact,
-//   see cells.cuh), weights in the mesh type, warp-aggregated atomics: lanes
-//   of a warp that fall in the same cell add their 8 corner charges with
-//   shuffles first, then one lane issues the 8 atomics.
+// deposit_atomic: the hand-written pipelines' unsorted deposit.  Same cell
+//   index (bit-exact, see cells.cuh), weights in the mesh type, several
+//   particles per thread with their loads in flight together, 8 atomics each.
 #include "cells.cuh"
 #include "sc_internal.cuh"
 
@@ -75,73 +74,55 @@ struct CellCalc<double> {
     __device__ __forceinline__ static double charge(P q) { return (double)q; }
 };
 
+// Particles per thread of the atomic deposit: all their loads are issued
+// before any arithmetic, so each thread keeps several requests in flight.
+constexpr int kDepPerThread = 4;
+
 template <typename P, typename A>
 __global__ void __launch_bounds__(256) deposit_atomic(const P* __restrict__ px, const P* __restrict__ py,
                                                       const P* __restrict__ pz, const P* __restrict__ pq,
                                                       int64_t n, Axes ax, A* __restrict__ rho,
                                                       unsigned long long* __restrict__ oob) {
-    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const unsigned full = 0xffffffffu;
-    const unsigned active = __ballot_sync(full, p < n);
-    if (p >= n) return;
-    int ix = 0, iy = 0, iz = 0;
-    A fx = 0, fy = 0, fz = 0;
-    const bool ok = CellCalc<A>::run(px[p], ax.a[0], ix, fx) & CellCalc<A>::run(py[p], ax.a[1], iy, fy) &
-                    CellCalc<A>::run(pz[p], ax.a[2], iz, fz);
+    const int64_t base = (int64_t)blockIdx.x * (blockDim.x * kDepPerThread) + threadIdx.x;
+    P x[kDepPerThread], y[kDepPerThread], z[kDepPerThread], qq[kDepPerThread];
+#pragma unroll
+    for (int k = 0; k < kDepPerThread; ++k) {
+        const int64_t p = base + (int64_t)k * blockDim.x;
+        const bool in = p < n;
+        x[k] = in ? __ldg(px + p) : P(0);
+        y[k] = in ? __ldg(py + p) : P(0);
+        z[k] = in ? __ldg(pz + p) : P(0);
+        qq[k] = in ? __ldg(pq + p) : P(0);
+    }
     const int nx = ax.a[0].n, ny = ax.a[1].n;
-    // key of the lower corner node; -1 for skipped particles
-    const long long key = ok ? (long long)ix + (long long)nx * (iy + (long long)ny * iz) : -1ll;
-    const unsigned okmask = __ballot_sync(active, ok);
-    if (!ok) {
-        if ((threadIdx.x & 31) == __ffs(active & ~okmask) - 1) atomicAdd(oob, (unsigned long long)__popc(active & ~okmask));
-        return;
-    }
-    const A q = CellCalc<A>::charge(pq[p]);
-    const A wx0 = A(1) - fx, wy0 = A(1) - fy, wz0 = A(1) - fz;
-    A c[8];
-    c[0] = q * wx0 * wy0 * wz0;
-    c[1] = q * fx * wy0 * wz0;
-    c[2] = q * wx0 * fy * wz0;
-    c[3] = q * fx * fy * wz0;
-    c[4] = q * wx0 * wy0 * fz;
-    c[5] = q * fx * wy0 * fz;
-    c[6] = q * wx0 * fy * fz;
-    c[7] = q * fx * fy * fz;
-    // Warp aggregation: lanes with the same cell reduce before the atomics.
-    const unsigned peers = __match_any_sync(okmask, key);
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(peers) - 1;
-    if (__popc(peers) > 1) {
-        // sum over the peer group with a lane-ordered scan of the group
-        unsigned rest = peers & ~(1u << leader);
-        // each peer sends its contributions to the leader by a rotating shuffle
-        // over the group members (group sizes are small in practice)
-        A acc[8];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) acc[k] = c[k];
-        while (rest) {
-            const int src = __ffs(rest) - 1;
-            rest &= rest - 1;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const A v = __shfl_sync(peers, c[k], src);
-                if (lane == leader) acc[k] += v;
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < 8; ++k) c[k] = acc[k];
-    }
-    if (lane != leader) return;
     const int64_t sy = nx, sz = (int64_t)nx * ny;
-    A* r = rho + key;
-    atomicAdd(r, c[0]);
-    atomicAdd(r + 1, c[1]);
-    atomicAdd(r + sy, c[2]);
-    atomicAdd(r + 1 + sy, c[3]);
-    atomicAdd(r + sz, c[4]);
-    atomicAdd(r + 1 + sz, c[5]);
-    atomicAdd(r + sy + sz, c[6]);
-    atomicAdd(r + 1 + sy + sz, c[7]);
+    unsigned skipped = 0;
+#pragma unroll
+    for (int k = 0; k < kDepPerThread; ++k) {
+        const int64_t p = base + (int64_t)k * blockDim.x;
+        if (p >= n) break;
+        int ix = 0, iy = 0, iz = 0;
+        A fx = 0, fy = 0, fz = 0;
+        const bool ok = CellCalc<A>::run(x[k], ax.a[0], ix, fx) & CellCalc<A>::run(y[k], ax.a[1], iy, fy) &
+                        CellCalc<A>::run(z[k], ax.a[2], iz, fz);
+        if (!ok) {
+            ++skipped;
+            continue;
+        }
+        const A q = CellCalc<A>::charge(qq[k]);
+        const A wx0 = A(1) - fx, wy0 = A(1) - fy, wz0 = A(1) - fz;
+        A* r = rho + (ix + sy * iy + sz * iz);
+        // deposition.jl:67-74 corner order and products
+        atomicAdd(r, q * wx0 * wy0 * wz0);
+        atomicAdd(r + 1, q * fx * wy0 * wz0);
+        atomicAdd(r + sy, q * wx0 * fy * wz0);
+        atomicAdd(r + 1 + sy, q * fx * fy * wz0);
+        atomicAdd(r + sz, q * wx0 * wy0 * fz);
+        atomicAdd(r + 1 + sz, q * fx * wy0 * fz);
+        atomicAdd(r + sy + sz, q * wx0 * fy * fz);
+        atomicAdd(r + 1 + sy + sz, q * fx * fy * fz);
+    }
+    if (skipped) atomicAdd(oob, (unsigned long long)skipped);
 }
 
 // sc_cell_index: bins with the same arithmetic the mesh's deposit uses.
@@ -211,28 +192,31 @@ int deposit_launch(sc_mesh* m, const void* x, const void* y, const void* z, cons
             deposit_plain<float><<<blocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z,
                                                        (const float*)q, n, ax, (double*)m->rho, m->oob);
         SC_LAUNCH_CHECK("deposit_plain");
+        m->launches += 1;
         return SC_OK;
     }
     if (mode != SC_DEPOSIT_ATOMIC) return deposit_sorted_launch(m, x, y, z, q, n, dtype, mode, s);
+    const int64_t ablocks = (n + 256 * kDepPerThread - 1) / (256 * kDepPerThread);
     if (m->precision == SC_PREC_MIXED) {
         if (dtype == SC_F64)
-            deposit_atomic<double, float><<<blocks, 256, 0, s>>>((const double*)x, (const double*)y,
+            deposit_atomic<double, float><<<ablocks, 256, 0, s>>>((const double*)x, (const double*)y,
                                                                 (const double*)z, (const double*)q, n, ax,
                                                                 (float*)m->rho, m->oob);
         else
-            deposit_atomic<float, float><<<blocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z,
+            deposit_atomic<float, float><<<ablocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z,
                                                                (const float*)q, n, ax, (float*)m->rho, m->oob);
     } else {
         if (dtype == SC_F64)
-            deposit_atomic<double, double><<<blocks, 256, 0, s>>>((const double*)x, (const double*)y,
+            deposit_atomic<double, double><<<ablocks, 256, 0, s>>>((const double*)x, (const double*)y,
                                                                  (const double*)z, (const double*)q, n, ax,
                                                                  (double*)m->rho, m->oob);
         else
-            deposit_atomic<float, double><<<blocks, 256, 0, s>>>((const float*)x, (const float*)y,
+            deposit_atomic<float, double><<<ablocks, 256, 0, s>>>((const float*)x, (const float*)y,
                                                                 (const float*)z, (const float*)q, n, ax,
                                                                 (double*)m->rho, m->oob);
     }
     SC_LAUNCH_CHECK("deposit_atomic");
+    m->launches += 1;
     return SC_OK;
 }
 

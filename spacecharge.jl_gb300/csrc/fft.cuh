@@ -1,8 +1,8 @@
 // Shared-memory batched FFT building blocks for the hand-written pruned
 // convolution.  A CTA holds `ncol` columns of a power-of-two length L in
 // shared memory, element (j, col) at [j * ncol + col], and transforms all of
-// them with Stockham autosort stages (radix 4, plus one radix-2 stage when
-// log2 L is odd) ping-ponging between two buffers.  Twiddles come from a
+// them with Stockham autosort stages (radix 16 butterflies in registers, one
+// radix 2/4/8 stage for the remainder) ping-ponging between two buffers.  Twiddles come from a
 // per-device table of exp(-2 pi i k / kMaxL) rounded once from FP64, so the
 // FP32 transform uses correctly rounded roots of unity.
 #pragma once
@@ -65,20 +65,98 @@ __device__ __forceinline__ T2 rot(T2 d) {
     return r;
 }
 
+// Twiddles of the in-register butterflies: cos/sin(2 pi k / 16), k < 8.
+__host__ __device__ constexpr double c16(int k) {
+    return k == 0 ? 1.0
+         : k == 1 ? 0.92387953251128675613
+         : k == 2 ? 0.70710678118654752440
+         : k == 3 ? 0.38268343236508977173
+         : k == 4 ? 0.0
+         : k == 5 ? -0.38268343236508977173
+         : k == 6 ? -0.70710678118654752440
+                  : -0.92387953251128675613;
+}
+// sin(2 pi k / 16) = cos(2 pi (k - 4) / 16)
+__host__ __device__ constexpr double s16(int k) { return k == 0 ? 0.0 : c16(k <= 4 ? 4 - k : k - 4); }
+
+// v * exp(-+2 pi i k / R) for a compile-time R in {2, 4, 8, 16} and k < R/2
+template <int R, int K, bool INV, typename T2>
+__device__ __forceinline__ T2 twc(T2 v) {
+    constexpr int k16 = K * (16 / R);  // same angle on the 16-point circle
+    if (k16 == 0) return v;
+    if (k16 == 4) return rot<INV>(v);  // -+i
+    using T = decltype(v.x);
+    constexpr double cd = c16(k16), sd = s16(k16);
+    const T c = (T)cd, s = INV ? (T)sd : -(T)sd;
+    T2 r;
+    r.x = v.x * c - v.y * s;
+    r.y = v.x * s + v.y * c;
+    return r;
+}
+
+template <bool INV, typename T2>
+__device__ __forceinline__ void dft2(T2& a, T2& b) {
+    const T2 t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+template <bool INV, typename T2>
+__device__ __forceinline__ void dft4(T2& v0, T2& v1, T2& v2, T2& v3) {
+    const T2 a0 = cadd(v0, v2), a1 = csub(v0, v2);
+    const T2 a2 = cadd(v1, v3), a3 = rot<INV>(csub(v1, v3));
+    v0 = cadd(a0, a2);
+    v2 = csub(a0, a2);
+    v1 = cadd(a1, a3);
+    v3 = csub(a1, a3);
+}
+template <bool INV, typename T2>
+__device__ __forceinline__ void dft8(T2* v) {
+    T2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+    T2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+    dft4<INV>(e0, e1, e2, e3);
+    dft4<INV>(o0, o1, o2, o3);
+    o1 = twc<8, 1, INV>(o1);
+    o2 = twc<8, 2, INV>(o2);
+    o3 = twc<8, 3, INV>(o3);
+    v[0] = cadd(e0, o0);
+    v[4] = csub(e0, o0);
+    v[1] = cadd(e1, o1);
+    v[5] = csub(e1, o1);
+    v[2] = cadd(e2, o2);
+    v[6] = csub(e2, o2);
+    v[3] = cadd(e3, o3);
+    v[7] = csub(e3, o3);
+}
+template <bool INV, typename T2>
+__device__ __forceinline__ void dft16(T2* v) {
+    T2 e[8], o[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        e[k] = v[2 * k];
+        o[k] = v[2 * k + 1];
+    }
+    dft8<INV>(e);
+    dft8<INV>(o);
+    o[1] = twc<16, 1, INV>(o[1]);
+    o[2] = twc<16, 2, INV>(o[2]);
+    o[3] = twc<16, 3, INV>(o[3]);
+    o[4] = twc<16, 4, INV>(o[4]);
+    o[5] = twc<16, 5, INV>(o[5]);
+    o[6] = twc<16, 6, INV>(o[6]);
+    o[7] = twc<16, 7, INV>(o[7]);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        v[k] = cadd(e[k], o[k]);
+        v[k + 8] = csub(e[k], o[k]);
+    }
+}
+
 template <int R, bool INV, typename T2>
 __device__ __forceinline__ void dft(T2* v) {
-    if (R == 2) {
-        const T2 a = v[0];
-        v[0] = cadd(a, v[1]);
-        v[1] = csub(a, v[1]);
-    } else {  // R == 4
-        const T2 a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
-        const T2 a2 = cadd(v[1], v[3]), a3 = rot<INV>(csub(v[1], v[3]));
-        v[0] = cadd(a0, a2);
-        v[2] = csub(a0, a2);
-        v[1] = cadd(a1, a3);
-        v[3] = csub(a1, a3);
-    }
+    if (R == 2) dft2<INV>(v[0], v[1]);
+    if (R == 4) dft4<INV>(v[0], v[1], v[2], v[3]);
+    if (R == 8) dft8<INV>(v);
+    if (R == 16) dft16<INV>(v);
 }
 
 // One Stockham stage: for every column and j in [0, L/R), read the R
@@ -86,13 +164,14 @@ __device__ __forceinline__ void dft(T2* v) {
 // do an R-point DFT and write them to (j/Ns) Ns R + (j mod Ns) + r Ns.
 template <int R, bool INV, typename T2>
 __device__ __forceinline__ void stockham_stage(const T2* __restrict__ in, T2* __restrict__ out, int L, int Ns,
-                                               int ncol, const T2* __restrict__ tw) {
+                                               int lgc, const T2* __restrict__ tw) {
+    const int ncol = 1 << lgc;
     const int m = L / R;
-    const int items = m * ncol;
+    const int items = m << lgc;
     const int tstep = kMaxL / (Ns * R);
     for (int it = threadIdx.x; it < items; it += blockDim.x) {
-        const int j = it / ncol;
-        const int col = it - j * ncol;
+        const int j = it >> lgc;
+        const int col = it & (ncol - 1);
         const int jm = j & (Ns - 1);
         T2 v[R];
 #pragma unroll
@@ -111,25 +190,29 @@ __device__ __forceinline__ void stockham_stage(const T2* __restrict__ in, T2* __
     }
 }
 
-// Transforms the ncol columns held in `a` (the caller has synchronised after
+// Transforms the 2^lgc columns held in `a` (the caller has synchronised after
 // filling it); returns the buffer holding the result, synchronised.  The
-// inverse is unnormalised.
+// inverse is unnormalised.  Radix-16 stages, with one smaller first stage
+// (no twiddles) when log2 L is not a multiple of 4.
 template <bool INV, typename T2>
-__device__ __forceinline__ T2* smem_fft(T2* a, T2* b, int L, int logL, int ncol, const T2* __restrict__ tw) {
+__device__ __forceinline__ T2* smem_fft(T2* a, T2* b, int L, int logL, int lgc, const T2* __restrict__ tw) {
     T2* in = a;
     T2* out = b;
     int Ns = 1;
-    if (logL & 1) {
-        stockham_stage<2, INV>(in, out, L, Ns, ncol, tw);
-        Ns = 2;
+    const int rem = logL & 3;
+    if (rem) {
+        if (rem == 1) stockham_stage<2, INV>(in, out, L, Ns, lgc, tw);
+        if (rem == 2) stockham_stage<4, INV>(in, out, L, Ns, lgc, tw);
+        if (rem == 3) stockham_stage<8, INV>(in, out, L, Ns, lgc, tw);
+        Ns = 1 << rem;
         T2* t = in;
         in = out;
         out = t;
         __syncthreads();
     }
     while (Ns < L) {
-        stockham_stage<4, INV>(in, out, L, Ns, ncol, tw);
-        Ns *= 4;
+        stockham_stage<16, INV>(in, out, L, Ns, lgc, tw);
+        Ns *= 16;
         T2* t = in;
         in = out;
         out = t;

@@ -110,43 +110,75 @@ struct GCell<double> {
     }
 };
 
+// Particles per thread of the packed gather: positions of all of them are
+// loaded first, then all their 8 node loads are issued before the sums.
+constexpr int kGathPerThread = 2;
+
 template <typename P, typename A>
 __global__ void __launch_bounds__(256) gather_packed(const P* __restrict__ px, const P* __restrict__ py,
                                                      const P* __restrict__ pz, int64_t n, Axes ax,
                                                      const typename Packed<A>::V* __restrict__ ef,
                                                      P* __restrict__ ex, P* __restrict__ ey, P* __restrict__ ez,
                                                      unsigned long long* __restrict__ oob) {
-    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (p >= n) return;
-    int ix, iy, iz;
-    A dx, dy, dz;
-    const bool ok = GCell<A>::run(px[p], ax.a[0], ix, dx) & GCell<A>::run(py[p], ax.a[1], iy, dy) &
-                    GCell<A>::run(pz[p], ax.a[2], iz, dz);
-    if (!ok) {
-        atomicAdd(oob, 1ull);
-        ex[p] = P(0);
-        ey[p] = P(0);
-        ez[p] = P(0);
-        return;
+    using V = typename Packed<A>::V;
+    const int64_t base = (int64_t)blockIdx.x * (blockDim.x * kGathPerThread) + threadIdx.x;
+    P x[kGathPerThread], y[kGathPerThread], z[kGathPerThread];
+#pragma unroll
+    for (int k = 0; k < kGathPerThread; ++k) {
+        const int64_t p = base + (int64_t)k * blockDim.x;
+        const bool in = p < n;
+        x[k] = in ? __ldg(px + p) : P(0);
+        y[k] = in ? __ldg(py + p) : P(0);
+        z[k] = in ? __ldg(pz + p) : P(0);
     }
     const int nx = ax.a[0].n, ny = ax.a[1].n;
     const int64_t sy = nx, sz = (int64_t)nx * ny;
-    const typename Packed<A>::V* e = ef + (ix + sy * iy + sz * iz);
-    const A ux = A(1) - dx, uy = A(1) - dy, uz = A(1) - dz;
-    const A w[8] = {ux * uy * uz, dx * uy * uz, ux * dy * uz, dx * dy * uz,
-                    ux * uy * dz, dx * uy * dz, ux * dy * dz, dx * dy * dz};
     const int64_t off[8] = {0, 1, sy, 1 + sy, sz, 1 + sz, sy + sz, 1 + sy + sz};
-    A sx = 0, sy_ = 0, sz_ = 0;
+    A w[kGathPerThread][8];
+    V v[kGathPerThread][8];
+    bool ok[kGathPerThread];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const typename Packed<A>::V v = ldg4(e + off[k]);
-        sx += v.x * w[k];
-        sy_ += v.y * w[k];
-        sz_ += v.z * w[k];
+    for (int k = 0; k < kGathPerThread; ++k) {
+        const int64_t p = base + (int64_t)k * blockDim.x;
+        int ix = 0, iy = 0, iz = 0;
+        A dx = 0, dy = 0, dz = 0;
+        ok[k] = p < n && (GCell<A>::run(x[k], ax.a[0], ix, dx) & GCell<A>::run(y[k], ax.a[1], iy, dy) &
+                          GCell<A>::run(z[k], ax.a[2], iz, dz));
+        const A ux = A(1) - dx, uy = A(1) - dy, uz = A(1) - dz;
+        // interpolation.jl:46-53
+        w[k][0] = ux * uy * uz;
+        w[k][1] = dx * uy * uz;
+        w[k][2] = ux * dy * uz;
+        w[k][3] = dx * dy * uz;
+        w[k][4] = ux * uy * dz;
+        w[k][5] = dx * uy * dz;
+        w[k][6] = ux * dy * dz;
+        w[k][7] = dx * dy * dz;
+        const V* e = ef + (ok[k] ? (ix + sy * iy + sz * iz) : 0);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) v[k][c] = ok[k] ? ldg4(e + off[c]) : V{};
     }
-    ex[p] = to_out<P, A>(sx);
-    ey[p] = to_out<P, A>(sy_);
-    ez[p] = to_out<P, A>(sz_);
+    unsigned skipped = 0;
+#pragma unroll
+    for (int k = 0; k < kGathPerThread; ++k) {
+        const int64_t p = base + (int64_t)k * blockDim.x;
+        if (p >= n) break;
+        A sx = 0, sy_ = 0, sz_ = 0;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            sx += v[k][c].x * w[k][c];
+            sy_ += v[k][c].y * w[k][c];
+            sz_ += v[k][c].z * w[k][c];
+        }
+        if (!ok[k]) {
+            ++skipped;
+            sx = sy_ = sz_ = A(0);
+        }
+        ex[p] = to_out<P, A>(sx);
+        ey[p] = to_out<P, A>(sy_);
+        ez[p] = to_out<P, A>(sz_);
+    }
+    if (skipped) atomicAdd(oob, (unsigned long long)skipped);
 }
 
 int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n, int dtype, void* ex,
@@ -163,28 +195,31 @@ int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64
                                                       (const double*)m->efield, (float*)ex, (float*)ey, (float*)ez,
                                                       m->oob);
         SC_LAUNCH_CHECK("gather_plain");
+        m->launches += 1;
         return SC_OK;
     }
+    const int64_t gblocks = (n + 256 * kGathPerThread - 1) / (256 * kGathPerThread);
     if (m->precision == SC_PREC_MIXED) {
         if (dtype == SC_F64)
-            gather_packed<double, float><<<blocks, 256, 0, s>>>((const double*)x, (const double*)y,
+            gather_packed<double, float><<<gblocks, 256, 0, s>>>((const double*)x, (const double*)y,
                                                                (const double*)z, n, ax, (const float4*)m->efield,
                                                                (double*)ex, (double*)ey, (double*)ez, m->oob);
         else
-            gather_packed<float, float><<<blocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z, n,
+            gather_packed<float, float><<<gblocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z, n,
                                                               ax, (const float4*)m->efield, (float*)ex, (float*)ey,
                                                               (float*)ez, m->oob);
     } else {
         if (dtype == SC_F64)
-            gather_packed<double, double><<<blocks, 256, 0, s>>>((const double*)x, (const double*)y,
+            gather_packed<double, double><<<gblocks, 256, 0, s>>>((const double*)x, (const double*)y,
                                                                 (const double*)z, n, ax, (const dnode4*)m->efield,
                                                                 (double*)ex, (double*)ey, (double*)ez, m->oob);
         else
-            gather_packed<float, double><<<blocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z,
+            gather_packed<float, double><<<gblocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z,
                                                                n, ax, (const dnode4*)m->efield, (float*)ex,
                                                                (float*)ey, (float*)ez, m->oob);
     }
     SC_LAUNCH_CHECK("gather_packed");
+    m->launches += 1;
     return SC_OK;
 }
 

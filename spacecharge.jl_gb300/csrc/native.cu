@@ -26,163 +26,74 @@
 // into it, so the inverse passes produce E directly.
 #include <math.h>
 
-#include "fft.cuh"
-#include "sc_internal.cuh"
+#include "pipeline.cuh"
 
 namespace sc {
-
-// green_functions.jl:35-38 (same expression as the plain path)
-__device__ __forceinline__ double field_green_n(double x, double y, double z) {
-    const double r = sqrt(x * x + y * y + z * z);
-    return x * atan((y * z) / (r * x)) - z * log(r + y) + y * log((r - z) / (r + z)) / 2;
-}
-
-static int ilog2(int v) {
-    int l = 0;
-    while ((1 << l) < v) ++l;
-    return l;
-}
-
-// ------------------------------------------------------------ pass kernels
-template <typename T>
-__global__ void __launch_bounds__(256) k_fwd_x(const T* __restrict__ rho, typename Cplx<T>::T2* __restrict__ A,
-                                               int nx, int rows, int Lx, int logLx, int Hx, int P,
-                                               const typename Cplx<T>::T2* __restrict__ tw) {
-    using T2 = typename Cplx<T>::T2;
-    extern __shared__ __align__(16) unsigned char smraw[];
-    T2* a = reinterpret_cast<T2*>(smraw);
-    T2* b = a + P * Lx;
-    const int pair0 = blockIdx.x * P;
-    for (int it = threadIdx.x; it < P * Lx; it += blockDim.x) {
-        const int p = it / Lx, x = it - p * Lx;
-        const int r0 = 2 * (pair0 + p), r1 = r0 + 1;
-        T re = 0, im = 0;
-        if (x < nx) {
-            if (r0 < rows) re = rho[(int64_t)r0 * nx + x];
-            if (r1 < rows) im = rho[(int64_t)r1 * nx + x];
-        }
-        a[x * P + p] = Cplx<T>::make(re, im);
-    }
-    __syncthreads();
-    const T2* res = smem_fft<false>(a, b, Lx, logLx, P, tw);
-    for (int it = threadIdx.x; it < P * Hx; it += blockDim.x) {
-        const int p = it / Hx, k = it - p * Hx;
-        const int r0 = 2 * (pair0 + p), r1 = r0 + 1;
-        if (r0 >= rows) continue;
-        const T2 Z = res[k * P + p];
-        const T2 Y = res[((Lx - k) & (Lx - 1)) * P + p];
-        // Xa = (Z + conj Y)/2, Xb = (Z - conj Y)/(2i)
-        A[(int64_t)r0 * Hx + k] = Cplx<T>::make(T(0.5) * (Z.x + Y.x), T(0.5) * (Z.y - Y.y));
-        if (r1 < rows) A[(int64_t)r1 * Hx + k] = Cplx<T>::make(T(0.5) * (Z.y + Y.y), T(0.5) * (Y.x - Z.x));
-    }
-}
-
-// Batched column FFT along a strided axis: element (col, j, batch, comp) of
-// the input at in[col + j*as_in + batch*bs_in + comp*cs_in]; the first
-// n_valid elements are read (the rest are zero), the first n_store written.
-template <bool INV, typename T>
-__global__ void __launch_bounds__(256) k_col_fft(const typename Cplx<T>::T2* __restrict__ in,
-                                                 typename Cplx<T>::T2* __restrict__ out, int ncols, int W, int L,
-                                                 int logL, int n_valid, int n_store, int64_t as_in, int64_t bs_in,
-                                                 int64_t cs_in, int64_t as_out, int64_t bs_out, int64_t cs_out,
-                                                 const typename Cplx<T>::T2* __restrict__ tw) {
-    using T2 = typename Cplx<T>::T2;
-    extern __shared__ __align__(16) unsigned char smraw[];
-    T2* a = reinterpret_cast<T2*>(smraw);
-    T2* b = a + W * L;
-    const int c0 = blockIdx.x * W;
-    const int64_t ib = blockIdx.y * bs_in + blockIdx.z * cs_in;
-    const int64_t ob = blockIdx.y * bs_out + blockIdx.z * cs_out;
-    for (int it = threadIdx.x; it < W * L; it += blockDim.x) {
-        const int j = it / W, w = it - j * W;
-        const int col = c0 + w;
-        T2 v = Cplx<T>::make(0, 0);
-        if (j < n_valid && col < ncols) v = in[ib + col + j * as_in];
-        a[it] = v;
-    }
-    __syncthreads();
-    const T2* res = smem_fft<INV>(a, b, L, logL, W, tw);
-    for (int it = threadIdx.x; it < W * n_store; it += blockDim.x) {
-        const int j = it / W, w = it - j * W;
-        const int col = c0 + w;
-        if (col < ncols) out[ob + col + j * as_out] = res[it];
-    }
-}
-
-// Green-spectrum lookup.  Free space: s[c] = Im(K^_c) at folded (kx, ky, kz),
-// purely imaginary, odd in the component's own axis.  Image: complex g[c] at
-// folded (kx, ky) and all kz, odd in y for c = 1, with the flip phase of the
-// reversed charge folded in.
-struct GreenView {
-    const void* gfree;
-    const void* gimg;
-    int Hx, Hy, Hz, Ly, Lz;
-    int64_t cs_free, cs_img;
-    int image;
-};
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_zpass(const typename Cplx<T>::T2* __restrict__ B,
                                                typename Cplx<T>::T2* __restrict__ C, int Hx, int Ly, int nz, int Lz,
-                                               int logLz, int W, GreenView gv,
+                                               int logLz, int lgW, GreenView gv,
                                                const typename Cplx<T>::T2* __restrict__ tw) {
     using T2 = typename Cplx<T>::T2;
     extern __shared__ __align__(16) unsigned char smraw[];
+    const int W = 1 << lgW;
+    const int n = W << logLz;
     T2* spec = reinterpret_cast<T2*>(smraw);
-    T2* a = spec + W * Lz;
-    T2* b = a + W * Lz;
-    const int kx0 = blockIdx.x * W;
+    T2* a = spec + n;
+    T2* b = a + n;
+    const int kx0 = blockIdx.x << lgW;
     const int ky = blockIdx.y;
     const int64_t plane = (int64_t)Hx * Ly;
-    for (int it = threadIdx.x; it < W * Lz; it += blockDim.x) {
-        const int z = it / W, w = it - z * W;
-        const int kx = kx0 + w;
+    // forward z FFT: put the input where the result lands in `spec`
+    const int stages = ((logLz & 3) ? 1 : 0) + (logLz >> 2);
+    T2* first = (stages & 1) ? a : spec;
+    T2* second = (stages & 1) ? spec : a;
+    for (int it = threadIdx.x; it < n; it += blockDim.x) {
+        const int z = it >> lgW, kx = kx0 + (it & (W - 1));
         T2 v = Cplx<T>::make(0, 0);
         if (z < nz && kx < Hx) v = B[kx + (int64_t)Hx * ky + plane * z];
-        spec[it] = v;
+        first[it] = v;
     }
     __syncthreads();
-    const T2* s = smem_fft<false>(spec, a, Lz, logLz, W, tw);
-    if (s != spec) {
-        // keep the spectrum in `spec`, free a and b for the inverse transforms
-        for (int it = threadIdx.x; it < W * Lz; it += blockDim.x) spec[it] = s[it];
-        __syncthreads();
-    }
+    smem_fft<false>(first, second, Lz, logLz, lgW, tw);  // result in spec
     const int kyf = ky <= Ly / 2 ? ky : Ly - ky;
     const T ysign = ky <= Ly / 2 ? T(1) : T(-1);
     const T* gf = reinterpret_cast<const T*>(gv.gfree);
     const T2* gi = reinterpret_cast<const T2*>(gv.gimg);
+    const int halfz = Lz >> 1;
     for (int comp = 0; comp < 3; ++comp) {
-        for (int it = threadIdx.x; it < W * Lz; it += blockDim.x) {
-            const int kz = it / W, w = it - kz * W;
+        const T* gfc = gf + comp * gv.cs_free + (int64_t)gv.Hx * kyf;
+        const T2* gic = gi + comp * gv.cs_img + (int64_t)gv.Hx * kyf;
+        for (int it = threadIdx.x; it < n; it += blockDim.x) {
+            const int kz = it >> lgW, w = it & (W - 1);
             const int kx = kx0 + w;
             T2 r = Cplx<T>::make(0, 0);
             if (kx < Hx) {
-                const int kzf = kz <= Lz / 2 ? kz : Lz - kz;
+                const int kzf = kz <= halfz ? kz : Lz - kz;
                 T sg = T(1);
                 if (comp == 1) sg = ysign;
-                if (comp == 2 && kz > Lz / 2) sg = T(-1);
-                const T g = sg * gf[comp * gv.cs_free + kx + (int64_t)gv.Hx * (kyf + (int64_t)gv.Hy * kzf)];
+                if (comp == 2 && kz > halfz) sg = T(-1);
+                const T g = sg * gfc[kx + (int64_t)gv.Hx * gv.Hy * kzf];
                 const T2 p = spec[it];
                 r = Cplx<T>::make(-p.y * g, p.x * g);  // p * (i g)
                 if (gv.image) {
-                    T2 gc = gi[comp * gv.cs_img + kx + (int64_t)gv.Hx * (kyf + (int64_t)gv.Hy * kz)];
+                    T2 gc = gic[kx + (int64_t)gv.Hx * gv.Hy * kz];
                     if (comp == 1) {
                         gc.x *= ysign;
                         gc.y *= ysign;
                     }
-                    const T2 pf = spec[((Lz - kz) & (Lz - 1)) * W + w];  // rho^(kx, ky, -kz)
+                    const T2 pf = spec[(((Lz - kz) & (Lz - 1)) << lgW) + w];  // rho^(kx, ky, -kz)
                     r = cadd(r, cmul(pf, gc));
                 }
             }
             a[it] = r;
         }
         __syncthreads();
-        const T2* res = smem_fft<true>(a, b, Lz, logLz, W, tw);
+        const T2* res = smem_fft<true>(a, b, Lz, logLz, lgW, tw);
         T2* Cc = C + comp * (plane * nz);
-        for (int it = threadIdx.x; it < W * nz; it += blockDim.x) {
-            const int z = it / W, w = it - z * W;
-            const int kx = kx0 + w;
+        for (int it = threadIdx.x; it < (nz << lgW); it += blockDim.x) {
+            const int z = it >> lgW, kx = kx0 + (it & (W - 1));
             if (kx < Hx) Cc[kx + (int64_t)Hx * ky + plane * z] = res[it];
         }
         __syncthreads();
@@ -190,50 +101,26 @@ __global__ void __launch_bounds__(256) k_zpass(const typename Cplx<T>::T2* __res
 }
 
 template <typename T>
-struct Vec4;
-template <>
-struct Vec4<float> {
-    using V = float4;
-    __device__ __forceinline__ static float4 make(float a, float b, float c) { return make_float4(a, b, c, 0.f); }
-};
-template <>
-struct Vec4<double> {
-    using V = dnode4;
-    __device__ __forceinline__ static dnode4 make(double a, double b, double c) {
-        return dnode4{a, b, c, 0.0};
-    }
-};
-
-template <typename T>
-__device__ __forceinline__ void st4(typename Vec4<T>::V* p, typename Vec4<T>::V v) {
-    *p = v;
-}
-template <>
-__device__ __forceinline__ void st4<double>(dnode4* p, dnode4 v) {
-    double2* q = reinterpret_cast<double2*>(p);
-    q[0] = make_double2(v.x, v.y);
-    q[1] = make_double2(v.z, v.w);
-}
-
-template <typename T>
 __global__ void __launch_bounds__(256) k_inv_x(const typename Cplx<T>::T2* __restrict__ D,
                                                typename Vec4<T>::V* __restrict__ E, int nx, int rows, int Lx,
-                                               int logLx, int Hx, int P, int64_t cs,
+                                               int logLx, int Hx, int lgP, int64_t cs,
                                                const typename Cplx<T>::T2* __restrict__ tw) {
     using T2 = typename Cplx<T>::T2;
     extern __shared__ __align__(16) unsigned char smraw[];
+    const int P = 1 << lgP;
+    const int n = P << logLx;
     T2* a = reinterpret_cast<T2*>(smraw);
-    T2* b = a + P * Lx;
-    T2* keep = b + P * Lx;  // [comp][p][x] for x < nx
-    const int pair0 = blockIdx.x * P;
+    T2* b = a + n;
+    T2* keep = b + n;  // [comp][p][x], x < Lx
+    const int pair0 = blockIdx.x << lgP;
     for (int comp = 0; comp < 3; ++comp) {
         const T2* Dc = D + comp * cs;
-        for (int it = threadIdx.x; it < P * Lx; it += blockDim.x) {
-            const int p = it / Lx, k = it - p * Lx;
+        for (int it = threadIdx.x; it < n; it += blockDim.x) {
+            const int p = it >> logLx, k = it & (Lx - 1);
             const int r0 = 2 * (pair0 + p), r1 = r0 + 1;
             T2 xa = Cplx<T>::make(0, 0), xb = Cplx<T>::make(0, 0);
-            const int kk = k < Hx ? k : Lx - k;
             const bool cj = k >= Hx;
+            const int kk = cj ? Lx - k : k;
             if (r0 < rows) xa = Dc[(int64_t)r0 * Hx + kk];
             if (r1 < rows) xb = Dc[(int64_t)r1 * Hx + kk];
             if (cj) {
@@ -241,24 +128,25 @@ __global__ void __launch_bounds__(256) k_inv_x(const typename Cplx<T>::T2* __res
                 xb.y = -xb.y;
             }
             // Z = Xa + i Xb
-            a[k * P + p] = Cplx<T>::make(xa.x - xb.y, xa.y + xb.x);
+            a[(k << lgP) + p] = Cplx<T>::make(xa.x - xb.y, xa.y + xb.x);
         }
         __syncthreads();
-        const T2* res = smem_fft<true>(a, b, Lx, logLx, P, tw);
-        for (int it = threadIdx.x; it < P * nx; it += blockDim.x) {
-            const int p = it / nx, x = it - p * nx;
-            keep[(comp * P + p) * nx + x] = res[x * P + p];
+        const T2* res = smem_fft<true>(a, b, Lx, logLx, lgP, tw);
+        for (int it = threadIdx.x; it < n; it += blockDim.x) {
+            const int p = it >> logLx, x = it & (Lx - 1);
+            if (x < nx) keep[comp * n + it] = res[(x << lgP) + p];
         }
         __syncthreads();
     }
-    for (int it = threadIdx.x; it < 2 * P * nx; it += blockDim.x) {
-        const int rp = it / nx, x = it - rp * nx;
+    for (int it = threadIdx.x; it < 2 * n; it += blockDim.x) {
+        const int rp = it >> logLx, x = it & (Lx - 1);
+        if (x >= nx) continue;
         const int p = rp >> 1, half = rp & 1;
         const int row = 2 * (pair0 + p) + half;
         if (row >= rows) continue;
-        const T2 ex = keep[(0 * P + p) * nx + x], ey = keep[(1 * P + p) * nx + x], ez = keep[(2 * P + p) * nx + x];
-        const typename Vec4<T>::V v =
-            half ? Vec4<T>::make(ex.y, ey.y, ez.y) : Vec4<T>::make(ex.x, ey.x, ez.x);
+        const int o = (p << logLx) + x;
+        const T2 ex = keep[o], ey = keep[n + o], ez = keep[2 * n + o];
+        const typename Vec4<T>::V v = half ? Vec4<T>::make(ex.y, ey.y, ez.y) : Vec4<T>::make(ex.x, ey.x, ez.x);
         st4<T>(E + (int64_t)row * nx + x, v);
     }
 }
@@ -362,80 +250,243 @@ __global__ void __launch_bounds__(256) k_green_compress(const typename Cplx<T>::
     }
 }
 
-// ------------------------------------------------------------- launching
-static int pick_rows(int L) {
-    int P = 2048 / L;
-    if (P < 1) P = 1;
-    return P;
-}
-static int pick_cols(int L) {
-    int W = 2048 / L;
-    if (W < 4) W = 4;
-    if (W > 32) W = 32;
-    return W;
+// ------------------------------------------- hybrid Green build (FP32 path)
+// One thread per displacement d of the stored region (octant in free space;
+// quadrant x all dz for the image) computes all three components.  Cells
+// within kNearRatio half-widths of the origin use the reference's FP64
+// antiderivative corner differences (green_functions.jl:35-38, 82-112, with
+// the reference's corner coordinates); elsewhere the cell integral of
+// (u, v, w)/r^3 is done by FP32 Gauss-Legendre quadrature (4 points per axis
+// below kQ3Ratio, 3 beyond), which is exact to < 5e-8 relative there while the
+// FP64 corner differences lose digits to cancellation.  The three components
+// integrate over the same cell: component y's antiderivative F(v, w, u) and
+// z's F(w, u, v) difference to the integrals of v/r^3 and w/r^3.
+constexpr double kNearRatio = 6.0;
+constexpr double kQ3Ratio = 16.0;
+
+struct OctantGeom {
+    int nx, ny, nz;
+    int image;           // dz range [-(nz-1), nz-1] instead of [0, nz-1]
+    double dx, dy, dz;   // full cell widths, dz already scaled by gamma
+    double offw;         // cathode offset * gamma on the w axis
+    double gamma;
+    double hmax;         // half of the largest width
+    double scale;        // FPEI / (Lx Ly Lz)
+    int64_t cs;          // component stride of the output
+};
+
+__device__ __forceinline__ void gl_accumulate(float cx, float cy, float cz, float hx, float hy, float hz,
+                                              const float* t, const float* w, int m, float& ax, float& ay,
+                                              float& az) {
+    for (int i = 0; i < m; ++i) {
+        const float px = fmaf(hx, t[i], cx);
+        for (int j = 0; j < m; ++j) {
+            const float py = fmaf(hy, t[j], cy);
+            const float wij = w[i] * w[j];
+            for (int k = 0; k < m; ++k) {
+                const float pz = fmaf(hz, t[k], cz);
+                const float r2 = fmaf(px, px, fmaf(py, py, pz * pz));
+                const float ir = rsqrtf(r2);
+                const float q = wij * w[k] * ir * ir * ir;
+                ax = fmaf(q, px, ax);
+                ay = fmaf(q, py, ay);
+                az = fmaf(q, pz, az);
+            }
+        }
+    }
 }
 
-template <typename T>
-static const typename Cplx<T>::T2* twiddles(DeviceCtx* c);
-template <>
-const float2* twiddles<float>(DeviceCtx* c) {
-    return c->tw32;
-}
-template <>
-const double2* twiddles<double>(DeviceCtx* c) {
-    return c->tw64;
+__global__ void __launch_bounds__(256) k_igf_octant(float* __restrict__ G, OctantGeom g) {
+    const int zc = g.image ? 2 * g.nz - 1 : g.nz;
+    const int64_t total = (int64_t)g.nx * g.ny * zc;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int ix = (int)(t % g.nx);
+    const int iy = (int)((t / g.nx) % g.ny);
+    const int iz = (int)(t / ((int64_t)g.nx * g.ny));
+    const int dz = g.image ? iz - (g.nz - 1) : iz;
+    const double cx = ix * g.dx, cy = iy * g.dy, cz = dz * g.dz + g.offw;
+    const double R = sqrt(cx * cx + cy * cy + cz * cz);
+    const double ratio = R / g.hmax;
+    double G3[3];
+    if (ratio < kNearRatio) {
+        // reference corner coordinates: point i0 = d + n - 1 (+1) of the
+        // doubled grid, u = i0*dx + (1 - 2n)*dx/2 (+ offset*gamma on w)
+        const double umin = (double)(1 - 2 * g.nx) * g.dx / 2;
+        const double vmin = (double)(1 - 2 * g.ny) * g.dy / 2;
+        const double wmin = (double)(1 - 2 * g.nz) * g.dz / 2 + g.offw;
+        double u[2], v[2], w[2];
+        for (int a = 0; a < 2; ++a) {
+            u[a] = (double)(ix + g.nx - 1 + a) * g.dx + umin;
+            v[a] = (double)(iy + g.ny - 1 + a) * g.dy + vmin;
+            w[a] = (double)(dz + g.nz - 1 + a) * g.dz + wmin;
+        }
+        const double fxy = g.gamma / (g.dx * g.dy * g.dz), fz = 1.0 / (g.dx * g.dy * g.dz);
+        for (int c = 0; c < 3; ++c) {
+            double F[2][2][2];
+            for (int a = 0; a < 2; ++a)
+                for (int b = 0; b < 2; ++b)
+                    for (int e = 0; e < 2; ++e) {
+                        const double val = c == 0 ? field_green_n(u[a], v[b], w[e])
+                                         : c == 1 ? field_green_n(v[b], w[e], u[a])
+                                                  : field_green_n(w[e], u[a], v[b]);
+                        F[a][b][e] = val * (c == 2 ? fz : fxy);
+                    }
+            // green_functions.jl:108-111
+            G3[c] = F[1][1][1] - F[0][1][1] - F[1][0][1] - F[1][1][0] - F[0][0][0] + F[0][0][1] + F[0][1][0] +
+                    F[1][0][0];
+        }
+    } else {
+        const float t4[4] = {-0.86113631159405258f, -0.33998104358485626f, 0.33998104358485626f,
+                             0.86113631159405258f};
+        const float w4[4] = {0.34785484513745386f, 0.65214515486254614f, 0.65214515486254614f,
+                             0.34785484513745386f};
+        const float t3[3] = {-0.77459666924148338f, 0.0f, 0.77459666924148338f};
+        const float w3[3] = {0.55555555555555556f, 0.88888888888888889f, 0.55555555555555556f};
+        const double sc = 1.0 / g.hmax;
+        const float px = (float)(cx * sc), py = (float)(cy * sc), pz = (float)(cz * sc);
+        const float hx = (float)(0.5 * g.dx * sc), hy = (float)(0.5 * g.dy * sc), hz = (float)(0.5 * g.dz * sc);
+        float ax = 0.f, ay = 0.f, az = 0.f;
+        if (ratio < kQ3Ratio)
+            gl_accumulate(px, py, pz, hx, hy, hz, t4, w4, 4, ax, ay, az);
+        else
+            gl_accumulate(px, py, pz, hx, hy, hz, t3, w3, 3, ax, ay, az);
+        // G_c = gamma_c / 8 * sum w w w p'_c / r'^3 / hmax^2
+        const double k = 0.125 * sc * sc;
+        G3[0] = g.gamma * k * ax;
+        G3[1] = g.gamma * k * ay;
+        G3[2] = k * az;
+    }
+    for (int c = 0; c < 3; ++c) G[c * g.cs + t] = (float)(G3[c] * g.scale);
 }
 
-template <typename K>
-static int set_smem(K kernel, size_t bytes) {
-    if (bytes > 48 * 1024) SC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    return SC_OK;
+// Rows of the L grid that hold kernel values: displacement index c in
+// [0, 2n-1) maps to L-grid row c (c < n) or L - (2n-1) + c (negative d).
+__device__ __forceinline__ int wrap_row(int c, int n, int L) { return c < n ? c : L - (2 * n - 1) + c; }
+
+// x pass of the kernel transform, three components (blockIdx.y): each valid
+// row (y, z) of the L grid is expanded from the stored octant/quadrant with
+// the component's parity, two rows per complex FFT.
+__global__ void __launch_bounds__(256) k_green_x(const float* __restrict__ G, float2* __restrict__ S, int nx,
+                                                 int ny, int nz, int image, int Lx, int logLx, int Ly, int Lz,
+                                                 int Hx, int lgP, int64_t gcs, int64_t scs,
+                                                 const float2* __restrict__ tw) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int P = 1 << lgP;
+    const int n = P << logLx;
+    float2* a = reinterpret_cast<float2*>(smraw);
+    float2* b = a + n;
+    const int comp = blockIdx.y;
+    const float* Gc = G + comp * gcs;
+    const int rows = (2 * ny - 1) * (2 * nz - 1);
+    const int pair0 = blockIdx.x << lgP;
+    for (int it = threadIdx.x; it < n; it += blockDim.x) {
+        const int p = it >> logLx, x = it & (Lx - 1);
+        float v[2] = {0.f, 0.f};
+        const int dx = x < nx ? x : (x > Lx - nx ? x - Lx : Lx);
+        if (dx != Lx) {
+            for (int h = 0; h < 2; ++h) {
+                const int r = 2 * (pair0 + p) + h;
+                if (r >= rows) continue;
+                const int cy = r % (2 * ny - 1), cz = r / (2 * ny - 1);
+                const int dy = cy < ny ? cy : cy - (2 * ny - 1);
+                const int dz = cz < nz ? cz : cz - (2 * nz - 1);
+                const int ax = dx < 0 ? -dx : dx, ay = dy < 0 ? -dy : dy;
+                const int iz = image ? dz + nz - 1 : (dz < 0 ? -dz : dz);
+                float val = Gc[ax + (int64_t)nx * (ay + (int64_t)ny * iz)];
+                const int sgn = comp == 0 ? dx : comp == 1 ? dy : (image ? 0 : dz);
+                if (sgn < 0) val = -val;
+                v[h] = val;
+            }
+        }
+        a[(x << lgP) + p] = make_float2(v[0], v[1]);
+    }
+    __syncthreads();
+    const float2* res = smem_fft<false>(a, b, Lx, logLx, lgP, tw);
+    float2* Sc = S + comp * scs;
+    const int lgh = logLx - 1, half = Lx >> 1;
+    for (int it = threadIdx.x; it < (P << lgh); it += blockDim.x) {
+        const int p = it >> lgh, k0 = it & (half - 1);
+        const int r0 = 2 * (pair0 + p), r1 = r0 + 1;
+        if (r0 >= rows) continue;
+        const int y0 = wrap_row(r0 % (2 * ny - 1), ny, Ly), z0 = wrap_row(r0 / (2 * ny - 1), nz, Lz);
+        const int y1 = wrap_row(r1 % (2 * ny - 1), ny, Ly), z1 = wrap_row(r1 / (2 * ny - 1), nz, Lz);
+        for (int e = 0; e < (k0 == 0 ? 2 : 1); ++e) {
+            const int k = e ? half : k0;
+            float2 xa, xb;
+            split_pair(res[(k << lgP) + p], res[(((Lx - k) & (Lx - 1)) << lgP) + p], xa, xb);
+            Sc[(int64_t)(y0 + (int64_t)Ly * z0) * Hx + k] = xa;
+            if (r1 < rows) Sc[(int64_t)(y1 + (int64_t)Ly * z1) * Hx + k] = xb;
+        }
+    }
 }
 
-// real rows (nx_valid of Lx nonzero) -> half spectra
-template <typename T>
-static int run_fwd_x(const T* src, typename Cplx<T>::T2* dst, int nx_valid, int rows, const NativeWork& w,
-                     const typename Cplx<T>::T2* tw, cudaStream_t s) {
-    using T2 = typename Cplx<T>::T2;
-    const int P = pick_rows(w.L[0]);
-    const size_t smem = sizeof(T2) * 2 * P * w.L[0];
-    SC_TRY(set_smem(k_fwd_x<T>, smem));
-    const int pairs = (rows + 1) / 2;
-    k_fwd_x<T><<<(pairs + P - 1) / P, 256, smem, s>>>(src, dst, nx_valid, rows, w.L[0], w.log2L[0], w.Hx, P, tw);
-    SC_LAUNCH_CHECK("k_fwd_x");
-    return SC_OK;
+// y pass in place: columns (kx) at every valid z (blockIdx.y over the
+// compact z index), inputs only on the valid rows, all Ly outputs.
+__global__ void __launch_bounds__(256) k_green_y(float2* __restrict__ S, int ny, int nz, int Ly, int logLy,
+                                                 int Lz, int Hx, int lgW, int64_t scs,
+                                                 const float2* __restrict__ tw) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int W = 1 << lgW;
+    const int n = W << logLy;
+    float2* a = reinterpret_cast<float2*>(smraw);
+    float2* b = a + n;
+    const int z = wrap_row(blockIdx.y, nz, Lz);
+    float2* Sc = S + blockIdx.z * scs + (int64_t)Hx * Ly * z;
+    const int c0 = blockIdx.x << lgW;
+    for (int it = threadIdx.x; it < n; it += blockDim.x) {
+        const int y = it >> lgW, col = c0 + (it & (W - 1));
+        float2 v = make_float2(0.f, 0.f);
+        if (col < Hx && (y < ny || y > Ly - ny)) v = Sc[col + (int64_t)Hx * y];
+        a[it] = v;
+    }
+    __syncthreads();
+    const float2* res = smem_fft<false>(a, b, Ly, logLy, lgW, tw);
+    for (int it = threadIdx.x; it < n; it += blockDim.x) {
+        const int y = it >> lgW, col = c0 + (it & (W - 1));
+        if (col < Hx) Sc[col + (int64_t)Hx * y] = res[it];
+    }
 }
 
-template <bool INV, typename T>
-static int run_col(const typename Cplx<T>::T2* in, typename Cplx<T>::T2* out, int ncols, int L, int logL,
-                   int n_valid, int n_store, int64_t as_in, int64_t bs_in, int64_t cs_in, int64_t as_out,
-                   int64_t bs_out, int64_t cs_out, int nbatch, int ncomp, const typename Cplx<T>::T2* tw,
-                   cudaStream_t s) {
-    using T2 = typename Cplx<T>::T2;
-    const int W = pick_cols(L);
-    const size_t smem = sizeof(T2) * 2 * W * L;
-    SC_TRY(set_smem(k_col_fft<INV, T>, smem));
-    dim3 grid((ncols + W - 1) / W, nbatch, ncomp);
-    k_col_fft<INV, T><<<grid, 256, smem, s>>>(in, out, ncols, W, L, logL, n_valid, n_store, as_in, bs_in, cs_in,
-                                               as_out, bs_out, cs_out, tw);
-    SC_LAUNCH_CHECK("k_col_fft");
-    return SC_OK;
-}
-
-template <typename T>
-static int alloc_work(sc_mesh* m) {
-    using T2 = typename Cplx<T>::T2;
-    NativeWork& w = m->nw;
-    if (w.A) return SC_OK;
-    const int64_t nx = m->n[0], ny = m->n[1], nz = m->n[2];
-    const int64_t Hx = w.Hx, Ly = w.L[1], Lz = w.L[2];
-    const int64_t Hy = Ly / 2 + 1, Hz = Lz / 2 + 1;
-    SC_CUDA(cudaMalloc(&w.A, sizeof(T2) * Hx * ny * nz));
-    SC_CUDA(cudaMalloc(&w.B, sizeof(T2) * Hx * Ly * nz));
-    SC_CUDA(cudaMalloc(&w.C, sizeof(T2) * 3 * Hx * Ly * nz));
-    SC_CUDA(cudaMalloc(&w.D, sizeof(T2) * 3 * Hx * ny * nz));
-    SC_CUDA(cudaMalloc(&w.gfree, sizeof(T) * 3 * Hx * Hy * Hz));
-    return SC_OK;
+// z pass for ky in [0, Ly/2] with the compression fused: free space keeps
+// Im(K^) for kz in [0, Lz/2]; the image keeps all kz with the flip phase
+// -exp(-2 pi i kz (nz-1)/Lz) folded in.
+__global__ void __launch_bounds__(256) k_green_z(const float2* __restrict__ S, void* __restrict__ dst, int nz,
+                                                 int image, int Ly, int Lz, int logLz, int Hx, int lgW, int64_t scs,
+                                                 int64_t dcs, const float2* __restrict__ tw) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int W = 1 << lgW;
+    const int n = W << logLz;
+    float2* a = reinterpret_cast<float2*>(smraw);
+    float2* b = a + n;
+    const int ky = blockIdx.y;
+    const int comp = blockIdx.z;
+    const int Hy = Ly / 2 + 1;
+    const float2* Sc = S + comp * scs;
+    const int c0 = blockIdx.x << lgW;
+    const int64_t plane = (int64_t)Hx * Ly;
+    for (int it = threadIdx.x; it < n; it += blockDim.x) {
+        const int z = it >> lgW, col = c0 + (it & (W - 1));
+        float2 v = make_float2(0.f, 0.f);
+        if (col < Hx && (z < nz || z > Lz - nz)) v = Sc[col + (int64_t)Hx * ky + plane * z];
+        a[it] = v;
+    }
+    __syncthreads();
+    const float2* res = smem_fft<false>(a, b, Lz, logLz, lgW, tw);
+    const int zc = image ? Lz : Lz / 2 + 1;
+    for (int it = threadIdx.x; it < (zc << lgW); it += blockDim.x) {
+        const int kz = it >> lgW, col = c0 + (it & (W - 1));
+        if (col >= Hx) continue;
+        const float2 v = res[it];
+        const int64_t o = col + (int64_t)Hx * (ky + (int64_t)Hy * kz);
+        if (!image) {
+            reinterpret_cast<float*>(dst)[comp * dcs + o] = v.y;
+        } else {
+            const float2 ph = tw[(int)(((int64_t)kz * (nz - 1)) & (Lz - 1)) * (kMaxL / Lz)];
+            const float2 r = cmul(v, ph);
+            reinterpret_cast<float2*>(dst)[comp * dcs + o] = make_float2(-r.x, -r.y);
+        }
+    }
 }
 
 template <typename T>
@@ -500,6 +551,86 @@ static int build_green(sc_mesh* m, bool image, double offz, cudaStream_t s) {
     return SC_OK;
 }
 
+// FP32 path: hybrid octant kernel + three batched transform passes.
+static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s) {
+    DeviceCtx* ctx = nullptr;
+    SC_TRY(device_ctx(&ctx));
+    const float2* tw = ctx->tw32;
+    NativeWork& w = m->nw;
+    const int nx = m->n[0], ny = m->n[1], nz = m->n[2];
+    const int Lx = w.L[0], Ly = w.L[1], Lz = w.L[2], Hx = w.Hx;
+    const int Hy = Ly / 2 + 1, Hz = Lz / 2 + 1;
+    const int64_t gcs = (int64_t)nx * ny * (2 * nz - 1);
+    const int64_t scs = (int64_t)Hx * Ly * Lz;
+    if (!w.goct) SC_CUDA(cudaMalloc(&w.goct, sizeof(float) * 3 * gcs));
+    if (!w.gspec) SC_CUDA(cudaMalloc(&w.gspec, sizeof(float2) * 3 * scs));
+    if (image && !w.gimg) SC_CUDA(cudaMalloc(&w.gimg, sizeof(float2) * 3 * (int64_t)Hx * Hy * Lz));
+    OctantGeom g;
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = nz;
+    g.image = image ? 1 : 0;
+    g.dx = m->delta[0];
+    g.dy = m->delta[1];
+    g.dz = m->delta[2] * m->gamma;  // green_functions.jl:73
+    g.offw = image ? offz * m->gamma : 0.0;
+    g.gamma = m->gamma;
+    g.hmax = 0.5 * fmax(g.dx, fmax(g.dy, g.dz));
+    g.scale = kFpei / ((double)Lx * Ly * Lz);
+    g.cs = gcs;
+    const int zc = image ? 2 * nz - 1 : nz;
+    const int64_t cells = (int64_t)nx * ny * zc;
+    k_igf_octant<<<(cells + 255) / 256, 256, 0, s>>>((float*)w.goct, g);
+    SC_LAUNCH_CHECK("k_igf_octant");
+    float2* S = (float2*)w.gspec;
+    {
+        const int lgP = pick_rows(w.log2L[0]);
+        const int P = 1 << lgP;
+        const size_t smem = sizeof(float2) * 2 * P * Lx;
+        SC_TRY(set_smem(k_green_x, smem));
+        const int rows = (2 * ny - 1) * (2 * nz - 1);
+        dim3 grid(((rows + 1) / 2 + P - 1) / P, 3);
+        k_green_x<<<grid, 256, smem, s>>>((const float*)w.goct, S, nx, ny, nz, g.image, Lx, w.log2L[0], Ly, Lz, Hx,
+                                          lgP, gcs, scs, tw);
+        SC_LAUNCH_CHECK("k_green_x");
+    }
+    {
+        const int lgW = pick_cols(w.log2L[1]);
+        const int W = 1 << lgW;
+        const size_t smem = sizeof(float2) * 2 * W * Ly;
+        SC_TRY(set_smem(k_green_y, smem));
+        dim3 grid((Hx + W - 1) / W, 2 * nz - 1, 3);
+        k_green_y<<<grid, 256, smem, s>>>(S, ny, nz, Ly, w.log2L[1], Lz, Hx, lgW, scs, tw);
+        SC_LAUNCH_CHECK("k_green_y");
+    }
+    {
+        const int lgW = pick_cols(w.log2L[2]);
+        const int W = 1 << lgW;
+        const size_t smem = sizeof(float2) * 2 * W * Lz;
+        SC_TRY(set_smem(k_green_z, smem));
+        dim3 grid((Hx + W - 1) / W, Hy, 3);
+        void* dst = image ? w.gimg : w.gfree;
+        const int64_t dcs = image ? (int64_t)Hx * Hy * Lz : (int64_t)Hx * Hy * Hz;
+        k_green_z<<<grid, 256, smem, s>>>(S, dst, nz, g.image, Ly, Lz, w.log2L[2], Hx, lgW, scs, dcs, tw);
+        SC_LAUNCH_CHECK("k_green_z");
+    }
+    m->launches += 4;
+    return SC_OK;
+}
+
+template <typename T>
+static int build_green_any(sc_mesh* m, bool image, double offz, cudaStream_t s);
+template <>
+int build_green_any<float>(sc_mesh* m, bool image, double offz, cudaStream_t s) {
+    return build_green_mixed(m, image, offz, s);
+}
+template <>
+int build_green_any<double>(sc_mesh* m, bool image, double offz, cudaStream_t s) {
+    SC_TRY(build_green<double>(m, image, offz, s));
+    m->launches += 18;
+    return SC_OK;
+}
+
 static bool key_matches(const GreenKey& k, const sc_mesh* m, double offz) {
     return k.valid && k.delta[0] == m->delta[0] && k.delta[1] == m->delta[1] && k.delta[2] == m->delta[2] &&
            k.gamma == m->gamma && k.offset_z == offz;
@@ -509,6 +640,32 @@ static void set_key(GreenKey& k, const sc_mesh* m, double offz) {
     k.gamma = m->gamma;
     k.offset_z = offz;
     k.valid = true;
+}
+
+// Build (or reuse) the compressed Green spectra the solve needs.
+template <typename T>
+static int ensure_green_t(sc_mesh* m, int at_cathode, cudaStream_t s) {
+    NativeWork& w = m->nw;
+    const double offz = 2 * m->lo[2] + (m->hi[2] - m->lo[2]);  // free_space.jl:39
+    StageScope st(m->timer, SC_STAGE_GREEN, s);
+    if (!(m->green_cache && key_matches(w.key_free, m, 0.0))) {
+        SC_TRY(build_green_any<T>(m, false, 0.0, s));
+        set_key(w.key_free, m, 0.0);
+    }
+    if (at_cathode && !(m->green_cache && key_matches(w.key_img, m, offz))) {
+        SC_TRY(build_green_any<T>(m, true, offz, s));
+        set_key(w.key_img, m, offz);
+    }
+    return SC_OK;
+}
+
+int native_ensure_green(sc_mesh* m, int at_cathode, cudaStream_t s) {
+    if (m->precision == SC_PREC_MIXED) {
+        SC_TRY(alloc_work<float>(m));
+        return ensure_green_t<float>(m, at_cathode, s);
+    }
+    SC_TRY(alloc_work<double>(m));
+    return ensure_green_t<double>(m, at_cathode, s);
 }
 
 template <typename T>
@@ -522,26 +679,26 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s) {
     const int nx = m->n[0], ny = m->n[1], nz = m->n[2];
     const int Lx = w.L[0], Ly = w.L[1], Lz = w.L[2], Hx = w.Hx;
     (void)Lx;
-    const double offz = 2 * m->lo[2] + (m->hi[2] - m->lo[2]);  // free_space.jl:39
-    if (!(m->green_cache && key_matches(w.key_free, m, 0.0))) {
-        SC_TRY(build_green<T>(m, false, 0.0, s));
-        set_key(w.key_free, m, 0.0);
-    }
-    if (at_cathode && !(m->green_cache && key_matches(w.key_img, m, offz))) {
-        SC_TRY(build_green<T>(m, true, offz, s));
-        set_key(w.key_img, m, offz);
-    }
+    SC_TRY(ensure_green_t<T>(m, at_cathode, s));
+    m->launches += 5;
     T2* A = (T2*)w.A;
     T2* B = (T2*)w.B;
     T2* C = (T2*)w.C;
     T2* D = (T2*)w.D;
     const int rows = ny * nz;
-    SC_TRY(run_fwd_x<T>((const T*)m->rho, A, nx, rows, w, tw, s));
-    // y: A (Hx x ny x nz) -> B (Hx x Ly x nz)
-    SC_TRY(run_col<false, T>(A, B, Hx, Ly, w.log2L[1], ny, Ly, Hx, (int64_t)Hx * ny, 0, Hx, (int64_t)Hx * Ly, 0, nz,
-                             1, tw, s));
+    {
+        StageScope st(m->timer, SC_STAGE_FWD_X, s);
+        SC_TRY(run_fwd_x<T>((const T*)m->rho, A, nx, rows, w, tw, s));
+    }
+    {
+        // y: A (Hx x ny x nz) -> B (Hx x Ly x nz)
+        StageScope st(m->timer, SC_STAGE_FWD_Y, s);
+        SC_TRY(run_col<false, T>(A, B, Hx, Ly, w.log2L[1], ny, Ly, Hx, (int64_t)Hx * ny, 0, Hx, (int64_t)Hx * Ly, 0,
+                                 nz, 1, tw, s));
+    }
     // z + Green + inverse z
     {
+        StageScope st(m->timer, SC_STAGE_ZPASS, s);
         GreenView gv;
         gv.gfree = w.gfree;
         gv.gimg = w.gimg;
@@ -553,24 +710,30 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s) {
         gv.cs_free = (int64_t)Hx * gv.Hy * gv.Hz;
         gv.cs_img = (int64_t)Hx * gv.Hy * Lz;
         gv.image = at_cathode ? 1 : 0;
-        const int W = pick_cols(Lz);
+        const int lgW = pick_cols(w.log2L[2]);
+        const int W = 1 << lgW;
         const size_t smem = sizeof(T2) * 3 * W * Lz;
         SC_TRY(set_smem(k_zpass<T>, smem));
         dim3 grid((Hx + W - 1) / W, Ly);
-        k_zpass<T><<<grid, 256, smem, s>>>(B, C, Hx, Ly, nz, Lz, w.log2L[2], W, gv, tw);
+        k_zpass<T><<<grid, 256, smem, s>>>(B, C, Hx, Ly, nz, Lz, w.log2L[2], lgW, gv, tw);
         SC_LAUNCH_CHECK("k_zpass");
     }
-    // inverse y: C (3 x Hx x Ly x nz) -> D (3 x Hx x ny x nz)
-    SC_TRY(run_col<true, T>(C, D, Hx, Ly, w.log2L[1], Ly, ny, Hx, (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, Hx,
-                            (int64_t)Hx * ny, (int64_t)Hx * ny * nz, nz, 3, tw, s));
-    // inverse x -> packed efield
     {
-        const int P = pick_rows(w.L[0]);
-        const size_t smem = sizeof(T2) * (2 * P * w.L[0] + 3 * P * nx);
+        // inverse y: C (3 x Hx x Ly x nz) -> D (3 x Hx x ny x nz)
+        StageScope st(m->timer, SC_STAGE_INV_Y, s);
+        SC_TRY(run_col<true, T>(C, D, Hx, Ly, w.log2L[1], Ly, ny, Hx, (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, Hx,
+                                (int64_t)Hx * ny, (int64_t)Hx * ny * nz, nz, 3, tw, s));
+    }
+    {
+        // inverse x -> packed efield
+        StageScope st(m->timer, SC_STAGE_INV_X, s);
+        const int lgP = pick_rows(w.log2L[0]);
+        const int P = 1 << lgP;
+        const size_t smem = sizeof(T2) * 5 * P * w.L[0];
         SC_TRY(set_smem(k_inv_x<T>, smem));
         const int pairs = (rows + 1) / 2;
         k_inv_x<T><<<(pairs + P - 1) / P, 256, smem, s>>>(D, (typename Vec4<T>::V*)m->efield, nx, rows, w.L[0],
-                                                           w.log2L[0], Hx, P, (int64_t)Hx * rows, tw);
+                                                           w.log2L[0], Hx, lgP, (int64_t)Hx * rows, tw);
         SC_LAUNCH_CHECK("k_inv_x");
     }
     return SC_OK;
@@ -600,7 +763,7 @@ int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s) {
 
 int native_release(sc_mesh* m) {
     NativeWork& w = m->nw;
-    void* ptrs[] = {w.A, w.B, w.C, w.D, w.fcorner, w.kgrid, w.kspec, w.gfree, w.gimg};
+    void* ptrs[] = {w.A, w.B, w.C, w.D, w.adjE, w.fcorner, w.kgrid, w.kspec, w.goct, w.gspec, w.gfree, w.gimg};
     for (void* p : ptrs) cudaFree(p);
     int L[3] = {w.L[0], w.L[1], w.L[2]};
     int lg[3] = {w.log2L[0], w.log2L[1], w.log2L[2]};

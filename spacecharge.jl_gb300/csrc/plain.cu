@@ -141,15 +141,20 @@ static int plain_solve_freespace(sc_mesh* m, double offz, int image, cudaStream_
     const int nx = m->n[0], ny = m->n[1], nz = m->n[2];
     const int64_t total = (int64_t)8 * m->N;
     const int64_t gb = (total + 255) / 256;
+    StageTimer& tm = m->timer;
+    StageScope st(tm, SC_STAGE_PLAIN_FFT, s);
     plain_pad<<<gb, 256, 0, s>>>((const double*)m->rho, w.crho, nx, ny, nz, image);
     SC_LAUNCH_CHECK("plain_pad");
     SC_TRY(fft(m, w.crho, CUFFT_FORWARD, s));
+    m->launches += 2 + 3 * 6;
     for (int comp = 1; comp <= 3; ++comp) {
+        if (tm.enabled) tm.begin(SC_STAGE_GREEN, s);
         plain_green_point<<<gb, 256, 0, s>>>(w.cgrn, 2 * nx, 2 * ny, 2 * nz, m->delta[0], m->delta[1],
                                              m->delta[2], m->gamma, comp, 0.0, 0.0, offz);
         SC_LAUNCH_CHECK("plain_green_point");
         plain_green_diff<<<gb, 256, 0, s>>>(w.cgrn, w.tmp, 2 * nx, 2 * ny, 2 * nz);
         SC_LAUNCH_CHECK("plain_green_diff");
+        if (tm.enabled) tm.begin(SC_STAGE_PLAIN_FFT, s);
         SC_TRY(fft(m, w.tmp, CUFFT_FORWARD, s));
         plain_mul<<<gb, 256, 0, s>>>(w.crho, w.tmp, total);
         SC_LAUNCH_CHECK("plain_mul");

@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/spacecharge_gb300.h"
 
@@ -78,10 +79,13 @@ struct NativeWork {
     void* B = nullptr;      // Hx x Ly x nz            (after y pass)
     void* C = nullptr;      // 3 x Hx x Ly x nz        (after z pass)
     void* D = nullptr;      // 3 x Hx x ny x nz        (after inverse y)
+    void* adjE = nullptr;   // adjoint: 3 x N accumulated dL/dE (T)
     // Green function construction
     double* fcorner = nullptr;  // FP64 antiderivative on corner lattice
     void* kgrid = nullptr;      // real kernel on the L grid (T)
     void* kspec = nullptr;      // its half spectrum (T2), Hx x Ly x Lz
+    void* goct = nullptr;       // FP32 path: kernel values on the octant/quadrant, 3 comps
+    void* gspec = nullptr;      // FP32 path: 3 half spectra Hx x Ly x Lz being transformed
     void* gfree = nullptr;      // compressed free-space spectra, 3 comps (T)
     void* gimg = nullptr;       // compressed image spectra, 3 comps (T2)
     GreenKey key_free, key_img;
@@ -97,6 +101,33 @@ struct PlainWork {
 
 }  // namespace sc
 
+namespace sc {
+// CUDA-event stage timer (used only while profiling is enabled).
+struct StageTimer {
+    bool enabled = false;
+    struct Pair {
+        cudaEvent_t a, b;
+    };
+    std::vector<Pair> ev[SC_NUM_STAGES];
+    size_t used[SC_NUM_STAGES] = {};
+    int open_stage = -1;
+    void begin(int stage, cudaStream_t s);
+    void end(cudaStream_t s);
+    void release();
+};
+// RAII bracket: `StageScope t(m, SC_STAGE_X, s);`
+struct StageScope {
+    StageTimer* t;
+    cudaStream_t s;
+    StageScope(StageTimer& tm, int stage, cudaStream_t st) : t(&tm), s(st) {
+        if (t->enabled) t->begin(stage, s);
+    }
+    ~StageScope() {
+        if (t->enabled) t->end(s);
+    }
+};
+}  // namespace sc
+
 struct sc_mesh {
     int n[3];
     int64_t N;
@@ -110,6 +141,8 @@ struct sc_mesh {
     unsigned long long* oob = nullptr;  // device counter of skipped particles
     sc::NativeWork nw;
     sc::PlainWork pw;
+    sc::StageTimer timer;
+    int64_t launches = 0;  // kernels launched by this mesh
 };
 
 namespace sc {
@@ -144,6 +177,10 @@ int plain_release(sc_mesh* m);
 
 int native_prepare(sc_mesh* m);  // sizes only (no allocation)
 int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s);
+int native_ensure_green(sc_mesh* m, int at_cathode, cudaStream_t s);
+int adjoint_launch(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
+                   int at_cathode, const void* gex, const void* gey, const void* gez, const void* ggrid, void* dx,
+                   void* dy, void* dz, void* dq, cudaStream_t s);
 int native_release(sc_mesh* m);
 
 }  // namespace sc

@@ -1,0 +1,194 @@
+"""
+    SpaceChargeGB300
+
+Drop-in replacement for SpaceCharge.jl's GPU hot path (src/SpaceCharge.jl:17
+exports): `Mesh3D`, `deposit!`, `clear_mesh!`, `solve!`, `interpolate_field`,
+backed by libspacecharge_gb300.so (hand-written sm_103a kernels) through
+`ccall`.  Particle arrays are `CuArray{Float32}` or `CuArray{Float64}`; work is
+enqueued on the task-local CUDA.jl stream, as the reference's kernels are.
+A non-zero library status becomes `error(msg)` (an `ErrorException`), as the
+reference's argument checks do.
+"""
+module SpaceChargeGB300
+
+using CUDA
+import ChainRulesCore
+
+export Mesh3D, deposit!, clear_mesh!, interpolate_field, solve!, kick
+
+const libsc = normpath(joinpath(@__DIR__, "..", "..", "..", "lib", "libspacecharge_gb300.so"))
+
+const SC_F32 = Cint(0)
+const SC_F64 = Cint(1)
+const SC_PREC_PLAIN64 = Cint(0)
+const SC_PREC_FP64 = Cint(1)
+const SC_PREC_MIXED = Cint(2)
+const SC_LAYOUT_PACKED = Cint(1)
+
+# include/spacecharge_gb300.h: sc_mesh_info
+struct MeshInfo
+    grid_size::NTuple{3,Int32}
+    precision::Int32
+    min_bounds::NTuple{3,Float64}
+    max_bounds::NTuple{3,Float64}
+    delta::NTuple{3,Float64}
+    gamma::Float64
+    total_charge::Float64
+    efield_layout::Int32
+    elem_bytes::Int32
+    fft_shape::NTuple{3,Int32}
+    device::Int32
+end
+
+check(st::Cint) = st == 0 ? nothing :
+    error(unsafe_string(ccall((:sc_last_error, libsc), Cstring, ())))
+
+dtype_code(::Type{Float32}) = SC_F32
+dtype_code(::Type{Float64}) = SC_F64
+stream_ptr() = CUDA.stream().handle
+
+mutable struct Mesh3D{T<:AbstractFloat}
+    ptr::Ptr{Cvoid}
+    grid_size::NTuple{3,Int}
+    min_bounds::NTuple{3,Float64}
+    max_bounds::NTuple{3,Float64}
+    delta::NTuple{3,Float64}
+    gamma::Float64
+    total_charge::Float64
+    rho::CuArray{T,3}
+    efield::AbstractArray{T,4}
+end
+
+function _wrap(ptr::Ptr{Cvoid}, ::Type{T}) where {T}
+    info = Ref{MeshInfo}()
+    check(ccall((:sc_mesh_get_info, libsc), Cint, (Ptr{Cvoid}, Ref{MeshInfo}), ptr, info))
+    inf = info[]
+    n = Int.(inf.grid_size)
+    prho = Ref{Ptr{Cvoid}}(C_NULL)
+    pef = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:sc_mesh_rho, libsc), Cint, (Ptr{Cvoid}, Ref{Ptr{Cvoid}}), ptr, prho))
+    check(ccall((:sc_mesh_efield, libsc), Cint, (Ptr{Cvoid}, Ref{Ptr{Cvoid}}), ptr, pef))
+    rho = unsafe_wrap(CuArray, CuPtr{T}(UInt(prho[])), n)
+    efield = if inf.efield_layout == SC_LAYOUT_PACKED
+        raw = unsafe_wrap(CuArray, CuPtr{T}(UInt(pef[])), (4, n...))
+        PermutedDimsArray(view(raw, 1:3, :, :, :), (2, 3, 4, 1))   # (nx, ny, nz, 3)
+    else
+        unsafe_wrap(CuArray, CuPtr{T}(UInt(pef[])), (n..., 3))
+    end
+    m = Mesh3D{T}(ptr, Tuple(n), inf.min_bounds, inf.max_bounds, inf.delta, inf.gamma,
+                  inf.total_charge, rho, efield)
+    finalizer(m) do mm
+        ccall((:sc_mesh_destroy, libsc), Cint, (Ptr{Cvoid},), mm.ptr)
+    end
+    return m
+end
+
+precision_code(::Type{Float64}, p) = p === :plain64 ? SC_PREC_PLAIN64 : SC_PREC_FP64
+precision_code(::Type{Float32}, p) = SC_PREC_MIXED
+storage_type(code) = code == SC_PREC_MIXED ? Float32 : Float64
+
+# Mesh3D(grid_size, px, py, pz; T, gamma, total_charge), src/mesh.jl:122-201
+function Mesh3D(grid_size::NTuple{3,Int}, particles_x::CuArray{P}, particles_y::CuArray{P},
+                particles_z::CuArray{P}; T::Type{<:AbstractFloat}=Float64, precision::Symbol=:native,
+                gamma::Real=1.0, total_charge::Real=0.0) where {P<:Union{Float32,Float64}}
+    if !(length(particles_x) == length(particles_y) == length(particles_z))
+        error("Particle coordinate arrays must have the same length.")
+    end
+    code = precision_code(T, precision)
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:sc_mesh_create_from_particles, libsc), Cint,
+                (Ptr{Int32}, CuPtr{P}, CuPtr{P}, CuPtr{P}, Int64, Cint, Float64, Float64, Cint, Ptr{Cvoid},
+                 Ref{Ptr{Cvoid}}),
+                Int32[grid_size...], particles_x, particles_y, particles_z, length(particles_x), dtype_code(P),
+                Float64(gamma), Float64(total_charge), code, stream_ptr(), out))
+    return _wrap(out[], storage_type(code))
+end
+
+# Mesh3D(grid_size, min_bounds, max_bounds; T, gamma, total_charge), src/mesh.jl:223-265
+function Mesh3D(grid_size::NTuple{3,Int}, min_bounds::NTuple{3,Real}, max_bounds::NTuple{3,Real};
+                T::Type{<:AbstractFloat}=Float64, precision::Symbol=:native, gamma::Real=1.0,
+                total_charge::Real=0.0)
+    code = precision_code(T, precision)
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:sc_mesh_create, libsc), Cint,
+                (Ptr{Int32}, Ptr{Float64}, Ptr{Float64}, Float64, Float64, Cint, Ref{Ptr{Cvoid}}),
+                Int32[grid_size...], Float64[min_bounds...], Float64[max_bounds...], Float64(gamma),
+                Float64(total_charge), code, out))
+    return _wrap(out[], storage_type(code))
+end
+
+# clear_mesh!(mesh), src/deposition.jl:10-12
+clear_mesh!(mesh::Mesh3D) =
+    check(ccall((:sc_clear_mesh, libsc), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), mesh.ptr, stream_ptr()))
+
+# deposit!(mesh, px, py, pz, pq; clear=true), src/deposition.jl:218-247
+function deposit!(mesh::Mesh3D, particles_x::CuArray{P}, particles_y::CuArray{P}, particles_z::CuArray{P},
+                  particles_q::CuArray{P}; clear::Bool=true, mode::Symbol=:atomic) where {P<:Union{Float32,Float64}}
+    if !(length(particles_x) == length(particles_y) == length(particles_z) == length(particles_q))
+        error("Particle coordinate and charge arrays must have the same length.")
+    end
+    m = mode === :atomic ? Cint(0) : mode === :sorted ? Cint(1) : Cint(2)
+    check(ccall((:sc_deposit, libsc), Cint,
+                (Ptr{Cvoid}, CuPtr{P}, CuPtr{P}, CuPtr{P}, CuPtr{P}, Int64, Cint, Cint, Cint, Ptr{Cvoid}),
+                mesh.ptr, particles_x, particles_y, particles_z, particles_q, length(particles_x),
+                dtype_code(P), Cint(clear), m, stream_ptr()))
+end
+
+# solve!(mesh; at_cathode=false), src/solvers/free_space.jl:14-47
+solve!(mesh::Mesh3D; at_cathode::Bool=false) =
+    check(ccall((:sc_solve, libsc), Cint, (Ptr{Cvoid}, Cint, Ptr{Cvoid}), mesh.ptr, Cint(at_cathode),
+                stream_ptr()))
+
+# interpolate_field(mesh, px, py, pz) -> (Ex, Ey, Ez), src/interpolation.jl:100-128
+function interpolate_field(mesh::Mesh3D, particles_x::CuArray{P}, particles_y::CuArray{P},
+                           particles_z::CuArray{P}) where {P<:Union{Float32,Float64}}
+    Ex = similar(particles_x); Ey = similar(particles_x); Ez = similar(particles_x)
+    check(ccall((:sc_interpolate_field, libsc), Cint,
+                (Ptr{Cvoid}, CuPtr{P}, CuPtr{P}, CuPtr{P}, Int64, Cint, CuPtr{P}, CuPtr{P}, CuPtr{P}, Ptr{Cvoid}),
+                mesh.ptr, particles_x, particles_y, particles_z, length(particles_x), dtype_code(P),
+                Ex, Ey, Ez, stream_ptr()))
+    return Ex, Ey, Ez
+end
+
+"""
+    kick(mesh, px, py, pz, pq; at_cathode=false) -> (Ex, Ey, Ez)
+
+deposit! + solve! + interpolate_field in one library call.  Differentiable:
+the `rrule` below runs the hand-written adjoint (sc_kick_adjoint) for
+d(loss)/d(px, py, pz, pq) with the mesh geometry held fixed.
+"""
+function kick(mesh::Mesh3D, px::CuArray{P}, py::CuArray{P}, pz::CuArray{P}, pq::CuArray{P};
+              at_cathode::Bool=false) where {P<:Union{Float32,Float64}}
+    Ex = similar(px); Ey = similar(px); Ez = similar(px)
+    check(ccall((:sc_kick, libsc), Cint,
+                (Ptr{Cvoid}, CuPtr{P}, CuPtr{P}, CuPtr{P}, CuPtr{P}, Int64, Cint, Cint, CuPtr{P}, CuPtr{P},
+                 CuPtr{P}, Ptr{Cvoid}),
+                mesh.ptr, px, py, pz, pq, length(px), dtype_code(P), Cint(at_cathode), Ex, Ey, Ez, stream_ptr()))
+    return Ex, Ey, Ez
+end
+
+function ChainRulesCore.rrule(::typeof(kick), mesh::Mesh3D, px::CuArray{P}, py::CuArray{P}, pz::CuArray{P},
+                              pq::CuArray{P}; at_cathode::Bool=false) where {P<:Union{Float32,Float64}}
+    out = kick(mesh, px, py, pz, pq; at_cathode=at_cathode)
+    function kick_pullback(Δ)
+        gx, gy, gz = map(d -> d isa ChainRulesCore.AbstractZero ? CUDA.zeros(P, length(px)) : CuArray{P}(d),
+                         ChainRulesCore.unthunk(Δ))
+        dx = similar(px); dy = similar(px); dz = similar(px); dq = similar(px)
+        check(ccall((:sc_kick_adjoint, libsc), Cint,
+                    (Ptr{Cvoid}, CuPtr{P}, CuPtr{P}, CuPtr{P}, CuPtr{P}, Int64, Cint, Cint, CuPtr{P}, CuPtr{P},
+                     CuPtr{P}, Ptr{Cvoid}, CuPtr{P}, CuPtr{P}, CuPtr{P}, CuPtr{P}, Ptr{Cvoid}),
+                    mesh.ptr, px, py, pz, pq, length(px), dtype_code(P), Cint(at_cathode), gx, gy, gz, C_NULL,
+                    dx, dy, dz, dq, stream_ptr()))
+        return (ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), dx, dy, dz, dq)
+    end
+    return out, kick_pullback
+end
+
+function Base.show(io::IO, mesh::Mesh3D{T}) where {T}  # src/mesh.jl:267-273
+    nx, ny, nz = mesh.grid_size
+    lo, hi = mesh.min_bounds, mesh.max_bounds
+    print(io, "Mesh3D{$T, CuArray} ($(nx)x$(ny)x$(nz)) bounds=[($(lo[1]),$(lo[2]),$(lo[3])), " *
+              "($(hi[1]),$(hi[2]),$(hi[3]))] gamma=$(mesh.gamma)")
+end
+
+end # module

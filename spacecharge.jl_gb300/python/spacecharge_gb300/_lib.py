@@ -29,6 +29,9 @@ SC_DEPOSIT_ATOMIC = 0
 SC_DEPOSIT_SORTED = 1
 SC_DEPOSIT_DETERMINISTIC = 2
 
+SC_NUM_STAGES = 9
+STAGES = ["deposit", "green", "fwd_x", "fwd_y", "zpass", "inv_y", "inv_x", "gather", "plain_fft"]
+
 SC_LAYOUT_PLANAR = 0
 SC_LAYOUT_PACKED = 1
 
@@ -82,6 +85,10 @@ SIGNATURES = {
     "sc_solve": [_vp, _int, _vp],
     "sc_interpolate_field": [_vp, _vp, _vp, _vp, _i64, _int, _vp, _vp, _vp, _vp],
     "sc_kick": [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _vp, _vp, _vp, _vp],
+    "sc_mesh_set_profiling": [_vp, _int],
+    "sc_mesh_stage_times": [_vp, _dp, C.POINTER(_i64), _vp],
+    "sc_mesh_launch_count": [_vp, C.POINTER(_i64)],
+    "sc_kick_adjoint": [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "sc_cell_index": [_vp, _vp, _vp, _vp, _i64, _int, _vp, _vp, _vp],
     "sc_mesh_out_of_range": [_vp, C.POINTER(_i64), _vp],
 }

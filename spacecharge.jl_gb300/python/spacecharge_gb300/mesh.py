@@ -257,3 +257,85 @@ def kick(mesh: Mesh3D, particles_x, particles_y, particles_z, particles_q, at_ca
            C.c_void_p(q.data_ptr()), lens[0], dt, 1 if at_cathode else 0, C.c_void_p(ex.data_ptr()),
            C.c_void_p(ey.data_ptr()), C.c_void_p(ez.data_ptr()), _stream())
     return _return_like(particles_x, (ex, ey, ez))
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _packed_grid_grad(mesh: Mesh3D, g):
+    """dL/d(mesh.efield) given as (nx, ny, nz, 3) -> the mesh's packed
+    (nz, ny, nx, 4) device layout of its element type."""
+    torch = _torch()
+    if mesh.efield_layout != L.SC_LAYOUT_PACKED:
+        raise SpaceChargeError("grid gradients need a packed-layout mesh", L.SC_ERR_UNSUPPORTED)
+    dt = torch.float32 if mesh.T == np.float32 else torch.float64
+    nx, ny, nz = mesh.grid_size
+    g = torch.as_tensor(g, dtype=dt, device="cuda")
+    if tuple(g.shape) != (nx, ny, nz, 3):
+        raise SpaceChargeError(f"grid gradient must have shape {(nx, ny, nz, 3)}")
+    out = torch.zeros((nz, ny, nx, 4), dtype=dt, device="cuda")
+    out[..., :3] = g.permute(2, 1, 0, 3)
+    return out
+
+
+def kick_adjoint(mesh: Mesh3D, particles_x, particles_y, particles_z, particles_q, gEx=None, gEy=None, gEz=None,
+                 gEgrid=None, at_cathode: bool = False):
+    """Hand-written adjoint of kick(): d(loss)/d(x, y, z, q) from the
+    upstream gradients d(loss)/d(Ex, Ey, Ez) at the particles and, optionally,
+    d(loss)/d(mesh.efield) of shape (nx, ny, nz, 3).  Recomputes the forward
+    deposit and solve.  Returns device tensors of the particle dtype."""
+    torch = _torch()
+    lens = [_length(a) for a in (particles_x, particles_y, particles_z, particles_q)]
+    if not (lens[0] == lens[1] == lens[2] == lens[3]):
+        raise SpaceChargeError("Particle coordinate and charge arrays must have the same length.")
+    (x, y, z, q), dt = _as_device((particles_x, particles_y, particles_z, particles_q))
+    tdt = x.dtype
+    gs = []
+    for g in (gEx, gEy, gEz):
+        if g is None:
+            gs.append(None)
+        else:
+            t, _ = _as_device((g,), dtype=tdt)
+            if t[0].numel() != lens[0]:
+                raise SpaceChargeError("field gradients must have one entry per particle")
+            gs.append(t[0])
+    gg = _packed_grid_grad(mesh, gEgrid) if gEgrid is not None else None
+    outs = [torch.empty_like(x) for _ in range(4)]
+    L.call("sc_kick_adjoint", mesh.ptr, _ptr(x), _ptr(y), _ptr(z), _ptr(q), lens[0], dt, 1 if at_cathode else 0,
+           _ptr(gs[0]), _ptr(gs[1]), _ptr(gs[2]), _ptr(gg), *[_ptr(o) for o in outs], _stream())
+    return tuple(outs)
+
+
+def _make_kick_function():
+    torch = _torch()
+
+    class KickFunction(torch.autograd.Function):
+        """(x, y, z, q) -> (Ex, Ey, Ez) at the particles through the library,
+        with the hand-written adjoint as backward (mesh geometry fixed)."""
+
+        @staticmethod
+        def forward(ctx, mesh, x, y, z, q, at_cathode=False):
+            ctx.mesh = mesh
+            ctx.at_cathode = at_cathode
+            ctx.save_for_backward(x, y, z, q)
+            return kick(mesh, x.detach(), y.detach(), z.detach(), q.detach(), at_cathode=at_cathode)
+
+        @staticmethod
+        def backward(ctx, gx, gy, gz):
+            x, y, z, q = ctx.saved_tensors
+            dx, dy, dz, dq = kick_adjoint(ctx.mesh, x, y, z, q, gx, gy, gz, at_cathode=ctx.at_cathode)
+            return None, dx, dy, dz, dq, None
+
+    return KickFunction
+
+
+_KICK_FN = None
+
+
+def kick_autograd(mesh: Mesh3D, x, y, z, q, at_cathode: bool = False):
+    """Differentiable kick on CUDA tensors (torch.autograd)."""
+    global _KICK_FN
+    if _KICK_FN is None:
+        _KICK_FN = _make_kick_function()
+    return _KICK_FN.apply(mesh, x, y, z, q, at_cathode)

@@ -70,7 +70,8 @@ def test_auto_bounds_match_oracle(sc, cuda, prec):
 
 
 @pytest.mark.parametrize("prec", PRECS)
-@pytest.mark.parametrize("grid,gamma", [((16, 16, 24), 2.0), ((10, 12, 7), 1.0), ((8, 8, 8), 10.0)])
+@pytest.mark.parametrize("grid,gamma", [((16, 16, 24), 2.0), ((10, 12, 7), 1.0), ((8, 8, 8), 10.0),
+                                        ((12, 12, 40), 50.0), ((33, 17, 9), 1.0)])
 def test_kick_parity(sc, cuda, prec, grid, gamma):
     n = 6000
     x, y, z = bunch(n, 11, sig=(1e-3, 0.7e-3, 1.5e-3))
@@ -208,12 +209,24 @@ def test_reference_gpu_suite(sc, cuda, prec):
     m.efield[...] = 1.0
     e = sc.interpolate_field(m, [0.0, 1.0], [0.0, 1.0], [0.0, 1.0])
     assert all(np.allclose(v, 1.0, rtol=1e-6) for v in e)
-    # Point charge field at the centre (test_interpolation.jl:87-112)
+    # Point charge field at the charge (test_interpolation.jl:87-112).  The
+    # reference asserts |E| > 1e7 at the charge's own node, where the exact
+    # field is 0 by symmetry: its 7e7 V/m there is FP64 FFT rounding next to
+    # 8.5e21 V/m one node away (oracle: test_interp_computed_field).  The plain
+    # path runs the reference's algorithm and reproduces it; the hand-written
+    # pipelines keep the kernel's odd symmetry exactly, so the self-field
+    # vanishes relative to the neighbouring field, which is > 1e7.
     m = sc.Mesh3D((8, 8, 8), [0.0], [0.0], [0.0], precision=prec)
     sc.deposit(m, [0.0], [0.0], [0.0], [1.0])
     sc.solve(m)
     e = sc.interpolate_field(m, [0.0], [0.0], [0.0])
-    assert all(abs(v[0]) > 1e7 for v in e)
+    ef = host(m.efield)
+    near = min(abs(ef[1, 0, 0, 0]), abs(ef[0, 1, 0, 1]), abs(ef[0, 0, 1, 2]))
+    assert near > 1e7
+    if prec == "plain64":
+        assert all(abs(v[0]) > 1e7 for v in e)
+    else:
+        assert all(abs(v[0]) < (1e-12 if prec == "fp64" else 1e-6) * near for v in e)
     # Cathode and gamma change the field (test_solvers.jl:33-78)
     a = sc.Mesh3D((16, 16, 16), [0.0], [0.0], [0.01], precision=prec, gamma=2.0)
     b = sc.Mesh3D((16, 16, 16), [0.0], [0.0], [0.01], precision=prec, gamma=2.0)
