@@ -295,6 +295,24 @@ def main():
             h.copy_(d, non_blocking=True)
 
     ms_e2e = max_over_ranks(timed(e2e_step, args.steps, args.warmup), ws)
+
+    # ---- gradient: hand-written adjoint of the kick for the loss
+    #      L = sum_i q_i Ez(x_i)^2 + eps0/2 sum_n |E_n|^2 dV
+    #      (upstream dL/dEz_i = 2 q_i Ez_i, dL/dE_n = eps0 dV E_n)
+    kick(mm)()
+    eps0 = 8.8541878128e-12
+    dV = float(np.prod([(BOUNDS[1][d] - BOUNDS[0][d]) / (GRID[d] - 1) for d in range(3)]))
+    gez = (2.0 * dev[3] * ez).contiguous()
+    gg = torch.zeros((GRID[2], GRID[1], GRID[0], 4), dtype=torch.float32, device="cuda")
+    gg[..., :3] = (eps0 * dV) * mm.efield.permute(2, 1, 0, 3)
+    dxyzq = [torch.empty_like(dev[0]) for _ in range(4)]
+
+    def grad_step():
+        L.call("sc_kick_adjoint", mm.ptr, *[C.c_void_p(t.data_ptr()) for t in dev[:4]], NP, L.SC_F64, 0, None,
+               None, C.c_void_p(gez.data_ptr()), C.c_void_p(gg.data_ptr()),
+               *[C.c_void_p(t.data_ptr()) for t in dxyzq], C.c_void_p(stream.cuda_stream))
+
+    ms_grad = max_over_ranks(timed(grad_step, args.steps, args.warmup), ws)
     clocks = sampler.stop()
 
     # ---- roofline of the dominant stage (CUDA events inside the timed loop)
@@ -344,7 +362,9 @@ def main():
         "ms_green_cached": round(ms_cached, 4),
         "max_rel_err_vs_fp64": {"mesh": err_grid[0], "particles": err_part[0]},
         "rms_rel_err_vs_fp64": {"mesh": err_grid[1], "particles": err_part[1]},
-        "grad_ms": None,
+        "grad_ms": round(ms_grad, 4),
+        "grad_over_forward": round(ms_grad / ms_mixed, 3),
+        "grad_loss": "sum_i q_i Ez_i^2 + eps0/2 sum |E|^2 dV (adjoint recomputes deposit+solve)",
         "particles_per_s": round(ws * NP / (ms_mixed * 1e-3), 1),
         "kick_algorithmic_bytes": kick_bytes,
         "kick_GBps": round(kick_bytes / (ms_mixed * 1e-3) / 1e9, 1),

@@ -265,6 +265,7 @@ int sc_mesh_destroy(sc_mesh* m) {
     else
         native_release(m);
     m->timer.release();
+    sorted_release(m);
     cudaFree(m->rho);
     cudaFree(m->efield);
     cudaFree(m->oob);

@@ -273,7 +273,38 @@ struct OctantGeom {
     double hmax;         // half of the largest width
     double scale;        // FPEI / (Lx Ly Lz)
     int64_t cs;          // component stride of the output
+    // FP32 copies for the quadrature branch, in units of hmax
+    float ux, uy, uz;    // cell widths / hmax
+    float uoff;          // offw / hmax
+    float kxy, kz;       // gamma_c * scale / (8 hmax^2), per component group
+    // box of cells (ix < nbx, iy < nby, bz0 <= dz < bz1) holding every near
+    // cell, with the FP64 antiderivative on its corners precomputed in fnear
+    int nbx, nby, bz0, bz1;
+    const double* fnear;  // [3][(bz1-bz0+1)][nby+1][nbx+1]
 };
+
+// FP64 antiderivative F * factor at the corners of the near box, one
+// evaluation per thread so that the FP64 pipe's long per-warp issue time is
+// spread over many warps and SMs (green_functions.jl:35-38, 69-101 with the
+// reference's corner coordinates u = i0*dx + (1 - 2n)*dx/2, i0 = e + n - 1).
+__global__ void __launch_bounds__(32) k_igf_near_F(double* __restrict__ F, OctantGeom g) {
+    const int cx = g.nbx + 1, cy = g.nby + 1, cz = g.bz1 - g.bz0 + 1;
+    const int64_t per = (int64_t)cx * cy * cz;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= 3 * per) return;
+    const int c = (int)(t / per);
+    const int64_t e = t - c * per;
+    const int ex = (int)(e % cx), ey = (int)((e / cx) % cy), ez = (int)(e / ((int64_t)cx * cy)) + g.bz0;
+    const double umin = (double)(1 - 2 * g.nx) * g.dx / 2;
+    const double vmin = (double)(1 - 2 * g.ny) * g.dy / 2;
+    const double wmin = (double)(1 - 2 * g.nz) * g.dz / 2 + g.offw;
+    const double u = (double)(ex + g.nx - 1) * g.dx + umin;
+    const double v = (double)(ey + g.ny - 1) * g.dy + vmin;
+    const double w = (double)(ez + g.nz - 1) * g.dz + wmin;
+    const double fxy = g.gamma / (g.dx * g.dy * g.dz), fz = 1.0 / (g.dx * g.dy * g.dz);
+    const double val = c == 0 ? field_green_n(u, v, w) : c == 1 ? field_green_n(v, w, u) : field_green_n(w, u, v);
+    F[t] = val * (c == 2 ? fz : fxy);
+}
 
 __device__ __forceinline__ void gl_accumulate(float cx, float cy, float cz, float hx, float hy, float hz,
                                               const float* t, const float* w, int m, float& ax, float& ay,
@@ -305,36 +336,23 @@ __global__ void __launch_bounds__(256) k_igf_octant(float* __restrict__ G, Octan
     const int iy = (int)((t / g.nx) % g.ny);
     const int iz = (int)(t / ((int64_t)g.nx * g.ny));
     const int dz = g.image ? iz - (g.nz - 1) : iz;
-    const double cx = ix * g.dx, cy = iy * g.dy, cz = dz * g.dz + g.offw;
-    const double R = sqrt(cx * cx + cy * cy + cz * cz);
-    const double ratio = R / g.hmax;
-    double G3[3];
-    if (ratio < kNearRatio) {
-        // reference corner coordinates: point i0 = d + n - 1 (+1) of the
-        // doubled grid, u = i0*dx + (1 - 2n)*dx/2 (+ offset*gamma on w)
-        const double umin = (double)(1 - 2 * g.nx) * g.dx / 2;
-        const double vmin = (double)(1 - 2 * g.ny) * g.dy / 2;
-        const double wmin = (double)(1 - 2 * g.nz) * g.dz / 2 + g.offw;
-        double u[2], v[2], w[2];
-        for (int a = 0; a < 2; ++a) {
-            u[a] = (double)(ix + g.nx - 1 + a) * g.dx + umin;
-            v[a] = (double)(iy + g.ny - 1 + a) * g.dy + vmin;
-            w[a] = (double)(dz + g.nz - 1 + a) * g.dz + wmin;
-        }
-        const double fxy = g.gamma / (g.dx * g.dy * g.dz), fz = 1.0 / (g.dx * g.dy * g.dz);
+    // cell centre in units of hmax (FP32: only decides near/far and feeds
+    // the quadrature, whose own error is ~1e-7)
+    const float px = (float)ix * g.ux, py = (float)iy * g.uy, pz = fmaf((float)dz, g.uz, g.uoff);
+    const float ratio = sqrtf(fmaf(px, px, fmaf(py, py, pz * pz)));
+    float out[3];
+    const bool inbox = ix < g.nbx && iy < g.nby && dz >= g.bz0 && dz < g.bz1;
+    if (ratio < (float)kNearRatio && inbox) {
+        // 8-point difference of the precomputed corners, green_functions.jl:108-111
+        const int cx = g.nbx + 1, cy = g.nby + 1, cz = g.bz1 - g.bz0 + 1;
+        const int64_t per = (int64_t)cx * cy * cz;
+        const int64_t sy = cx, sz = (int64_t)cx * cy;
         for (int c = 0; c < 3; ++c) {
-            double F[2][2][2];
-            for (int a = 0; a < 2; ++a)
-                for (int b = 0; b < 2; ++b)
-                    for (int e = 0; e < 2; ++e) {
-                        const double val = c == 0 ? field_green_n(u[a], v[b], w[e])
-                                         : c == 1 ? field_green_n(v[b], w[e], u[a])
-                                                  : field_green_n(w[e], u[a], v[b]);
-                        F[a][b][e] = val * (c == 2 ? fz : fxy);
-                    }
-            // green_functions.jl:108-111
-            G3[c] = F[1][1][1] - F[0][1][1] - F[1][0][1] - F[1][1][0] - F[0][0][0] + F[0][0][1] + F[0][1][0] +
-                    F[1][0][0];
+            const double* f = g.fnear + c * per + ix + sy * iy + sz * (dz - g.bz0);
+            auto F = [&](int a, int b, int e) { return f[a + sy * b + sz * e]; };
+            const double G3 = F(1, 1, 1) - F(0, 1, 1) - F(1, 0, 1) - F(1, 1, 0) - F(0, 0, 0) + F(0, 0, 1) +
+                              F(0, 1, 0) + F(1, 0, 0);
+            out[c] = (float)(G3 * g.scale);
         }
     } else {
         const float t4[4] = {-0.86113631159405258f, -0.33998104358485626f, 0.33998104358485626f,
@@ -343,21 +361,18 @@ __global__ void __launch_bounds__(256) k_igf_octant(float* __restrict__ G, Octan
                              0.34785484513745386f};
         const float t3[3] = {-0.77459666924148338f, 0.0f, 0.77459666924148338f};
         const float w3[3] = {0.55555555555555556f, 0.88888888888888889f, 0.55555555555555556f};
-        const double sc = 1.0 / g.hmax;
-        const float px = (float)(cx * sc), py = (float)(cy * sc), pz = (float)(cz * sc);
-        const float hx = (float)(0.5 * g.dx * sc), hy = (float)(0.5 * g.dy * sc), hz = (float)(0.5 * g.dz * sc);
+        const float hx = 0.5f * g.ux, hy = 0.5f * g.uy, hz = 0.5f * g.uz;
         float ax = 0.f, ay = 0.f, az = 0.f;
-        if (ratio < kQ3Ratio)
+        if (ratio < (float)kQ3Ratio)
             gl_accumulate(px, py, pz, hx, hy, hz, t4, w4, 4, ax, ay, az);
         else
             gl_accumulate(px, py, pz, hx, hy, hz, t3, w3, 3, ax, ay, az);
-        // G_c = gamma_c / 8 * sum w w w p'_c / r'^3 / hmax^2
-        const double k = 0.125 * sc * sc;
-        G3[0] = g.gamma * k * ax;
-        G3[1] = g.gamma * k * ay;
-        G3[2] = k * az;
+        // G_c = gamma_c / 8 * sum w w w p'_c / r'^3 / hmax^2, times FPEI/(L^3)
+        out[0] = g.kxy * ax;
+        out[1] = g.kxy * ay;
+        out[2] = g.kz * az;
     }
-    for (int c = 0; c < 3; ++c) G[c * g.cs + t] = (float)(G3[c] * g.scale);
+    for (int c = 0; c < 3; ++c) G[c * g.cs + t] = out[c];
 }
 
 // Rows of the L grid that hold kernel values: displacement index c in
@@ -376,27 +391,43 @@ __global__ void __launch_bounds__(256) k_green_x(const float* __restrict__ G, fl
     const int n = P << logLx;
     float2* a = reinterpret_cast<float2*>(smraw);
     float2* b = a + n;
+    int* meta = reinterpret_cast<int*>(b + n);  // per row: source offset, sign flags, output row
     const int comp = blockIdx.y;
     const float* Gc = G + comp * gcs;
     const int rows = (2 * ny - 1) * (2 * nz - 1);
     const int pair0 = blockIdx.x << lgP;
+    for (int h = threadIdx.x; h < 2 * P; h += blockDim.x) {
+        const int r = 2 * pair0 + h;
+        int src = -1, neg = 0, orow = 0;
+        if (r < rows) {
+            const int cy = r % (2 * ny - 1), cz = r / (2 * ny - 1);
+            const int dy = cy < ny ? cy : cy - (2 * ny - 1);
+            const int dz = cz < nz ? cz : cz - (2 * nz - 1);
+            const int ay = dy < 0 ? -dy : dy;
+            const int iz = image ? dz + nz - 1 : (dz < 0 ? -dz : dz);
+            src = nx * (ay + ny * iz);
+            // parity: comp 0 odd in x (per element), comp 1 odd in y, comp 2 odd in z (free space)
+            neg = (comp == 1 && dy < 0) || (comp == 2 && !image && dz < 0);
+            orow = wrap_row(cy, ny, Ly) + Ly * wrap_row(cz, nz, Lz);
+        }
+        meta[3 * h] = src;
+        meta[3 * h + 1] = neg;
+        meta[3 * h + 2] = orow;
+    }
+    __syncthreads();
     for (int it = threadIdx.x; it < n; it += blockDim.x) {
         const int p = it >> logLx, x = it & (Lx - 1);
         float v[2] = {0.f, 0.f};
         const int dx = x < nx ? x : (x > Lx - nx ? x - Lx : Lx);
         if (dx != Lx) {
+            const int ax = dx < 0 ? -dx : dx;
+            const bool xneg = comp == 0 && dx < 0;
+#pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int r = 2 * (pair0 + p) + h;
-                if (r >= rows) continue;
-                const int cy = r % (2 * ny - 1), cz = r / (2 * ny - 1);
-                const int dy = cy < ny ? cy : cy - (2 * ny - 1);
-                const int dz = cz < nz ? cz : cz - (2 * nz - 1);
-                const int ax = dx < 0 ? -dx : dx, ay = dy < 0 ? -dy : dy;
-                const int iz = image ? dz + nz - 1 : (dz < 0 ? -dz : dz);
-                float val = Gc[ax + (int64_t)nx * (ay + (int64_t)ny * iz)];
-                const int sgn = comp == 0 ? dx : comp == 1 ? dy : (image ? 0 : dz);
-                if (sgn < 0) val = -val;
-                v[h] = val;
+                const int src = meta[3 * (2 * p + h)];
+                if (src < 0) continue;
+                const float val = Gc[src + ax];
+                v[h] = (xneg != (meta[3 * (2 * p + h) + 1] != 0)) ? -val : val;
             }
         }
         a[(x << lgP) + p] = make_float2(v[0], v[1]);
@@ -407,16 +438,15 @@ __global__ void __launch_bounds__(256) k_green_x(const float* __restrict__ G, fl
     const int lgh = logLx - 1, half = Lx >> 1;
     for (int it = threadIdx.x; it < (P << lgh); it += blockDim.x) {
         const int p = it >> lgh, k0 = it & (half - 1);
-        const int r0 = 2 * (pair0 + p), r1 = r0 + 1;
-        if (r0 >= rows) continue;
-        const int y0 = wrap_row(r0 % (2 * ny - 1), ny, Ly), z0 = wrap_row(r0 / (2 * ny - 1), nz, Lz);
-        const int y1 = wrap_row(r1 % (2 * ny - 1), ny, Ly), z1 = wrap_row(r1 / (2 * ny - 1), nz, Lz);
+        if (meta[3 * (2 * p)] < 0) continue;
+        const int o0 = meta[3 * (2 * p) + 2], o1 = meta[3 * (2 * p + 1) + 2];
+        const bool has1 = meta[3 * (2 * p + 1)] >= 0;
         for (int e = 0; e < (k0 == 0 ? 2 : 1); ++e) {
             const int k = e ? half : k0;
             float2 xa, xb;
             split_pair(res[(k << lgP) + p], res[(((Lx - k) & (Lx - 1)) << lgP) + p], xa, xb);
-            Sc[(int64_t)(y0 + (int64_t)Ly * z0) * Hx + k] = xa;
-            if (r1 < rows) Sc[(int64_t)(y1 + (int64_t)Ly * z1) * Hx + k] = xb;
+            Sc[(int64_t)o0 * Hx + k] = xa;
+            if (has1) Sc[(int64_t)o1 * Hx + k] = xb;
         }
     }
 }
@@ -578,6 +608,34 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
     g.hmax = 0.5 * fmax(g.dx, fmax(g.dy, g.dz));
     g.scale = kFpei / ((double)Lx * Ly * Lz);
     g.cs = gcs;
+    g.ux = (float)(g.dx / g.hmax);
+    g.uy = (float)(g.dy / g.hmax);
+    g.uz = (float)(g.dz / g.hmax);
+    g.uoff = (float)(g.offw / g.hmax);
+    g.kxy = (float)(g.gamma * g.scale / (8.0 * g.hmax * g.hmax));
+    g.kz = (float)(g.scale / (8.0 * g.hmax * g.hmax));
+    // near box: every cell with |centre| < kNearRatio * hmax, plus a margin
+    {
+        const double reach = kNearRatio * g.hmax;
+        g.nbx = (int)fmin((double)nx, floor(reach / g.dx) + 2.0);
+        g.nby = (int)fmin((double)ny, floor(reach / g.dy) + 2.0);
+        const int dzmin = image ? -(nz - 1) : 0;
+        g.bz0 = (int)fmax((double)dzmin, floor((-reach - g.offw) / g.dz) - 1.0);
+        g.bz1 = (int)fmin((double)nz, ceil((reach - g.offw) / g.dz) + 2.0);
+        if (g.bz1 <= g.bz0) g.nbx = g.nby = 0, g.bz0 = g.bz1 = 0;
+    }
+    const int64_t nfar = 3 * (int64_t)(g.nbx + 1) * (g.nby + 1) * (g.bz1 - g.bz0 + 1);
+    if (w.fnear_cap < nfar) {
+        cudaFree(w.fnear);
+        w.fnear = nullptr;
+        SC_CUDA(cudaMalloc(&w.fnear, sizeof(double) * nfar));
+        w.fnear_cap = nfar;
+    }
+    g.fnear = w.fnear;
+    if (g.nbx > 0 && g.nby > 0) {
+        k_igf_near_F<<<(nfar + 31) / 32, 32, 0, s>>>(w.fnear, g);
+        SC_LAUNCH_CHECK("k_igf_near_F");
+    }
     const int zc = image ? 2 * nz - 1 : nz;
     const int64_t cells = (int64_t)nx * ny * zc;
     k_igf_octant<<<(cells + 255) / 256, 256, 0, s>>>((float*)w.goct, g);
@@ -586,7 +644,7 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
     {
         const int lgP = pick_rows(w.log2L[0]);
         const int P = 1 << lgP;
-        const size_t smem = sizeof(float2) * 2 * P * Lx;
+        const size_t smem = sizeof(float2) * 2 * P * Lx + sizeof(int) * 6 * P;
         SC_TRY(set_smem(k_green_x, smem));
         const int rows = (2 * ny - 1) * (2 * nz - 1);
         dim3 grid(((rows + 1) / 2 + P - 1) / P, 3);
@@ -614,7 +672,7 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
         k_green_z<<<grid, 256, smem, s>>>(S, dst, nz, g.image, Ly, Lz, w.log2L[2], Hx, lgW, scs, dcs, tw);
         SC_LAUNCH_CHECK("k_green_z");
     }
-    m->launches += 4;
+    m->launches += 5;
     return SC_OK;
 }
 
@@ -763,7 +821,7 @@ int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s) {
 
 int native_release(sc_mesh* m) {
     NativeWork& w = m->nw;
-    void* ptrs[] = {w.A, w.B, w.C, w.D, w.adjE, w.fcorner, w.kgrid, w.kspec, w.goct, w.gspec, w.gfree, w.gimg};
+    void* ptrs[] = {w.A, w.B, w.C, w.D, w.adjE, w.fnear, w.fcorner, w.kgrid, w.kspec, w.goct, w.gspec, w.gfree, w.gimg};
     for (void* p : ptrs) cudaFree(p);
     int L[3] = {w.L[0], w.L[1], w.L[2]};
     int lg[3] = {w.log2L[0], w.log2L[1], w.log2L[2]};

