@@ -196,6 +196,28 @@ int sc_kick_adjoint(sc_mesh* mesh, const void* x, const void* y, const void* z, 
                     int dtype, int at_cathode, const void* gex, const void* gey, const void* gez,
                     const void* ggrid, void* dx, void* dy, void* dz, void* dq, void* stream);
 
+/* Allocation-free free-space solve.  This entry point has no counterpart in
+ * the reference.  It is for callers that cannot let a library call
+ * cudaMalloc: a host code that owns all device memory through its own pool,
+ * or a loop that forbids device allocation once it is running.  It computes
+ * the same field as sc_solve(at_cathode = 0) on an SC_PREC_MIXED mesh of
+ * this grid, delta and gamma (Green function rebuilt on every call), from
+ * the caller's rho (FP32, nx*ny*nz, x fastest) into the caller's efield
+ * (FP32, packed (4, nx, ny, nz) = (Ex, Ey, Ez, 0) per node).  It calls no
+ * cudaMalloc, cudaFree or allocating library routine: its workspace is one
+ * file-scope device array of about 8.6 MB, which every GPU that loads the
+ * library holds until exit.
+ *  - Grids are limited to 32 nodes per axis; larger ones return
+ *    SC_ERR_UNSUPPORTED with a message naming the limit.
+ *  - The first call on a device looks up the array's device address and
+ *    uploads an 8 KB twiddle table (synchronous); make that first call
+ *    before any stream capture.
+ *  - All calls on a device share the array and it keeps the last call's
+ *    contents; calls that overlap on the GPU (other streams, other host
+ *    threads) race and must be serialised by the caller. */
+int sc_solve_noalloc(const int32_t grid_size[3], const double delta[3], double gamma, const float* rho,
+                     float* efield, void* stream);
+
 /* Number of particles skipped as out of range since the last call
  * (deposit and interpolate); resets the counter.  Synchronises `stream`. */
 int sc_mesh_out_of_range(sc_mesh* mesh, int64_t* count, void* stream);

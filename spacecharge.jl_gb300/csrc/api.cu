@@ -420,6 +420,12 @@ int sc_cell_index(sc_mesh* m, const void* x, const void* y, const void* z, int64
     return cell_index_launch(m, x, y, z, n, dtype, idx, frac, (cudaStream_t)stream);
 }
 
+int sc_solve_noalloc(const int32_t grid_size[3], const double delta[3], double gamma, const float* rho,
+                     float* efield, void* stream) {
+    if (!grid_size || !delta || !rho || !efield) return fail(SC_ERR_INVALID, "NULL argument");
+    return native_solve_noalloc(grid_size, delta, gamma, rho, efield, (cudaStream_t)stream);
+}
+
 int sc_mesh_out_of_range(sc_mesh* m, int64_t* count, void* stream) {
     SC_TRY(check_mesh(m));
     DeviceGuard g(m->device);

@@ -26,6 +26,8 @@
 // into it, so the inverse passes produce E directly.
 #include <math.h>
 
+#include <mutex>
+
 #include "pipeline.cuh"
 
 namespace sc {
@@ -834,6 +836,212 @@ int native_release(sc_mesh* m) {
     }
     w.Hx = Hx;
     w.elem = el;
+    return SC_OK;
+}
+
+// ------------------------------------------------ allocation-free solve
+// sc_solve_noalloc: the mixed-precision free-space solve of a caller's rho
+// into a caller's packed efield with every intermediate (FFT workspace,
+// Green-function build, twiddle table) in one file-scope device array.  It
+// serves callers that cannot let a library call cudaMalloc: host codes that
+// own all device memory through their own pool, and loops that forbid device
+// allocation once they are running.  Grids up to kNaMaxN nodes per axis.
+// The array is shared by every call on a device and keeps the last call's
+// contents; every buffer a call reads is written earlier in the same call,
+// so nothing needs clearing, but calls that overlap on the GPU race.
+constexpr int kNaMaxN = 32;                     // nodes per axis
+constexpr int kNaMaxL = 64;                     // transform length per axis
+constexpr int kNaMaxHx = kNaMaxL / 2 + 1;
+constexpr size_t na_up(size_t b) { return (b + 255) / 256 * 256; }
+constexpr size_t kNaA = na_up(sizeof(float2) * kNaMaxHx * kNaMaxN * kNaMaxN);
+constexpr size_t kNaB = na_up(sizeof(float2) * kNaMaxHx * kNaMaxL * kNaMaxN);
+constexpr size_t kNaC = 3 * kNaB;
+constexpr size_t kNaD = 3 * kNaA;
+constexpr size_t kNaGoct = na_up(sizeof(float) * 3 * kNaMaxN * kNaMaxN * (2 * kNaMaxN - 1));
+constexpr size_t kNaGspec = na_up(sizeof(float2) * 3 * kNaMaxHx * kNaMaxL * kNaMaxL);
+constexpr size_t kNaGfree = na_up(sizeof(float) * 3 * kNaMaxHx * (kNaMaxL / 2 + 1) * (kNaMaxL / 2 + 1));
+constexpr size_t kNaFnear = na_up(sizeof(double) * 3 * (kNaMaxN + 1) * (kNaMaxN + 1) * (kNaMaxN + 1));
+constexpr size_t kNaTw = na_up(sizeof(float2) * kMaxL);
+constexpr size_t kNaBytes = kNaA + kNaB + kNaC + kNaD + kNaGoct + kNaGspec + kNaGfree + kNaFnear + kNaTw;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+// Device address of the array for the current device, looked up (and the
+// twiddle table uploaded) on the first call on that device.
+static std::mutex g_na_mu;
+static void* g_na_base[256] = {};
+
+static int noalloc_base(unsigned char** out) {
+    int dev = 0;
+    SC_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return fail(SC_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    if (!g_na_base[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        float2 tw[kMaxL];
+        for (int k = 0; k < kMaxL; ++k) {
+            long double a = -2.0L * 3.141592653589793238462643383279502884L * (long double)k / (long double)kMaxL;
+            tw[k] = make_float2((float)(double)cosl(a), (float)(double)sinl(a));
+        }
+        const size_t off = kNaBytes - kNaTw;
+        e = cudaMemcpy((unsigned char*)p + off, tw, sizeof(tw), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(e, "twiddle upload");
+        g_na_base[dev] = p;
+    }
+    *out = (unsigned char*)g_na_base[dev];
+    return SC_OK;
+}
+
+int native_solve_noalloc(const int32_t* grid, const double* delta, double gamma, const float* rho, float* efield,
+                         cudaStream_t s) {
+    for (int d = 0; d < 3; ++d) {
+        if (grid[d] <= 1) return fail(SC_ERR_INVALID, "All elements of grid_size must be at least 2.");
+        if (grid[d] > kNaMaxN)
+            return fail(SC_ERR_UNSUPPORTED,
+                        "sc_solve_noalloc handles at most %d nodes per axis (grid_size[%d] = %d); its fixed "
+                        "scratch is %zu bytes",
+                        kNaMaxN, d, grid[d], kNaBytes);
+        if (!(delta[d] > 0) || !isfinite(delta[d])) return fail(SC_ERR_INVALID, "delta must be positive and finite");
+    }
+    if (!(gamma > 0) || !isfinite(gamma)) return fail(SC_ERR_INVALID, "gamma must be a positive finite number");
+    unsigned char* base = nullptr;
+    SC_TRY(noalloc_base(&base));
+    float2* A = (float2*)base;
+    float2* B = (float2*)(base + kNaA);
+    float2* Cb = (float2*)(base + kNaA + kNaB);
+    float2* D = (float2*)(base + kNaA + kNaB + kNaC);
+    float* goct = (float*)(base + kNaA + kNaB + kNaC + kNaD);
+    float2* S = (float2*)(base + kNaA + kNaB + kNaC + kNaD + kNaGoct);
+    float* gfree = (float*)(base + kNaA + kNaB + kNaC + kNaD + kNaGoct + kNaGspec);
+    double* fnear = (double*)(base + kNaA + kNaB + kNaC + kNaD + kNaGoct + kNaGspec + kNaGfree);
+    const float2* tw = (const float2*)(base + kNaBytes - kNaTw);
+
+    const int nx = grid[0], ny = grid[1], nz = grid[2];
+    NativeWork w;  // sizes only; no buffer of it is used
+    for (int d = 0; d < 3; ++d) {
+        int L = 4;
+        while (L < 2 * grid[d] - 1) L *= 2;
+        w.L[d] = L;
+        w.log2L[d] = ilog2(L);
+    }
+    w.Hx = w.L[0] / 2 + 1;
+    const int Lx = w.L[0], Ly = w.L[1], Lz = w.L[2], Hx = w.Hx;
+    const int Hy = Ly / 2 + 1, Hz = Lz / 2 + 1;
+
+    // Green function: the same kernels as the mesh path (free space)
+    OctantGeom g;
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = nz;
+    g.image = 0;
+    g.dx = delta[0];
+    g.dy = delta[1];
+    g.dz = delta[2] * gamma;
+    g.offw = 0.0;
+    g.gamma = gamma;
+    g.hmax = 0.5 * fmax(g.dx, fmax(g.dy, g.dz));
+    g.scale = kFpei / ((double)Lx * Ly * Lz);
+    g.cs = (int64_t)nx * ny * (2 * nz - 1);
+    g.ux = (float)(g.dx / g.hmax);
+    g.uy = (float)(g.dy / g.hmax);
+    g.uz = (float)(g.dz / g.hmax);
+    g.uoff = 0.f;
+    g.kxy = (float)(g.gamma * g.scale / (8.0 * g.hmax * g.hmax));
+    g.kz = (float)(g.scale / (8.0 * g.hmax * g.hmax));
+    {
+        const double reach = kNearRatio * g.hmax;
+        g.nbx = (int)fmin((double)nx, floor(reach / g.dx) + 2.0);
+        g.nby = (int)fmin((double)ny, floor(reach / g.dy) + 2.0);
+        g.bz0 = 0;
+        g.bz1 = (int)fmin((double)nz, ceil(reach / g.dz) + 2.0);
+    }
+    g.fnear = fnear;
+    const int64_t nfar = 3 * (int64_t)(g.nbx + 1) * (g.nby + 1) * (g.bz1 - g.bz0 + 1);
+    k_igf_near_F<<<(nfar + 31) / 32, 32, 0, s>>>(fnear, g);
+    SC_LAUNCH_CHECK("k_igf_near_F");
+    const int64_t cells = (int64_t)nx * ny * nz;
+    k_igf_octant<<<(cells + 255) / 256, 256, 0, s>>>(goct, g);
+    SC_LAUNCH_CHECK("k_igf_octant");
+    const int64_t scs = (int64_t)Hx * Ly * Lz;
+    {
+        const int lgP = pick_rows(w.log2L[0]);
+        const int P = 1 << lgP;
+        const size_t smem = sizeof(float2) * 2 * P * Lx + sizeof(int) * 6 * P;
+        const int rows = (2 * ny - 1) * (2 * nz - 1);
+        dim3 gr(((rows + 1) / 2 + P - 1) / P, 3);
+        k_green_x<<<gr, 256, smem, s>>>(goct, S, nx, ny, nz, 0, Lx, w.log2L[0], Ly, Lz, Hx, lgP, g.cs, scs, tw);
+        SC_LAUNCH_CHECK("k_green_x");
+    }
+    {
+        const int lgW = pick_cols(w.log2L[1]);
+        const int W = 1 << lgW;
+        dim3 gr((Hx + W - 1) / W, 2 * nz - 1, 3);
+        k_green_y<<<gr, 256, sizeof(float2) * 2 * W * Ly, s>>>(S, ny, nz, Ly, w.log2L[1], Lz, Hx, lgW, scs, tw);
+        SC_LAUNCH_CHECK("k_green_y");
+    }
+    {
+        const int lgW = pick_cols(w.log2L[2]);
+        const int W = 1 << lgW;
+        dim3 gr((Hx + W - 1) / W, Hy, 3);
+        k_green_z<<<gr, 256, sizeof(float2) * 2 * W * Lz, s>>>(S, gfree, nz, 0, Ly, Lz, w.log2L[2], Hx, lgW, scs,
+                                                               (int64_t)Hx * Hy * Hz, tw);
+        SC_LAUNCH_CHECK("k_green_z");
+    }
+    // convolution passes, as the mesh path's solve_t<float>
+    const int rows = ny * nz;
+    {
+        const int lgP = pick_rows(w.log2L[0]);
+        const int P = 1 << lgP;
+        k_fwd_x<float><<<((rows + 1) / 2 + P - 1) / P, 256, sizeof(float2) * 2 * P * Lx, s>>>(
+            rho, A, nx, rows, Lx, w.log2L[0], Hx, lgP, tw);
+        SC_LAUNCH_CHECK("k_fwd_x");
+    }
+    {
+        const int lgW = pick_cols(w.log2L[1]);
+        const int W = 1 << lgW;
+        dim3 gr((Hx + W - 1) / W, nz, 1);
+        k_col_fft<false, float><<<gr, 256, sizeof(float2) * 2 * W * Ly, s>>>(
+            A, B, Hx, lgW, Ly, w.log2L[1], ny, Ly, Hx, (int64_t)Hx * ny, 0, Hx, (int64_t)Hx * Ly, 0, tw);
+        SC_LAUNCH_CHECK("k_col_fft");
+    }
+    {
+        GreenView gv;
+        gv.gfree = gfree;
+        gv.gimg = nullptr;
+        gv.Hx = Hx;
+        gv.Hy = Hy;
+        gv.Hz = Hz;
+        gv.Ly = Ly;
+        gv.Lz = Lz;
+        gv.cs_free = (int64_t)Hx * Hy * Hz;
+        gv.cs_img = 0;
+        gv.image = 0;
+        const int lgW = pick_cols(w.log2L[2]);
+        const int W = 1 << lgW;
+        dim3 gr((Hx + W - 1) / W, Ly);
+        k_zpass<float><<<gr, 256, sizeof(float2) * 3 * W * Lz, s>>>(B, Cb, Hx, Ly, nz, Lz, w.log2L[2], lgW, gv, tw);
+        SC_LAUNCH_CHECK("k_zpass");
+    }
+    {
+        const int lgW = pick_cols(w.log2L[1]);
+        const int W = 1 << lgW;
+        dim3 gr((Hx + W - 1) / W, nz, 3);
+        k_col_fft<true, float><<<gr, 256, sizeof(float2) * 2 * W * Ly, s>>>(
+            Cb, D, Hx, lgW, Ly, w.log2L[1], Ly, ny, Hx, (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, Hx, (int64_t)Hx * ny,
+            (int64_t)Hx * ny * nz, tw);
+        SC_LAUNCH_CHECK("k_col_fft");
+    }
+    {
+        const int lgP = pick_rows(w.log2L[0]);
+        const int P = 1 << lgP;
+        const size_t smem = sizeof(float2) * 5 * P * Lx;
+        SC_CUDA(cudaFuncSetAttribute(k_inv_x<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_inv_x<float><<<((rows + 1) / 2 + P - 1) / P, 256, smem, s>>>(D, (float4*)efield, nx, rows, Lx, w.log2L[0],
+                                                                       Hx, lgP, (int64_t)Hx * rows, tw);
+        SC_LAUNCH_CHECK("k_inv_x");
+    }
     return SC_OK;
 }
 

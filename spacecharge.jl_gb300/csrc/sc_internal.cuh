@@ -183,6 +183,8 @@ int plain_release(sc_mesh* m);
 int native_prepare(sc_mesh* m);  // sizes only (no allocation)
 int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s);
 int native_ensure_green(sc_mesh* m, int at_cathode, cudaStream_t s);
+int native_solve_noalloc(const int32_t* grid, const double* delta, double gamma, const float* rho, float* efield,
+                         cudaStream_t s);
 int adjoint_launch(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
                    int at_cathode, const void* gex, const void* gey, const void* gez, const void* ggrid, void* dx,
                    void* dy, void* dz, void* dq, cudaStream_t s);

@@ -89,6 +89,7 @@ SIGNATURES = {
     "sc_mesh_stage_times": [_vp, _dp, C.POINTER(_i64), _vp],
     "sc_mesh_launch_count": [_vp, C.POINTER(_i64)],
     "sc_kick_adjoint": [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "sc_solve_noalloc": [_i32p, _dp, C.c_double, _vp, _vp, _vp],
     "sc_cell_index": [_vp, _vp, _vp, _vp, _i64, _int, _vp, _vp, _vp],
     "sc_mesh_out_of_range": [_vp, C.POINTER(_i64), _vp],
 }
