@@ -145,6 +145,86 @@ def barrier(ws):
         dist.barrier()
 
 
+# ------------------------------------------------------ batched bunches
+BATCH_GRIDS = [(32, 32, 32), (64, 64, 64), (64, 64, 128), (128, 128, 128)]
+
+
+def make_batch(nb=64, seed=7):
+    """64 independent Gaussian bunches: particle counts log-uniform in
+    [1e4, 2e6], sigma uniform in [0.2, 2] mm per axis, gamma uniform in
+    [1, 50], charge uniform in [10 pC, 1 nC], grid drawn from BATCH_GRIDS."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(nb):
+        n = int(np.exp(rng.uniform(np.log(1e4), np.log(2e6))))
+        sig = rng.uniform(0.2e-3, 2e-3, 3)
+        gamma = float(rng.uniform(1.0, 50.0))
+        qtot = float(rng.uniform(10e-12, 1e-9))
+        grid = BATCH_GRIDS[int(rng.integers(0, len(BATCH_GRIDS)))]
+        v = rng.standard_normal((3, n)) * sig[:, None]
+        out.append((grid, gamma, v[0].copy(), v[1].copy(), v[2].copy(), np.full(n, qtot / n)))
+    return out
+
+
+def bench_batch(sc, L, C, torch, flush, stream, ws, rank, steps, warmup):
+    """Batched graph kick of this rank's shard of 64 bunches against the same
+    bunches kicked one by one (mixed) and with the plain FP64 path."""
+    from spacecharge_gb300.shard import shard_bunches
+
+    spec_all = make_batch()
+    mine = shard_bunches([len(s[2]) for s in spec_all], ws, rank)
+    spec = [spec_all[i] for i in mine]
+    dev = [[torch.from_numpy(a).cuda() for a in s[2:]] for s in spec]
+    meshes = [sc.Mesh3D(g, d[0], d[1], d[2], precision="mixed", gamma=gm) for (g, gm, *_), d in zip(spec, dev)]
+    batch = sc.Batch(meshes)
+    xs, ys, zs, qs = zip(*dev)
+
+    def ev_time(fn, reps):
+        times = []
+        for _ in range(reps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            times.append(a.elapsed_time(b))
+        return float(np.mean(times))
+
+    for _ in range(max(2, warmup)):
+        batch.kick(xs, ys, zs, qs)  # first call eager + capture, then replays
+    torch.cuda.synchronize()
+    ms_batch = max_over_ranks(ev_time(lambda: batch.kick(xs, ys, zs, qs), steps), ws)
+    nodes = batch.graph_nodes
+
+    outs = [[torch.empty_like(d[0]) for _ in range(3)] for d in dev]
+
+    def seq_mixed():
+        for m, d, o in zip(meshes, dev, outs):
+            L.call("sc_kick", m.ptr, *[C.c_void_p(t.data_ptr()) for t in d], d[0].numel(), L.SC_F64, 0,
+                   *[C.c_void_p(t.data_ptr()) for t in o], C.c_void_p(stream.cuda_stream))
+
+    seq_mixed()
+    ms_seq = max_over_ranks(ev_time(seq_mixed, max(2, steps // 4)), ws)
+    # plain FP64 path, one bunch at a time (meshes created and freed outside the timed region)
+    ms_plain = 0.0
+    for (g, gm, *_), d, o in zip(spec, dev, outs):
+        mp = sc.Mesh3D(g, d[0], d[1], d[2], precision="plain64", gamma=gm)
+        k = lambda: L.call("sc_kick", mp.ptr, *[C.c_void_p(t.data_ptr()) for t in d], d[0].numel(), L.SC_F64, 0,
+                           *[C.c_void_p(t.data_ptr()) for t in o], C.c_void_p(stream.cuda_stream))
+        k()
+        ms_plain += ev_time(k, 1)
+        del mp
+    ms_plain = max_over_ranks(ms_plain, ws)
+    npart = sum(len(s[2]) for s in spec)
+    del batch
+    return {"bunches": len(spec), "bunches_total": len(spec_all), "particles": npart,
+            "grids": sorted({str(s[0]) for s in spec}), "ms_batched_graph": round(ms_batch, 3),
+            "ms_sequential_mixed": round(ms_seq, 3), "ms_sequential_fp64_plain": round(ms_plain, 3),
+            "speedup_vs_fp64_plain": round(ms_plain / ms_batch, 2), "graph_nodes": nodes,
+            "green": "cached per bunch (fixed geometry)", "l2": "flushed between calls"}
+
+
 # ---------------------------------------------------------- CPU reference
 def cpu_kick_time(steps, warmup, bunch, max_seconds=None):
     """Time the oracle (FP64 NumPy/SciPy restatement of the reference) on the
@@ -194,6 +274,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -315,6 +396,22 @@ def main():
     ms_grad = max_over_ranks(timed(grad_step, args.steps, args.warmup), ws)
     clocks = sampler.stop()
 
+    # ---- deposit alone in each mode (same particles, mixed mesh)
+    dep_ms = {}
+    for name, mode in (("atomic", L.SC_DEPOSIT_ATOMIC), ("sorted", L.SC_DEPOSIT_SORTED),
+                       ("deterministic", L.SC_DEPOSIT_DETERMINISTIC), ("tiled", L.SC_DEPOSIT_TILED),
+                       ("vector", L.SC_DEPOSIT_VECTOR)):
+        dep = lambda: L.call("sc_deposit", mm.ptr, *[C.c_void_p(t.data_ptr()) for t in dev[:4]], NP, L.SC_F64, 1,
+                             mode, C.c_void_p(stream.cuda_stream))
+        dep_ms[name] = round(max_over_ranks(timed(dep, max(3, args.steps // 2), args.warmup), ws), 4)
+
+    # ---- batched bunches (64 uneven bunches in one graph-replayed call)
+    batch_res = None
+    if not args.no_batch:
+        del mp
+        torch.cuda.empty_cache()
+        batch_res = bench_batch(sc, L, C, torch, flush, stream, ws, rank, max(3, args.steps // 2), args.warmup)
+
     # ---- roofline of the dominant stage (CUDA events inside the timed loop)
     names = L.STAGES
     per = {names[k]: stage_ms[k] / max(1, stage_n[k]) for k in range(L.SC_NUM_STAGES) if stage_n[k]}
@@ -373,6 +470,8 @@ def main():
         "cpu_baseline": cpu,
         "e2e": {"value": round(ms_e2e, 4), "unit": "ms", "h2d_bytes_per_step": 4 * NP * 8,
                 "d2h_bytes_per_step": 3 * NP * 8},
+        "deposit_modes_ms": dep_ms,
+        "batch": batch_res,
         "gpu_launches": int(round(launches_per_kick * args.steps)),
         "clocks": clocks,
     }

@@ -56,7 +56,11 @@ extern "C" {
 /* deposit modes */
 #define SC_DEPOSIT_ATOMIC        0 /* one thread per particle, 8 atomics */
 #define SC_DEPOSIT_SORTED        1 /* bin by cell, warp-segmented sums, few atomics */
-#define SC_DEPOSIT_DETERMINISTIC 2 /* sorted, fixed reduction order, no float atomics */
+#define SC_DEPOSIT_DETERMINISTIC 2 /* sorted, fixed-point sums: bitwise reproducible */
+#define SC_DEPOSIT_TILED         3 /* sorted by 8x8x8-cell tile, shared-memory accumulation */
+#define SC_DEPOSIT_VECTOR        4 /* mixed meshes: two 16-byte vector atomics per particle
+                                      into per-cell corners, then a node sum; on FP64
+                                      meshes the same as SC_DEPOSIT_ATOMIC */
 
 /* pipeline stages timed by sc_mesh_stage_times */
 #define SC_STAGE_DEPOSIT   0 /* clear + deposit kernels */
@@ -134,6 +138,14 @@ int sc_mesh_efield(sc_mesh* mesh, void** dptr);
  * The reference rebuilds it on every solve! (free_space.jl:77-96). */
 int sc_mesh_set_green_cache(sc_mesh* mesh, int enabled);
 
+/* FFT kernels of the hand-written pipelines (process-wide).  SC_FFT_AUTO
+ * (default): register-resident two-step transforms for FP32 lengths up to
+ * 256, shared-memory Stockham transforms otherwise; SC_FFT_STOCKHAM: the
+ * Stockham transforms everywhere.  Both give the same result to rounding. */
+#define SC_FFT_AUTO     0
+#define SC_FFT_STOCKHAM 1
+int sc_set_fft_engine(int engine);
+
 /* clear_mesh!(mesh), src/deposition.jl:10-12. */
 int sc_clear_mesh(sc_mesh* mesh, void* stream);
 
@@ -144,6 +156,12 @@ int sc_clear_mesh(sc_mesh* mesh, void* stream);
  * deposition.jl:64); read the count with sc_mesh_out_of_range. */
 int sc_deposit(sc_mesh* mesh, const void* x, const void* y, const void* z,
                const void* q, int64_t n, int dtype, int clear, int mode, void* stream);
+
+/* Deposit mode sc_kick uses for this mesh (default SC_DEPOSIT_VECTOR for
+ * SC_PREC_MIXED, SC_DEPOSIT_ATOMIC otherwise).  With SC_DEPOSIT_TILED the
+ * kick also gathers through the same tiles.  SC_PREC_PLAIN64 meshes always
+ * kick with the atomic deposit. */
+int sc_mesh_set_kick_mode(sc_mesh* mesh, int mode);
 
 /* solve!(mesh; at_cathode), src/solvers/free_space.jl:14-101. */
 int sc_solve(sc_mesh* mesh, int at_cathode, void* stream);
@@ -217,6 +235,37 @@ int sc_kick_adjoint(sc_mesh* mesh, const void* x, const void* y, const void* z, 
  *    threads) race and must be serialised by the caller. */
 int sc_solve_noalloc(const int32_t grid_size[3], const double delta[3], double gamma, const float* rho,
                      float* efield, void* stream);
+
+/* ---- many bunches: one call for their kicks, replayed as a CUDA graph ----
+ * No counterpart in the reference (a tracking code calls its kick once per
+ * bunch).  A batch references caller-owned meshes (SC_PREC_FP64 or MIXED,
+ * all on the current device; each with its own grid, bounds and gamma).
+ * sc_batch_kick runs every bunch's deposit -> solve -> interpolate with
+ * bunch i on internal stream i % nstreams, forked from and joined back into
+ * `stream`.  The first call with a given set of pointers, counts, dtype,
+ * at_cathode and stream runs eagerly (allocating workspaces and building
+ * Green spectra) and captures the same work into a CUDA graph; later calls
+ * with identical arguments replay the graph in one launch.  Meshes must not
+ * be destroyed while their batch exists. */
+typedef struct sc_batch sc_batch;
+int sc_batch_create(sc_mesh* const* meshes, int nbunch, int nstreams, sc_batch** out);
+int sc_batch_kick(sc_batch* batch, const void* const* x, const void* const* y, const void* const* z,
+                  const void* const* q, const int64_t* n, int dtype, int at_cathode, void* const* ex,
+                  void* const* ey, void* const* ez, void* stream);
+int sc_batch_set_graph(sc_batch* batch, int enabled); /* default 1 */
+int sc_batch_graph_nodes(const sc_batch* batch, int64_t* count);
+int sc_batch_destroy(sc_batch* batch);
+
+/* FFT autotuner (no counterpart in the reference): times this mesh's solve
+ * with each candidate kernel configuration -- the register two-step
+ * transforms, and the Stockham transforms with 4, 8, 16 or 32 columns per
+ * CTA -- and keeps the fastest for this mesh and for every later mesh with
+ * the same transform shape and precision on this device.  When the
+ * environment variable SC_AUTOTUNE_FILE names a file, choices are appended
+ * to it and read back by later processes.  Synchronises `stream`; the
+ * chosen configuration is written to *choice (0 = two-step, 2..5 = Stockham
+ * with 2^choice columns) when choice is not NULL. */
+int sc_autotune(sc_mesh* mesh, void* stream, int* choice);
 
 /* Number of particles skipped as out of range since the last call
  * (deposit and interpolate); resets the counter.  Synchronises `stream`. */

@@ -13,8 +13,10 @@
 // The Green spectrum is the one the forward solve cached: K_c is odd in its
 // own axis, so conj(K^_c) = -K^_c in free space; for the image the flipped
 // charge's phase is already folded into the stored spectrum and cancels.
+#include <type_traits>
+
 #include "cells.cuh"
-#include "pipeline.cuh"
+#include "pipeline2.cuh"
 
 namespace sc {
 
@@ -283,10 +285,19 @@ static int adjoint_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q,
     T2* D = (T2*)w.D;
     const int rows = ny * nz;
     const int64_t dcs = (int64_t)Hx * ny * nz;
-    for (int c = 0; c < 3; ++c) SC_TRY(run_fwd_x<T>(adjE + c * N, D + c * dcs, nx, rows, w, tw, s));
-    SC_TRY(run_col<false, T>(D, C, Hx, Ly, w.log2L[1], ny, Ly, Hx, (int64_t)Hx * ny, dcs, Hx, (int64_t)Hx * Ly,
-                             (int64_t)Hx * Ly * nz, nz, 3, tw, s));
-    {
+    const bool two = std::is_same<T, float>::value && fft_engine() == 0;
+    for (int c = 0; c < 3; ++c)
+        if (!(two && launch2_fwd_x(w.log2L[0], (const float*)(adjE + c * N), (float2*)(D + c * dcs), nx, rows, Hx,
+                                   (const float2*)tw, s)))
+            SC_TRY(run_fwd_x<T>(adjE + c * N, D + c * dcs, nx, rows, w, tw, s));
+    if (!(two && launch2_col(false, w.log2L[1], (const float2*)D, (float2*)C, Hx, ny, Ly, Hx, (int64_t)Hx * ny, dcs,
+                             Hx, (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, nz, 3, (const float2*)tw, s)))
+        SC_TRY(run_col<false, T>(D, C, Hx, Ly, w.log2L[1], ny, Ly, Hx, (int64_t)Hx * ny, dcs, Hx, (int64_t)Hx * Ly,
+                                 (int64_t)Hx * Ly * nz, nz, 3, tw, s));
+    if (two && launch2_adj_zpass(w.log2L[2], (const float2*)C, (float2*)B, Hx, Ly, nz,
+                                 make_green_view(w, at_cathode ? 1 : 0), (const float2*)tw, s)) {
+        SC_LAUNCH_CHECK("k2_adj_zpass");
+    } else {
         const GreenView gv = make_green_view(w, at_cathode ? 1 : 0);
         const int lgW = pick_cols(w.log2L[2]);
         const int W = 1 << lgW;
@@ -296,9 +307,13 @@ static int adjoint_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q,
         k_adj_zpass<T><<<grid, 256, smem, s>>>(C, B, Hx, Ly, nz, Lz, w.log2L[2], lgW, gv, tw);
         SC_LAUNCH_CHECK("k_adj_zpass");
     }
-    SC_TRY(run_col<true, T>(B, A, Hx, Ly, w.log2L[1], Ly, ny, Hx, (int64_t)Hx * Ly, 0, Hx, (int64_t)Hx * ny, 0, nz, 1,
-                            tw, s));
-    {
+    if (!(two && launch2_col(true, w.log2L[1], (const float2*)B, (float2*)A, Hx, Ly, ny, Hx, (int64_t)Hx * Ly, 0, Hx,
+                             (int64_t)Hx * ny, 0, nz, 1, (const float2*)tw, s)))
+        SC_TRY(run_col<true, T>(B, A, Hx, Ly, w.log2L[1], Ly, ny, Hx, (int64_t)Hx * Ly, 0, Hx, (int64_t)Hx * ny, 0, nz,
+                                1, tw, s));
+    if (two && launch2_inv_x1(w.log2L[0], (const float2*)A, (float*)m->efield, nx, rows, Hx, (const float2*)tw, s)) {
+        SC_LAUNCH_CHECK("k2_inv_x1");
+    } else {
         const int lgP = pick_rows(w.log2L[0]);
         const int P_ = 1 << lgP;
         const size_t smem = sizeof(T2) * 2 * P_ * Lx;

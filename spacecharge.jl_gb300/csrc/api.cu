@@ -5,6 +5,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -71,6 +72,9 @@ int device_ctx(DeviceCtx** out) {
     *out = c;
     return SC_OK;
 }
+
+static std::atomic<int> g_fft_engine{0};
+int fft_engine() { return g_fft_engine.load(std::memory_order_relaxed); }
 
 Geom make_geom(const sc_mesh* m) {
     Geom g;
@@ -154,6 +158,7 @@ static int mesh_alloc(const int32_t* g, const double* lo, const double* hi, cons
         delete m;
         return st;
     }
+    if (precision == SC_PREC_MIXED) m->kick_mode = SC_DEPOSIT_VECTOR;
     if (precision != SC_PREC_PLAIN64) {
         st = native_prepare(m);
         if (st != SC_OK) {
@@ -202,6 +207,11 @@ struct DeviceGuard {
 }  // namespace sc
 
 using namespace sc;
+
+static bool valid_deposit_mode(int mode) {
+    return mode == SC_DEPOSIT_ATOMIC || mode == SC_DEPOSIT_SORTED || mode == SC_DEPOSIT_DETERMINISTIC ||
+           mode == SC_DEPOSIT_TILED || mode == SC_DEPOSIT_VECTOR;
+}
 
 extern "C" {
 
@@ -266,6 +276,8 @@ int sc_mesh_destroy(sc_mesh* m) {
         native_release(m);
     m->timer.release();
     sorted_release(m);
+    tiled_release(m);
+    cudaFree(m->corner);
     cudaFree(m->rho);
     cudaFree(m->efield);
     cudaFree(m->oob);
@@ -337,6 +349,18 @@ int sc_mesh_efield(sc_mesh* m, void** p) {
     return SC_OK;
 }
 
+int sc_autotune(sc_mesh* m, void* stream, int* choice) {
+    SC_TRY(check_mesh(m));
+    DeviceGuard g(m->device);
+    return native_autotune(m, (cudaStream_t)stream, choice);
+}
+
+int sc_set_fft_engine(int engine) {
+    if (engine != SC_FFT_AUTO && engine != SC_FFT_STOCKHAM) return fail(SC_ERR_INVALID, "unknown FFT engine %d", engine);
+    g_fft_engine.store(engine);
+    return SC_OK;
+}
+
 int sc_mesh_set_green_cache(sc_mesh* m, int enabled) {
     SC_TRY(check_mesh(m));
     m->green_cache = enabled != 0;
@@ -360,8 +384,7 @@ int sc_deposit(sc_mesh* m, const void* x, const void* y, const void* z, const vo
     SC_TRY(check_dtype(dtype));
     if (n < 0) return fail(SC_ERR_INVALID, "Particle coordinate and charge arrays must have the same length.");
     if (n > 0 && (!x || !y || !z || !q)) return fail(SC_ERR_INVALID, "particle pointer is NULL");
-    if (mode != SC_DEPOSIT_ATOMIC && mode != SC_DEPOSIT_SORTED && mode != SC_DEPOSIT_DETERMINISTIC)
-        return fail(SC_ERR_INVALID, "unknown deposit mode %d", mode);
+    if (!valid_deposit_mode(mode)) return fail(SC_ERR_INVALID, "unknown deposit mode %d", mode);
     DeviceGuard g(m->device);
     StageScope st(m->timer, SC_STAGE_DEPOSIT, (cudaStream_t)stream);
     if (clear) SC_TRY(sc_clear_mesh(m, stream));
@@ -390,9 +413,25 @@ int sc_interpolate_field(sc_mesh* m, const void* x, const void* y, const void* z
 
 int sc_kick(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
             int at_cathode, void* ex, void* ey, void* ez, void* stream) {
-    SC_TRY(sc_deposit(m, x, y, z, q, n, dtype, 1, SC_DEPOSIT_ATOMIC, stream));
+    SC_TRY(check_mesh(m));
+    const int mode = m->precision == SC_PREC_PLAIN64 ? SC_DEPOSIT_ATOMIC : m->kick_mode;
+    SC_TRY(sc_deposit(m, x, y, z, q, n, dtype, 1, mode, stream));
     SC_TRY(sc_solve(m, at_cathode, stream));
+    if (mode == SC_DEPOSIT_TILED && n > 0) {
+        // the tiled deposit binned exactly these particles: gather through the tiles
+        if (!ex || !ey || !ez) return fail(SC_ERR_INVALID, "output pointer is NULL");
+        DeviceGuard g(m->device);
+        StageScope st(m->timer, SC_STAGE_GATHER, (cudaStream_t)stream);
+        return gather_tiled_launch(m, x, n, dtype, ex, ey, ez, (cudaStream_t)stream);
+    }
     return sc_interpolate_field(m, x, y, z, n, dtype, ex, ey, ez, stream);
+}
+
+int sc_mesh_set_kick_mode(sc_mesh* m, int mode) {
+    SC_TRY(check_mesh(m));
+    if (!valid_deposit_mode(mode)) return fail(SC_ERR_INVALID, "unknown deposit mode %d", mode);
+    m->kick_mode = mode;
+    return SC_OK;
 }
 
 int sc_kick_adjoint(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,

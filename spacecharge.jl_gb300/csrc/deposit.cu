@@ -6,6 +6,8 @@
 // deposit_atomic: the hand-written pipelines' unsorted deposit.  Same cell
 //   index (bit-exact, see cells.cuh), weights in the mesh type, several
 //   particles per thread with their loads in flight together, 8 atomics each.
+// deposit_vector: mixed meshes; 2 vector atomics per particle into per-cell
+//   corner slots, then a pass that sums each node's 8 slots.
 #include "cells.cuh"
 #include "sc_internal.cuh"
 
@@ -125,6 +127,98 @@ __global__ void __launch_bounds__(256) deposit_atomic(const P* __restrict__ px, 
     if (skipped) atomicAdd(oob, (unsigned long long)skipped);
 }
 
+// ------------------------------------------------ vector (mixed meshes)
+// The 8 CIC weights of a particle in cell c = (ix, iy, iz) go with two 16-byte
+// vector atomics into corner[8c .. 8c+7]: the 4 nodes of the cell's lower z
+// face, then the 4 of its upper face, x fastest (one 32-byte sector per cell).
+// That is a quarter of the atomic operations of deposit_atomic.
+// k_corner_sum then adds, for every node, the entries the (up to) 8 cells
+// around it hold for it.  Cells with an index n-1 are never written and stay
+// zero from the clear.
+template <typename P>
+__global__ void __launch_bounds__(256) deposit_vector(const P* __restrict__ px, const P* __restrict__ py,
+                                                      const P* __restrict__ pz, const P* __restrict__ pq,
+                                                      int64_t n, Axes ax, float4* __restrict__ corner,
+                                                      unsigned long long* __restrict__ oob) {
+    const int64_t base = (int64_t)blockIdx.x * (blockDim.x * kDepPerThread) + threadIdx.x;
+    P x[kDepPerThread], y[kDepPerThread], z[kDepPerThread], qq[kDepPerThread];
+#pragma unroll
+    for (int k = 0; k < kDepPerThread; ++k) {
+        const int64_t p = base + (int64_t)k * blockDim.x;
+        const bool in = p < n;
+        x[k] = in ? __ldg(px + p) : P(0);
+        y[k] = in ? __ldg(py + p) : P(0);
+        z[k] = in ? __ldg(pz + p) : P(0);
+        qq[k] = in ? __ldg(pq + p) : P(0);
+    }
+    const int nx = ax.a[0].n, ny = ax.a[1].n;
+    const int64_t sy = nx, sz = (int64_t)nx * ny;
+    unsigned skipped = 0;
+#pragma unroll
+    for (int k = 0; k < kDepPerThread; ++k) {
+        const int64_t p = base + (int64_t)k * blockDim.x;
+        if (p >= n) break;
+        int ix = 0, iy = 0, iz = 0;
+        float fx = 0, fy = 0, fz = 0;
+        const bool ok = cell_df32(x[k], ax.a[0], ix, fx) & cell_df32(y[k], ax.a[1], iy, fy) &
+                        cell_df32(z[k], ax.a[2], iz, fz);
+        if (!ok) {
+            ++skipped;
+            continue;
+        }
+        const float q = f64_to_f32(qq[k]);
+        const float wx0 = 1.0f - fx, wy0 = 1.0f - fy, wz0 = 1.0f - fz;
+        float4* c = corner + 2 * (ix + sy * iy + sz * iz);
+        // deposition.jl:67-74 products
+        atomicAdd(c, make_float4(q * wx0 * wy0 * wz0, q * fx * wy0 * wz0, q * wx0 * fy * wz0, q * fx * fy * wz0));
+        atomicAdd(c + 1, make_float4(q * wx0 * wy0 * fz, q * fx * wy0 * fz, q * wx0 * fy * fz, q * fx * fy * fz));
+    }
+    if (skipped) atomicAdd(oob, (unsigned long long)skipped);
+}
+
+__global__ void __launch_bounds__(256) k_corner_sum(const float* __restrict__ corner, int nx, int ny, int64_t N,
+                                                    float* __restrict__ rho) {
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= N) return;
+    const int i = (int)(node % nx);
+    const int64_t r = node / nx;
+    const int j = (int)(r % ny), k = (int)(r / ny);
+    const int64_t sy = nx, sz = (int64_t)nx * ny;
+    float s = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                if (i >= a && j >= b && k >= c)
+                    s += __ldg(corner + 8 * (node - a - b * sy - c * sz) + 4 * c + 2 * b + a);
+            }
+        }
+    }
+    rho[node] += s;
+}
+
+static int deposit_vector_launch(sc_mesh* m, const Axes& ax, const void* x, const void* y, const void* z,
+                                 const void* q, int64_t n, int dtype, cudaStream_t s) {
+    const size_t bytes = sizeof(float) * 8 * (size_t)m->N;
+    if (!m->corner) SC_CUDA(cudaMalloc(&m->corner, bytes));
+    SC_CUDA(cudaMemsetAsync(m->corner, 0, bytes, s));
+    const int64_t blocks = (n + 256 * kDepPerThread - 1) / (256 * kDepPerThread);
+    if (dtype == SC_F64)
+        deposit_vector<double><<<blocks, 256, 0, s>>>((const double*)x, (const double*)y, (const double*)z,
+                                                     (const double*)q, n, ax, (float4*)m->corner, m->oob);
+    else
+        deposit_vector<float><<<blocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z,
+                                                    (const float*)q, n, ax, (float4*)m->corner, m->oob);
+    SC_LAUNCH_CHECK("deposit_vector");
+    k_corner_sum<<<(m->N + 255) / 256, 256, 0, s>>>((const float*)m->corner, m->n[0], m->n[1], m->N,
+                                                     (float*)m->rho);
+    SC_LAUNCH_CHECK("k_corner_sum");
+    m->launches += 2;
+    return SC_OK;
+}
+
 // sc_cell_index: bins with the same arithmetic the mesh's deposit uses.
 template <typename P, typename A>
 __global__ void __launch_bounds__(256) cell_index_kernel(const P* __restrict__ px, const P* __restrict__ py,
@@ -195,7 +289,11 @@ int deposit_launch(sc_mesh* m, const void* x, const void* y, const void* z, cons
         m->launches += 1;
         return SC_OK;
     }
-    if (mode != SC_DEPOSIT_ATOMIC) return deposit_sorted_launch(m, x, y, z, q, n, dtype, mode, s);
+    if (mode == SC_DEPOSIT_TILED) return deposit_tiled_launch(m, x, y, z, q, n, dtype, s);
+    if (mode == SC_DEPOSIT_VECTOR && m->precision == SC_PREC_MIXED)
+        return deposit_vector_launch(m, ax, x, y, z, q, n, dtype, s);
+    if (mode == SC_DEPOSIT_SORTED || mode == SC_DEPOSIT_DETERMINISTIC)
+        return deposit_sorted_launch(m, x, y, z, q, n, dtype, mode, s);
     const int64_t ablocks = (n + 256 * kDepPerThread - 1) / (256 * kDepPerThread);
     if (m->precision == SC_PREC_MIXED) {
         if (dtype == SC_F64)

@@ -26,9 +26,17 @@
 // into it, so the inverse passes produce E directly.
 #include <math.h>
 
-#include <mutex>
+#include <stdio.h>
+#include <stdlib.h>
 
-#include "pipeline.cuh"
+#include <atomic>
+#include <map>
+#include <mutex>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "pipeline2.cuh"
 
 namespace sc {
 
@@ -595,7 +603,6 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
     const int64_t gcs = (int64_t)nx * ny * (2 * nz - 1);
     const int64_t scs = (int64_t)Hx * Ly * Lz;
     if (!w.goct) SC_CUDA(cudaMalloc(&w.goct, sizeof(float) * 3 * gcs));
-    if (!w.gspec) SC_CUDA(cudaMalloc(&w.gspec, sizeof(float2) * 3 * scs));
     if (image && !w.gimg) SC_CUDA(cudaMalloc(&w.gimg, sizeof(float2) * 3 * (int64_t)Hx * Hy * Lz));
     OctantGeom g;
     g.nx = nx;
@@ -642,6 +649,25 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
     const int64_t cells = (int64_t)nx * ny * zc;
     k_igf_octant<<<(cells + 255) / 256, 256, 0, s>>>((float*)w.goct, g);
     SC_LAUNCH_CHECK("k_igf_octant");
+    if (fft_engine() == 0 && w.log2L[0] <= 8 && w.log2L[1] <= 8 && w.log2L[2] <= 8) {
+        // parity-reduced transform: real octant lines only (pipeline2.cuh)
+        const int64_t t1max = (int64_t)Hx * ny * (2 * nz - 1), t2max = (int64_t)Hx * Hy * (2 * nz - 1);
+        if (!w.gtmp) SC_CUDA(cudaMalloc(&w.gtmp, sizeof(float) * 3 * (t1max + t2max)));
+        float* T1 = (float*)w.gtmp;
+        float* T2 = T1 + 3 * t1max;
+        const int64_t t1cs = (int64_t)Hx * ny * zc, t2cs = (int64_t)Hx * Hy * zc;
+        const int64_t plane = (int64_t)Hx * Hy;
+        if (launch3_green_x(w.log2L[0], (const float*)w.goct, T1, nx, ny * zc, Hx, gcs, t1cs, tw, s) &&
+            launch3_green_col(false, w.log2L[1], T1, T2, Hx, zc, ny, 1, Hx, (int64_t)Hx * ny, t1cs, Hx, plane, t2cs,
+                              tw, s) &&
+            launch3_green_col(image, w.log2L[2], T2, image ? w.gimg : w.gfree, (int)plane, 1, nz, 2, plane, 0, t2cs,
+                              plane, 0, image ? plane * Lz : plane * Hz, tw, s)) {
+            SC_LAUNCH_CHECK("green two-step");
+            m->launches += 5;
+            return SC_OK;
+        }
+    }
+    if (!w.gspec) SC_CUDA(cudaMalloc(&w.gspec, sizeof(float2) * 3 * scs));
     float2* S = (float2*)w.gspec;
     {
         const int lgP = pick_rows(w.log2L[0]);
@@ -746,47 +772,64 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s) {
     T2* C = (T2*)w.C;
     T2* D = (T2*)w.D;
     const int rows = ny * nz;
+    // FP32 with transforms of at most 256 points: register two-step kernels
+    // (unless this mesh's autotuned or the process-wide choice says Stockham)
+    const int eng = w.engine >= 0 ? w.engine : fft_engine();
+    const bool two = std::is_same<T, float>::value && eng == 0;
+    const int lgWy = w.lgW >= 0 ? w.lgW : pick_cols(w.log2L[1]);
     {
         StageScope st(m->timer, SC_STAGE_FWD_X, s);
-        SC_TRY(run_fwd_x<T>((const T*)m->rho, A, nx, rows, w, tw, s));
+        if (!(two && launch2_fwd_x(w.log2L[0], (const float*)m->rho, (float2*)A, nx, rows, Hx, (const float2*)tw, s)))
+            SC_TRY(run_fwd_x<T>((const T*)m->rho, A, nx, rows, w, tw, s));
+        SC_LAUNCH_CHECK("fwd_x");
     }
     {
         // y: A (Hx x ny x nz) -> B (Hx x Ly x nz)
         StageScope st(m->timer, SC_STAGE_FWD_Y, s);
-        SC_TRY(run_col<false, T>(A, B, Hx, Ly, w.log2L[1], ny, Ly, Hx, (int64_t)Hx * ny, 0, Hx, (int64_t)Hx * Ly, 0,
-                                 nz, 1, tw, s));
+        if (!(two && launch2_col(false, w.log2L[1], (const float2*)A, (float2*)B, Hx, ny, Ly, Hx, (int64_t)Hx * ny,
+                                 0, Hx, (int64_t)Hx * Ly, 0, nz, 1, (const float2*)tw, s)))
+            SC_TRY(run_col<false, T>(A, B, Hx, Ly, w.log2L[1], ny, Ly, Hx, (int64_t)Hx * ny, 0, Hx, (int64_t)Hx * Ly,
+                                     0, nz, 1, tw, s, lgWy));
+        SC_LAUNCH_CHECK("fwd_y");
     }
     // z + Green + inverse z
     {
         StageScope st(m->timer, SC_STAGE_ZPASS, s);
-        GreenView gv;
-        gv.gfree = w.gfree;
-        gv.gimg = w.gimg;
-        gv.Hx = Hx;
-        gv.Hy = Ly / 2 + 1;
-        gv.Hz = Lz / 2 + 1;
-        gv.Ly = Ly;
-        gv.Lz = Lz;
-        gv.cs_free = (int64_t)Hx * gv.Hy * gv.Hz;
-        gv.cs_img = (int64_t)Hx * gv.Hy * Lz;
-        gv.image = at_cathode ? 1 : 0;
-        const int lgW = pick_cols(w.log2L[2]);
+        const GreenView gv = make_green_view(w, at_cathode ? 1 : 0);
+        if (two && launch2_zpass(w.log2L[2], (const float2*)B, (float2*)C, Hx, Ly, nz, gv, (const float2*)tw, s)) {
+            SC_LAUNCH_CHECK("k2_zpass");
+            goto zdone;
+        }
+        {
+        int lgW = w.lgW >= 0 ? w.lgW : pick_cols(w.log2L[2]);
+        while (lgW > 0 && sizeof(T2) * 3 * ((size_t)1 << lgW) * Lz > 200 * 1024) --lgW;  // shared-memory cap
         const int W = 1 << lgW;
         const size_t smem = sizeof(T2) * 3 * W * Lz;
         SC_TRY(set_smem(k_zpass<T>, smem));
         dim3 grid((Hx + W - 1) / W, Ly);
         k_zpass<T><<<grid, 256, smem, s>>>(B, C, Hx, Ly, nz, Lz, w.log2L[2], lgW, gv, tw);
         SC_LAUNCH_CHECK("k_zpass");
+        }
+    zdone:;
     }
     {
         // inverse y: C (3 x Hx x Ly x nz) -> D (3 x Hx x ny x nz)
         StageScope st(m->timer, SC_STAGE_INV_Y, s);
-        SC_TRY(run_col<true, T>(C, D, Hx, Ly, w.log2L[1], Ly, ny, Hx, (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, Hx,
-                                (int64_t)Hx * ny, (int64_t)Hx * ny * nz, nz, 3, tw, s));
+        if (!(two && launch2_col(true, w.log2L[1], (const float2*)C, (float2*)D, Hx, Ly, ny, Hx, (int64_t)Hx * Ly,
+                                 (int64_t)Hx * Ly * nz, Hx, (int64_t)Hx * ny, (int64_t)Hx * ny * nz, nz, 3,
+                                 (const float2*)tw, s)))
+            SC_TRY(run_col<true, T>(C, D, Hx, Ly, w.log2L[1], Ly, ny, Hx, (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, Hx,
+                                    (int64_t)Hx * ny, (int64_t)Hx * ny * nz, nz, 3, tw, s, lgWy));
+        SC_LAUNCH_CHECK("inv_y");
     }
     {
         // inverse x -> packed efield
         StageScope st(m->timer, SC_STAGE_INV_X, s);
+        if (two && launch2_inv_x(w.log2L[0], (const float2*)D, (float4*)m->efield, nx, rows, Hx, (int64_t)Hx * rows,
+                                 (const float2*)tw, s)) {
+            SC_LAUNCH_CHECK("k2_inv_x");
+            return SC_OK;
+        }
         const int lgP = pick_rows(w.log2L[0]);
         const int P = 1 << lgP;
         const size_t smem = sizeof(T2) * 5 * P * w.L[0];
@@ -798,6 +841,117 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s) {
     }
     return SC_OK;
 }
+
+// ----------------------------------------------------------- autotuner
+// Choices per (GPU name, precision, Lx, Ly, Lz): engine 0 = register
+// two-step, 1 = Stockham with 2^lgW columns per CTA.
+struct TuneKey {
+    std::string gpu;
+    int prec, L0, L1, L2;
+    bool operator<(const TuneKey& o) const {
+        if (gpu != o.gpu) return gpu < o.gpu;
+        if (prec != o.prec) return prec < o.prec;
+        if (L0 != o.L0) return L0 < o.L0;
+        if (L1 != o.L1) return L1 < o.L1;
+        return L2 < o.L2;
+    }
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, std::pair<int, int>> g_tune;
+static bool g_tune_loaded = false;
+
+static std::string gpu_name(int dev) {
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) return "unknown";
+    std::string n(p.name);
+    for (char& c : n)
+        if (c == ' ') c = '_';
+    return n;
+}
+
+static void tune_load_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char* path = getenv("SC_AUTOTUNE_FILE");
+    if (!path) return;
+    FILE* f = fopen(path, "r");
+    if (!f) return;
+    char name[256];
+    int prec, l0, l1, l2, eng, lg;
+    while (fscanf(f, "%255s %d %d %d %d %d %d", name, &prec, &l0, &l1, &l2, &eng, &lg) == 7)
+        g_tune[TuneKey{name, prec, l0, l1, l2}] = {eng, lg};
+    fclose(f);
+}
+
+bool tuned_choice(int device, int precision, const int L[3], int* engine, int* lgW) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_load_locked();
+    auto it = g_tune.find(TuneKey{gpu_name(device), precision, L[0], L[1], L[2]});
+    if (it == g_tune.end()) return false;
+    *engine = it->second.first;
+    *lgW = it->second.second;
+    return true;
+}
+
+static int autotune(sc_mesh* m, cudaStream_t s, int* choice) {
+    if (m->precision == SC_PREC_PLAIN64)
+        return fail(SC_ERR_UNSUPPORTED, "the autotuner tunes the hand-written pipelines (precision fp64 or mixed)");
+    NativeWork& w = m->nw;
+    const bool keep_cache = m->green_cache;
+    m->green_cache = true;
+    std::vector<std::pair<int, int>> cand;
+    if (m->precision == SC_PREC_MIXED && w.L[0] <= 256 && w.L[1] <= 256 && w.L[2] <= 256) cand.push_back({0, -1});
+    for (int lg = 2; lg <= 5; ++lg) cand.push_back({1, lg});
+    cudaEvent_t a, b;
+    SC_CUDA(cudaEventCreate(&a));
+    SC_CUDA(cudaEventCreate(&b));
+    float best = 1e30f;
+    std::pair<int, int> pick = cand[0];
+    int st = SC_OK;
+    for (auto c : cand) {
+        w.engine = c.first;
+        w.lgW = c.second;
+        for (int r = 0; r < 2 && st == SC_OK; ++r) st = native_solve(m, 0, s);
+        if (st != SC_OK) break;
+        cudaEventRecord(a, s);
+        for (int r = 0; r < 5 && st == SC_OK; ++r) st = native_solve(m, 0, s);
+        cudaEventRecord(b, s);
+        if (st != SC_OK) break;
+        if (cudaEventSynchronize(b) != cudaSuccess) {
+            st = cuda_fail(cudaGetLastError(), "autotune timing");
+            break;
+        }
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best) {
+            best = ms;
+            pick = c;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    m->green_cache = keep_cache;
+    w.engine = pick.first;
+    w.lgW = pick.second;
+    if (st != SC_OK) return st;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        tune_load_locked();
+        TuneKey k{gpu_name(m->device), m->precision, w.L[0], w.L[1], w.L[2]};
+        g_tune[k] = pick;
+        if (const char* path = getenv("SC_AUTOTUNE_FILE")) {
+            if (FILE* f = fopen(path, "a")) {
+                fprintf(f, "%s %d %d %d %d %d %d\n", k.gpu.c_str(), k.prec, k.L0, k.L1, k.L2, pick.first,
+                        pick.second);
+                fclose(f);
+            }
+        }
+    }
+    if (choice) *choice = pick.first == 0 ? 0 : pick.second;
+    return SC_OK;
+}
+
+int native_autotune(sc_mesh* m, cudaStream_t s, int* choice) { return autotune(m, s, choice); }
 
 int native_prepare(sc_mesh* m) {
     NativeWork& w = m->nw;
@@ -813,6 +967,11 @@ int native_prepare(sc_mesh* m) {
     }
     w.Hx = w.L[0] / 2 + 1;
     w.elem = m->precision == SC_PREC_MIXED ? sizeof(float2) : sizeof(double2);
+    int eng = -1, lg = -1;
+    if (tuned_choice(m->device, m->precision, w.L, &eng, &lg)) {
+        w.engine = eng;
+        w.lgW = lg;
+    }
     return SC_OK;
 }
 
@@ -823,13 +982,17 @@ int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s) {
 
 int native_release(sc_mesh* m) {
     NativeWork& w = m->nw;
-    void* ptrs[] = {w.A, w.B, w.C, w.D, w.adjE, w.fnear, w.fcorner, w.kgrid, w.kspec, w.goct, w.gspec, w.gfree, w.gimg};
+    void* ptrs[] = {w.A,     w.B,     w.C,    w.D,     w.adjE,  w.fnear, w.fcorner,
+                    w.kgrid, w.kspec, w.goct, w.gspec, w.gtmp, w.gfree, w.gimg};
     for (void* p : ptrs) cudaFree(p);
     int L[3] = {w.L[0], w.L[1], w.L[2]};
     int lg[3] = {w.log2L[0], w.log2L[1], w.log2L[2]};
     int Hx = w.Hx;
     size_t el = w.elem;
+    const int eng = w.engine, lgw = w.lgW;
     w = NativeWork();
+    w.engine = eng;
+    w.lgW = lgw;
     for (int d = 0; d < 3; ++d) {
         w.L[d] = L[d];
         w.log2L[d] = lg[d];

@@ -220,9 +220,9 @@ template <bool INV, typename T>
 static int run_col(const typename Cplx<T>::T2* in, typename Cplx<T>::T2* out, int ncols, int L, int logL,
                    int n_valid, int n_store, int64_t as_in, int64_t bs_in, int64_t cs_in, int64_t as_out,
                    int64_t bs_out, int64_t cs_out, int nbatch, int ncomp, const typename Cplx<T>::T2* tw,
-                   cudaStream_t s) {
+                   cudaStream_t s, int lgW_override = -1) {
     using T2 = typename Cplx<T>::T2;
-    const int lgW = pick_cols(logL);
+    const int lgW = lgW_override >= 0 ? lgW_override : pick_cols(logL);
     const int W = 1 << lgW;
     const size_t smem = sizeof(T2) * 2 * W * L;
     SC_TRY(set_smem(k_col_fft<INV, T>, smem));

@@ -1,0 +1,638 @@
+// FP32 pass kernels on the register-resident two-step FFT (fft2.cuh), for
+// transform lengths 4..256; the Stockham kernels of pipeline.cuh remain for
+// FP64 and for longer transforms.
+//
+// Column passes (y, z: columns are consecutive kx, contiguous in memory) map
+// threads column-fastest, tid = c + W*t, W = 16 columns per CTA; row passes
+// (x: rows contiguous) map tid = t + NT*p over P row pairs.
+#pragma once
+
+#include "fft2.cuh"
+#include "pipeline.cuh"
+
+namespace sc {
+
+constexpr int kColW = 16;  // columns per CTA of the column passes
+
+// Batched strided column FFT.  Forward (INV = false): inputs n < n_valid
+// (natural order, zero beyond; with `wrap` also n > L - n_valid), all L
+// outputs.  Inverse: all L inputs, outputs n < n_store.  Element
+// (col, n, batch, comp) at base + col + n*as + b*bs + comp*cs, where b is the
+// batch index, or wrap_row(batch, bwrap_n, bwrap_L) when bwrap_n > 0.  In and
+// out may alias (each CTA reads all of its columns before writing them).
+__device__ __forceinline__ int wrap_row2(int c, int n, int L) { return c < n ? c : L - (2 * n - 1) + c; }
+
+template <int L, bool INV>
+__global__ void __launch_bounds__(kColW * F2<L>::NT) k2_col(const float2* in, float2* out, int ncols, int nbatch,
+                                                            int n_valid, int n_store, int wrap, int bwrap_n, int bwrap_L,
+                                                            int64_t as_in, int64_t bs_in, int64_t cs_in,
+                                                            int64_t as_out, int64_t bs_out, int64_t cs_out,
+                                                            const float2* __restrict__ tw) {
+    using E = F2<L>;
+    __shared__ float2 xb[kColW * E::S];
+    // columns of all batches flattened: f = col + ncols * batch (a tile may
+    // straddle two batches: two contiguous segments)
+    const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
+    const int64_t f = (int64_t)blockIdx.x * kColW + c;
+    const bool cok = f < (int64_t)ncols * nbatch;
+    const int bb = cok ? (int)(f / ncols) : 0;
+    const int col = (int)(f - (int64_t)bb * ncols);
+    const int b = bwrap_n > 0 ? wrap_row2(bb, bwrap_n, bwrap_L) : bb;
+    const float2* src = in + b * bs_in + blockIdx.y * cs_in + col;
+    float2* dst = out + b * bs_out + blockIdx.y * cs_out + col;
+    float2 v[16];
+    if (!INV) {
+        if (t < E::R2) {
+#pragma unroll
+            for (int s = 0; s < E::R1; ++s) {
+                const int n = t + E::R2 * s;
+                const bool ok = n < n_valid || (wrap && n > L - n_valid);
+                v[s] = (cok && ok) ? src[n * as_in] : make_float2(0.f, 0.f);
+            }
+        }
+        E::template fwd<false>(v, xb + c * E::S, t, tw);
+        if (t < E::R1 && cok) {
+#pragma unroll
+            for (int r = 0; r < E::R2; ++r) dst[(t + E::R1 * r) * as_out] = v[r];
+        }
+    } else {
+        if (t < E::R1) {
+#pragma unroll
+            for (int r = 0; r < E::R2; ++r) {
+                const int k = t + E::R1 * r;
+                v[r] = cok ? src[k * as_in] : make_float2(0.f, 0.f);
+            }
+        }
+        E::template inv<true>(v, xb + c * E::S, t, tw);
+        if (t < E::R2 && cok) {
+#pragma unroll
+            for (int s = 0; s < E::R1; ++s) {
+                const int n = t + E::R2 * s;
+                if (n < n_store) dst[n * as_out] = v[s];
+            }
+        }
+    }
+}
+
+// x pass: two real rows per complex FFT -> their half spectra.
+template <int L>
+__global__ void __launch_bounds__(256) k2_fwd_x(const float* __restrict__ rho, float2* __restrict__ A, int nx,
+                                                int rows, int Hx, const float2* __restrict__ tw) {
+    using E = F2<L>;
+    constexpr int P = 256 / E::NT;  // row pairs per CTA
+    __shared__ float2 xb[P * E::S];
+    const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
+    const int r0 = 2 * (blockIdx.x * P + p), r1 = r0 + 1;
+    float2* col = xb + p * E::S;
+    float2 v[16];
+    if (t < E::R2) {
+#pragma unroll
+        for (int s = 0; s < E::R1; ++s) {
+            const int x = t + E::R2 * s;
+            float re = 0.f, im = 0.f;
+            if (x < nx) {
+                if (r0 < rows) re = rho[(int64_t)r0 * nx + x];
+                if (r1 < rows) im = rho[(int64_t)r1 * nx + x];
+            }
+            v[s] = make_float2(re, im);
+        }
+    }
+    E::template fwd<false>(v, col, t, tw);
+    if (t < E::R1) {
+#pragma unroll
+        for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+    }
+    __syncthreads();
+    if (r0 < rows) {
+        for (int k = t; k <= L / 2; k += E::NT) {
+            float2 xa, xbv;
+            split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
+            A[(int64_t)r0 * Hx + k] = xa;
+            if (r1 < rows) A[(int64_t)r1 * Hx + k] = xbv;
+        }
+    }
+}
+
+// Inverse x pass of the three components, two rows per complex IFFT, packed
+// float4 output nodes.
+template <int L>
+__global__ void __launch_bounds__(256) k2_inv_x(const float2* __restrict__ D, float4* __restrict__ E4, int nx,
+                                                int rows, int Hx, int64_t cs, const float2* __restrict__ tw) {
+    using E = F2<L>;
+    constexpr int P = 256 / E::NT;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float2* xb = reinterpret_cast<float2*>(smraw);
+    float2* keep = xb + P * E::S;  // [2][P][L]: components 0, 1 until the float4 store
+    const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
+    const int r0 = 2 * (blockIdx.x * P + p), r1 = r0 + 1;
+    float2* col = xb + p * E::S;
+    float2 v[16];
+    for (int comp = 0; comp < 3; ++comp) {
+        const float2* Dc = D + comp * cs;
+        if (t < E::R1) {
+#pragma unroll
+            for (int r = 0; r < E::R2; ++r) {
+                const int k = t + E::R1 * r;
+                const bool cj = k > L / 2;
+                const int kk = cj ? L - k : k;
+                float2 xa = make_float2(0.f, 0.f), xbv = make_float2(0.f, 0.f);
+                if (r0 < rows) xa = Dc[(int64_t)r0 * Hx + kk];
+                if (r1 < rows) xbv = Dc[(int64_t)r1 * Hx + kk];
+                if (cj) {
+                    xa.y = -xa.y;
+                    xbv.y = -xbv.y;
+                }
+                v[r] = make_float2(xa.x - xbv.y, xa.y + xbv.x);  // Xa + i Xb
+            }
+        }
+        E::template inv<true>(v, col, t, tw);
+        if (comp < 2) {
+            if (t < E::R2) {
+#pragma unroll
+                for (int s = 0; s < E::R1; ++s) keep[(comp * P + p) * L + t + E::R2 * s] = v[s];
+            }
+        }
+    }
+    __syncthreads();
+    if (t < E::R2) {
+#pragma unroll
+        for (int s = 0; s < E::R1; ++s) {
+            const int x = t + E::R2 * s;
+            if (x >= nx) continue;
+            const float2 ex = keep[p * L + x], ey = keep[(P + p) * L + x], ez = v[s];
+            if (r0 < rows) E4[(int64_t)r0 * nx + x] = make_float4(ex.x, ey.x, ez.x, 0.f);
+            if (r1 < rows) E4[(int64_t)r1 * nx + x] = make_float4(ex.y, ey.y, ez.y, 0.f);
+        }
+    }
+}
+
+// z pass: forward z transform of rho^(kx, ky, .), products with the three
+// Green spectra (image: rho^ at -kz times the image spectrum), three inverse
+// transforms, z < nz stored.
+template <int L>
+__global__ void __launch_bounds__(kColW * F2<L>::NT, 2) k2_zpass(const float2* __restrict__ B,
+                                                                 float2* __restrict__ C, int Hx, int Ly, int nz,
+                                                                 GreenView gv, const float2* __restrict__ tw) {
+    using E = F2<L>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float2* xb = reinterpret_cast<float2*>(smraw);
+    float2* spec = xb + kColW * E::S;  // natural-order spectrum of this tile's columns
+    // columns are the (kx, ky) plane flattened: f = kx + Hx*ky is contiguous
+    const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
+    const int64_t plane = (int64_t)Hx * Ly;
+    const int f = blockIdx.x * kColW + c;
+    const bool cok = f < plane;
+    const int ky = cok ? f / Hx : 0;
+    const int kx = f - ky * Hx;
+    float2* col = xb + c * E::S;
+    float2* sc = spec + c * E::S;
+    float2 v[16];
+    if (t < E::R2) {
+#pragma unroll
+        for (int s = 0; s < E::R1; ++s) {
+            const int z = t + E::R2 * s;
+            v[s] = (cok && z < nz) ? B[f + plane * z] : make_float2(0.f, 0.f);
+        }
+    }
+    E::template fwd<false>(v, col, t, tw);
+    if (t < E::R1) {
+#pragma unroll
+        for (int r = 0; r < E::R2; ++r) sc[xsw(t + E::R1 * r)] = v[r];
+    }
+    __syncthreads();
+    const int kyf = ky <= Ly / 2 ? ky : Ly - ky;
+    const float ysign = ky <= Ly / 2 ? 1.f : -1.f;
+    const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
+    for (int comp = 0; comp < 3; ++comp) {
+        if (t < E::R1) {
+            const float* gfc = reinterpret_cast<const float*>(gv.gfree) + comp * gv.cs_free + kx + gv.Hx * kyf;
+            const float2* gic = reinterpret_cast<const float2*>(gv.gimg) + comp * gv.cs_img + kx + gv.Hx * kyf;
+#pragma unroll
+            for (int r = 0; r < E::R2; ++r) {
+                const int kz = t + E::R1 * r;
+                float2 out = make_float2(0.f, 0.f);
+                if (cok) {
+                    const int kzf = kz <= L / 2 ? kz : L - kz;
+                    float sg = 1.f;
+                    if (comp == 1) sg = ysign;
+                    if (comp == 2 && kz > L / 2) sg = -1.f;
+                    const float g = sg * __ldg(gfc + gstep * kzf);
+                    const float2 X = sc[xsw(kz)];
+                    out = make_float2(-X.y * g, X.x * g);  // X * (i g)
+                    if (gv.image) {
+                        float2 gc = __ldg(gic + gstep * kz);
+                        if (comp == 1) {
+                            gc.x *= ysign;
+                            gc.y *= ysign;
+                        }
+                        out = cadd(out, cmul(sc[xsw((L - kz) & (L - 1))], gc));
+                    }
+                }
+                v[r] = out;
+            }
+        }
+        E::template inv<true>(v, col, t, tw);
+        if (t < E::R2 && cok) {
+            float2* Cc = C + comp * (plane * nz) + f;
+#pragma unroll
+            for (int s = 0; s < E::R1; ++s) {
+                const int z = t + E::R2 * s;
+                if (z < nz) Cc[plane * z] = v[s];
+            }
+        }
+    }
+}
+
+// Adjoint z pass: three forward z transforms of Ebar_c, correlation with the
+// conjugate Green spectra summed over components, one inverse transform.
+template <int L>
+__global__ void __launch_bounds__(kColW * F2<L>::NT, 2) k2_adj_zpass(const float2* __restrict__ C,
+                                                                     float2* __restrict__ B, int Hx, int Ly, int nz,
+                                                                     GreenView gv, const float2* __restrict__ tw) {
+    using E = F2<L>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float2* xb = reinterpret_cast<float2*>(smraw);
+    float2* spec = xb + kColW * E::S;
+    const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
+    const int64_t plane = (int64_t)Hx * Ly;
+    const int f = blockIdx.x * kColW + c;
+    const bool cok = f < plane;
+    const int ky = cok ? f / Hx : 0;
+    const int kx = f - ky * Hx;
+    float2* col = xb + c * E::S;
+    float2* sc = spec + c * E::S;
+    const int kyf = ky <= Ly / 2 ? ky : Ly - ky;
+    const float ysign = ky <= Ly / 2 ? 1.f : -1.f;
+    const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
+    float2 acc[16], v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) acc[r] = make_float2(0.f, 0.f);
+    for (int comp = 0; comp < 3; ++comp) {
+        const float2* Cc = C + comp * (plane * nz) + f;
+        if (t < E::R2) {
+#pragma unroll
+            for (int s = 0; s < E::R1; ++s) {
+                const int z = t + E::R2 * s;
+                v[s] = (cok && z < nz) ? Cc[plane * z] : make_float2(0.f, 0.f);
+            }
+        }
+        E::template fwd<false>(v, col, t, tw);
+        if (gv.image) {
+            if (t < E::R1) {
+#pragma unroll
+                for (int r = 0; r < E::R2; ++r) sc[xsw(t + E::R1 * r)] = v[r];
+            }
+            __syncthreads();
+        }
+        if (t < E::R1 && cok) {
+            const float* gfc = reinterpret_cast<const float*>(gv.gfree) + comp * gv.cs_free + kx + gv.Hx * kyf;
+            const float2* gic = reinterpret_cast<const float2*>(gv.gimg) + comp * gv.cs_img + kx + gv.Hx * kyf;
+#pragma unroll
+            for (int r = 0; r < E::R2; ++r) {
+                const int kz = t + E::R1 * r;
+                const int kzf = kz <= L / 2 ? kz : L - kz;
+                float sg = 1.f;
+                if (comp == 1) sg = ysign;
+                if (comp == 2 && kz > L / 2) sg = -1.f;
+                const float g = sg * __ldg(gfc + gstep * kzf);
+                // Ebar^ * conj(i g) = Ebar^ * (-i g)
+                acc[r].x += v[r].y * g;
+                acc[r].y -= v[r].x * g;
+                if (gv.image) {
+                    const int kzm = (L - kz) & (L - 1);
+                    float2 gc = __ldg(gic + gstep * kzm);
+                    if (comp == 1) {
+                        gc.x *= ysign;
+                        gc.y *= ysign;
+                    }
+                    acc[r] = cadd(acc[r], cmulc(sc[xsw(kzm)], gc));
+                }
+            }
+        }
+        if (gv.image) __syncthreads();  // spec is rewritten by the next component
+    }
+    E::template inv<true>(acc, col, t, tw);
+    if (t < E::R2 && cok) {
+        float2* Bc = B + f;
+#pragma unroll
+        for (int s = 0; s < E::R1; ++s) {
+            const int z = t + E::R2 * s;
+            if (z < nz) Bc[plane * z] = acc[s];
+        }
+    }
+}
+
+// Adjoint inverse x pass of one component into the fourth lane of the
+// packed nodes (rhobar).
+template <int L>
+__global__ void __launch_bounds__(256) k2_inv_x1(const float2* __restrict__ D, float* __restrict__ E4, int nx,
+                                                 int rows, int Hx, const float2* __restrict__ tw) {
+    using E = F2<L>;
+    constexpr int P = 256 / E::NT;
+    __shared__ float2 xb[P * E::S];
+    const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
+    const int r0 = 2 * (blockIdx.x * P + p), r1 = r0 + 1;
+    float2 v[16];
+    if (t < E::R1) {
+#pragma unroll
+        for (int r = 0; r < E::R2; ++r) {
+            const int k = t + E::R1 * r;
+            const bool cj = k > L / 2;
+            const int kk = cj ? L - k : k;
+            float2 xa = make_float2(0.f, 0.f), xbv = make_float2(0.f, 0.f);
+            if (r0 < rows) xa = D[(int64_t)r0 * Hx + kk];
+            if (r1 < rows) xbv = D[(int64_t)r1 * Hx + kk];
+            if (cj) {
+                xa.y = -xa.y;
+                xbv.y = -xbv.y;
+            }
+            v[r] = make_float2(xa.x - xbv.y, xa.y + xbv.x);
+        }
+    }
+    E::template inv<true>(v, xb + p * E::S, t, tw);
+    if (t < E::R2) {
+#pragma unroll
+        for (int s = 0; s < E::R1; ++s) {
+            const int x = t + E::R2 * s;
+            if (x >= nx) continue;
+            if (r0 < rows) E4[4 * ((int64_t)r0 * nx + x) + 3] = v[s].x;
+            if (r1 < rows) E4[4 * ((int64_t)r1 * nx + x) + 3] = v[s].y;
+        }
+    }
+}
+
+// Green transform on the parity-reduced lattice.  Kernel component c is odd
+// along x for c = 0 and along y for c = 1, even along the other of the two,
+// and in free space odd along z for c = 2 and even otherwise.  The transform
+// of a full line (2n-1 samples, d = -(n-1)..n-1) is then the transform of its
+// d >= 0 half extended with that parity: real for an even line, imaginary for
+// an odd one.  Each pass stores that one real part for k <= L/2, so the three
+// passes read and write real arrays over the d >= 0 octant only, two lines per
+// complex FFT.  With exactly one odd axis per free-space component, the last
+// pass leaves Im(K^), the compressed spectrum.  The image kernel has no parity
+// in z: its z pass transforms the full line and forms the complex spectrum.
+//
+// x pass: rows r = ay + ny*iz of the stored octant G (iz = |dz| in free space,
+// dz + nz - 1 for the image), out T[comp][r][kx], kx <= L/2.
+template <int L>
+__global__ void __launch_bounds__(256) k3_green_x(const float* __restrict__ G, float* __restrict__ T, int nx,
+                                                  int rows, int Hx, int64_t gcs, int64_t tcs,
+                                                  const float2* __restrict__ tw) {
+    using E = F2<L>;
+    constexpr int P = 256 / E::NT;
+    __shared__ float2 xb[P * E::S];
+    const int comp = blockIdx.y;
+    const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
+    const int r0 = 2 * (blockIdx.x * P + p), r1 = r0 + 1;
+    const bool ok0 = r0 < rows, ok1 = r1 < rows;
+    const float* g0 = G + comp * gcs + (int64_t)nx * r0;
+    const float* g1 = g0 + nx;
+    float2* col = xb + p * E::S;
+    float2 v[16];
+    if (t < E::R2) {
+#pragma unroll
+        for (int s = 0; s < E::R1; ++s) {
+            const int x = t + E::R2 * s;
+            const int dx = x < nx ? x : (x > L - nx ? x - L : L);
+            float a = 0.f, b = 0.f;
+            if (dx != L) {
+                const int ax = dx < 0 ? -dx : dx;
+                if (ok0) a = __ldg(g0 + ax);
+                if (ok1) b = __ldg(g1 + ax);
+                if (comp == 0 && dx < 0) a = -a, b = -b;
+            }
+            v[s] = make_float2(a, b);
+        }
+    }
+    E::template fwd<false>(v, col, t, tw);
+    if (t < E::R1) {
+#pragma unroll
+        for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+    }
+    __syncthreads();
+    if (ok0) {
+        float* T0 = T + comp * tcs + (int64_t)Hx * r0;
+        for (int k = t; k <= L / 2; k += E::NT) {
+            float2 xa, xbv;
+            split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
+            T0[k] = comp == 0 ? xa.y : xa.x;
+            if (ok1) T0[Hx + k] = comp == 0 ? xbv.y : xbv.x;
+        }
+    }
+}
+
+// y or z pass of the parity-reduced Green transform: real lines along a
+// strided axis, 2*kColW lines per CTA (line f and f + kColW share one complex
+// FFT).  Line (col, b): input sample d >= 0 at in + b*bs_in + col + d*as_in,
+// d < nh; with `odd_comp` == comp the extension is odd.  IMG (image z pass):
+// the input holds the full line, d + nh - 1 for d = -(nh-1)..nh-1, and the
+// output is the complex image spectrum -i^p X(kz) e^{-2 pi i kz (nh-1)/L}
+// for all kz (p = 1 for components 0 and 1); otherwise k <= L/2 of the kept
+// real part is stored at out + b*bs_out + col + k*as_out.
+template <int L, bool IMG>
+__global__ void __launch_bounds__(kColW * F2<L>::NT) k3_green_col(const float* __restrict__ in, void* __restrict__ out,
+                                                                  int ncols, int nbatch, int nh, int odd_comp,
+                                                                  int64_t as_in, int64_t bs_in, int64_t cs_in,
+                                                                  int64_t as_out, int64_t bs_out, int64_t cs_out,
+                                                                  const float2* __restrict__ tw) {
+    using E = F2<L>;
+    __shared__ float2 xb[kColW * E::S];
+    const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
+    const int comp = blockIdx.y;
+    const int64_t total = (int64_t)ncols * nbatch;
+    const int64_t fa = (int64_t)blockIdx.x * (2 * kColW) + c, fb = fa + kColW;
+    const bool oka = fa < total, okb = fb < total;
+    const int ba = oka ? (int)(fa / ncols) : 0, bb = okb ? (int)(fb / ncols) : 0;
+    const int ca = (int)(fa - (int64_t)ba * ncols), cb = (int)(fb - (int64_t)bb * ncols);
+    const float* sa = in + comp * cs_in + ba * bs_in + ca;
+    const float* sb = in + comp * cs_in + bb * bs_in + cb;
+    const bool odd = comp == odd_comp;
+    float2* col = xb + c * E::S;
+    float2 v[16];
+    if (t < E::R2) {
+#pragma unroll
+        for (int s = 0; s < E::R1; ++s) {
+            const int n = t + E::R2 * s;
+            const int d = n < nh ? n : (n > L - nh ? n - L : L);
+            float a = 0.f, b = 0.f;
+            if (d != L) {
+                const int64_t o = (IMG ? d + nh - 1 : (d < 0 ? -d : d)) * as_in;
+                if (oka) a = __ldg(sa + o);
+                if (okb) b = __ldg(sb + o);
+                if (!IMG && odd && d < 0) a = -a, b = -b;
+            }
+            v[s] = make_float2(a, b);
+        }
+    }
+    E::template fwd<false>(v, col, t, tw);
+    if (t < E::R1) {
+#pragma unroll
+        for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+    }
+    __syncthreads();
+    for (int k = t; k <= L / 2; k += E::NT) {
+        float2 xa, xbv;
+        split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
+        if (!IMG) {
+            float* o = reinterpret_cast<float*>(out) + comp * cs_out + k * as_out;
+            if (oka) o[ba * bs_out + ca] = odd ? xa.y : xa.x;
+            if (okb) o[bb * bs_out + cb] = odd ? xbv.y : xbv.x;
+        } else {
+            // real line: X(L - k) = conj X(k)
+            const int k2 = (L - k) & (L - 1);
+            const float2 ph1 = tw[(int)(((int64_t)k * (nh - 1)) & (L - 1)) * (kMaxL / L)];
+            const float2 ph2 = tw[(int)(((int64_t)k2 * (nh - 1)) & (L - 1)) * (kMaxL / L)];
+            float2* o = reinterpret_cast<float2*>(out) + comp * cs_out;
+            for (int w = 0; w < 2; ++w) {
+                const bool okw = w == 0 ? oka : okb;
+                if (!okw) continue;
+                const float2 x = w == 0 ? xa : xbv;
+                float2 x1 = x, x2 = make_float2(x.x, -x.y);  // X(k), X(L - k)
+                if (comp < 2) {                               // times i
+                    x1 = make_float2(-x1.y, x1.x);
+                    x2 = make_float2(-x2.y, x2.x);
+                }
+                const int64_t base = w == 0 ? (ba * bs_out + ca) : (bb * bs_out + cb);
+                const float2 q1 = cmul(x1, ph1);
+                o[base + k * as_out] = make_float2(-q1.x, -q1.y);
+                if (k2 != k) {
+                    const float2 q2 = cmul(x2, ph2);
+                    o[base + k2 * as_out] = make_float2(-q2.x, -q2.y);
+                }
+            }
+        }
+    }
+}
+
+// Launch helpers: run the two-step kernel when L <= 256, report false
+// otherwise (the caller falls back to the Stockham kernels).
+#define SC_L_SWITCH(logL, MACRO) \
+    switch (logL) {              \
+        case 2: MACRO(4); break; \
+        case 3: MACRO(8); break; \
+        case 4: MACRO(16); break; \
+        case 5: MACRO(32); break; \
+        case 6: MACRO(64); break; \
+        case 7: MACRO(128); break; \
+        case 8: MACRO(256); break; \
+        default: return false;   \
+    }
+
+static bool launch2_col(bool inv, int logL, const float2* in, float2* out, int ncols, int n_valid, int n_store,
+                        int64_t as_in, int64_t bs_in, int64_t cs_in, int64_t as_out, int64_t bs_out, int64_t cs_out,
+                        int nbatch, int ncomp, const float2* tw, cudaStream_t s, int wrap = 0, int bwrap_n = 0,
+                        int bwrap_L = 0) {
+    dim3 grid((unsigned)(((int64_t)ncols * nbatch + kColW - 1) / kColW), ncomp);
+#define SC_K2COL(LL)                                                                                            \
+    if (inv)                                                                                                    \
+        k2_col<LL, true><<<grid, kColW * F2<LL>::NT, 0, s>>>(in, out, ncols, nbatch, n_valid, n_store, wrap, bwrap_n, \
+                                                              bwrap_L, as_in, bs_in, cs_in, as_out, bs_out,     \
+                                                              cs_out, tw);                                      \
+    else                                                                                                        \
+        k2_col<LL, false><<<grid, kColW * F2<LL>::NT, 0, s>>>(in, out, ncols, nbatch, n_valid, n_store, wrap, bwrap_n, \
+                                                               bwrap_L, as_in, bs_in, cs_in, as_out, bs_out,    \
+                                                               cs_out, tw);
+    SC_L_SWITCH(logL, SC_K2COL)
+#undef SC_K2COL
+    return true;
+}
+
+static bool launch2_fwd_x(int logL, const float* rho, float2* A, int nx, int rows, int Hx, const float2* tw,
+                          cudaStream_t s) {
+#define SC_K2FX(LL)                                                          \
+    {                                                                        \
+        constexpr int P = 256 / F2<LL>::NT;                                  \
+        const int pairs = (rows + 1) / 2;                                    \
+        k2_fwd_x<LL><<<(pairs + P - 1) / P, 256, 0, s>>>(rho, A, nx, rows, Hx, tw); \
+    }
+    SC_L_SWITCH(logL, SC_K2FX)
+#undef SC_K2FX
+    return true;
+}
+
+static bool launch2_inv_x(int logL, const float2* D, float4* E4, int nx, int rows, int Hx, int64_t cs,
+                          const float2* tw, cudaStream_t s) {
+#define SC_K2IX(LL)                                                                         \
+    {                                                                                       \
+        constexpr int P = 256 / F2<LL>::NT;                                                 \
+        const size_t smem = sizeof(float2) * (P * F2<LL>::S + 2 * P * LL);                  \
+        if (set_smem(k2_inv_x<LL>, smem) != SC_OK) return false;                            \
+        const int pairs = (rows + 1) / 2;                                                   \
+        k2_inv_x<LL><<<(pairs + P - 1) / P, 256, smem, s>>>(D, E4, nx, rows, Hx, cs, tw);   \
+    }
+    SC_L_SWITCH(logL, SC_K2IX)
+#undef SC_K2IX
+    return true;
+}
+
+static bool launch2_zpass(int logL, const float2* B, float2* C, int Hx, int Ly, int nz, const GreenView& gv,
+                          const float2* tw, cudaStream_t s) {
+#define SC_K2Z(LL)                                                                          \
+    {                                                                                       \
+        const size_t smem = sizeof(float2) * kColW * F2<LL>::S * 2;                         \
+        if (set_smem(k2_zpass<LL>, smem) != SC_OK) return false;                            \
+        const int64_t ncol = (int64_t)Hx * Ly;                                              \
+        k2_zpass<LL><<<(unsigned)((ncol + kColW - 1) / kColW), kColW * F2<LL>::NT, smem, s>>>(B, C, Hx, Ly, nz, gv, tw); \
+    }
+    SC_L_SWITCH(logL, SC_K2Z)
+#undef SC_K2Z
+    return true;
+}
+
+static bool launch2_adj_zpass(int logL, const float2* C, float2* B, int Hx, int Ly, int nz, const GreenView& gv,
+                              const float2* tw, cudaStream_t s) {
+#define SC_K2AZ(LL)                                                                         \
+    {                                                                                       \
+        const size_t smem = sizeof(float2) * kColW * F2<LL>::S * 2;                         \
+        if (set_smem(k2_adj_zpass<LL>, smem) != SC_OK) return false;                        \
+        const int64_t ncol = (int64_t)Hx * Ly;                                              \
+        k2_adj_zpass<LL><<<(unsigned)((ncol + kColW - 1) / kColW), kColW * F2<LL>::NT, smem, s>>>(C, B, Hx, Ly, nz, gv, tw); \
+    }
+    SC_L_SWITCH(logL, SC_K2AZ)
+#undef SC_K2AZ
+    return true;
+}
+
+static bool launch2_inv_x1(int logL, const float2* D, float* E4, int nx, int rows, int Hx, const float2* tw,
+                           cudaStream_t s) {
+#define SC_K2IX1(LL)                                                                  \
+    {                                                                                 \
+        constexpr int P = 256 / F2<LL>::NT;                                           \
+        const int pairs = (rows + 1) / 2;                                             \
+        k2_inv_x1<LL><<<(pairs + P - 1) / P, 256, 0, s>>>(D, E4, nx, rows, Hx, tw);   \
+    }
+    SC_L_SWITCH(logL, SC_K2IX1)
+#undef SC_K2IX1
+    return true;
+}
+
+static bool launch3_green_x(int logL, const float* G, float* T, int nx, int rows, int Hx, int64_t gcs, int64_t tcs,
+                            const float2* tw, cudaStream_t s) {
+#define SC_K3GX(LL)                                                                 \
+    {                                                                               \
+        constexpr int P = 256 / F2<LL>::NT;                                         \
+        dim3 grid(((rows + 1) / 2 + P - 1) / P, 3);                                 \
+        k3_green_x<LL><<<grid, 256, 0, s>>>(G, T, nx, rows, Hx, gcs, tcs, tw);      \
+    }
+    SC_L_SWITCH(logL, SC_K3GX)
+#undef SC_K3GX
+    return true;
+}
+
+static bool launch3_green_col(bool img, int logL, const float* in, void* out, int ncols, int nbatch, int nh,
+                              int odd_comp, int64_t as_in, int64_t bs_in, int64_t cs_in, int64_t as_out,
+                              int64_t bs_out, int64_t cs_out, const float2* tw, cudaStream_t s) {
+    dim3 grid((unsigned)(((int64_t)ncols * nbatch + 2 * kColW - 1) / (2 * kColW)), 3);
+#define SC_K3GC(LL)                                                                                           \
+    if (img)                                                                                                  \
+        k3_green_col<LL, true><<<grid, kColW * F2<LL>::NT, 0, s>>>(in, out, ncols, nbatch, nh, odd_comp, as_in, \
+                                                                   bs_in, cs_in, as_out, bs_out, cs_out, tw);   \
+    else                                                                                                      \
+        k3_green_col<LL, false><<<grid, kColW * F2<LL>::NT, 0, s>>>(in, out, ncols, nbatch, nh, odd_comp,      \
+                                                                    as_in, bs_in, cs_in, as_out, bs_out, cs_out, tw);
+    SC_L_SWITCH(logL, SC_K3GC)
+#undef SC_K3GC
+    return true;
+}
+
+}  // namespace sc

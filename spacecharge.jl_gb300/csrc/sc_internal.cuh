@@ -59,6 +59,9 @@ struct DeviceCtx {
     int sm_count = 0;
 };
 int device_ctx(DeviceCtx** out);  // for the current device
+int fft_engine();                 // 0 = register two-step where possible, 1 = Stockham only
+// autotuned (engine, lgW) for a transform shape, if any (returns false if none)
+bool tuned_choice(int device, int precision, const int L[3], int* engine, int* lgW);
 
 // ----------------------------------------------------------- Green cache
 struct GreenKey {
@@ -87,10 +90,13 @@ struct NativeWork {
     void* kgrid = nullptr;      // real kernel on the L grid (T)
     void* kspec = nullptr;      // its half spectrum (T2), Hx x Ly x Lz
     void* goct = nullptr;       // FP32 path: kernel values on the octant/quadrant, 3 comps
-    void* gspec = nullptr;      // FP32 path: 3 half spectra Hx x Ly x Lz being transformed
+    void* gspec = nullptr;      // FP32 Stockham path: 3 half spectra Hx x Ly x Lz being transformed
+    void* gtmp = nullptr;       // FP32 two-step path: parity-reduced x and y pass outputs (float)
     void* gfree = nullptr;      // compressed free-space spectra, 3 comps (T)
     void* gimg = nullptr;       // compressed image spectra, 3 comps (T2)
     GreenKey key_free, key_img;
+    int engine = -1;  // -1: process-wide setting; 0: two-step; 1: Stockham
+    int lgW = -1;     // Stockham column tile (log2), -1: default
 };
 
 struct PlainWork {
@@ -146,6 +152,9 @@ struct sc_mesh {
     sc::StageTimer timer;
     int64_t launches = 0;     // kernels launched by this mesh
     void* sortwork = nullptr; // sorted-deposit buffers (deposit_sorted.cu)
+    void* tilework = nullptr; // tiled-deposit buffers (deposit_tiled.cu)
+    void* corner = nullptr;   // vector-deposit per-cell corners, float[8N]
+    int kick_mode = SC_DEPOSIT_ATOMIC;  // deposit mode of sc_kick
 };
 
 namespace sc {
@@ -176,6 +185,11 @@ int cell_index_launch(sc_mesh* m, const void* x, const void* y, const void* z, i
                       int32_t* idx, double* frac, cudaStream_t s);
 
 void sorted_release(sc_mesh* m);
+void tiled_release(sc_mesh* m);
+int deposit_tiled_launch(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n,
+                         int dtype, cudaStream_t s);
+int gather_tiled_launch(sc_mesh* m, const void* x, int64_t n, int dtype, void* ex, void* ey, void* ez,
+                        cudaStream_t s);
 
 int plain_solve(sc_mesh* m, int at_cathode, cudaStream_t s);
 int plain_release(sc_mesh* m);
@@ -183,6 +197,7 @@ int plain_release(sc_mesh* m);
 int native_prepare(sc_mesh* m);  // sizes only (no allocation)
 int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s);
 int native_ensure_green(sc_mesh* m, int at_cathode, cudaStream_t s);
+int native_autotune(sc_mesh* m, cudaStream_t s, int* choice);
 int native_solve_noalloc(const int32_t* grid, const double* delta, double gamma, const float* rho, float* efield,
                          cudaStream_t s);
 int adjoint_launch(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,

@@ -5,9 +5,9 @@ Mirrors SpaceCharge.jl's exports (src/SpaceCharge.jl:17): Mesh3D, deposit
 kick (the three in one library call).
 """
 from ._lib import SpaceChargeError, load  # noqa: F401
-from .mesh import (CLIGHT, FPEI, Mesh3D, clear_mesh, deposit, interpolate_field, kick, kick_adjoint,  # noqa: F401
-                   kick_autograd, solve)
+from .mesh import (CLIGHT, FPEI, Batch, Mesh3D, autotune, clear_mesh, deposit, interpolate_field, kick,  # noqa: F401
+                   kick_adjoint, kick_autograd, solve)
 
 __all__ = ["Mesh3D", "deposit", "clear_mesh", "interpolate_field", "solve", "kick", "kick_adjoint",
-           "kick_autograd", "SpaceChargeError",
+           "kick_autograd", "Batch", "autotune", "SpaceChargeError",
            "CLIGHT", "FPEI", "load"]

@@ -28,9 +28,14 @@ SC_PREC_MIXED = 2
 SC_DEPOSIT_ATOMIC = 0
 SC_DEPOSIT_SORTED = 1
 SC_DEPOSIT_DETERMINISTIC = 2
+SC_DEPOSIT_TILED = 3
+SC_DEPOSIT_VECTOR = 4
 
 SC_NUM_STAGES = 9
 STAGES = ["deposit", "green", "fwd_x", "fwd_y", "zpass", "inv_y", "inv_x", "gather", "plain_fft"]
+
+SC_FFT_AUTO = 0
+SC_FFT_STOCKHAM = 1
 
 SC_LAYOUT_PLANAR = 0
 SC_LAYOUT_PACKED = 1
@@ -80,6 +85,8 @@ SIGNATURES = {
     "sc_mesh_rho": [_vp, C.POINTER(_vp)],
     "sc_mesh_efield": [_vp, C.POINTER(_vp)],
     "sc_mesh_set_green_cache": [_vp, _int],
+    "sc_mesh_set_kick_mode": [_vp, _int],
+    "sc_set_fft_engine": [_int],
     "sc_clear_mesh": [_vp, _vp],
     "sc_deposit": [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _int, _vp],
     "sc_solve": [_vp, _int, _vp],
@@ -90,6 +97,13 @@ SIGNATURES = {
     "sc_mesh_launch_count": [_vp, C.POINTER(_i64)],
     "sc_kick_adjoint": [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "sc_solve_noalloc": [_i32p, _dp, C.c_double, _vp, _vp, _vp],
+    "sc_batch_create": [C.POINTER(_vp), _int, _int, C.POINTER(_vp)],
+    "sc_batch_kick": [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_i64), _int,
+                      _int, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), _vp],
+    "sc_batch_set_graph": [_vp, _int],
+    "sc_batch_graph_nodes": [_vp, C.POINTER(_i64)],
+    "sc_batch_destroy": [_vp],
+    "sc_autotune": [_vp, _vp, C.POINTER(_int)],
     "sc_cell_index": [_vp, _vp, _vp, _vp, _i64, _int, _vp, _vp, _vp],
     "sc_mesh_out_of_range": [_vp, C.POINTER(_i64), _vp],
 }

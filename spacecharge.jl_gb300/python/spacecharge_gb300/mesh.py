@@ -18,7 +18,8 @@ FPEI = CLIGHT ** 2 * 1.0e-7  # src/utils.jl:8
 
 _PRECISIONS = {"plain64": L.SC_PREC_PLAIN64, "fp64": L.SC_PREC_FP64, "mixed": L.SC_PREC_MIXED}
 _MODES = {"atomic": L.SC_DEPOSIT_ATOMIC, "sorted": L.SC_DEPOSIT_SORTED,
-          "deterministic": L.SC_DEPOSIT_DETERMINISTIC}
+          "deterministic": L.SC_DEPOSIT_DETERMINISTIC, "tiled": L.SC_DEPOSIT_TILED,
+          "vector": L.SC_DEPOSIT_VECTOR}
 
 
 def _torch():
@@ -171,6 +172,14 @@ class Mesh3D:
                 base = torch.as_tensor(_CudaView(self._h, p.value, (3, nz, ny, nx), ts), device="cuda")
                 self._efield = base.permute(3, 2, 1, 0)
         return self._efield
+
+    def set_kick_mode(self, mode: str) -> None:
+        """Deposit mode used by kick(): "vector" (default for mixed meshes),
+        "atomic" (default otherwise), "tiled" (the kick then also gathers
+        through the same tiles), "sorted" or "deterministic"."""
+        if mode not in _MODES:
+            raise SpaceChargeError(f"unknown deposit mode {mode!r}")
+        L.call("sc_mesh_set_kick_mode", self._h.ptr, _MODES[mode])
 
     def set_green_cache(self, enabled: bool) -> None:
         L.call("sc_mesh_set_green_cache", self._h.ptr, 1 if enabled else 0)
@@ -339,3 +348,73 @@ def kick_autograd(mesh: Mesh3D, x, y, z, q, at_cathode: bool = False):
     if _KICK_FN is None:
         _KICK_FN = _make_kick_function()
     return _KICK_FN.apply(mesh, x, y, z, q, at_cathode)
+
+
+def autotune(mesh: Mesh3D) -> int:
+    """Pick the fastest FFT kernel configuration for this mesh's transform
+    shape (sc_autotune): 0 = register two-step transforms, 2..5 = Stockham
+    transforms with 2**k columns per CTA.  Synchronises."""
+    c = C.c_int()
+    L.call("sc_autotune", mesh.ptr, _stream(), C.byref(c))
+    return int(c.value)
+
+
+class Batch:
+    """Kicks of many independent bunches in one call (sc_batch_kick): each
+    bunch has its own mesh; repeated calls with the same particle tensors
+    replay a captured CUDA graph.  Output tensors are owned by the batch and
+    overwritten by every call with the same inputs."""
+
+    def __init__(self, meshes, nstreams: int = 8):
+        self.meshes = list(meshes)  # keep the meshes alive
+        arr = (C.c_void_p * len(self.meshes))(*[m.ptr.value for m in self.meshes])
+        out = C.c_void_p()
+        L.call("sc_batch_create", arr, len(self.meshes), int(nstreams), C.byref(out))
+        self._ptr = out
+        self._outs = None
+        self._key = None
+
+    def __del__(self):
+        if getattr(self, "_ptr", None) is not None and self._ptr.value and L._lib is not None:
+            L._lib.sc_batch_destroy(self._ptr)
+            self._ptr = None
+
+    def set_graph(self, enabled: bool) -> None:
+        L.call("sc_batch_set_graph", self._ptr, 1 if enabled else 0)
+
+    @property
+    def graph_nodes(self) -> int:
+        n = C.c_int64()
+        L.call("sc_batch_graph_nodes", self._ptr, C.byref(n))
+        return int(n.value)
+
+    def kick(self, xs, ys, zs, qs, at_cathode: bool = False):
+        torch = _torch()
+        nb = len(self.meshes)
+        if not (len(xs) == len(ys) == len(zs) == len(qs) == nb):
+            raise SpaceChargeError(f"need particle arrays for each of the {nb} bunches")
+        dev = []
+        dt = None
+        for i in range(nb):
+            lens = [_length(a) for a in (xs[i], ys[i], zs[i], qs[i])]
+            if not (lens[0] == lens[1] == lens[2] == lens[3]):
+                raise SpaceChargeError("Particle coordinate and charge arrays must have the same length.")
+            # all bunches take the first bunch's element type; CUDA tensors
+            # of that type are used in place (stable pointers: graph replay)
+            want = None if dt is None else (torch.float64 if dt == L.SC_F64 else torch.float32)
+            t, d = _as_device((xs[i], ys[i], zs[i], qs[i]), dtype=want)
+            dt = d
+            dev.append(t)
+        key = tuple(tuple(t.data_ptr() for t in b) for b in dev)
+        if self._outs is None or self._key != key:
+            self._outs = [[torch.empty_like(b[0]) for _ in range(3)] for b in dev]
+            self._key = key
+        self._dev = dev  # keep device copies alive while the graph may read them
+
+        def ptrs(k, src):
+            return (C.c_void_p * nb)(*[src[i][k].data_ptr() for i in range(nb)])
+
+        n = (C.c_int64 * nb)(*[int(b[0].numel()) for b in dev])
+        L.call("sc_batch_kick", self._ptr, ptrs(0, dev), ptrs(1, dev), ptrs(2, dev), ptrs(3, dev), n, dt,
+               1 if at_cathode else 0, ptrs(0, self._outs), ptrs(1, self._outs), ptrs(2, self._outs), _stream())
+        return [tuple(o) for o in self._outs]

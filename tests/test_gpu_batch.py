@@ -1,0 +1,88 @@
+"""Batched multi-bunch kicks (sc_batch_kick, graph replay) and the FFT
+autotuner."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def bunches(nb, seed):
+    rng = np.random.default_rng(seed)
+    grids = [(16, 16, 16), (24, 16, 32), (32, 32, 32), (12, 12, 20), (16, 16, 16)]
+    out = []
+    for i in range(nb):
+        n = int(rng.integers(2000, 40000))
+        sig = rng.uniform(0.2e-3, 2e-3, 3)
+        v = rng.standard_normal((3, n)).clip(-4.5, 4.5) * sig[:, None]
+        q = np.full(n, rng.uniform(1e-11, 1e-9) / n)
+        out.append((grids[i % len(grids)], float(rng.uniform(1, 50)), v[0], v[1], v[2], q))
+    return out
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+def test_batch_matches_single_kicks_and_replays(sc, cuda):
+    import torch
+
+    spec = bunches(5, 1)
+    meshes = [sc.Mesh3D(g, x, y, z, precision="mixed", gamma=gm) for g, gm, x, y, z, q in spec]
+    singles = [sc.Mesh3D(g, x, y, z, precision="mixed", gamma=gm) for g, gm, x, y, z, q in spec]
+    dev = [[torch.from_numpy(a).cuda() for a in (x, y, z, q)] for _, _, x, y, z, q in spec]
+    b = sc.Batch(meshes, nstreams=3)
+    out1 = [tuple(t.clone() for t in o) for o in b.kick(*zip(*dev))]
+    assert b.graph_nodes > 0
+    ref = [sc.kick(m, *d) for m, d in zip(singles, dev)]
+    for o, r in zip(out1, ref):
+        for a, c in zip(o, r):
+            assert rel(a.cpu().numpy(), c.cpu().numpy()) < 1e-5
+    # graph replay after the particles move in place gives the moved fields
+    for d in dev:
+        d[2].mul_(1.1)
+    out2 = b.kick(*zip(*dev))
+    ref2 = [sc.kick(m, *d) for m, d in zip(singles, dev)]
+    for o, r in zip(out2, ref2):
+        for a, c in zip(o, r):
+            assert rel(a.cpu().numpy(), c.cpu().numpy()) < 1e-5
+
+
+def test_batch_cathode_and_eager(sc, cuda):
+    import torch
+
+    spec = bunches(3, 2)
+    meshes = []
+    dev = []
+    for g, gm, x, y, z, q in spec:
+        z = np.abs(z) + 0.1e-3
+        meshes.append(sc.Mesh3D(g, x, y, z, precision="mixed", gamma=gm))
+        dev.append([torch.from_numpy(a).cuda() for a in (x, y, z, q)])
+    b = sc.Batch(meshes)
+    b.set_graph(False)
+    out = b.kick(*zip(*dev), at_cathode=True)
+    assert b.graph_nodes == 0
+    for m, d, o in zip(meshes, dev, out):
+        r = sc.kick(m, *d, at_cathode=True)
+        for a, c in zip(o, r):
+            assert rel(a.cpu().numpy(), c.cpu().numpy()) < 1e-5
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_autotune_choice_keeps_parity(sc, cuda, prec):
+    import oracle as O
+
+    n = 20000
+    rng = np.random.default_rng(5)
+    x, y, z = rng.standard_normal((3, n)).clip(-4.5, 4.5) * 1e-3
+    q = np.full(n, 1e-9 / n)
+    m = sc.Mesh3D((20, 24, 40), x, y, z, precision=prec, gamma=3.0)
+    choice = sc.autotune(m)
+    assert choice in (0, 2, 3, 4, 5)
+    om = O.mesh_auto((20, 24, 40), x, y, z, gamma=3.0)
+    O.deposit(om, x, y, z, q)
+    O.solve(om)
+    sc.deposit(m, x, y, z, q)
+    sc.solve(m)
+    tol = 1e-5 if prec == "mixed" else 1e-10
+    assert rel(m.efield.double().cpu().numpy(), om.efield) < tol

@@ -284,3 +284,27 @@ def test_mixed_vs_fp64_tolerance(sc, cuda):
     assert relerr(res["mixed"][0], res["plain64"][0]) < 1e-5
     for a, b_ in zip(res["mixed"][1], res["plain64"][1]):
         assert relerr(a, b_) < 1e-5
+
+
+@pytest.mark.parametrize("grid,cath", [((64, 64, 128), False), ((12, 20, 33), True), ((3, 5, 9), False)])
+def test_fft_engines_agree(sc, cuda, grid, cath):
+    """The register two-step FFT kernels and the shared-memory Stockham
+    kernels give the same mixed-precision field."""
+    from spacecharge_gb300 import _lib as L
+
+    n = 50_000
+    x, y, z = bunch(n, 13, sig=(1e-3, 1e-3, 0.3e-3))
+    if cath:
+        z = np.abs(z) + 0.1e-3
+    q = np.full(n, 1e-9 / n)
+    m = sc.Mesh3D(grid, x, y, z, precision="mixed", gamma=4.0)
+    out = {}
+    try:
+        for eng in (L.SC_FFT_STOCKHAM, L.SC_FFT_AUTO):
+            L.call("sc_set_fft_engine", eng)
+            sc.deposit(m, x, y, z, q, mode="deterministic")
+            sc.solve(m, at_cathode=cath)
+            out[eng] = host(m.efield)
+    finally:
+        L.call("sc_set_fft_engine", L.SC_FFT_AUTO)
+    assert relerr(out[L.SC_FFT_AUTO], out[L.SC_FFT_STOCKHAM]) < 2e-6
