@@ -163,6 +163,15 @@ int sc_deposit(sc_mesh* mesh, const void* x, const void* y, const void* z,
  * kick with the atomic deposit. */
 int sc_mesh_set_kick_mode(sc_mesh* mesh, int mode);
 
+/* Graph replay of sc_kick (default on; no counterpart in the reference).  A
+ * call with the same particle and output pointers, count, dtype and cathode
+ * flag as the previous one, on an unchanged mesh, replays a CUDA graph of the
+ * kick (one launch on the caller's stream).  The first call with new
+ * arguments runs the kick eagerly and then captures it.  Kicks with stage
+ * profiling on, on SC_PREC_PLAIN64 meshes, or issued into a stream that is
+ * being captured run eagerly. */
+int sc_mesh_set_kick_graph(sc_mesh* mesh, int enabled);
+
 /* solve!(mesh; at_cathode), src/solvers/free_space.jl:14-101. */
 int sc_solve(sc_mesh* mesh, int at_cathode, void* stream);
 

@@ -91,6 +91,35 @@ __global__ void __launch_bounds__(256) k_adj_scatter(const P* __restrict__ px, c
     }
 }
 
+// The same scatter for mixed meshes with the vector deposit's layout: per
+// component with an upstream gradient, two 16-byte vector atomics into that
+// component's per-cell corner slots (corner + 8N*c), summed onto the nodes
+// afterwards by corner_sum_launch.
+template <typename P>
+__global__ void __launch_bounds__(256) k_adj_scatter_vec(const P* __restrict__ px, const P* __restrict__ py,
+                                                         const P* __restrict__ pz, const P* __restrict__ gx,
+                                                         const P* __restrict__ gy, const P* __restrict__ gz,
+                                                         int64_t n, Axes ax, float4* __restrict__ corner, int64_t N) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    int ix, iy, iz;
+    float fx, fy, fz;
+    if (!(cell_df32(px[p], ax.a[0], ix, fx) & cell_df32(py[p], ax.a[1], iy, fy) &
+          cell_df32(pz[p], ax.a[2], iz, fz)))
+        return;
+    const P* gp[3] = {gx, gy, gz};
+    const float ux = 1.0f - fx, uy = 1.0f - fy, uz = 1.0f - fz;
+    const int64_t cell = ix + (int64_t)ax.a[0].n * (iy + (int64_t)ax.a[1].n * iz);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (!gp[c]) continue;
+        const float g = f64_to_f32(gp[c][p]);
+        float4* r = corner + 2 * (c * N + cell);
+        atomicAdd(r, make_float4(g * ux * uy * uz, g * fx * uy * uz, g * ux * fy * uz, g * fx * fy * uz));
+        atomicAdd(r + 1, make_float4(g * ux * uy * fz, g * fx * uy * fz, g * ux * fy * fz, g * fx * fy * fz));
+    }
+}
+
 // z pass of the adjoint: three forward z transforms of Ebar_c, correlation
 // with the Green spectra summed over components, one inverse z transform.
 template <typename T>
@@ -262,10 +291,20 @@ static int adjoint_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q,
     DeviceCtx* ctx = nullptr;
     SC_TRY(device_ctx(&ctx));
     const T2* tw = twiddles<T>(ctx);
-    // forward recompute: rho and E for these particles, Green spectra cached
-    SC_CUDA(cudaMemsetAsync(m->rho, 0, sizeof(T) * m->N, s));
-    SC_TRY(deposit_launch(m, x, y, z, q, n, sizeof(P) == 8 ? SC_F64 : SC_F32, SC_DEPOSIT_ATOMIC, s));
-    SC_TRY(native_solve(m, at_cathode, s));
+    // forward recompute: rho and E for these particles (a Green build, when
+    // needed, overlaps the deposit on the mesh's side stream)
+    cudaEvent_t ready = nullptr;
+    if (n > 0) SC_TRY(native_green_async(m, at_cathode, s, &ready));
+    int st = cudaMemsetAsync(m->rho, 0, sizeof(T) * m->N, s) == cudaSuccess ? SC_OK
+                                                                             : cuda_fail(cudaGetLastError(), "memset");
+    if (st == SC_OK)
+        st = deposit_launch(m, x, y, z, q, n, sizeof(P) == 8 ? SC_F64 : SC_F32,
+                            m->precision == SC_PREC_MIXED ? SC_DEPOSIT_VECTOR : SC_DEPOSIT_ATOMIC, s);
+    if (st != SC_OK) {
+        if (ready) cudaStreamWaitEvent(s, ready, 0);
+        return st;
+    }
+    SC_TRY(native_solve(m, at_cathode, s, ready));
     NativeWork& w = m->nw;
     const int nx = m->n[0], ny = m->n[1], nz = m->n[2];
     const int Lx = w.L[0], Ly = w.L[1], Lz = w.L[2], Hx = w.Hx;
@@ -275,9 +314,25 @@ static int adjoint_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q,
     const Axes ax = make_axes(m);
     k_adj_init<T><<<(N + 255) / 256, 256, 0, s>>>(adjE, (const typename Vec4<T>::V*)ggrid, N);
     SC_LAUNCH_CHECK("k_adj_init");
-    if (gex || gey || gez) {
-        k_adj_scatter<P, T><<<(n + 255) / 256, 256, 0, s>>>(x, y, z, gex, gey, gez, n, ax, adjE, N);
-        SC_LAUNCH_CHECK("k_adj_scatter");
+    if ((gex || gey || gez) && n > 0) {
+        if (std::is_same<T, float>::value) {
+            const size_t slice = sizeof(float) * 8 * (size_t)N;
+            if (!w.adjcorner) SC_CUDA(cudaMalloc(&w.adjcorner, 3 * slice));
+            const P* g[3] = {gex, gey, gez};
+            for (int c = 0; c < 3; ++c)
+                if (g[c]) SC_CUDA(cudaMemsetAsync((char*)w.adjcorner + c * slice, 0, slice, s));
+            k_adj_scatter_vec<P><<<(n + 255) / 256, 256, 0, s>>>(x, y, z, gex, gey, gez, n, ax,
+                                                                 (float4*)w.adjcorner, N);
+            SC_LAUNCH_CHECK("k_adj_scatter_vec");
+            m->launches += 1;
+            for (int c = 0; c < 3; ++c)
+                if (g[c]) SC_TRY(corner_sum_launch(m, (const float*)((char*)w.adjcorner + c * slice),
+                                                   (float*)(adjE + c * N), s));
+        } else {
+            k_adj_scatter<P, T><<<(n + 255) / 256, 256, 0, s>>>(x, y, z, gex, gey, gez, n, ax, adjE, N);
+            SC_LAUNCH_CHECK("k_adj_scatter");
+            m->launches += 1;
+        }
     }
     T2* A = (T2*)w.A;
     T2* B = (T2*)w.B;
@@ -325,7 +380,7 @@ static int adjoint_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q,
     k_adj_particles<P, T><<<(n + 255) / 256, 256, 0, s>>>(x, y, z, q, gex, gey, gez, n, ax, (const T*)m->efield, dx,
                                                          dy, dz, dq);
     SC_LAUNCH_CHECK("k_adj_particles");
-    m->launches += 11;
+    m->launches += 9;  // init, 3 x fwd_x, fwd_y, z pass, inverse y, inverse x, particles
     return SC_OK;
 }
 

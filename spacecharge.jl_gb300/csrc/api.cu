@@ -213,6 +213,115 @@ static bool valid_deposit_mode(int mode) {
            mode == SC_DEPOSIT_TILED || mode == SC_DEPOSIT_VECTOR;
 }
 
+namespace sc {
+
+// The kick as issued stream work: deposit, solve (Green build on the side
+// stream when needed), gather.  Arguments are already validated.
+int kick_issue(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
+               int at_cathode, void* ex, void* ey, void* ez, cudaStream_t s) {
+    if (m->precision == SC_PREC_PLAIN64) {
+        SC_TRY(sc_deposit(m, x, y, z, q, n, dtype, 1, SC_DEPOSIT_ATOMIC, s));
+        SC_TRY(sc_solve(m, at_cathode, s));
+        return sc_interpolate_field(m, x, y, z, n, dtype, ex, ey, ez, s);
+    }
+    DeviceGuard g(m->device);
+    const int mode = m->kick_mode;
+    // The Green spectra do not depend on the charge: when this solve would
+    // build them, they are built on the mesh's side stream during the deposit
+    // and the forward x and y transforms; the z pass waits for them.
+    cudaEvent_t ready = nullptr;
+    if (n > 0) SC_TRY(native_green_async(m, at_cathode, s, &ready));
+    const int st = sc_deposit(m, x, y, z, q, n, dtype, 1, mode, s);
+    if (st != SC_OK) {
+        if (ready) cudaStreamWaitEvent(s, ready, 0);
+        return st;
+    }
+    SC_TRY(native_solve(m, at_cathode, s, ready));
+    if (n == 0) return SC_OK;
+    StageScope sg(m->timer, SC_STAGE_GATHER, s);
+    // the tiled deposit binned exactly these particles: gather through the tiles
+    if (mode == SC_DEPOSIT_TILED) return gather_tiled_launch(m, x, n, dtype, ex, ey, ez, s);
+    return gather_launch(m, x, y, z, n, dtype, ex, ey, ez, s);
+}
+
+// ------------------------------------------------------------ kick graph
+// A repeated sc_kick with the same arguments and mesh state replays a CUDA
+// graph of the kick instead of issuing its ~15 launches from the host.  The
+// first call with new arguments runs eagerly (it also allocates workspaces and
+// builds cached Green spectra) and then captures the same work; the graph is
+// launched on the caller's stream.
+struct KickGraph {
+    cudaStream_t cap = nullptr;  // capture origin (the caller's stream may be the legacy stream)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<int64_t> key;
+    int64_t launches = 0;  // kernels one replay runs
+};
+
+static std::vector<int64_t> kick_key(const sc_mesh* m, const void* const* ptr, int64_t n, int dtype,
+                                      int at_cathode) {
+    std::vector<int64_t> k;
+    for (int i = 0; i < 7; ++i) k.push_back((int64_t)(intptr_t)ptr[i]);
+    k.push_back(n);
+    k.push_back(dtype);
+    k.push_back(at_cathode);
+    k.push_back(m->green_cache);
+    k.push_back(m->kick_mode);
+    k.push_back(fft_engine());
+    k.push_back(m->nw.engine);
+    k.push_back(m->nw.lgW);
+    return k;
+}
+
+void kick_graph_release(sc_mesh* m) {
+    KickGraph* kg = reinterpret_cast<KickGraph*>(m->kickgraph);
+    if (!kg) return;
+    if (kg->exec) cudaGraphExecDestroy(kg->exec);
+    if (kg->graph) cudaGraphDestroy(kg->graph);
+    if (kg->cap) cudaStreamDestroy(kg->cap);
+    delete kg;
+    m->kickgraph = nullptr;
+}
+
+static void kick_graph_drop(KickGraph* kg) {
+    if (kg->exec) cudaGraphExecDestroy(kg->exec);
+    if (kg->graph) cudaGraphDestroy(kg->graph);
+    kg->exec = nullptr;
+    kg->graph = nullptr;
+    kg->key.clear();
+}
+
+static int kick_graph_capture(sc_mesh* m, KickGraph* kg, const void* const* p, int64_t n, int dtype,
+                              int at_cathode, std::vector<int64_t> key) {
+    kick_graph_drop(kg);
+    if (!kg->cap) SC_CUDA(cudaStreamCreateWithFlags(&kg->cap, cudaStreamNonBlocking));
+    const int64_t l0 = m->launches;
+    SC_CUDA(cudaStreamBeginCapture(kg->cap, cudaStreamCaptureModeThreadLocal));
+    int st = kick_issue(m, p[0], p[1], p[2], p[3], n, dtype, at_cathode, const_cast<void*>(p[4]),
+                        const_cast<void*>(p[5]), const_cast<void*>(p[6]), kg->cap);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(kg->cap, &g);
+    kg->launches = m->launches - l0;
+    m->launches = l0;  // captured, not run
+    if (st == SC_OK && e != cudaSuccess) st = cuda_fail(e, "cudaStreamEndCapture");
+    if (st != SC_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&kg->exec, g, 0);
+    if (ei != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return cuda_fail(ei, "cudaGraphInstantiate");
+    }
+    kg->graph = g;
+    kg->key = std::move(key);
+    return SC_OK;
+}
+
+}  // namespace sc
+
+using namespace sc;
+
 extern "C" {
 
 int sc_version(void) { return 10000; }
@@ -277,7 +386,11 @@ int sc_mesh_destroy(sc_mesh* m) {
     m->timer.release();
     sorted_release(m);
     tiled_release(m);
+    kick_graph_release(m);
     cudaFree(m->corner);
+    if (m->side) cudaStreamDestroy(m->side);
+    if (m->ev_fork) cudaEventDestroy(m->ev_fork);
+    if (m->ev_join) cudaEventDestroy(m->ev_join);
     cudaFree(m->rho);
     cudaFree(m->efield);
     cudaFree(m->oob);
@@ -414,17 +527,42 @@ int sc_interpolate_field(sc_mesh* m, const void* x, const void* y, const void* z
 int sc_kick(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
             int at_cathode, void* ex, void* ey, void* ez, void* stream) {
     SC_TRY(check_mesh(m));
-    const int mode = m->precision == SC_PREC_PLAIN64 ? SC_DEPOSIT_ATOMIC : m->kick_mode;
-    SC_TRY(sc_deposit(m, x, y, z, q, n, dtype, 1, mode, stream));
-    SC_TRY(sc_solve(m, at_cathode, stream));
-    if (mode == SC_DEPOSIT_TILED && n > 0) {
-        // the tiled deposit binned exactly these particles: gather through the tiles
-        if (!ex || !ey || !ez) return fail(SC_ERR_INVALID, "output pointer is NULL");
-        DeviceGuard g(m->device);
-        StageScope st(m->timer, SC_STAGE_GATHER, (cudaStream_t)stream);
-        return gather_tiled_launch(m, x, n, dtype, ex, ey, ez, (cudaStream_t)stream);
+    SC_TRY(check_dtype(dtype));
+    if (n < 0) return fail(SC_ERR_INVALID, "Particle coordinate and charge arrays must have the same length.");
+    if (n > 0 && (!x || !y || !z || !q)) return fail(SC_ERR_INVALID, "particle pointer is NULL");
+    if (n > 0 && (!ex || !ey || !ez)) return fail(SC_ERR_INVALID, "particle or output pointer is NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) return cuda_fail(cudaGetLastError(), "cudaStreamIsCapturing");
+    const bool graph = m->kick_graph && m->precision != SC_PREC_PLAIN64 && n > 0 && !m->timer.enabled &&
+                       cs == cudaStreamCaptureStatusNone;
+    if (!graph) return kick_issue(m, x, y, z, q, n, dtype, at_cathode, ex, ey, ez, s);
+    DeviceGuard g(m->device);
+    const void* p[7] = {x, y, z, q, ex, ey, ez};
+    std::vector<int64_t> key = kick_key(m, p, n, dtype, at_cathode);
+    KickGraph* kg = reinterpret_cast<KickGraph*>(m->kickgraph);
+    if (kg && kg->exec && kg->key == key) {
+        SC_CUDA(cudaGraphLaunch(kg->exec, s));
+        m->launches += kg->launches;
+        return SC_OK;
     }
-    return sc_interpolate_field(m, x, y, z, n, dtype, ex, ey, ez, stream);
+    SC_TRY(kick_issue(m, x, y, z, q, n, dtype, at_cathode, ex, ey, ez, s));
+    if (!kg) {
+        kg = new KickGraph();
+        m->kickgraph = kg;
+    }
+    // key again: the eager run may have autotuned or built cached spectra
+    return kick_graph_capture(m, kg, p, n, dtype, at_cathode, kick_key(m, p, n, dtype, at_cathode));
+}
+
+int sc_mesh_set_kick_graph(sc_mesh* m, int enabled) {
+    SC_TRY(check_mesh(m));
+    m->kick_graph = enabled != 0;
+    if (!m->kick_graph) {
+        KickGraph* kg = reinterpret_cast<KickGraph*>(m->kickgraph);
+        if (kg) kick_graph_drop(kg);
+    }
+    return SC_OK;
 }
 
 int sc_mesh_set_kick_mode(sc_mesh* m, int mode) {

@@ -42,7 +42,7 @@ static int batch_issue(sc_batch* b, const void* const* x, const void* const* y, 
     const int ns = (int)b->streams.size();
     for (size_t i = 0; i < b->meshes.size(); ++i) {
         cudaStream_t st = b->streams[i % ns];
-        SC_TRY(sc_kick(b->meshes[i], x[i], y[i], z[i], q[i], n[i], dtype, at_cathode, ex[i], ey[i], ez[i], st));
+        SC_TRY(kick_issue(b->meshes[i], x[i], y[i], z[i], q[i], n[i], dtype, at_cathode, ex[i], ey[i], ez[i], st));
     }
     for (int k = 0; k < ns; ++k) {
         SC_CUDA(cudaEventRecord(b->join[k], b->streams[k]));

@@ -199,10 +199,20 @@ __global__ void __launch_bounds__(256) k_corner_sum(const float* __restrict__ co
     rho[node] += s;
 }
 
+int corner_sum_launch(sc_mesh* m, const float* corner, float* out, cudaStream_t s) {
+    k_corner_sum<<<(m->N + 255) / 256, 256, 0, s>>>(corner, m->n[0], m->n[1], m->N, out);
+    SC_LAUNCH_CHECK("k_corner_sum");
+    m->launches += 1;
+    return SC_OK;
+}
+
 static int deposit_vector_launch(sc_mesh* m, const Axes& ax, const void* x, const void* y, const void* z,
                                  const void* q, int64_t n, int dtype, cudaStream_t s) {
     const size_t bytes = sizeof(float) * 8 * (size_t)m->N;
     if (!m->corner) SC_CUDA(cudaMalloc(&m->corner, bytes));
+    // Clearing here rather than in the node sum: the clear writes whole
+    // sectors, so the atomics then find every line in L2 instead of
+    // fetching it from DRAM.
     SC_CUDA(cudaMemsetAsync(m->corner, 0, bytes, s));
     const int64_t blocks = (n + 256 * kDepPerThread - 1) / (256 * kDepPerThread);
     if (dtype == SC_F64)
@@ -212,11 +222,8 @@ static int deposit_vector_launch(sc_mesh* m, const Axes& ax, const void* x, cons
         deposit_vector<float><<<blocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z,
                                                     (const float*)q, n, ax, (float4*)m->corner, m->oob);
     SC_LAUNCH_CHECK("deposit_vector");
-    k_corner_sum<<<(m->N + 255) / 256, 256, 0, s>>>((const float*)m->corner, m->n[0], m->n[1], m->N,
-                                                     (float*)m->rho);
-    SC_LAUNCH_CHECK("k_corner_sum");
-    m->launches += 2;
-    return SC_OK;
+    m->launches += 1;
+    return corner_sum_launch(m, (const float*)m->corner, (float*)m->rho, s);
 }
 
 // sc_cell_index: bins with the same arithmetic the mesh's deposit uses.

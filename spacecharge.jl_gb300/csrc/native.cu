@@ -745,6 +745,13 @@ static int ensure_green_t(sc_mesh* m, int at_cathode, cudaStream_t s) {
     return SC_OK;
 }
 
+bool native_green_stale(const sc_mesh* m, int at_cathode) {
+    const NativeWork& w = m->nw;
+    const double offz = 2 * m->lo[2] + (m->hi[2] - m->lo[2]);  // free_space.jl:39
+    if (!(m->green_cache && key_matches(w.key_free, m, 0.0))) return true;
+    return at_cathode && !(m->green_cache && key_matches(w.key_img, m, offz));
+}
+
 int native_ensure_green(sc_mesh* m, int at_cathode, cudaStream_t s) {
     if (m->precision == SC_PREC_MIXED) {
         SC_TRY(alloc_work<float>(m));
@@ -755,7 +762,7 @@ int native_ensure_green(sc_mesh* m, int at_cathode, cudaStream_t s) {
 }
 
 template <typename T>
-static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s) {
+static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green_ready) {
     using T2 = typename Cplx<T>::T2;
     DeviceCtx* ctx = nullptr;
     SC_TRY(device_ctx(&ctx));
@@ -765,7 +772,8 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s) {
     const int nx = m->n[0], ny = m->n[1], nz = m->n[2];
     const int Lx = w.L[0], Ly = w.L[1], Lz = w.L[2], Hx = w.Hx;
     (void)Lx;
-    SC_TRY(ensure_green_t<T>(m, at_cathode, s));
+    // green_ready: the spectra are being built on another stream (native_green_async)
+    if (!green_ready) SC_TRY(ensure_green_t<T>(m, at_cathode, s));
     m->launches += 5;
     T2* A = (T2*)w.A;
     T2* B = (T2*)w.B;
@@ -794,6 +802,7 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s) {
     }
     // z + Green + inverse z
     {
+        if (green_ready) SC_CUDA(cudaStreamWaitEvent(s, green_ready, 0));
         StageScope st(m->timer, SC_STAGE_ZPASS, s);
         const GreenView gv = make_green_view(w, at_cathode ? 1 : 0);
         if (two && launch2_zpass(w.log2L[2], (const float2*)B, (float2*)C, Hx, Ly, nz, gv, (const float2*)tw, s)) {
@@ -975,15 +984,33 @@ int native_prepare(sc_mesh* m) {
     return SC_OK;
 }
 
-int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s) {
-    if (m->precision == SC_PREC_MIXED) return solve_t<float>(m, at_cathode, s);
-    return solve_t<double>(m, at_cathode, s);
+int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green_ready) {
+    if (m->precision == SC_PREC_MIXED) return solve_t<float>(m, at_cathode, s, green_ready);
+    return solve_t<double>(m, at_cathode, s, green_ready);
+}
+
+int native_green_async(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t* ready) {
+    *ready = nullptr;
+    if (!native_green_stale(m, at_cathode)) return SC_OK;
+    if (!m->side) SC_CUDA(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
+    if (!m->ev_fork) SC_CUDA(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
+    if (!m->ev_join) SC_CUDA(cudaEventCreateWithFlags(&m->ev_join, cudaEventDisableTiming));
+    SC_CUDA(cudaEventRecord(m->ev_fork, s));
+    SC_CUDA(cudaStreamWaitEvent(m->side, m->ev_fork, 0));
+    const int st = native_ensure_green(m, at_cathode, m->side);
+    const cudaError_t e = cudaEventRecord(m->ev_join, m->side);
+    if (st != SC_OK || e != cudaSuccess) {
+        cudaStreamWaitEvent(s, m->ev_join, 0);
+        return st != SC_OK ? st : cuda_fail(e, "cudaEventRecord");
+    }
+    *ready = m->ev_join;
+    return SC_OK;
 }
 
 int native_release(sc_mesh* m) {
     NativeWork& w = m->nw;
-    void* ptrs[] = {w.A,     w.B,     w.C,    w.D,     w.adjE,  w.fnear, w.fcorner,
-                    w.kgrid, w.kspec, w.goct, w.gspec, w.gtmp, w.gfree, w.gimg};
+    void* ptrs[] = {w.A,     w.B,     w.C,    w.D,     w.adjE,  w.adjcorner, w.fnear, w.fcorner,
+                    w.kgrid, w.kspec, w.goct, w.gspec, w.gtmp,  w.gfree,     w.gimg};
     for (void* p : ptrs) cudaFree(p);
     int L[3] = {w.L[0], w.L[1], w.L[2]};
     int lg[3] = {w.log2L[0], w.log2L[1], w.log2L[2]};

@@ -14,6 +14,15 @@ namespace sc {
 
 constexpr int kColW = 16;  // columns per CTA of the column passes
 
+// CTAs per SM the register allocation of the z passes and the column passes
+// is sized for (the z pass's two shared buffers, 70 KB at L = 256, allow 3)
+#ifndef SC_ZPASS_MINB
+#define SC_ZPASS_MINB 2
+#endif
+#ifndef SC_COL_MINB
+#define SC_COL_MINB 1
+#endif
+
 // Batched strided column FFT.  Forward (INV = false): inputs n < n_valid
 // (natural order, zero beyond; with `wrap` also n > L - n_valid), all L
 // outputs.  Inverse: all L inputs, outputs n < n_store.  Element
@@ -23,7 +32,7 @@ constexpr int kColW = 16;  // columns per CTA of the column passes
 __device__ __forceinline__ int wrap_row2(int c, int n, int L) { return c < n ? c : L - (2 * n - 1) + c; }
 
 template <int L, bool INV>
-__global__ void __launch_bounds__(kColW * F2<L>::NT) k2_col(const float2* in, float2* out, int ncols, int nbatch,
+__global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k2_col(const float2* in, float2* out, int ncols, int nbatch,
                                                             int n_valid, int n_store, int wrap, int bwrap_n, int bwrap_L,
                                                             int64_t as_in, int64_t bs_in, int64_t cs_in,
                                                             int64_t as_out, int64_t bs_out, int64_t cs_out,
@@ -170,7 +179,7 @@ __global__ void __launch_bounds__(256) k2_inv_x(const float2* __restrict__ D, fl
 // Green spectra (image: rho^ at -kz times the image spectrum), three inverse
 // transforms, z < nz stored.
 template <int L>
-__global__ void __launch_bounds__(kColW * F2<L>::NT, 2) k2_zpass(const float2* __restrict__ B,
+__global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(const float2* __restrict__ B,
                                                                  float2* __restrict__ C, int Hx, int Ly, int nz,
                                                                  GreenView gv, const float2* __restrict__ tw) {
     using E = F2<L>;
@@ -246,7 +255,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, 2) k2_zpass(const float2* _
 // Adjoint z pass: three forward z transforms of Ebar_c, correlation with the
 // conjugate Green spectra summed over components, one inverse transform.
 template <int L>
-__global__ void __launch_bounds__(kColW * F2<L>::NT, 2) k2_adj_zpass(const float2* __restrict__ C,
+__global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass(const float2* __restrict__ C,
                                                                      float2* __restrict__ B, int Hx, int Ly, int nz,
                                                                      GreenView gv, const float2* __restrict__ tw) {
     using E = F2<L>;
@@ -430,7 +439,7 @@ __global__ void __launch_bounds__(256) k3_green_x(const float* __restrict__ G, f
 // for all kz (p = 1 for components 0 and 1); otherwise k <= L/2 of the kept
 // real part is stored at out + b*bs_out + col + k*as_out.
 template <int L, bool IMG>
-__global__ void __launch_bounds__(kColW * F2<L>::NT) k3_green_col(const float* __restrict__ in, void* __restrict__ out,
+__global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(const float* __restrict__ in, void* __restrict__ out,
                                                                   int ncols, int nbatch, int nh, int odd_comp,
                                                                   int64_t as_in, int64_t bs_in, int64_t cs_in,
                                                                   int64_t as_out, int64_t bs_out, int64_t cs_out,

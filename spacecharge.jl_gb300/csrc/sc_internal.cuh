@@ -83,6 +83,7 @@ struct NativeWork {
     void* C = nullptr;      // 3 x Hx x Ly x nz        (after z pass)
     void* D = nullptr;      // 3 x Hx x ny x nz        (after inverse y)
     void* adjE = nullptr;   // adjoint: 3 x N accumulated dL/dE (T)
+    void* adjcorner = nullptr;  // adjoint, mixed: 3 x 8N per-cell corner slots (float)
     // Green function construction
     double* fcorner = nullptr;  // FP64 antiderivative on corner lattice
     double* fnear = nullptr;    // FP32 path: FP64 antiderivative on the near-box corners
@@ -154,6 +155,10 @@ struct sc_mesh {
     void* sortwork = nullptr; // sorted-deposit buffers (deposit_sorted.cu)
     void* tilework = nullptr; // tiled-deposit buffers (deposit_tiled.cu)
     void* corner = nullptr;   // vector-deposit per-cell corners, float[8N]
+    cudaStream_t side = nullptr;  // Green build concurrent with the deposit (native_green_async)
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    bool kick_graph = true;       // sc_kick replays a captured graph on repeated calls
+    void* kickgraph = nullptr;    // its state (api.cu)
     int kick_mode = SC_DEPOSIT_ATOMIC;  // deposit mode of sc_kick
 };
 
@@ -178,6 +183,15 @@ int bounds_reduce(const void* x, const void* y, const void* z, int64_t n, int dt
 
 int deposit_launch(sc_mesh* m, const void* x, const void* y, const void* z, const void* q,
                    int64_t n, int dtype, int mode, cudaStream_t s);
+// out[node] += sum of the node's entries in the 8 cells around it (float[8N]
+// per-cell corner slots, the vector deposit's layout)
+int corner_sum_launch(sc_mesh* m, const float* corner, float* out, cudaStream_t s);
+// the kick as stream work, without graph replay (api.cu)
+int kick_issue(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
+               int at_cathode, void* ex, void* ey, void* ez, cudaStream_t s);
+void kick_graph_release(sc_mesh* m);
+// true when the next solve would (re)build a Green spectrum
+bool native_green_stale(const sc_mesh* m, int at_cathode);
 int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n,
                   int dtype, void* ex, void* ey, void* ez, cudaStream_t s);
 
@@ -195,7 +209,14 @@ int plain_solve(sc_mesh* m, int at_cathode, cudaStream_t s);
 int plain_release(sc_mesh* m);
 
 int native_prepare(sc_mesh* m);  // sizes only (no allocation)
-int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s);
+// green_ready: the Green spectra of this solve are being built on another
+// stream and are complete when this event fires (native_green_async)
+int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green_ready = nullptr);
+// When the next solve would build Green spectra, starts that build on the
+// mesh's side stream (forked from s) and returns in *ready the event that
+// marks its end; otherwise *ready = nullptr.  The spectra do not depend on
+// rho, so the caller's deposit overlaps the build.
+int native_green_async(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t* ready);
 int native_ensure_green(sc_mesh* m, int at_cathode, cudaStream_t s);
 int native_autotune(sc_mesh* m, cudaStream_t s, int* choice);
 int native_solve_noalloc(const int32_t* grid, const double* delta, double gamma, const float* rho, float* efield,

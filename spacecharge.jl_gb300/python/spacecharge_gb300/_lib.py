@@ -86,6 +86,7 @@ SIGNATURES = {
     "sc_mesh_efield": [_vp, C.POINTER(_vp)],
     "sc_mesh_set_green_cache": [_vp, _int],
     "sc_mesh_set_kick_mode": [_vp, _int],
+    "sc_mesh_set_kick_graph": [_vp, _int],
     "sc_set_fft_engine": [_int],
     "sc_clear_mesh": [_vp, _vp],
     "sc_deposit": [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _int, _vp],

@@ -181,6 +181,17 @@ class Mesh3D:
             raise SpaceChargeError(f"unknown deposit mode {mode!r}")
         L.call("sc_mesh_set_kick_mode", self._h.ptr, _MODES[mode])
 
+    def launch_count(self) -> int:
+        """Kernels this mesh's calls have launched (graph replays included)."""
+        n = C.c_int64()
+        L.call("sc_mesh_launch_count", self._h.ptr, C.byref(n))
+        return int(n.value)
+
+    def set_kick_graph(self, enabled: bool) -> None:
+        """Replay repeated kick() calls with the same particle and output
+        arrays as one CUDA graph launch (default on)."""
+        L.call("sc_mesh_set_kick_graph", self._h.ptr, 1 if enabled else 0)
+
     def set_green_cache(self, enabled: bool) -> None:
         L.call("sc_mesh_set_green_cache", self._h.ptr, 1 if enabled else 0)
 

