@@ -367,17 +367,15 @@ def main():
     errs_p = [rel(a, b) for a, b in zip(mixed_e, plain_e)]
     err_part = (max(e[0] for e in errs_p), max(e[1] for e in errs_p))
 
-    # ---- end to end through the public API with host buffers
+    # ---- end to end through the public API with host buffers: sc_kick_host
+    #      copies the page-locked particles in, kicks, copies the field out
     host_in = [torch.from_numpy(v).pin_memory() for v in bunch]
     host_out = [torch.empty(NP, dtype=torch.float64).pin_memory() for _ in range(3)]
     mm.set_green_cache(False)
 
     def e2e_step():
-        for h, d in zip(host_in, dev):
-            d.copy_(h, non_blocking=True)
-        kick(mm)()
-        for h, d in zip(host_out, (ex, ey, ez)):
-            h.copy_(d, non_blocking=True)
+        L.call("sc_kick_host", mm.ptr, *[C.c_void_p(t.data_ptr()) for t in host_in], NP, L.SC_F64, 0,
+               *[C.c_void_p(t.data_ptr()) for t in host_out], C.c_void_p(stream.cuda_stream))
 
     ms_e2e = max_over_ranks(timed(e2e_step, args.steps, args.warmup), ws)
 

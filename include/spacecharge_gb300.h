@@ -163,6 +163,17 @@ int sc_deposit(sc_mesh* mesh, const void* x, const void* y, const void* z,
  * kick with the atomic deposit. */
 int sc_mesh_set_kick_mode(sc_mesh* mesh, int mode);
 
+/* sc_kick with the particles and outputs in HOST memory (no counterpart in
+ * the reference, whose arrays are CuArrays).  The library copies the
+ * particles to its own device buffers in chunks on a copy stream,
+ * depositing each chunk as it arrives, and copies each chunk's field back
+ * while the next is gathered.  Page-locked host buffers give the overlap;
+ * pageable ones work but copy synchronously.  The outputs are valid once
+ * `stream` has reached this call's end.  The sorted, deterministic and tiled
+ * kick modes copy everything first. */
+int sc_kick_host(sc_mesh* mesh, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
+                 int at_cathode, void* ex, void* ey, void* ez, void* stream);
+
 /* Graph replay of sc_kick (default on; no counterpart in the reference).  A
  * call with the same particle and output pointers, count, dtype and cathode
  * flag as the previous one, on an unchanged mesh, replays a CUDA graph of the

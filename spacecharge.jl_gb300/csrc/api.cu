@@ -5,6 +5,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
 #include <mutex>
 #include <vector>
@@ -308,13 +309,141 @@ static int kick_graph_capture(sc_mesh* m, KickGraph* kg, const void* const* p, i
         if (g) cudaGraphDestroy(g);
         return st;
     }
-    const cudaError_t ei = cudaGraphInstantiate(&kg->exec, g, 0);
+    // keep the side stream's priority for the Green build's nodes
+    const cudaError_t ei = cudaGraphInstantiateWithFlags(&kg->exec, g, cudaGraphInstantiateFlagUseNodePriority);
     if (ei != cudaSuccess) {
         cudaGraphDestroy(g);
         return cuda_fail(ei, "cudaGraphInstantiate");
     }
     kg->graph = g;
     kg->key = std::move(key);
+    return SC_OK;
+}
+
+// ------------------------------------------------------ host-buffer kick
+// sc_kick_host: particles and outputs in host memory.  The particles go to
+// device staging buffers in chunks on an H2D copy stream and each chunk is
+// deposited as soon as it has arrived; after the solve, each chunk is
+// gathered and copied back on a D2H copy stream while the next is gathered.
+// The Green build runs on the side stream from the start.
+constexpr int kHostChunks = 4;
+
+struct HostPipe {
+    void* stage = nullptr;  // x, y, z, q, ex, ey, ez, each cap particles
+    int64_t cap = 0;
+    size_t elem = 0;
+    cudaStream_t h2d = nullptr, d2h = nullptr;
+    cudaEvent_t fork = nullptr, done = nullptr;
+    cudaEvent_t in[kHostChunks] = {}, out[kHostChunks] = {};
+};
+
+void host_pipe_release(sc_mesh* m) {
+    HostPipe* hp = reinterpret_cast<HostPipe*>(m->hostpipe);
+    if (!hp) return;
+    cudaFree(hp->stage);
+    if (hp->h2d) cudaStreamDestroy(hp->h2d);
+    if (hp->d2h) cudaStreamDestroy(hp->d2h);
+    cudaEvent_t evs[] = {hp->fork, hp->done};
+    for (cudaEvent_t e : evs)
+        if (e) cudaEventDestroy(e);
+    for (int c = 0; c < kHostChunks; ++c) {
+        if (hp->in[c]) cudaEventDestroy(hp->in[c]);
+        if (hp->out[c]) cudaEventDestroy(hp->out[c]);
+    }
+    delete hp;
+    m->hostpipe = nullptr;
+}
+
+static int host_pipe(sc_mesh* m, int64_t n, size_t elem, HostPipe** out) {
+    HostPipe* hp = reinterpret_cast<HostPipe*>(m->hostpipe);
+    if (!hp) {
+        hp = new HostPipe();
+        m->hostpipe = hp;
+        SC_CUDA(cudaStreamCreateWithFlags(&hp->h2d, cudaStreamNonBlocking));
+        SC_CUDA(cudaStreamCreateWithFlags(&hp->d2h, cudaStreamNonBlocking));
+        SC_CUDA(cudaEventCreateWithFlags(&hp->fork, cudaEventDisableTiming));
+        SC_CUDA(cudaEventCreateWithFlags(&hp->done, cudaEventDisableTiming));
+        for (int c = 0; c < kHostChunks; ++c) {
+            SC_CUDA(cudaEventCreateWithFlags(&hp->in[c], cudaEventDisableTiming));
+            SC_CUDA(cudaEventCreateWithFlags(&hp->out[c], cudaEventDisableTiming));
+        }
+    }
+    if (hp->cap < n || hp->elem != elem) {
+        cudaFree(hp->stage);
+        hp->stage = nullptr;
+        hp->cap = 0;
+        SC_CUDA(cudaMalloc(&hp->stage, 7 * elem * (size_t)n));
+        hp->cap = n;
+        hp->elem = elem;
+    }
+    *out = hp;
+    return SC_OK;
+}
+
+static int kick_host_issue(sc_mesh* m, const void* const* hin, int64_t n, int dtype, int at_cathode,
+                           void* const* hout, cudaStream_t s) {
+    const size_t elem = dtype == SC_F64 ? 8 : 4;
+    HostPipe* hp = nullptr;
+    SC_TRY(host_pipe(m, n, elem, &hp));
+    char* st = (char*)hp->stage;
+    char* d[7];
+    for (int i = 0; i < 7; ++i) d[i] = st + (size_t)i * elem * (size_t)hp->cap;
+    const int mode = m->precision == SC_PREC_PLAIN64 ? SC_DEPOSIT_ATOMIC : m->kick_mode;
+    const bool chunked = deposit_chunkable(m, mode);
+    const int K = chunked ? (int)std::min<int64_t>(kHostChunks, std::max<int64_t>(1, n / 65536)) : 1;
+    const int64_t per = (n + K - 1) / K;
+    SC_CUDA(cudaEventRecord(hp->fork, s));
+    SC_CUDA(cudaStreamWaitEvent(hp->h2d, hp->fork, 0));
+    SC_CUDA(cudaStreamWaitEvent(hp->d2h, hp->fork, 0));
+    if (!chunked) {
+        // sorted, deterministic and tiled deposits need every particle at once
+        for (int i = 0; i < 4; ++i)
+            SC_CUDA(cudaMemcpyAsync(d[i], hin[i], elem * (size_t)n, cudaMemcpyHostToDevice, hp->h2d));
+        SC_CUDA(cudaEventRecord(hp->in[0], hp->h2d));
+        SC_CUDA(cudaStreamWaitEvent(s, hp->in[0], 0));
+        SC_TRY(kick_issue(m, d[0], d[1], d[2], d[3], n, dtype, at_cathode, d[4], d[5], d[6], s));
+        SC_CUDA(cudaEventRecord(hp->out[0], s));
+        SC_CUDA(cudaStreamWaitEvent(hp->d2h, hp->out[0], 0));
+        for (int i = 0; i < 3; ++i)
+            SC_CUDA(cudaMemcpyAsync(hout[i], d[4 + i], elem * (size_t)n, cudaMemcpyDeviceToHost, hp->d2h));
+    } else {
+        cudaEvent_t ready = nullptr;
+        if (m->precision != SC_PREC_PLAIN64) SC_TRY(native_green_async(m, at_cathode, s, &ready));
+        {
+            StageScope sd(m->timer, SC_STAGE_DEPOSIT, s);
+            SC_TRY(deposit_chunk_begin(m, mode, s));
+            for (int c = 0; c < K; ++c) {
+                const int64_t off = c * per, cnt = std::min<int64_t>(per, n - off);
+                if (cnt <= 0) break;
+                for (int i = 0; i < 4; ++i)
+                    SC_CUDA(cudaMemcpyAsync(d[i] + off * elem, (const char*)hin[i] + off * elem, elem * (size_t)cnt,
+                                            cudaMemcpyHostToDevice, hp->h2d));
+                SC_CUDA(cudaEventRecord(hp->in[c], hp->h2d));
+                SC_CUDA(cudaStreamWaitEvent(s, hp->in[c], 0));
+                SC_TRY(deposit_chunk_add(m, d[0] + off * elem, d[1] + off * elem, d[2] + off * elem,
+                                         d[3] + off * elem, cnt, dtype, mode, s));
+            }
+            SC_TRY(deposit_chunk_finish(m, mode, s));
+        }
+        if (m->precision == SC_PREC_PLAIN64)
+            SC_TRY(plain_solve(m, at_cathode, s));
+        else
+            SC_TRY(native_solve(m, at_cathode, s, ready));
+        StageScope sg(m->timer, SC_STAGE_GATHER, s);
+        for (int c = 0; c < K; ++c) {
+            const int64_t off = c * per, cnt = std::min<int64_t>(per, n - off);
+            if (cnt <= 0) break;
+            SC_TRY(gather_launch(m, d[0] + off * elem, d[1] + off * elem, d[2] + off * elem, cnt, dtype,
+                                 d[4] + off * elem, d[5] + off * elem, d[6] + off * elem, s));
+            SC_CUDA(cudaEventRecord(hp->out[c], s));
+            SC_CUDA(cudaStreamWaitEvent(hp->d2h, hp->out[c], 0));
+            for (int i = 0; i < 3; ++i)
+                SC_CUDA(cudaMemcpyAsync((char*)hout[i] + off * elem, d[4 + i] + off * elem, elem * (size_t)cnt,
+                                        cudaMemcpyDeviceToHost, hp->d2h));
+        }
+    }
+    SC_CUDA(cudaEventRecord(hp->done, hp->d2h));
+    SC_CUDA(cudaStreamWaitEvent(s, hp->done, 0));
     return SC_OK;
 }
 
@@ -387,6 +516,7 @@ int sc_mesh_destroy(sc_mesh* m) {
     sorted_release(m);
     tiled_release(m);
     kick_graph_release(m);
+    host_pipe_release(m);
     cudaFree(m->corner);
     if (m->side) cudaStreamDestroy(m->side);
     if (m->ev_fork) cudaEventDestroy(m->ev_fork);
@@ -553,6 +683,21 @@ int sc_kick(sc_mesh* m, const void* x, const void* y, const void* z, const void*
     }
     // key again: the eager run may have autotuned or built cached spectra
     return kick_graph_capture(m, kg, p, n, dtype, at_cathode, kick_key(m, p, n, dtype, at_cathode));
+}
+
+int sc_kick_host(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
+                 int at_cathode, void* ex, void* ey, void* ez, void* stream) {
+    SC_TRY(check_mesh(m));
+    SC_TRY(check_dtype(dtype));
+    if (n < 0) return fail(SC_ERR_INVALID, "Particle coordinate and charge arrays must have the same length.");
+    if (n > 0 && (!x || !y || !z || !q)) return fail(SC_ERR_INVALID, "particle pointer is NULL");
+    if (n > 0 && (!ex || !ey || !ez)) return fail(SC_ERR_INVALID, "particle or output pointer is NULL");
+    if (n == 0) return sc_kick(m, nullptr, nullptr, nullptr, nullptr, 0, dtype, at_cathode, nullptr, nullptr, nullptr,
+                               stream);
+    DeviceGuard g(m->device);
+    const void* hin[4] = {x, y, z, q};
+    void* hout[3] = {ex, ey, ez};
+    return kick_host_issue(m, hin, n, dtype, at_cathode, hout, (cudaStream_t)stream);
 }
 
 int sc_mesh_set_kick_graph(sc_mesh* m, int enabled) {

@@ -150,7 +150,7 @@ int sc_batch_kick(sc_batch* b, const void* const* x, const void* const* y, const
         e = cudaStreamEndCapture(b->cap, &g);
         if (st == SC_OK && e != cudaSuccess) st = cuda_fail(e, "cudaStreamEndCapture");
         if (st == SC_OK) {
-            e = cudaGraphInstantiate(&b->exec, g, 0);
+            e = cudaGraphInstantiateWithFlags(&b->exec, g, cudaGraphInstantiateFlagUseNodePriority);
             if (e != cudaSuccess) {
                 st = cuda_fail(e, "cudaGraphInstantiate");
                 cudaGraphDestroy(g);

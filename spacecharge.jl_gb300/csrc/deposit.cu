@@ -78,7 +78,10 @@ struct CellCalc<double> {
 
 // Particles per thread of the atomic deposit: all their loads are issued
 // before any arithmetic, so each thread keeps several requests in flight.
-constexpr int kDepPerThread = 4;
+#ifndef SC_DEP_PT
+#define SC_DEP_PT 4
+#endif
+constexpr int kDepPerThread = SC_DEP_PT;
 
 template <typename P, typename A>
 __global__ void __launch_bounds__(256) deposit_atomic(const P* __restrict__ px, const P* __restrict__ py,
@@ -206,14 +209,18 @@ int corner_sum_launch(sc_mesh* m, const float* corner, float* out, cudaStream_t 
     return SC_OK;
 }
 
-static int deposit_vector_launch(sc_mesh* m, const Axes& ax, const void* x, const void* y, const void* z,
-                                 const void* q, int64_t n, int dtype, cudaStream_t s) {
+static int corner_clear(sc_mesh* m, cudaStream_t s) {
     const size_t bytes = sizeof(float) * 8 * (size_t)m->N;
     if (!m->corner) SC_CUDA(cudaMalloc(&m->corner, bytes));
     // Clearing here rather than in the node sum: the clear writes whole
     // sectors, so the atomics then find every line in L2 instead of
     // fetching it from DRAM.
     SC_CUDA(cudaMemsetAsync(m->corner, 0, bytes, s));
+    return SC_OK;
+}
+
+static int deposit_vector_add(sc_mesh* m, const Axes& ax, const void* x, const void* y, const void* z,
+                              const void* q, int64_t n, int dtype, cudaStream_t s) {
     const int64_t blocks = (n + 256 * kDepPerThread - 1) / (256 * kDepPerThread);
     if (dtype == SC_F64)
         deposit_vector<double><<<blocks, 256, 0, s>>>((const double*)x, (const double*)y, (const double*)z,
@@ -223,7 +230,40 @@ static int deposit_vector_launch(sc_mesh* m, const Axes& ax, const void* x, cons
                                                     (const float*)q, n, ax, (float4*)m->corner, m->oob);
     SC_LAUNCH_CHECK("deposit_vector");
     m->launches += 1;
+    return SC_OK;
+}
+
+static int deposit_vector_launch(sc_mesh* m, const Axes& ax, const void* x, const void* y, const void* z,
+                                 const void* q, int64_t n, int dtype, cudaStream_t s) {
+    SC_TRY(corner_clear(m, s));
+    SC_TRY(deposit_vector_add(m, ax, x, y, z, q, n, dtype, s));
     return corner_sum_launch(m, (const float*)m->corner, (float*)m->rho, s);
+}
+
+// Deposit in chunks (sc_kick_host): the atomic and vector modes accumulate,
+// so chunks can be deposited as their particles arrive.
+bool deposit_chunkable(const sc_mesh* m, int mode) {
+    return m->precision == SC_PREC_PLAIN64 || mode == SC_DEPOSIT_ATOMIC || mode == SC_DEPOSIT_VECTOR;
+}
+
+int deposit_chunk_begin(sc_mesh* m, int mode, cudaStream_t s) {
+    SC_CUDA(cudaMemsetAsync(m->rho, 0, field_elem_bytes(m->precision) * m->N, s));
+    if (mode == SC_DEPOSIT_VECTOR && m->precision == SC_PREC_MIXED) SC_TRY(corner_clear(m, s));
+    return SC_OK;
+}
+
+int deposit_chunk_add(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
+                      int mode, cudaStream_t s) {
+    if (n == 0) return SC_OK;
+    if (mode == SC_DEPOSIT_VECTOR && m->precision == SC_PREC_MIXED)
+        return deposit_vector_add(m, make_axes(m), x, y, z, q, n, dtype, s);
+    return deposit_launch(m, x, y, z, q, n, dtype, SC_DEPOSIT_ATOMIC, s);
+}
+
+int deposit_chunk_finish(sc_mesh* m, int mode, cudaStream_t s) {
+    if (mode == SC_DEPOSIT_VECTOR && m->precision == SC_PREC_MIXED)
+        return corner_sum_launch(m, (const float*)m->corner, (float*)m->rho, s);
+    return SC_OK;
 }
 
 // sc_cell_index: bins with the same arithmetic the mesh's deposit uses.

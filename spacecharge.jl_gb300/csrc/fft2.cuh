@@ -39,17 +39,26 @@ template <> struct Split<64> { static constexpr int R1 = 8, R2 = 8; };
 template <> struct Split<128> { static constexpr int R1 = 16, R2 = 8; };
 template <> struct Split<256> { static constexpr int R1 = 16, R2 = 16; };
 
+// Stage w_L^j = exp(-2 pi i j / L), j < L, from the device table of
+// exp(-2 pi i k / kMaxL) into shared memory: the transforms below read their
+// twiddles there (a shared-memory load instead of a global one).
+template <int L, typename T2>
+__device__ __forceinline__ void stage_twiddles(T2* sw, const T2* __restrict__ tw) {
+    for (int j = threadIdx.x; j < L; j += blockDim.x) sw[j] = __ldg(tw + j * (kMaxL / L));
+    __syncthreads();
+}
+
 template <int L>
 struct F2 {
     static constexpr int R1 = Split<L>::R1, R2 = Split<L>::R2;
     static constexpr int NT = R1 > R2 ? R1 : R2;
     static constexpr int S = XS<L>::value;
-    static constexpr int TSTEP = kMaxL / L;
 
     // A -> B.  v holds R1 (data) values on entry when t < R2; on exit R2
-    // (spectrum) values when t < R1.  `col` is this column's exchange buffer.
+    // (spectrum) values when t < R1.  `col` is this column's exchange buffer,
+    // `sw` the staged twiddles w_L^j.
     template <bool INV, typename T2>
-    __device__ __forceinline__ static void fwd(T2 (&v)[16], T2* col, int t, const T2* __restrict__ tw) {
+    __device__ __forceinline__ static void fwd(T2 (&v)[16], T2* col, int t, const T2* sw) {
         if (t < R2) {
             dft<R1, INV>(v);
 #pragma unroll
@@ -61,7 +70,7 @@ struct F2 {
             for (int r = 0; r < R2; ++r) {
                 T2 a = col[xsw(t + R1 * r)];
                 if (r > 0) {
-                    const T2 w = __ldg(tw + r * t * TSTEP);
+                    const T2 w = sw[r * t];
                     a = INV ? cmulc(a, w) : cmul(a, w);
                 }
                 v[r] = a;
@@ -74,14 +83,14 @@ struct F2 {
     // B -> A (unnormalised inverse when INV).  v holds R2 spectrum values on
     // entry when t < R1; on exit R1 data values when t < R2.
     template <bool INV, typename T2>
-    __device__ __forceinline__ static void inv(T2 (&v)[16], T2* col, int t, const T2* __restrict__ tw) {
+    __device__ __forceinline__ static void inv(T2 (&v)[16], T2* col, int t, const T2* sw) {
         if (t < R1) {
             dft<R2, INV>(v);
 #pragma unroll
             for (int n1 = 0; n1 < R2; ++n1) {
                 T2 a = v[n1];
                 if (n1 > 0 && t > 0) {
-                    const T2 w = __ldg(tw + n1 * t * TSTEP);
+                    const T2 w = sw[n1 * t];
                     a = INV ? cmulc(a, w) : cmul(a, w);
                 }
                 col[xsw(t * R2 + n1)] = a;

@@ -112,10 +112,16 @@ struct GCell<double> {
 
 // Particles per thread of the packed gather: positions of all of them are
 // loaded first, then all their 8 node loads are issued before the sums.
-constexpr int kGathPerThread = 2;
+#ifndef SC_GATH_PT
+#define SC_GATH_PT 2
+#endif
+#ifndef SC_GATH_MINB
+#define SC_GATH_MINB 1
+#endif
+constexpr int kGathPerThread = SC_GATH_PT;
 
 template <typename P, typename A>
-__global__ void __launch_bounds__(256) gather_packed(const P* __restrict__ px, const P* __restrict__ py,
+__global__ void __launch_bounds__(256, SC_GATH_MINB) gather_packed(const P* __restrict__ px, const P* __restrict__ py,
                                                      const P* __restrict__ pz, int64_t n, Axes ax,
                                                      const typename Packed<A>::V* __restrict__ ef,
                                                      P* __restrict__ ex, P* __restrict__ ey, P* __restrict__ ez,

@@ -337,6 +337,129 @@ __device__ __forceinline__ void gl_accumulate(float cx, float cy, float cz, floa
     }
 }
 
+// Cell centre in units of hmax and whether the cell takes the FP64 corner
+// difference (FP32: the test only decides near/far and the centre feeds the
+// quadrature, whose own error is ~1e-7).
+struct OctCell {
+    float px, py, pz;
+    bool near;
+};
+__device__ __forceinline__ OctCell oct_cell(const OctantGeom& g, int ix, int iy, int dz) {
+    OctCell c;
+    c.px = (float)ix * g.ux;
+    c.py = (float)iy * g.uy;
+    c.pz = fmaf((float)dz, g.uz, g.uoff);
+    const float ratio = sqrtf(fmaf(c.px, c.px, fmaf(c.py, c.py, c.pz * c.pz)));
+    c.near = ratio < (float)kNearRatio && ix < g.nbx && iy < g.nby && dz >= g.bz0 && dz < g.bz1;
+    return c;
+}
+
+// Far cell: Gauss-Legendre quadrature of (u, v, w)/r^3 over the cell.
+__device__ __forceinline__ void oct_far(const OctantGeom& g, const OctCell& c, float out[3]) {
+    const float t4[4] = {-0.86113631159405258f, -0.33998104358485626f, 0.33998104358485626f, 0.86113631159405258f};
+    const float w4[4] = {0.34785484513745386f, 0.65214515486254614f, 0.65214515486254614f, 0.34785484513745386f};
+    const float t3[3] = {-0.77459666924148338f, 0.0f, 0.77459666924148338f};
+    const float w3[3] = {0.55555555555555556f, 0.88888888888888889f, 0.55555555555555556f};
+    const float hx = 0.5f * g.ux, hy = 0.5f * g.uy, hz = 0.5f * g.uz;
+    const float ratio = sqrtf(fmaf(c.px, c.px, fmaf(c.py, c.py, c.pz * c.pz)));
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    if (ratio < (float)kQ3Ratio)
+        gl_accumulate(c.px, c.py, c.pz, hx, hy, hz, t4, w4, 4, ax, ay, az);
+    else
+        gl_accumulate(c.px, c.py, c.pz, hx, hy, hz, t3, w3, 3, ax, ay, az);
+    // G_c = gamma_c / 8 * sum w w w p'_c / r'^3 / hmax^2, times FPEI/(L^3)
+    out[0] = g.kxy * ax;
+    out[1] = g.kxy * ay;
+    out[2] = g.kz * az;
+}
+
+// The three terms of field_green_n (green_functions.jl:35-38),
+// F = T0 - T1 + T2: T0 = x atan(yz/(rx)), T1 = z log(r+y),
+// T2 = y log((r-z)/(r+z)) / 2, each on its own thread.
+__device__ __forceinline__ double field_green_term(int term, double x, double y, double z) {
+    const double r = sqrt(x * x + y * y + z * z);
+    if (term == 0) return x * atan((y * z) / (r * x));
+    if (term == 1) return z * log(r + y);
+    return y * log((r - z) / (r + z)) / 2;
+}
+
+// One launch, two block roles.  Blocks [0, near_blocks): the FP64
+// antiderivative terms on the near-box corners, T[term][comp][corner],
+// one per thread, spread over as many SMs as there are blocks.  The other
+// blocks: every far cell of the octant by quadrature (near cells are left to
+// k_igf_near_cells, which runs after this).
+__global__ void __launch_bounds__(64) k_igf_split(float* __restrict__ G, double* __restrict__ T, OctantGeom g,
+                                                  int near_blocks) {
+    if ((int)blockIdx.x < near_blocks) {
+        const int cx = g.nbx + 1, cy = g.nby + 1, cz = g.bz1 - g.bz0 + 1;
+        const int64_t per = (int64_t)cx * cy * cz;
+        const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+        if (t >= 9 * per) return;
+        const int term = (int)(t / (3 * per));
+        const int64_t rest = t - term * 3 * per;
+        const int c = (int)(rest / per);
+        const int64_t e = rest - c * per;
+        const int ex = (int)(e % cx), ey = (int)((e / cx) % cy), ez = (int)(e / ((int64_t)cx * cy)) + g.bz0;
+        const double umin = (double)(1 - 2 * g.nx) * g.dx / 2;
+        const double vmin = (double)(1 - 2 * g.ny) * g.dy / 2;
+        const double wmin = (double)(1 - 2 * g.nz) * g.dz / 2 + g.offw;
+        const double u = (double)(ex + g.nx - 1) * g.dx + umin;
+        const double v = (double)(ey + g.ny - 1) * g.dy + vmin;
+        const double w = (double)(ez + g.nz - 1) * g.dz + wmin;
+        // argument permutations of get_green_kernel!, green_functions.jl:76-80
+        T[t] = c == 0 ? field_green_term(term, u, v, w)
+             : c == 1 ? field_green_term(term, v, w, u)
+                      : field_green_term(term, w, u, v);
+        return;
+    }
+    const int zc = g.image ? 2 * g.nz - 1 : g.nz;
+    const int64_t total = (int64_t)g.nx * g.ny * zc;
+    const int64_t t = (blockIdx.x - near_blocks) * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const int ix = (int)(t % g.nx);
+    const int iy = (int)((t / g.nx) % g.ny);
+    const int iz = (int)(t / ((int64_t)g.nx * g.ny));
+    const int dz = g.image ? iz - (g.nz - 1) : iz;
+    const OctCell cell = oct_cell(g, ix, iy, dz);
+    if (cell.near) return;
+    float out[3];
+    oct_far(g, cell, out);
+    for (int c = 0; c < 3; ++c) G[c * g.cs + t] = out[c];
+}
+
+// Near cells: the 8-point difference (green_functions.jl:108-111) of the
+// corner antiderivatives F = (T0 - T1 + T2) * factor_c, one (cell,
+// component) per thread.
+__global__ void __launch_bounds__(64) k_igf_near_cells(float* __restrict__ G, const double* __restrict__ T,
+                                                       OctantGeom g) {
+    const int bz = g.bz1 - g.bz0;
+    const int64_t box = (int64_t)g.nbx * g.nby * bz;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= 3 * box) return;
+    const int c = (int)(t / box);
+    const int64_t e = t - c * box;
+    const int ix = (int)(e % g.nbx), iy = (int)((e / g.nbx) % g.nby), dz = (int)(e / ((int64_t)g.nbx * g.nby)) + g.bz0;
+    const OctCell cell = oct_cell(g, ix, iy, dz);
+    if (!cell.near) return;
+    const int cx = g.nbx + 1, cy = g.nby + 1, cz = bz + 1;
+    const int64_t per = (int64_t)cx * cy * cz;
+    const int64_t sy = cx, sz = (int64_t)cx * cy;
+    const double fc = c == 2 ? 1.0 / (g.dx * g.dy * g.dz) : g.gamma / (g.dx * g.dy * g.dz);  // :82-86
+    const int iz = g.image ? dz + g.nz - 1 : dz;
+    const int64_t o = ix + (int64_t)g.nx * (iy + (int64_t)g.ny * iz);
+    const double* t0 = T + c * per + ix + sy * iy + sz * (dz - g.bz0);
+    const double* t1 = t0 + 3 * per;
+    const double* t2 = t1 + 3 * per;
+    double F[8];  // corner (a, b, e) at a + 2b + 4e
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int64_t q = (k & 1) + sy * ((k >> 1) & 1) + sz * (k >> 2);
+        F[k] = (__ldg(t0 + q) - __ldg(t1 + q) + __ldg(t2 + q)) * fc;
+    }
+    const double G3 = F[7] - F[6] - F[5] - F[3] - F[0] + F[4] + F[2] + F[1];
+    G[c * g.cs + o] = (float)(G3 * g.scale);
+}
+
 __global__ void __launch_bounds__(256) k_igf_octant(float* __restrict__ G, OctantGeom g) {
     const int zc = g.image ? 2 * g.nz - 1 : g.nz;
     const int64_t total = (int64_t)g.nx * g.ny * zc;
@@ -346,13 +469,9 @@ __global__ void __launch_bounds__(256) k_igf_octant(float* __restrict__ G, Octan
     const int iy = (int)((t / g.nx) % g.ny);
     const int iz = (int)(t / ((int64_t)g.nx * g.ny));
     const int dz = g.image ? iz - (g.nz - 1) : iz;
-    // cell centre in units of hmax (FP32: only decides near/far and feeds
-    // the quadrature, whose own error is ~1e-7)
-    const float px = (float)ix * g.ux, py = (float)iy * g.uy, pz = fmaf((float)dz, g.uz, g.uoff);
-    const float ratio = sqrtf(fmaf(px, px, fmaf(py, py, pz * pz)));
+    const OctCell cell = oct_cell(g, ix, iy, dz);
     float out[3];
-    const bool inbox = ix < g.nbx && iy < g.nby && dz >= g.bz0 && dz < g.bz1;
-    if (ratio < (float)kNearRatio && inbox) {
+    if (cell.near) {
         // 8-point difference of the precomputed corners, green_functions.jl:108-111
         const int cx = g.nbx + 1, cy = g.nby + 1, cz = g.bz1 - g.bz0 + 1;
         const int64_t per = (int64_t)cx * cy * cz;
@@ -365,22 +484,7 @@ __global__ void __launch_bounds__(256) k_igf_octant(float* __restrict__ G, Octan
             out[c] = (float)(G3 * g.scale);
         }
     } else {
-        const float t4[4] = {-0.86113631159405258f, -0.33998104358485626f, 0.33998104358485626f,
-                             0.86113631159405258f};
-        const float w4[4] = {0.34785484513745386f, 0.65214515486254614f, 0.65214515486254614f,
-                             0.34785484513745386f};
-        const float t3[3] = {-0.77459666924148338f, 0.0f, 0.77459666924148338f};
-        const float w3[3] = {0.55555555555555556f, 0.88888888888888889f, 0.55555555555555556f};
-        const float hx = 0.5f * g.ux, hy = 0.5f * g.uy, hz = 0.5f * g.uz;
-        float ax = 0.f, ay = 0.f, az = 0.f;
-        if (ratio < (float)kQ3Ratio)
-            gl_accumulate(px, py, pz, hx, hy, hz, t4, w4, 4, ax, ay, az);
-        else
-            gl_accumulate(px, py, pz, hx, hy, hz, t3, w3, 3, ax, ay, az);
-        // G_c = gamma_c / 8 * sum w w w p'_c / r'^3 / hmax^2, times FPEI/(L^3)
-        out[0] = g.kxy * ax;
-        out[1] = g.kxy * ay;
-        out[2] = g.kz * az;
+        oct_far(g, cell, out);
     }
     for (int c = 0; c < 3; ++c) G[c * g.cs + t] = out[c];
 }
@@ -633,22 +737,26 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
         g.bz1 = (int)fmin((double)nz, ceil((reach - g.offw) / g.dz) + 2.0);
         if (g.bz1 <= g.bz0) g.nbx = g.nby = 0, g.bz0 = g.bz1 = 0;
     }
-    const int64_t nfar = 3 * (int64_t)(g.nbx + 1) * (g.nby + 1) * (g.bz1 - g.bz0 + 1);
-    if (w.fnear_cap < nfar) {
+    // FP64 antiderivative terms on the near-box corners (3 terms x 3 comps)
+    const bool has_near = g.nbx > 0 && g.nby > 0 && g.bz1 > g.bz0;
+    const int64_t nterm = has_near ? 9 * (int64_t)(g.nbx + 1) * (g.nby + 1) * (g.bz1 - g.bz0 + 1) : 0;
+    if (w.fnear_cap < nterm) {
         cudaFree(w.fnear);
         w.fnear = nullptr;
-        SC_CUDA(cudaMalloc(&w.fnear, sizeof(double) * nfar));
-        w.fnear_cap = nfar;
+        SC_CUDA(cudaMalloc(&w.fnear, sizeof(double) * nterm));
+        w.fnear_cap = nterm;
     }
     g.fnear = w.fnear;
-    if (g.nbx > 0 && g.nby > 0) {
-        k_igf_near_F<<<(nfar + 31) / 32, 32, 0, s>>>(w.fnear, g);
-        SC_LAUNCH_CHECK("k_igf_near_F");
-    }
     const int zc = image ? 2 * nz - 1 : nz;
     const int64_t cells = (int64_t)nx * ny * zc;
-    k_igf_octant<<<(cells + 255) / 256, 256, 0, s>>>((float*)w.goct, g);
-    SC_LAUNCH_CHECK("k_igf_octant");
+    const int near_blocks = (int)((nterm + 63) / 64);
+    k_igf_split<<<(unsigned)(near_blocks + (cells + 63) / 64), 64, 0, s>>>((float*)w.goct, w.fnear, g, near_blocks);
+    SC_LAUNCH_CHECK("k_igf_split");
+    if (has_near) {
+        const int64_t box = (int64_t)g.nbx * g.nby * (g.bz1 - g.bz0);
+        k_igf_near_cells<<<(unsigned)((3 * box + 63) / 64), 64, 0, s>>>((float*)w.goct, w.fnear, g);
+        SC_LAUNCH_CHECK("k_igf_near_cells");
+    }
     if (fft_engine() == 0 && w.log2L[0] <= 8 && w.log2L[1] <= 8 && w.log2L[2] <= 8) {
         // parity-reduced transform: real octant lines only (pipeline2.cuh)
         const int64_t t1max = (int64_t)Hx * ny * (2 * nz - 1), t2max = (int64_t)Hx * Hy * (2 * nz - 1);
@@ -663,7 +771,7 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
             launch3_green_col(image, w.log2L[2], T2, image ? w.gimg : w.gfree, (int)plane, 1, nz, 2, plane, 0, t2cs,
                               plane, 0, image ? plane * Lz : plane * Hz, tw, s)) {
             SC_LAUNCH_CHECK("green two-step");
-            m->launches += 5;
+            m->launches += has_near ? 5 : 4;
             return SC_OK;
         }
     }
@@ -700,7 +808,7 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
         k_green_z<<<grid, 256, smem, s>>>(S, dst, nz, g.image, Ly, Lz, w.log2L[2], Hx, lgW, scs, dcs, tw);
         SC_LAUNCH_CHECK("k_green_z");
     }
-    m->launches += 5;
+    m->launches += has_near ? 5 : 4;
     return SC_OK;
 }
 
@@ -992,7 +1100,13 @@ int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green_r
 int native_green_async(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t* ready) {
     *ready = nullptr;
     if (!native_green_stale(m, at_cathode)) return SC_OK;
-    if (!m->side) SC_CUDA(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
+    if (!m->side) {
+        // highest priority: the z pass waits for this build, the deposit on
+        // the caller's stream does not
+        int least = 0, greatest = 0;
+        SC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        SC_CUDA(cudaStreamCreateWithPriority(&m->side, cudaStreamNonBlocking, greatest));
+    }
     if (!m->ev_fork) SC_CUDA(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
     if (!m->ev_join) SC_CUDA(cudaEventCreateWithFlags(&m->ev_join, cudaEventDisableTiming));
     SC_CUDA(cudaEventRecord(m->ev_fork, s));

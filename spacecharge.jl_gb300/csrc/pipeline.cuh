@@ -238,7 +238,7 @@ static int alloc_work(sc_mesh* m) {
     using T2 = typename Cplx<T>::T2;
     NativeWork& w = m->nw;
     if (w.A) return SC_OK;
-    const int64_t nx = m->n[0], ny = m->n[1], nz = m->n[2];
+    const int64_t ny = m->n[1], nz = m->n[2];
     const int64_t Hx = w.Hx, Ly = w.L[1], Lz = w.L[2];
     const int64_t Hy = Ly / 2 + 1, Hz = Lz / 2 + 1;
     SC_CUDA(cudaMalloc(&w.A, sizeof(T2) * Hx * ny * nz));

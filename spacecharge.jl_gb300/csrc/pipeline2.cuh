@@ -38,6 +38,8 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k2_col(const f
                                                             int64_t as_out, int64_t bs_out, int64_t cs_out,
                                                             const float2* __restrict__ tw) {
     using E = F2<L>;
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
     __shared__ float2 xb[kColW * E::S];
     // columns of all batches flattened: f = col + ncols * batch (a tile may
     // straddle two batches: two contiguous segments)
@@ -59,7 +61,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k2_col(const f
                 v[s] = (cok && ok) ? src[n * as_in] : make_float2(0.f, 0.f);
             }
         }
-        E::template fwd<false>(v, xb + c * E::S, t, tw);
+        E::template fwd<false>(v, xb + c * E::S, t, swt);
         if (t < E::R1 && cok) {
 #pragma unroll
             for (int r = 0; r < E::R2; ++r) dst[(t + E::R1 * r) * as_out] = v[r];
@@ -72,7 +74,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k2_col(const f
                 v[r] = cok ? src[k * as_in] : make_float2(0.f, 0.f);
             }
         }
-        E::template inv<true>(v, xb + c * E::S, t, tw);
+        E::template inv<true>(v, xb + c * E::S, t, swt);
         if (t < E::R2 && cok) {
 #pragma unroll
             for (int s = 0; s < E::R1; ++s) {
@@ -88,6 +90,8 @@ template <int L>
 __global__ void __launch_bounds__(256) k2_fwd_x(const float* __restrict__ rho, float2* __restrict__ A, int nx,
                                                 int rows, int Hx, const float2* __restrict__ tw) {
     using E = F2<L>;
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
     constexpr int P = 256 / E::NT;  // row pairs per CTA
     __shared__ float2 xb[P * E::S];
     const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
@@ -106,7 +110,7 @@ __global__ void __launch_bounds__(256) k2_fwd_x(const float* __restrict__ rho, f
             v[s] = make_float2(re, im);
         }
     }
-    E::template fwd<false>(v, col, t, tw);
+    E::template fwd<false>(v, col, t, swt);
     if (t < E::R1) {
 #pragma unroll
         for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
@@ -128,6 +132,8 @@ template <int L>
 __global__ void __launch_bounds__(256) k2_inv_x(const float2* __restrict__ D, float4* __restrict__ E4, int nx,
                                                 int rows, int Hx, int64_t cs, const float2* __restrict__ tw) {
     using E = F2<L>;
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
     constexpr int P = 256 / E::NT;
     extern __shared__ __align__(16) unsigned char smraw[];
     float2* xb = reinterpret_cast<float2*>(smraw);
@@ -154,7 +160,7 @@ __global__ void __launch_bounds__(256) k2_inv_x(const float2* __restrict__ D, fl
                 v[r] = make_float2(xa.x - xbv.y, xa.y + xbv.x);  // Xa + i Xb
             }
         }
-        E::template inv<true>(v, col, t, tw);
+        E::template inv<true>(v, col, t, swt);
         if (comp < 2) {
             if (t < E::R2) {
 #pragma unroll
@@ -175,20 +181,47 @@ __global__ void __launch_bounds__(256) k2_inv_x(const float2* __restrict__ D, fl
     }
 }
 
+// Asynchronous 4-byte global -> shared copies (cp.async, sm_80+), waited
+// for with cp_async_wait_all before a barrier.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // z pass: forward z transform of rho^(kx, ky, .), products with the three
 // Green spectra (image: rho^ at -kz times the image spectrum), three inverse
-// transforms, z < nz stored.
+// transforms, z < nz stored.  The tile's free-space Green values (3 x
+// (L/2+1) x kColW floats) are copied to shared memory asynchronously at the
+// start, so their L2 latency overlaps the forward transform.
 template <int L>
 __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(const float2* __restrict__ B,
                                                                  float2* __restrict__ C, int Hx, int Ly, int nz,
                                                                  GreenView gv, const float2* __restrict__ tw) {
     using E = F2<L>;
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
     extern __shared__ __align__(16) unsigned char smraw[];
     float2* xb = reinterpret_cast<float2*>(smraw);
     float2* spec = xb + kColW * E::S;  // natural-order spectrum of this tile's columns
+    constexpr int HZ = L / 2 + 1;
+    float* gsm = reinterpret_cast<float*>(spec + kColW * E::S);  // [3][HZ][kColW]
     // columns are the (kx, ky) plane flattened: f = kx + Hx*ky is contiguous
     const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
     const int64_t plane = (int64_t)Hx * Ly;
+    const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
+    for (int i = threadIdx.x; i < 3 * HZ * kColW; i += blockDim.x) {
+        const int cc = i % kColW, kzf = (i / kColW) % HZ, comp = i / (kColW * HZ);
+        const int ff = blockIdx.x * kColW + cc;
+        if (ff < plane) {
+            const int kyy = ff / Hx, kxx = ff - kyy * Hx;
+            const int kyf = kyy <= Ly / 2 ? kyy : Ly - kyy;
+            cp_async4(gsm + i, reinterpret_cast<const float*>(gv.gfree) + comp * gv.cs_free + kxx + gv.Hx * kyf +
+                                   gstep * kzf);
+        }
+    }
+    cp_async_commit();
     const int f = blockIdx.x * kColW + c;
     const bool cok = f < plane;
     const int ky = cok ? f / Hx : 0;
@@ -203,18 +236,18 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(con
             v[s] = (cok && z < nz) ? B[f + plane * z] : make_float2(0.f, 0.f);
         }
     }
-    E::template fwd<false>(v, col, t, tw);
+    E::template fwd<false>(v, col, t, swt);
     if (t < E::R1) {
 #pragma unroll
         for (int r = 0; r < E::R2; ++r) sc[xsw(t + E::R1 * r)] = v[r];
     }
+    cp_async_wait_all();
     __syncthreads();
     const int kyf = ky <= Ly / 2 ? ky : Ly - ky;
     const float ysign = ky <= Ly / 2 ? 1.f : -1.f;
-    const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
     for (int comp = 0; comp < 3; ++comp) {
         if (t < E::R1) {
-            const float* gfc = reinterpret_cast<const float*>(gv.gfree) + comp * gv.cs_free + kx + gv.Hx * kyf;
+            const float* gfc = gsm + comp * HZ * kColW + c;
             const float2* gic = reinterpret_cast<const float2*>(gv.gimg) + comp * gv.cs_img + kx + gv.Hx * kyf;
 #pragma unroll
             for (int r = 0; r < E::R2; ++r) {
@@ -225,7 +258,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(con
                     float sg = 1.f;
                     if (comp == 1) sg = ysign;
                     if (comp == 2 && kz > L / 2) sg = -1.f;
-                    const float g = sg * __ldg(gfc + gstep * kzf);
+                    const float g = sg * gfc[kzf * kColW];
                     const float2 X = sc[xsw(kz)];
                     out = make_float2(-X.y * g, X.x * g);  // X * (i g)
                     if (gv.image) {
@@ -240,7 +273,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(con
                 v[r] = out;
             }
         }
-        E::template inv<true>(v, col, t, tw);
+        E::template inv<true>(v, col, t, swt);
         if (t < E::R2 && cok) {
             float2* Cc = C + comp * (plane * nz) + f;
 #pragma unroll
@@ -259,6 +292,8 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass
                                                                      float2* __restrict__ B, int Hx, int Ly, int nz,
                                                                      GreenView gv, const float2* __restrict__ tw) {
     using E = F2<L>;
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
     extern __shared__ __align__(16) unsigned char smraw[];
     float2* xb = reinterpret_cast<float2*>(smraw);
     float2* spec = xb + kColW * E::S;
@@ -285,7 +320,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass
                 v[s] = (cok && z < nz) ? Cc[plane * z] : make_float2(0.f, 0.f);
             }
         }
-        E::template fwd<false>(v, col, t, tw);
+        E::template fwd<false>(v, col, t, swt);
         if (gv.image) {
             if (t < E::R1) {
 #pragma unroll
@@ -320,7 +355,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass
         }
         if (gv.image) __syncthreads();  // spec is rewritten by the next component
     }
-    E::template inv<true>(acc, col, t, tw);
+    E::template inv<true>(acc, col, t, swt);
     if (t < E::R2 && cok) {
         float2* Bc = B + f;
 #pragma unroll
@@ -337,6 +372,8 @@ template <int L>
 __global__ void __launch_bounds__(256) k2_inv_x1(const float2* __restrict__ D, float* __restrict__ E4, int nx,
                                                  int rows, int Hx, const float2* __restrict__ tw) {
     using E = F2<L>;
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
     constexpr int P = 256 / E::NT;
     __shared__ float2 xb[P * E::S];
     const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
@@ -358,7 +395,7 @@ __global__ void __launch_bounds__(256) k2_inv_x1(const float2* __restrict__ D, f
             v[r] = make_float2(xa.x - xbv.y, xa.y + xbv.x);
         }
     }
-    E::template inv<true>(v, xb + p * E::S, t, tw);
+    E::template inv<true>(v, xb + p * E::S, t, swt);
     if (t < E::R2) {
 #pragma unroll
         for (int s = 0; s < E::R1; ++s) {
@@ -388,6 +425,8 @@ __global__ void __launch_bounds__(256) k3_green_x(const float* __restrict__ G, f
                                                   int rows, int Hx, int64_t gcs, int64_t tcs,
                                                   const float2* __restrict__ tw) {
     using E = F2<L>;
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
     constexpr int P = 256 / E::NT;
     __shared__ float2 xb[P * E::S];
     const int comp = blockIdx.y;
@@ -413,7 +452,7 @@ __global__ void __launch_bounds__(256) k3_green_x(const float* __restrict__ G, f
             v[s] = make_float2(a, b);
         }
     }
-    E::template fwd<false>(v, col, t, tw);
+    E::template fwd<false>(v, col, t, swt);
     if (t < E::R1) {
 #pragma unroll
         for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
@@ -445,6 +484,8 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(c
                                                                   int64_t as_out, int64_t bs_out, int64_t cs_out,
                                                                   const float2* __restrict__ tw) {
     using E = F2<L>;
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
     __shared__ float2 xb[kColW * E::S];
     const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
     const int comp = blockIdx.y;
@@ -473,7 +514,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(c
             v[s] = make_float2(a, b);
         }
     }
-    E::template fwd<false>(v, col, t, tw);
+    E::template fwd<false>(v, col, t, swt);
     if (t < E::R1) {
 #pragma unroll
         for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
@@ -578,7 +619,8 @@ static bool launch2_zpass(int logL, const float2* B, float2* C, int Hx, int Ly, 
                           const float2* tw, cudaStream_t s) {
 #define SC_K2Z(LL)                                                                          \
     {                                                                                       \
-        const size_t smem = sizeof(float2) * kColW * F2<LL>::S * 2;                         \
+        const size_t smem = sizeof(float2) * kColW * F2<LL>::S * 2 +                        \
+                            sizeof(float) * 3 * (LL / 2 + 1) * kColW;                           \
         if (set_smem(k2_zpass<LL>, smem) != SC_OK) return false;                            \
         const int64_t ncol = (int64_t)Hx * Ly;                                              \
         k2_zpass<LL><<<(unsigned)((ncol + kColW - 1) / kColW), kColW * F2<LL>::NT, smem, s>>>(B, C, Hx, Ly, nz, gv, tw); \

@@ -159,6 +159,7 @@ struct sc_mesh {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     bool kick_graph = true;       // sc_kick replays a captured graph on repeated calls
     void* kickgraph = nullptr;    // its state (api.cu)
+    void* hostpipe = nullptr;     // sc_kick_host staging buffers and copy streams (api.cu)
     int kick_mode = SC_DEPOSIT_ATOMIC;  // deposit mode of sc_kick
 };
 
@@ -186,10 +187,17 @@ int deposit_launch(sc_mesh* m, const void* x, const void* y, const void* z, cons
 // out[node] += sum of the node's entries in the 8 cells around it (float[8N]
 // per-cell corner slots, the vector deposit's layout)
 int corner_sum_launch(sc_mesh* m, const float* corner, float* out, cudaStream_t s);
+// chunked deposit of sc_kick_host (deposit.cu)
+bool deposit_chunkable(const sc_mesh* m, int mode);
+int deposit_chunk_begin(sc_mesh* m, int mode, cudaStream_t s);
+int deposit_chunk_add(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
+                      int mode, cudaStream_t s);
+int deposit_chunk_finish(sc_mesh* m, int mode, cudaStream_t s);
 // the kick as stream work, without graph replay (api.cu)
 int kick_issue(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
                int at_cathode, void* ex, void* ey, void* ez, cudaStream_t s);
 void kick_graph_release(sc_mesh* m);
+void host_pipe_release(sc_mesh* m);
 // true when the next solve would (re)build a Green spectrum
 bool native_green_stale(const sc_mesh* m, int at_cathode);
 int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n,

@@ -6,8 +6,8 @@ kick (the three in one library call).
 """
 from ._lib import SpaceChargeError, load  # noqa: F401
 from .mesh import (CLIGHT, FPEI, Batch, Mesh3D, autotune, clear_mesh, deposit, interpolate_field, kick,  # noqa: F401
-                   kick_adjoint, kick_autograd, solve)
+                   kick_adjoint, kick_autograd, kick_host, solve)
 
-__all__ = ["Mesh3D", "deposit", "clear_mesh", "interpolate_field", "solve", "kick", "kick_adjoint",
+__all__ = ["Mesh3D", "deposit", "clear_mesh", "interpolate_field", "solve", "kick", "kick_host", "kick_adjoint",
            "kick_autograd", "Batch", "autotune", "SpaceChargeError",
            "CLIGHT", "FPEI", "load"]

@@ -93,6 +93,7 @@ SIGNATURES = {
     "sc_solve": [_vp, _int, _vp],
     "sc_interpolate_field": [_vp, _vp, _vp, _vp, _i64, _int, _vp, _vp, _vp, _vp],
     "sc_kick": [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _vp, _vp, _vp, _vp],
+    "sc_kick_host": [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _vp, _vp, _vp, _vp],
     "sc_mesh_set_profiling": [_vp, _int],
     "sc_mesh_stage_times": [_vp, _dp, C.POINTER(_i64), _vp],
     "sc_mesh_launch_count": [_vp, C.POINTER(_i64)],

@@ -279,6 +279,32 @@ def kick(mesh: Mesh3D, particles_x, particles_y, particles_z, particles_q, at_ca
     return _return_like(particles_x, (ex, ey, ez))
 
 
+def kick_host(mesh: Mesh3D, particles_x, particles_y, particles_z, particles_q, at_cathode: bool = False,
+              out=None):
+    """kick() for particles in host memory (numpy arrays or CPU tensors):
+    the library streams them to the GPU in chunks, overlapping the copies
+    with the deposit and the gather (sc_kick_host).  Returns host arrays of
+    the particle type (page-locked torch tensors, or `out` if given); the
+    call returns when they hold the field."""
+    torch = _torch()
+    lens = [_length(a) for a in (particles_x, particles_y, particles_z, particles_q)]
+    if not (lens[0] == lens[1] == lens[2] == lens[3]):
+        raise SpaceChargeError("Particle coordinate and charge arrays must have the same length.")
+    ts = [a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(np.asarray(a)))
+          for a in (particles_x, particles_y, particles_z, particles_q)]
+    if any(t.is_cuda for t in ts):
+        raise SpaceChargeError("kick_host takes host arrays; use kick() for device arrays")
+    dt = torch.float64 if any(t.dtype == torch.float64 for t in ts) else torch.float32
+    ts = [t.to(dt).contiguous() for t in ts]
+    if out is None:
+        out = [torch.empty(lens[0], dtype=dt, pin_memory=True) for _ in range(3)]
+    L.call("sc_kick_host", mesh.ptr, *[C.c_void_p(t.data_ptr()) for t in ts], lens[0],
+           L.SC_F64 if dt == torch.float64 else L.SC_F32, 1 if at_cathode else 0,
+           *[C.c_void_p(o.data_ptr()) for o in out], _stream())
+    torch.cuda.current_stream().synchronize()
+    return tuple(out)
+
+
 def _ptr(t):
     return C.c_void_p(t.data_ptr()) if t is not None else None
 
