@@ -291,6 +291,52 @@ int sc_autotune(sc_mesh* mesh, void* stream, int* choice);
  * (deposit and interpolate); resets the counter.  Synchronises `stream`. */
 int sc_mesh_out_of_range(sc_mesh* mesh, int64_t* count, void* stream);
 
+/* ---- beside the kick (no counterpart in the reference) ---------------- */
+
+/* Magnetic field of the bunch at the particles from its electric field
+ * there, for a bunch moving along +z at the mesh's gamma:
+ * B = (beta / c) z x E, i.e. Bx = -beta Ey / c, By = beta Ex / c, Bz = 0,
+ * beta = sqrt(1 - 1/gamma^2).  Device arrays of the particle type. */
+int sc_magnetic_field(const sc_mesh* mesh, const void* ex, const void* ey, int64_t n, int dtype, void* bx,
+                      void* by, void* stream);
+
+/* Array-of-structs particle records -> the SoA arrays the kick takes.
+ * Record i starts at element i*stride; x, y, z, q sit at offs[0..3]. */
+int sc_aos_to_soa(const void* aos, int64_t n, int stride, const int32_t offs[4], int dtype, void* x, void* y,
+                  void* z, void* q, void* stream);
+
+/* The kick's field components back into the records, at offs[0..2]. */
+int sc_soa_to_aos(const void* ex, const void* ey, const void* ez, int64_t n, int dtype, int stride,
+                  const int32_t offs[3], void* aos, void* stream);
+
+/* FP32 positions relative to an FP64 reference point (e.g. the bunch
+ * centroid) -> FP64 absolute positions x = ref + r (one rounding). */
+int sc_relative_to_absolute(const float* rx, const float* ry, const float* rz, int64_t n, const double ref[3],
+                            double* x, double* y, double* z, void* stream);
+
+/* `steps` tracking steps of the bunch in its own field (the kick's caller
+ * in a tracking code; no counterpart in the reference).  Each step: when
+ * `refit`, new mesh bounds from the particles (the particle constructor's
+ * arithmetic, mesh.jl:122-201; this synchronises), the kick, B = (beta/c)
+ * z x E, and one relativistic Boris step of the dimensionless momenta
+ * u = gamma*beta and the positions over `dt` seconds for a species of
+ * charge/mass `qm` [C/kg].  x, y, z, ux, uy, uz are updated in place on the
+ * device; q is the macro-particle charge [C].  Without `refit` the mesh keeps
+ * its bounds and the kick replays its graph from the second step on. */
+int sc_track(sc_mesh* mesh, void* x, void* y, void* z, void* ux, void* uy, void* uz, const void* q, int64_t n,
+             int dtype, double dt, double qm, int steps, int refit, int at_cathode, void* stream);
+
+/* Scalar potential on the mesh nodes from the deposited charge (the step
+ * beside the field solve; the reference defines the potential
+ * antiderivative, potential_green_function in green_functions.jl:13-22, but
+ * never calls it).  The field solve's schedule (free_space.jl:14-101) with
+ * that antiderivative and the transverse factor gamma/(dx dy dz): the
+ * lab-frame potential gamma*phi' of the bunch's rest-frame potential.
+ * `phi` is a device array of nx*ny*nz elements of the mesh type, x fastest;
+ * `at_cathode` adds the image charge's potential.  Computed in FP64 with
+ * cuFFT for every mesh precision. */
+int sc_solve_potential(sc_mesh* mesh, int at_cathode, void* phi, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

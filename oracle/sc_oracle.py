@@ -19,7 +19,8 @@ __all__ = [
     "CLIGHT", "FPEI", "EPSILON_0", "OMesh", "mesh_auto", "mesh_manual",
     "clear_mesh", "deposit", "field_green_function", "green_function",
     "solve_freespace", "solve", "interpolate_field", "cic_cells",
-    "gaussian_field", "kick", "linear_green_kernel",
+    "gaussian_field", "kick", "linear_green_kernel", "magnetic_field", "boris_push", "track",
+    "potential_green_function", "potential_green", "solve_potential", "gaussian_potential",
 ]
 
 # src/utils.jl:7-8
@@ -274,3 +275,124 @@ def gaussian_field(x, y, z, Q, sigma):
         s = Q / (4 * math.pi * EPSILON_0 * r ** 3) * (erf - math.sqrt(2 / math.pi) * r / sigma * np.exp(-(r / sigma) ** 2 / 2))
         s = np.where(r == 0, 0.0, s)
     return s * x, s * y, s * z
+
+
+# ------------------------------------------------ beside the kick (no reference code)
+# The rows next to the kick: the bunch's magnetic field and the tracking step
+# that calls the kick.  The reference package has neither; these restate the
+# library's documented definitions so its GPU path has an FP64 checker.
+def magnetic_field(mesh: OMesh, ex, ey):
+    """B of a bunch moving along +z at the mesh's gamma: B = (beta/c) z x E,
+    Bx = -beta Ey / c, By = beta Ex / c, Bz = 0."""
+    beta = math.sqrt(1.0 - 1.0 / (mesh.gamma * mesh.gamma))
+    k = beta / CLIGHT
+    return -k * np.asarray(ey, np.float64), k * np.asarray(ex, np.float64)
+
+
+def boris_push(x, y, z, ux, uy, uz, ex, ey, ez, bx, by, dt, qm):
+    """One relativistic Boris step (J. P. Boris 1970; Birdsall & Langdon,
+    Plasma Physics via Computer Simulation, section 15-4) of u = gamma*beta
+    (dimensionless) under SI fields E [V/m], B = (bx, by, 0) [T], for a
+    species of charge/mass qm [C/kg], then the drift x += c u/gamma dt.
+    du/dt = qm/c (E + v x B); all arrays FP64, returns the new state."""
+    a = qm * dt / (2.0 * CLIGHT)  # half electric kick, in units of u per V/m
+    umx, umy, umz = ux + a * ex, uy + a * ey, uz + a * ez
+    g = np.sqrt(1.0 + umx * umx + umy * umy + umz * umz)
+    tb = qm * dt / (2.0 * g)
+    tx, ty = tb * bx, tb * by  # tz = 0
+    # u' = u- + u- x t
+    upx = umx - umz * ty
+    upy = umy + umz * tx
+    upz = umz + (umx * ty - umy * tx)
+    s = 2.0 / (1.0 + tx * tx + ty * ty)
+    sx, sy = s * tx, s * ty
+    # u+ = u- + u' x s
+    upl_x = umx - upz * sy
+    upl_y = umy + upz * sx
+    upl_z = umz + (upx * sy - upy * sx)
+    nx, ny, nz = upl_x + a * ex, upl_y + a * ey, upl_z + a * ez
+    gn = np.sqrt(1.0 + nx * nx + ny * ny + nz * nz)
+    f = CLIGHT * dt / gn
+    return x + f * nx, y + f * ny, z + f * nz, nx, ny, nz
+
+
+def track(grid_size, x, y, z, ux, uy, uz, q, dt, qm, steps, gamma=1.0, at_cathode=False):
+    """`steps` tracking steps of a bunch in its own field: refit a mesh to
+    the particles (the particle constructor, mesh.jl:122-201), kick, B from
+    E, one Boris step.  Returns the final (x, y, z, ux, uy, uz)."""
+    state = [np.array(a, dtype=np.float64) for a in (x, y, z, ux, uy, uz)]
+    for _ in range(steps):
+        m = mesh_auto(grid_size, state[0], state[1], state[2], gamma=gamma)
+        ex, ey, ez = kick(m, state[0], state[1], state[2], q, at_cathode=at_cathode)
+        bx, by = magnetic_field(m, ex, ey)
+        state = list(boris_push(*state, ex, ey, ez, bx, by, dt, qm))
+    return tuple(state)
+
+
+# ------------------------------------------------ scalar potential (reference code unused)
+def potential_green_function(x, y, z):
+    """Antiderivative of 1/r, src/green_functions.jl:13-22 (defined in the
+    reference, never called): zero at r = 0, same expression and order."""
+    r = np.sqrt(x ** 2 + y ** 2 + z ** 2)
+    half = 0.5
+    with np.errstate(divide="ignore", invalid="ignore"):
+        v = (-half * z ** 2 * np.arctan(x * y / (z * r)) - half * y ** 2 * np.arctan(x * z / (y * r))
+             - half * x ** 2 * np.arctan(y * z / (x * r)) + y * z * np.log(x + r)
+             + x * z * np.log(y + r) + x * y * np.log(z + r))
+    return np.where(r == 0, 0.0, v)
+
+
+def potential_green(shape2, delta, gamma, offset=(0.0, 0.0, 0.0)):
+    """Integrated potential Green function on the doubled grid: the corner
+    lattice, gamma scaling and 8-point difference of green_function() with
+    potential_green_function and the transverse factor gamma/(dx dy dz), so
+    that the solve gives the lab-frame potential gamma*phi' of the bunch's
+    rest-frame potential phi' (the time component of the four-potential)."""
+    isize, jsize, ksize = shape2
+    dx, dy, dz = float(delta[0]), float(delta[1]), float(delta[2]) * float(gamma)
+    factor = float(gamma) / (dx * dy * dz)
+    umin = (1 - isize) * dx / 2 + float(offset[0])
+    vmin = (1 - jsize) * dy / 2 + float(offset[1])
+    wmin = (1 - ksize) * dz / 2 + float(offset[2]) * float(gamma)
+    u = np.arange(isize) * dx + umin
+    v = np.arange(jsize) * dy + vmin
+    w = np.arange(ksize) * dz + wmin
+    U, V, W = np.meshgrid(u, v, w, indexing="ij")
+    g = np.asfortranarray(potential_green_function(U, V, W) * factor)
+    out = g.copy(order="F")
+    out[:-1, :-1, :-1] = (g[1:, 1:, 1:] - g[:-1, 1:, 1:] - g[1:, :-1, 1:] - g[1:, 1:, :-1]
+                          - g[:-1, :-1, :-1] + g[:-1, :-1, 1:] + g[:-1, 1:, :-1] + g[1:, :-1, :-1])
+    return out
+
+
+def _solve_potential_freespace(mesh: OMesh, offset, rho):
+    nx, ny, nz = mesh.grid_size
+    crho = np.zeros((2 * nx, 2 * ny, 2 * nz), dtype=np.complex128, order="F")
+    crho[:nx, :ny, :nz] = rho
+    crho = sfft.fftn(crho, workers=_WORKERS)
+    cgrn = sfft.fftn(potential_green(crho.shape, mesh.delta, mesh.gamma, offset).astype(np.complex128),
+                     workers=_WORKERS)
+    tmp = sfft.ifftn(crho * cgrn, workers=_WORKERS)
+    return FPEI * np.real(tmp[nx - 1:2 * nx - 1, ny - 1:2 * ny - 1, nz - 1:2 * nz - 1])
+
+
+def solve_potential(mesh: OMesh, at_cathode=False):
+    """Scalar potential on the mesh from mesh.rho, the schedule of solve()
+    (free_space.jl:14-101) with the potential Green function; the cathode
+    image enters as in the field solve (-rho flipped in z, offset zmin+zmax)."""
+    phi = _solve_potential_freespace(mesh, (0.0, 0.0, 0.0), mesh.rho)
+    if at_cathode:
+        offset_z = 2.0 * mesh.min_bounds[2] + (mesh.max_bounds[2] - mesh.min_bounds[2])
+        phi = phi + _solve_potential_freespace(mesh, (0.0, 0.0, offset_z), -mesh.rho[:, :, ::-1])
+    return phi
+
+
+def gaussian_potential(x, y, z, Q, sigma):
+    """Exact potential of an isotropic Gaussian bunch: Q/(4 pi eps0 r) erf(r/(sqrt2 sigma)),
+    Q sqrt(2/pi)/(4 pi eps0 sigma) at r = 0."""
+    r = np.sqrt(np.asarray(x) ** 2 + np.asarray(y) ** 2 + np.asarray(z) ** 2)
+    k = Q / (4 * math.pi * EPSILON_0)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        erf = np.vectorize(math.erf)(r / (math.sqrt(2) * sigma))
+        v = k * erf / r
+    return np.where(r == 0, k * math.sqrt(2 / math.pi) / sigma, v)

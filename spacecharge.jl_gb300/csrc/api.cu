@@ -191,20 +191,6 @@ static int check_mesh(const sc_mesh* m) {
     return SC_OK;
 }
 
-// Make the mesh's device current for the duration of a call.
-struct DeviceGuard {
-    int prev = -1;
-    bool ok = true;
-    explicit DeviceGuard(int dev) {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
-    }
-    ~DeviceGuard() {
-        int cur = -1;
-        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-    }
-};
-
 }  // namespace sc
 
 using namespace sc;
@@ -271,6 +257,13 @@ static std::vector<int64_t> kick_key(const sc_mesh* m, const void* const* ptr, i
     k.push_back(fft_engine());
     k.push_back(m->nw.engine);
     k.push_back(m->nw.lgW);
+    // geometry and gamma: kernel arguments captured by value
+    const double geo[7] = {m->lo[0], m->lo[1], m->lo[2], m->delta[0], m->delta[1], m->delta[2], m->gamma};
+    for (double v : geo) {
+        int64_t b;
+        memcpy(&b, &v, sizeof b);
+        k.push_back(b);
+    }
     return k;
 }
 
@@ -317,6 +310,17 @@ static int kick_graph_capture(sc_mesh* m, KickGraph* kg, const void* const* p, i
     }
     kg->graph = g;
     kg->key = std::move(key);
+    return SC_OK;
+}
+
+int mesh_set_geometry(sc_mesh* m, const double lo[3], const double hi[3], const double delta[3]) {
+    for (int d = 0; d < 3; ++d) {
+        if (!(hi[d] > lo[d]) || !(delta[d] > 0))
+            return fail(SC_ERR_INVALID, "max_bounds must be strictly greater than min_bounds for all dimensions.");
+        m->lo[d] = lo[d];
+        m->hi[d] = hi[d];
+        m->delta[d] = delta[d];
+    }
     return SC_OK;
 }
 
@@ -517,6 +521,7 @@ int sc_mesh_destroy(sc_mesh* m) {
     tiled_release(m);
     kick_graph_release(m);
     host_pipe_release(m);
+    cudaFree(m->trackE);
     cudaFree(m->corner);
     if (m->side) cudaStreamDestroy(m->side);
     if (m->ev_fork) cudaEventDestroy(m->ev_fork);
@@ -698,6 +703,13 @@ int sc_kick_host(sc_mesh* m, const void* x, const void* y, const void* z, const 
     const void* hin[4] = {x, y, z, q};
     void* hout[3] = {ex, ey, ez};
     return kick_host_issue(m, hin, n, dtype, at_cathode, hout, (cudaStream_t)stream);
+}
+
+int sc_solve_potential(sc_mesh* m, int at_cathode, void* phi, void* stream) {
+    SC_TRY(check_mesh(m));
+    if (!phi) return fail(SC_ERR_INVALID, "phi is NULL");
+    DeviceGuard g(m->device);
+    return plain_potential(m, at_cathode, phi, (cudaStream_t)stream);
 }
 
 int sc_mesh_set_kick_graph(sc_mesh* m, int enabled) {

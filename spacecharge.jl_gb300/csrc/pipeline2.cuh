@@ -190,6 +190,29 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Copies this CTA's free-space Green values, gsm[comp][kzf][column] for
+// kzf <= L/2 and the tile's kColW columns (kx, ky folded to ky <= Ly/2), to
+// shared memory asynchronously; cp_async_wait_all + a barrier before use.
+// blockDim.x is a multiple of kColW, so each thread keeps one column.
+template <int L>
+__device__ __forceinline__ void prefetch_green(float* gsm, const GreenView& gv, int Hx, int Ly) {
+    constexpr int HZ = L / 2 + 1;
+    const int64_t plane = (int64_t)Hx * Ly;
+    const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
+    const int cc = threadIdx.x % kColW;
+    const int ff = blockIdx.x * kColW + cc;
+    if (ff < plane) {
+        const int kyy = ff / Hx, kxx = ff - kyy * Hx;
+        const int kyf = kyy <= Ly / 2 ? kyy : Ly - kyy;
+        const float* src = reinterpret_cast<const float*>(gv.gfree) + kxx + (int64_t)gv.Hx * kyf;
+        for (int row = threadIdx.x / kColW; row < 3 * HZ; row += blockDim.x / kColW) {
+            const int comp = row / HZ, kzf = row - comp * HZ;
+            cp_async4(gsm + row * kColW + cc, src + comp * gv.cs_free + gstep * kzf);
+        }
+    }
+    cp_async_commit();
+}
+
 // z pass: forward z transform of rho^(kx, ky, .), products with the three
 // Green spectra (image: rho^ at -kz times the image spectrum), three inverse
 // transforms, z < nz stored.  The tile's free-space Green values (3 x
@@ -210,18 +233,8 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(con
     // columns are the (kx, ky) plane flattened: f = kx + Hx*ky is contiguous
     const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
     const int64_t plane = (int64_t)Hx * Ly;
+    prefetch_green<L>(gsm, gv, Hx, Ly);
     const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
-    for (int i = threadIdx.x; i < 3 * HZ * kColW; i += blockDim.x) {
-        const int cc = i % kColW, kzf = (i / kColW) % HZ, comp = i / (kColW * HZ);
-        const int ff = blockIdx.x * kColW + cc;
-        if (ff < plane) {
-            const int kyy = ff / Hx, kxx = ff - kyy * Hx;
-            const int kyf = kyy <= Ly / 2 ? kyy : Ly - kyy;
-            cp_async4(gsm + i, reinterpret_cast<const float*>(gv.gfree) + comp * gv.cs_free + kxx + gv.Hx * kyf +
-                                   gstep * kzf);
-        }
-    }
-    cp_async_commit();
     const int f = blockIdx.x * kColW + c;
     const bool cok = f < plane;
     const int ky = cok ? f / Hx : 0;
@@ -305,6 +318,9 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass
     const int kx = f - ky * Hx;
     float2* col = xb + c * E::S;
     float2* sc = spec + c * E::S;
+    constexpr int HZ = L / 2 + 1;
+    float* gsm = reinterpret_cast<float*>(spec + kColW * E::S);  // [3][HZ][kColW]
+    prefetch_green<L>(gsm, gv, Hx, Ly);
     const int kyf = ky <= Ly / 2 ? ky : Ly - ky;
     const float ysign = ky <= Ly / 2 ? 1.f : -1.f;
     const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
@@ -326,10 +342,11 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass
 #pragma unroll
                 for (int r = 0; r < E::R2; ++r) sc[xsw(t + E::R1 * r)] = v[r];
             }
-            __syncthreads();
         }
+        if (comp == 0) cp_async_wait_all();
+        if (gv.image || comp == 0) __syncthreads();
         if (t < E::R1 && cok) {
-            const float* gfc = reinterpret_cast<const float*>(gv.gfree) + comp * gv.cs_free + kx + gv.Hx * kyf;
+            const float* gfc = gsm + comp * HZ * kColW + c;
             const float2* gic = reinterpret_cast<const float2*>(gv.gimg) + comp * gv.cs_img + kx + gv.Hx * kyf;
 #pragma unroll
             for (int r = 0; r < E::R2; ++r) {
@@ -338,7 +355,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass
                 float sg = 1.f;
                 if (comp == 1) sg = ysign;
                 if (comp == 2 && kz > L / 2) sg = -1.f;
-                const float g = sg * __ldg(gfc + gstep * kzf);
+                const float g = sg * gfc[kzf * kColW];
                 // Ebar^ * conj(i g) = Ebar^ * (-i g)
                 acc[r].x += v[r].y * g;
                 acc[r].y -= v[r].x * g;
@@ -634,7 +651,8 @@ static bool launch2_adj_zpass(int logL, const float2* C, float2* B, int Hx, int 
                               const float2* tw, cudaStream_t s) {
 #define SC_K2AZ(LL)                                                                         \
     {                                                                                       \
-        const size_t smem = sizeof(float2) * kColW * F2<LL>::S * 2;                         \
+        const size_t smem = sizeof(float2) * kColW * F2<LL>::S * 2 +                        \
+                            sizeof(float) * 3 * (LL / 2 + 1) * kColW;                           \
         if (set_smem(k2_adj_zpass<LL>, smem) != SC_OK) return false;                        \
         const int64_t ncol = (int64_t)Hx * Ly;                                              \
         k2_adj_zpass<LL><<<(unsigned)((ncol + kColW - 1) / kColW), kColW * F2<LL>::NT, smem, s>>>(C, B, Hx, Ly, nz, gv, tw); \

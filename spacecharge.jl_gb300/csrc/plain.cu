@@ -17,7 +17,19 @@ __device__ __forceinline__ double field_green(double x, double y, double z) {
     return x * atan((y * z) / (r * x)) - z * log(r + y) + y * log((r - z) / (r + z)) / 2;
 }
 
+// src/green_functions.jl:13-22 (the reference defines it and never calls it):
+// the antiderivative of 1/r, zero at r = 0.
+__device__ __forceinline__ double potential_green(double x, double y, double z) {
+    const double r = sqrt(x * x + y * y + z * z);
+    if (r == 0.0) return 0.0;
+    const double half = 0.5;
+    return -half * z * z * atan(x * y / (z * r)) - half * y * y * atan(x * z / (y * r)) -
+           half * x * x * atan(y * z / (x * r)) + y * z * log(x + r) + x * z * log(y + r) + x * y * log(z + r);
+}
+
 // green_functions.jl:69-101: F * factor at every point of the doubled grid.
+// icomp 4 is the scalar potential: potential_green with the transverse
+// factor gamma/(dx dy dz), which gives the lab-frame potential gamma*phi'.
 __global__ void __launch_bounds__(256) plain_green_point(double2* __restrict__ g, int isize, int jsize, int ksize,
                                                          double dx, double dy, double dz_lab, double gamma,
                                                          int icomp, double offx, double offy, double offz) {
@@ -28,7 +40,8 @@ __global__ void __launch_bounds__(256) plain_green_point(double2* __restrict__ g
     const int j = (int)((t / isize) % jsize);
     const int k = (int)(t / ((int64_t)isize * jsize));
     const double dz = dz_lab * gamma;  // :73
-    const double factor = (icomp == 1 || icomp == 2) ? gamma / (dx * dy * dz) : 1.0 / (dx * dy * dz);  // :76-80
+    const double factor = (icomp == 1 || icomp == 2 || icomp == 4) ? gamma / (dx * dy * dz)  // :76-80
+                                                                   : 1.0 / (dx * dy * dz);
     const double umin = (double)(1 - isize) * dx / 2 + offx;  // :82-84
     const double vmin = (double)(1 - jsize) * dy / 2 + offy;
     const double wmin = (double)(1 - ksize) * dz / 2 + offz * gamma;
@@ -40,8 +53,10 @@ __global__ void __launch_bounds__(256) plain_green_point(double2* __restrict__ g
         val = field_green(u, v, w) * factor;
     else if (icomp == 2)
         val = field_green(v, w, u) * factor;
-    else
+    else if (icomp == 3)
         val = field_green(w, u, v) * factor;
+    else
+        val = potential_green(u, v, w) * factor;
     g[t] = make_double2(val, 0.0);
 }
 
@@ -67,8 +82,10 @@ __global__ void __launch_bounds__(256) plain_green_diff(const double2* __restric
     out[t] = make_double2(v, 0.0);
 }
 
-// free_space.jl:68-69 (and :34 for the image: -rho[:, :, end:-1:1])
-__global__ void __launch_bounds__(256) plain_pad(const double* __restrict__ rho, double2* __restrict__ c, int nx,
+// free_space.jl:68-69 (and :34 for the image: -rho[:, :, end:-1:1]); rho of
+// the mesh type (the potential solve pads FP32 meshes' rho too)
+template <typename T>
+__global__ void __launch_bounds__(256) plain_pad(const T* __restrict__ rho, double2* __restrict__ c, int nx,
                                                  int ny, int nz, int image) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t total = (int64_t)8 * nx * ny * nz;
@@ -79,7 +96,7 @@ __global__ void __launch_bounds__(256) plain_pad(const double* __restrict__ rho,
     double v = 0.0;
     if (i < nx && j < ny && k < nz) {
         const int ks = image ? nz - 1 - k : k;
-        v = rho[i + (int64_t)nx * (j + (int64_t)ny * ks)];
+        v = (double)rho[i + (int64_t)nx * (j + (int64_t)ny * ks)];
         if (image) v = -v;
     }
     c[t] = make_double2(v, 0.0);
@@ -143,7 +160,7 @@ static int plain_solve_freespace(sc_mesh* m, double offz, int image, cudaStream_
     const int64_t gb = (total + 255) / 256;
     StageTimer& tm = m->timer;
     StageScope st(tm, SC_STAGE_PLAIN_FFT, s);
-    plain_pad<<<gb, 256, 0, s>>>((const double*)m->rho, w.crho, nx, ny, nz, image);
+    plain_pad<double><<<gb, 256, 0, s>>>((const double*)m->rho, w.crho, nx, ny, nz, image);
     SC_LAUNCH_CHECK("plain_pad");
     SC_TRY(fft(m, w.crho, CUFFT_FORWARD, s));
     m->launches += 2 + 3 * 6;
@@ -162,6 +179,65 @@ static int plain_solve_freespace(sc_mesh* m, double offz, int image, cudaStream_
         plain_extract<<<(m->N + 255) / 256, 256, 0, s>>>(w.tmp, (double*)m->efield, nx, ny, nz, comp - 1,
                                                           1.0 / (double)total, image);
         SC_LAUNCH_CHECK("plain_extract");
+    }
+    return SC_OK;
+}
+
+// window extraction of the potential into a mesh-type array (free_space.jl:98-99)
+template <typename T>
+__global__ void __launch_bounds__(256) plain_extract_phi(const double2* __restrict__ c, T* __restrict__ phi, int nx,
+                                                         int ny, int nz, double inv_total, int accumulate) {
+    const int64_t N = (int64_t)nx * ny * nz;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    const int i = (int)(t % nx);
+    const int j = (int)((t / nx) % ny);
+    const int k = (int)(t / ((int64_t)nx * ny));
+    const int64_t src = (i + nx - 1) + (int64_t)(2 * nx) * ((j + ny - 1) + (int64_t)(2 * ny) * (k + nz - 1));
+    const double v = kFpei * (c[src].x * inv_total);
+    phi[t] = accumulate ? (T)((double)phi[t] + v) : (T)v;
+}
+
+static int plain_potential_freespace(sc_mesh* m, double offz, int image, void* phi, cudaStream_t s) {
+    PlainWork& w = m->pw;
+    const int nx = m->n[0], ny = m->n[1], nz = m->n[2];
+    const int64_t total = (int64_t)8 * m->N;
+    const int64_t gb = (total + 255) / 256;
+    const bool f32 = m->precision == SC_PREC_MIXED;
+    if (f32)
+        plain_pad<float><<<gb, 256, 0, s>>>((const float*)m->rho, w.crho, nx, ny, nz, image);
+    else
+        plain_pad<double><<<gb, 256, 0, s>>>((const double*)m->rho, w.crho, nx, ny, nz, image);
+    SC_LAUNCH_CHECK("plain_pad");
+    SC_TRY(fft(m, w.crho, CUFFT_FORWARD, s));
+    plain_green_point<<<gb, 256, 0, s>>>(w.cgrn, 2 * nx, 2 * ny, 2 * nz, m->delta[0], m->delta[1], m->delta[2],
+                                         m->gamma, 4, 0.0, 0.0, offz);
+    SC_LAUNCH_CHECK("plain_green_point");
+    plain_green_diff<<<gb, 256, 0, s>>>(w.cgrn, w.tmp, 2 * nx, 2 * ny, 2 * nz);
+    SC_LAUNCH_CHECK("plain_green_diff");
+    SC_TRY(fft(m, w.tmp, CUFFT_FORWARD, s));
+    plain_mul<<<gb, 256, 0, s>>>(w.crho, w.tmp, total);
+    SC_LAUNCH_CHECK("plain_mul");
+    SC_TRY(fft(m, w.tmp, CUFFT_INVERSE, s));
+    const double inv = 1.0 / (double)total;
+    if (f32)
+        plain_extract_phi<float><<<(m->N + 255) / 256, 256, 0, s>>>(w.tmp, (float*)phi, nx, ny, nz, inv, image);
+    else
+        plain_extract_phi<double><<<(m->N + 255) / 256, 256, 0, s>>>(w.tmp, (double*)phi, nx, ny, nz, inv, image);
+    SC_LAUNCH_CHECK("plain_extract_phi");
+    m->launches += 6;
+    return SC_OK;
+}
+
+// Scalar potential from the mesh's rho: the field solve's schedule in FP64
+// with cuFFT for every mesh precision (free_space.jl:14-101 with the
+// potential Green function; the image as in :19-46).
+int plain_potential(sc_mesh* m, int at_cathode, void* phi, cudaStream_t s) {
+    SC_TRY(plain_workspace(m, s));
+    SC_TRY(plain_potential_freespace(m, 0.0, 0, phi, s));
+    if (at_cathode) {
+        const double offz = 2 * m->lo[2] + (m->hi[2] - m->lo[2]);
+        SC_TRY(plain_potential_freespace(m, offz, 1, phi, s));
     }
     return SC_OK;
 }

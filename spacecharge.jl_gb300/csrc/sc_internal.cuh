@@ -160,10 +160,27 @@ struct sc_mesh {
     bool kick_graph = true;       // sc_kick replays a captured graph on repeated calls
     void* kickgraph = nullptr;    // its state (api.cu)
     void* hostpipe = nullptr;     // sc_kick_host staging buffers and copy streams (api.cu)
+    void* trackE = nullptr;       // sc_track: E at the particles, 3 x track_cap
+    int64_t track_cap = 0;
+    size_t track_elem = 0;
     int kick_mode = SC_DEPOSIT_ATOMIC;  // deposit mode of sc_kick
 };
 
 namespace sc {
+
+// Makes a mesh's device current for the scope of an entry point.
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) ok = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
 
 inline size_t field_elem_bytes(int precision) {
     return precision == SC_PREC_MIXED ? 4 : 8;
@@ -198,6 +215,9 @@ int kick_issue(sc_mesh* m, const void* x, const void* y, const void* z, const vo
                int at_cathode, void* ex, void* ey, void* ez, cudaStream_t s);
 void kick_graph_release(sc_mesh* m);
 void host_pipe_release(sc_mesh* m);
+// new bounds for a mesh (sc_track's refit); cached spectra and graphs see the
+// change through their keys
+int mesh_set_geometry(sc_mesh* m, const double lo[3], const double hi[3], const double delta[3]);
 // true when the next solve would (re)build a Green spectrum
 bool native_green_stale(const sc_mesh* m, int at_cathode);
 int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n,
@@ -214,6 +234,7 @@ int gather_tiled_launch(sc_mesh* m, const void* x, int64_t n, int dtype, void* e
                         cudaStream_t s);
 
 int plain_solve(sc_mesh* m, int at_cathode, cudaStream_t s);
+int plain_potential(sc_mesh* m, int at_cathode, void* phi, cudaStream_t s);
 int plain_release(sc_mesh* m);
 
 int native_prepare(sc_mesh* m);  // sizes only (no allocation)

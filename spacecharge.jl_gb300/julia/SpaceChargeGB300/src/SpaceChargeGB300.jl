@@ -14,7 +14,7 @@ module SpaceChargeGB300
 using CUDA
 import ChainRulesCore
 
-export Mesh3D, deposit!, clear_mesh!, interpolate_field, solve!, kick
+export Mesh3D, deposit!, clear_mesh!, interpolate_field, solve!, kick, kick_host, track!, magnetic_field
 
 const libsc = normpath(joinpath(@__DIR__, "..", "..", "..", "lib", "libspacecharge_gb300.so"))
 
@@ -182,6 +182,56 @@ function ChainRulesCore.rrule(::typeof(kick), mesh::Mesh3D, px::CuArray{P}, py::
         return (ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent(), dx, dy, dz, dq)
     end
     return out, kick_pullback
+end
+
+"""
+    kick_host(mesh, px, py, pz, pq; at_cathode=false) -> (Ex, Ey, Ez)
+
+`kick` for particles in host memory (sc_kick_host): the library streams the
+arrays to the GPU in chunks, overlapping the copies with the deposit and the
+gather.  Page-locked arrays (`CUDA.Mem.pin`) give the overlap.
+"""
+function kick_host(mesh::Mesh3D, px::Vector{P}, py::Vector{P}, pz::Vector{P}, pq::Vector{P};
+                   at_cathode::Bool=false) where {P<:Union{Float32,Float64}}
+    length(px) == length(py) == length(pz) == length(pq) ||
+        error("Particle coordinate and charge arrays must have the same length.")
+    Ex = similar(px); Ey = similar(px); Ez = similar(px)
+    check(ccall((:sc_kick_host, libsc), Cint,
+                (Ptr{Cvoid}, Ptr{P}, Ptr{P}, Ptr{P}, Ptr{P}, Int64, Cint, Cint, Ptr{P}, Ptr{P}, Ptr{P}, Ptr{Cvoid}),
+                mesh.ptr, px, py, pz, pq, length(px), dtype_code(P), Cint(at_cathode), Ex, Ey, Ez, stream_ptr()))
+    CUDA.synchronize()
+    return Ex, Ey, Ez
+end
+
+"""
+    track!(mesh, x, y, z, ux, uy, uz, q; dt, qm, steps=1, refit=true, at_cathode=false)
+
+`steps` tracking steps of the bunch in its own field (sc_track): refit the
+mesh bounds, kick, B = (beta/c) z x E, one relativistic Boris step of
+u = gamma*beta and the positions over `dt` seconds for charge/mass `qm`.
+"""
+function track!(mesh::Mesh3D, x::CuArray{P}, y::CuArray{P}, z::CuArray{P}, ux::CuArray{P}, uy::CuArray{P},
+                uz::CuArray{P}, q::CuArray{P}; dt::Real, qm::Real, steps::Integer=1, refit::Bool=true,
+                at_cathode::Bool=false) where {P<:Union{Float32,Float64}}
+    check(ccall((:sc_track, libsc), Cint,
+                (Ptr{Cvoid}, CuPtr{P}, CuPtr{P}, CuPtr{P}, CuPtr{P}, CuPtr{P}, CuPtr{P}, CuPtr{P}, Int64, Cint,
+                 Cdouble, Cdouble, Cint, Cint, Cint, Ptr{Cvoid}),
+                mesh.ptr, x, y, z, ux, uy, uz, q, length(x), dtype_code(P), Float64(dt), Float64(qm), Cint(steps),
+                Cint(refit), Cint(at_cathode), stream_ptr()))
+    return nothing
+end
+
+"""
+    magnetic_field(mesh, Ex, Ey) -> (Bx, By)
+
+B = (beta/c) z x E of a bunch moving along +z at the mesh's gamma.
+"""
+function magnetic_field(mesh::Mesh3D, Ex::CuArray{P}, Ey::CuArray{P}) where {P<:Union{Float32,Float64}}
+    Bx = similar(Ex); By = similar(Ex)
+    check(ccall((:sc_magnetic_field, libsc), Cint,
+                (Ptr{Cvoid}, CuPtr{P}, CuPtr{P}, Int64, Cint, CuPtr{P}, CuPtr{P}, Ptr{Cvoid}),
+                mesh.ptr, Ex, Ey, length(Ex), dtype_code(P), Bx, By, stream_ptr()))
+    return Bx, By
 end
 
 function Base.show(io::IO, mesh::Mesh3D{T}) where {T}  # src/mesh.jl:267-273

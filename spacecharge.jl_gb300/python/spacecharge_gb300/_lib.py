@@ -94,6 +94,12 @@ SIGNATURES = {
     "sc_interpolate_field": [_vp, _vp, _vp, _vp, _i64, _int, _vp, _vp, _vp, _vp],
     "sc_kick": [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _vp, _vp, _vp, _vp],
     "sc_kick_host": [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _vp, _vp, _vp, _vp],
+    "sc_magnetic_field": [_vp, _vp, _vp, _i64, _int, _vp, _vp, _vp],
+    "sc_aos_to_soa": [_vp, _i64, _int, _i32p, _int, _vp, _vp, _vp, _vp, _vp],
+    "sc_soa_to_aos": [_vp, _vp, _vp, _i64, _int, _int, _i32p, _vp, _vp],
+    "sc_relative_to_absolute": [_vp, _vp, _vp, _i64, _dp, _vp, _vp, _vp, _vp],
+    "sc_solve_potential": [_vp, _int, _vp, _vp],
+    "sc_track": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _int, C.c_double, C.c_double, _int, _int, _int, _vp],
     "sc_mesh_set_profiling": [_vp, _int],
     "sc_mesh_stage_times": [_vp, _dp, C.POINTER(_i64), _vp],
     "sc_mesh_launch_count": [_vp, C.POINTER(_i64)],

@@ -305,6 +305,87 @@ def kick_host(mesh: Mesh3D, particles_x, particles_y, particles_z, particles_q, 
     return tuple(out)
 
 
+def solve_potential(mesh: Mesh3D, at_cathode: bool = False):
+    """Scalar potential on the mesh nodes from mesh.rho (sc_solve_potential):
+    a device tensor of shape (nx, ny, nz) of the mesh type."""
+    torch = _torch()
+    nx, ny, nz = mesh.grid_size
+    dt = torch.float32 if mesh.T == np.float32 else torch.float64
+    phi = torch.empty((nz, ny, nx), dtype=dt, device="cuda")
+    L.call("sc_solve_potential", mesh.ptr, 1 if at_cathode else 0, _ptr(phi), _stream())
+    return phi.permute(2, 1, 0)
+
+
+def track(mesh: Mesh3D, x, y, z, ux, uy, uz, q, dt: float, qm: float, steps: int = 1, refit: bool = True,
+          at_cathode: bool = False) -> None:
+    """`steps` tracking steps of the bunch in its own field (sc_track): refit
+    the mesh bounds (when `refit`), kick, B from E, one relativistic Boris
+    step of u = gamma*beta and the positions over dt [s] for charge/mass qm
+    [C/kg].  x, y, z, ux, uy, uz are CUDA tensors of one float type, updated
+    in place; q the macro charges."""
+    torch = _torch()
+    ts = (x, y, z, ux, uy, uz, q)
+    if not all(isinstance(t, torch.Tensor) and t.is_cuda and t.is_contiguous() for t in ts):
+        raise SpaceChargeError("track updates contiguous CUDA tensors in place")
+    if len({t.dtype for t in ts}) != 1 or x.dtype not in (torch.float32, torch.float64):
+        raise SpaceChargeError("track needs all arrays float32 or all float64")
+    if len({t.numel() for t in ts}) != 1:
+        raise SpaceChargeError("Particle coordinate and charge arrays must have the same length.")
+    L.call("sc_track", mesh.ptr, *[_ptr(t) for t in ts], x.numel(), L.SC_F64 if x.dtype == torch.float64 else L.SC_F32,
+           float(dt), float(qm), int(steps), 1 if refit else 0, 1 if at_cathode else 0, _stream())
+
+
+def magnetic_field(mesh: Mesh3D, ex, ey):
+    """B at the particles of a bunch moving along +z at the mesh's gamma:
+    Bx = -beta Ey / c, By = beta Ex / c, Bz = 0 (sc_magnetic_field).  ex, ey
+    are the kick's outputs (device tensors or host arrays)."""
+    torch = _torch()
+    (tx, ty), dt = _as_device((ex, ey))
+    bx, by = torch.empty_like(tx), torch.empty_like(tx)
+    L.call("sc_magnetic_field", mesh.ptr, _ptr(tx), _ptr(ty), tx.numel(), dt, _ptr(bx), _ptr(by), _stream())
+    return _return_like(ex, (bx, by))
+
+
+def aos_to_soa(records, offsets=(0, 1, 2, 3)):
+    """Particle records (n, stride) on the device -> x, y, z, q arrays
+    (sc_aos_to_soa); `offsets` are the record positions of x, y, z, q."""
+    torch = _torch()
+    r = torch.as_tensor(records, device="cuda").contiguous()
+    if r.dim() != 2 or r.dtype not in (torch.float32, torch.float64):
+        raise SpaceChargeError("records must be a float32/float64 (n, stride) array")
+    n, stride = r.shape
+    outs = [torch.empty(n, dtype=r.dtype, device="cuda") for _ in range(4)]
+    offs = (C.c_int32 * 4)(*offsets)
+    L.call("sc_aos_to_soa", _ptr(r), n, stride, offs, L.SC_F64 if r.dtype == torch.float64 else L.SC_F32,
+           *[_ptr(o) for o in outs], _stream())
+    return tuple(outs)
+
+
+def soa_to_aos(ex, ey, ez, records, offsets=(4, 5, 6)):
+    """Write the field components into device particle records (n, stride)
+    at `offsets` (sc_soa_to_aos)."""
+    torch = _torch()
+    (tx, ty, tz), dt = _as_device((ex, ey, ez), dtype=records.dtype)
+    if not (records.is_cuda and records.is_contiguous() and records.dim() == 2):
+        raise SpaceChargeError("records must be a contiguous (n, stride) device tensor")
+    offs = (C.c_int32 * 3)(*offsets)
+    L.call("sc_soa_to_aos", _ptr(tx), _ptr(ty), _ptr(tz), tx.numel(), dt, records.shape[1], offs, _ptr(records),
+           _stream())
+    return records
+
+
+def relative_to_absolute(rx, ry, rz, ref):
+    """FP32 positions relative to the FP64 point `ref` -> FP64 absolute
+    positions on the device (sc_relative_to_absolute)."""
+    torch = _torch()
+    (tx, ty, tz), _ = _as_device((rx, ry, rz), dtype=torch.float32)
+    outs = [torch.empty(tx.numel(), dtype=torch.float64, device="cuda") for _ in range(3)]
+    r = (C.c_double * 3)(*ref)
+    L.call("sc_relative_to_absolute", _ptr(tx), _ptr(ty), _ptr(tz), tx.numel(), r, *[_ptr(o) for o in outs],
+           _stream())
+    return tuple(outs)
+
+
 def _ptr(t):
     return C.c_void_p(t.data_ptr()) if t is not None else None
 

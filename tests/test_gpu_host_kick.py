@@ -32,7 +32,8 @@ def test_kick_host_matches_device_kick(sc, cuda, prec, mode, cath):
     hx, hy, hz, hq = (torch.from_numpy(a).pin_memory() for a in (x, y, z, q))
     eh = sc.kick_host(m, hx, hy, hz, hq, at_cathode=cath)
     ed = sc.kick(m, x, y, z, q, at_cathode=cath)
-    tol = 1e-5 if prec == "mixed" else 1e-12
+    # FP64: the atomic deposit's summation order differs between the two kicks
+    tol = 1e-5 if prec == "mixed" else 1e-10
     for a, b in zip(eh, ed):
         assert not a.is_cuda
         assert rel(a.numpy(), b) < tol

@@ -269,3 +269,88 @@ def test_image_charge():
         r = np.array([xn - xs, yn - ys, zn - zs])
         e_img += -rho[a, b, c] * O.FPEI * r / np.linalg.norm(r) ** 3
     assert np.allclose(img[node], e_img, rtol=2e-3)
+
+
+# ------------------------------------------------ beside the kick: Boris push
+def test_boris_pure_electric_field_is_exact():
+    """A uniform E alone: u(t) = u0 + qm E t / c after any number of steps,
+    and the drift matches the exact relativistic motion to the step's order."""
+    qm, E, dt = -1.75882001076e11, 2.0e6, 1e-12
+    st = [np.zeros(1) for _ in range(6)]
+    for _ in range(100):
+        st = list(O.boris_push(*st, np.zeros(1), np.zeros(1), np.full(1, E), np.zeros(1), np.zeros(1), dt, qm))
+    assert np.isclose(st[5][0], qm * E * 100 * dt / O.CLIGHT, rtol=1e-12)
+
+
+def test_boris_pure_magnetic_field_rotates():
+    """B alone conserves |u| and rotates u about B by the Boris angle
+    2 atan(w dt / 2) per step, w = qm B / gamma the relativistic cyclotron
+    frequency (du/dt = w u x B/|B|)."""
+    qm, B, dt = -1.75882001076e11, 0.01, 1e-13
+    u0 = 0.5
+    st = [np.zeros(1), np.zeros(1), np.zeros(1), np.full(1, u0), np.zeros(1), np.zeros(1)]
+    z1 = np.zeros(1)
+    n = 2000
+    for _ in range(n):
+        st = list(O.boris_push(*st, z1, z1, z1, z1, np.full(1, B), dt, qm))
+    ux, uy, uz = st[3][0], st[4][0], st[5][0]
+    assert np.isclose(np.sqrt(ux * ux + uy * uy + uz * uz), u0, rtol=1e-13)
+    w = qm * B / np.sqrt(1 + u0 * u0)
+    # B along y: dux/dt = -w uz, duz/dt = w ux
+    assert np.isclose(np.arctan2(uz, ux), n * 2 * np.arctan(w * dt / 2), rtol=1e-9)
+
+
+def test_track_conserves_charge_centroid_momentum():
+    """Internal forces only: the bunch's total momentum (charge-weighted,
+    equal weights) stays near zero while the bunch expands."""
+    rng = np.random.default_rng(4)
+    n = 20_000
+    x, y, z = rng.standard_normal((3, n)) * 1e-3
+    zeros = np.zeros(n)
+    q = np.full(n, -1e-12 / n)
+    st = O.track((16, 16, 16), x, y, z, zeros, zeros, zeros, q, 1e-11, -1.75882001076e11, 5)
+    r0 = np.sqrt(np.mean(x * x + y * y + z * z))
+    r1 = np.sqrt(np.mean(st[0] ** 2 + st[1] ** 2 + st[2] ** 2))
+    assert r1 > r0  # a negative bunch of electrons expands
+    p = np.array([st[3].sum(), st[4].sum(), st[5].sum()])
+    assert np.abs(p).max() < 1e-3 * np.abs(st[3]).sum()
+
+
+# ------------------------------------------------ scalar potential
+def test_potential_antiderivative_is_one_over_r():
+    """The 8-point difference of potential_green_function over a cell equals
+    the cell integral of 1/r (midpoint-refined cubature, 2e-5)."""
+    h = 0.1
+    for c in ((0.35, 0.2, -0.45), (1.0, 0.7, 0.3), (0.06, 0.07, 0.6)):
+        lo = np.array(c) - h / 2
+        hi = np.array(c) + h / 2
+        F = O.potential_green_function
+        val = 0.0
+        for a in (0, 1):
+            for b in (0, 1):
+                for e in (0, 1):
+                    sgn = (-1) ** (3 - a - b - e)
+                    val += sgn * F(*(lo + np.array([a, b, e]) * h))
+        m = 40
+        t = (np.arange(m) + 0.5) / m * h
+        X, Y, Z = np.meshgrid(lo[0] + t, lo[1] + t, lo[2] + t, indexing="ij")
+        ref = np.sum(1 / np.sqrt(X * X + Y * Y + Z * Z)) * (h / m) ** 3
+        assert abs(val - ref) < 2e-5 * abs(ref)
+
+
+def test_potential_of_a_gaussian_bunch():
+    """solve_potential of a Gaussian bunch against the analytic potential on
+    the z axis (the reference's analytical_test bound, 10 %), and E = -grad phi
+    against the field solve (central differences, 3 %)."""
+    m = _gaussian_mesh(1_000_000, (32, 32, 32))
+    phi = O.solve_potential(m)
+    nx, ny, nz = m.grid_size
+    zc = np.array([m.min_bounds[2] + k * m.delta[2] for k in range(nz)])
+    xi = int(np.argmin(np.abs([m.min_bounds[0] + i * m.delta[0] for i in range(nx)])))
+    yi = int(np.argmin(np.abs([m.min_bounds[1] + i * m.delta[1] for i in range(ny)])))
+    xc, yc = m.min_bounds[0] + xi * m.delta[0], m.min_bounds[1] + yi * m.delta[1]
+    pa = O.gaussian_potential(np.full(nz, xc), np.full(nz, yc), zc, 1e-9, 1e-3)
+    assert np.abs(phi[xi, yi, :] - pa).max() / np.abs(pa).max() < 0.10
+    ez = -(phi[xi, yi, 2:] - phi[xi, yi, :-2]) / (2 * m.delta[2])
+    ref = m.efield[xi, yi, 1:-1, 2]
+    assert np.abs(ez - ref).max() / np.abs(ref).max() < 0.03
