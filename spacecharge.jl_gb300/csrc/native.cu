@@ -869,6 +869,11 @@ int native_ensure_green(sc_mesh* m, int at_cathode, cudaStream_t s) {
     return ensure_green_t<double>(m, at_cathode, s);
 }
 
+// inverse y and x as one pass (k2_inv_yx) where it applies
+#ifndef SC_FUSED_INV_YX
+#define SC_FUSED_INV_YX 1
+#endif
+
 template <typename T>
 static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green_ready) {
     using T2 = typename Cplx<T>::T2;
@@ -932,6 +937,13 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
     {
         // inverse y: C (3 x Hx x Ly x nz) -> D (3 x Hx x ny x nz)
         StageScope st(m->timer, SC_STAGE_INV_Y, s);
+        if (two && SC_FUSED_INV_YX &&
+            launch2_inv_yx(w.log2L[0], w.log2L[1], (const float2*)C, (float4*)m->efield, nx, ny, nz, Hx,
+                           (const float2*)tw, s)) {
+            SC_LAUNCH_CHECK("k2_inv_yx");
+            m->launches -= 1;  // one launch for the two passes
+            return SC_OK;
+        }
         if (!(two && launch2_col(true, w.log2L[1], (const float2*)C, (float2*)D, Hx, Ly, ny, Hx, (int64_t)Hx * Ly,
                                  (int64_t)Hx * Ly * nz, Hx, (int64_t)Hx * ny, (int64_t)Hx * ny * nz, nz, 3,
                                  (const float2*)tw, s)))

@@ -85,6 +85,86 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k2_col(const f
     }
 }
 
+// Inverse y and x fused, one CTA per (z plane, component), Lx = Ly = L: the
+// plane's Hx columns are inverse-transformed along y (the outputs y < ny stay
+// in shared memory), then its rows, two per complex IFFT, along x into the
+// component's lane of the packed float4 nodes.  Replaces inverse y + inverse
+// x when the plane fits in shared memory; the intermediate D never goes to
+// global memory.
+template <int L>
+__global__ void __launch_bounds__(256) k2_inv_yx(const float2* __restrict__ C, float* __restrict__ E4, int nx,
+                                                 int ny, int nz, int Hx, const float2* __restrict__ tw) {
+    using E = F2<L>;
+    constexpr int W = 256 / E::NT;  // columns (phase 1) or row pairs (phase 2) per round
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float2* xb = reinterpret_cast<float2*>(smraw);  // W exchange columns
+    float2* ds = xb + W * E::S;                     // [ny][Hx]: the plane after inverse y
+    const int z = blockIdx.x, comp = blockIdx.y;
+    const int64_t plane = (int64_t)Hx * L;
+    const float2* Cp = C + (int64_t)comp * plane * nz + plane * z;
+    float2 v[16];
+    // phase 1: inverse y of the Hx columns (column-fastest thread map)
+    {
+        const int c = threadIdx.x % W, t = threadIdx.x / W;
+        float2* col = xb + c * E::S;
+        for (int k0 = 0; k0 < Hx; k0 += W) {
+            const int kx = k0 + c;
+            const bool ok = kx < Hx;
+            if (t < E::R1) {
+#pragma unroll
+                for (int r = 0; r < E::R2; ++r) v[r] = ok ? Cp[kx + (int64_t)Hx * (t + E::R1 * r)] : make_float2(0.f, 0.f);
+            }
+            E::template inv<true>(v, col, t, swt);
+            if (t < E::R2 && ok) {
+#pragma unroll
+                for (int s = 0; s < E::R1; ++s) {
+                    const int y = t + E::R2 * s;
+                    if (y < ny) ds[y * Hx + kx] = v[s];
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // phase 2: inverse x of the rows, two per complex IFFT (row-pair-fastest map)
+    {
+        const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
+        float2* col = xb + p * E::S;
+        float* out = E4 + comp;
+        for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
+            const int y0 = 2 * (q0 + p), y1 = y0 + 1;
+            if (t < E::R1) {
+#pragma unroll
+                for (int r = 0; r < E::R2; ++r) {
+                    const int k = t + E::R1 * r;
+                    const bool cj = k > L / 2;
+                    const int kk = cj ? L - k : k;
+                    float2 xa = make_float2(0.f, 0.f), xbv = make_float2(0.f, 0.f);
+                    if (y0 < ny) xa = ds[y0 * Hx + kk];
+                    if (y1 < ny) xbv = ds[y1 * Hx + kk];
+                    if (cj) {
+                        xa.y = -xa.y;
+                        xbv.y = -xbv.y;
+                    }
+                    v[r] = make_float2(xa.x - xbv.y, xa.y + xbv.x);  // Xa + i Xb
+                }
+            }
+            E::template inv<true>(v, col, t, swt);
+            if (t < E::R2) {
+#pragma unroll
+                for (int s = 0; s < E::R1; ++s) {
+                    const int x = t + E::R2 * s;
+                    if (x >= nx) continue;
+                    const int64_t node = x + (int64_t)nx * (y0 + (int64_t)ny * z);
+                    if (y0 < ny) out[4 * node] = v[s].x;
+                    if (y1 < ny) out[4 * (node + nx)] = v[s].y;
+                }
+            }
+        }
+    }
+}
+
 // x pass: two real rows per complex FFT -> their half spectra.
 template <int L>
 __global__ void __launch_bounds__(256) k2_fwd_x(const float* __restrict__ rho, float2* __restrict__ A, int nx,
@@ -614,6 +694,23 @@ static bool launch2_fwd_x(int logL, const float* rho, float2* A, int nx, int row
     }
     SC_L_SWITCH(logL, SC_K2FX)
 #undef SC_K2FX
+    return true;
+}
+
+// The fused inverse y+x pass needs Lx = Ly and the plane in shared memory.
+static bool launch2_inv_yx(int logLx, int logLy, const float2* C, float4* E4, int nx, int ny, int nz, int Hx,
+                           const float2* tw, cudaStream_t s) {
+    if (logLx != logLy) return false;
+#define SC_K2YX(LL)                                                                                   \
+    {                                                                                                 \
+        constexpr int W = 256 / F2<LL>::NT;                                                           \
+        const size_t smem = sizeof(float2) * ((size_t)W * F2<LL>::S + (size_t)ny * Hx);               \
+        if (smem > 100 * 1024) return false;                                                          \
+        if (set_smem(k2_inv_yx<LL>, smem) != SC_OK) return false;                                     \
+        k2_inv_yx<LL><<<dim3(nz, 3), 256, smem, s>>>(C, reinterpret_cast<float*>(E4), nx, ny, nz, Hx, tw); \
+    }
+    SC_L_SWITCH(logLx, SC_K2YX)
+#undef SC_K2YX
     return true;
 }
 
