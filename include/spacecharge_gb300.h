@@ -116,6 +116,12 @@ int sc_auto_bounds(const int32_t grid_size[3], const void* x, const void* y,
                    const void* z, int64_t n, int dtype, double min_bounds[3],
                    double max_bounds[3], double delta[3], void* stream);
 
+/* The same bounds from extrema the caller already has (for instance reduced
+ * over the ranks that each hold part of a bunch): the padding and delta
+ * arithmetic of mesh.jl:152-177 on mins[3], maxs[3].  Host only. */
+int sc_bounds_from_extrema(const int32_t grid_size[3], const double mins[3], const double maxs[3],
+                           double min_bounds[3], double max_bounds[3], double delta[3]);
+
 /* Particle-bounds constructor: Mesh3D(grid_size, px, py, pz; T, gamma,
  * total_charge), src/mesh.jl:122-201.  Synchronises `stream`. */
 int sc_mesh_create_from_particles(const int32_t grid_size[3], const void* x,

@@ -481,6 +481,13 @@ int sc_auto_bounds(const int32_t grid_size[3], const void* x, const void* y, con
     if (n <= 0 || !x || !y || !z) return fail(SC_ERR_INVALID, "Particle arrays cannot be empty.");  // :137-139
     double mins[3], maxs[3];
     SC_TRY(bounds_reduce(x, y, z, n, dtype, mins, maxs, (cudaStream_t)stream));
+    return sc_bounds_from_extrema(grid_size, mins, maxs, min_bounds, max_bounds, delta);
+}
+
+int sc_bounds_from_extrema(const int32_t grid_size[3], const double mins[3], const double maxs[3],
+                           double min_bounds[3], double max_bounds[3], double delta[3]) {
+    SC_TRY(check_grid(grid_size));
+    if (!mins || !maxs) return fail(SC_ERR_INVALID, "extrema are NULL");
     for (int d = 0; d < 3; ++d)
         if (!isfinite(mins[d]) || !isfinite(maxs[d]))
             return fail(SC_ERR_INVALID, "particle coordinates must be finite");

@@ -99,6 +99,7 @@ SIGNATURES = {
     "sc_soa_to_aos": [_vp, _vp, _vp, _i64, _int, _int, _i32p, _vp, _vp],
     "sc_relative_to_absolute": [_vp, _vp, _vp, _i64, _dp, _vp, _vp, _vp, _vp],
     "sc_solve_potential": [_vp, _int, _vp, _vp],
+    "sc_bounds_from_extrema": [_i32p, _dp, _dp, _dp, _dp, _dp],
     "sc_track": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _int, C.c_double, C.c_double, _int, _int, _int, _vp],
     "sc_mesh_set_profiling": [_vp, _int],
     "sc_mesh_stage_times": [_vp, _dp, C.POINTER(_i64), _vp],

@@ -70,3 +70,80 @@ def test_shard_single_rank_is_everything():
     assert shard_bunches([5, 1, 9], 1, 0) == [0, 1, 2]
     with pytest.raises(ValueError):
         shard_bunches([1], 2, 2)
+
+
+# ------------------------------------------- one bunch split over ranks
+def _bunch(n=6000, seed=11):
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal((3, n)).clip(-4.5, 4.5) * np.array([[1e-3], [0.8e-3], [0.3e-3]])
+    return v[0], v[1], v[2], np.full(n, 1e-9 / n)
+
+
+class _OracleMesh:
+    """Stand-in mesh for the host-logic test: the oracle's mesh with its rho
+    exposed as a torch view, as Mesh3D.rho exposes the device array."""
+
+    def __init__(self, grid, lo, hi):
+        import oracle as O
+
+        self.om = O.mesh_manual(grid, lo, hi)
+        self.rho = torch.from_numpy(self.om.rho)  # x fastest: permute(2, 1, 0) is contiguous
+
+
+def _sharded_worker(rank, world, port, q):
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, root)
+    sys.path.insert(0, os.path.join(root, "spacecharge.jl_gb300", "python"))
+    import oracle as O
+    import spacecharge_gb300.mesh as M
+    from spacecharge_gb300 import shard
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    x, y, z, qq = _bunch()
+    mine = slice(rank, None, world)  # this rank's particles
+    grid = (10, 12, 16)
+    lo, hi = shard.global_bounds(grid, torch.from_numpy(x[mine]), torch.from_numpy(y[mine]),
+                                 torch.from_numpy(z[mine]))
+    # the library's deposit/solve/gather replaced by the oracle's (no GPU here)
+    M.deposit = lambda m, px, py, pz, pq: O.deposit(m.om, px, py, pz, pq)
+    M.solve = lambda m, at_cathode=False: O.solve(m.om, at_cathode=at_cathode)
+    M.interpolate_field = lambda m, px, py, pz: O.interpolate_field(m.om, px, py, pz)
+    m = _OracleMesh(grid, lo, hi)
+    e = shard.kick_sharded(m, x[mine], y[mine], z[mine], qq[mine])
+    got = [None] * world
+    dist.all_gather_object(got, (rank, lo, hi, [np.asarray(c) for c in e]))
+    if rank == 0:
+        q.put(got)
+    dist.destroy_process_group()
+
+
+def test_one_bunch_split_over_two_ranks():
+    """Two gloo ranks each hold half of one bunch: global_bounds gives both the
+    whole bunch's constructor bounds, and kick_sharded (local deposit, rho
+    all-reduce, solve, local gather) gives each rank's particles the field of
+    the whole bunch."""
+    import oracle as O
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_sharded_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = q.get(timeout=180)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    x, y, z, qq = _bunch()
+    ref_mesh = O.mesh_auto((10, 12, 16), x, y, z)
+    ref = O.kick(ref_mesh, x, y, z, qq)
+    for rank, lo, hi, e in got:
+        assert np.allclose(lo, ref_mesh.min_bounds, rtol=0, atol=0)
+        assert np.allclose(hi, ref_mesh.max_bounds, rtol=0, atol=0)
+        for c in range(3):
+            want = ref[c][rank::2]
+            assert np.abs(e[c] - want).max() <= 1e-12 * np.abs(ref[c]).max()
