@@ -531,6 +531,8 @@ int sc_mesh_destroy(sc_mesh* m) {
     cudaFree(m->trackE);
     cudaFree(m->corner);
     if (m->side) cudaStreamDestroy(m->side);
+    if (m->side2) cudaStreamDestroy(m->side2);
+    if (m->ev_join2) cudaEventDestroy(m->ev_join2);
     if (m->ev_fork) cudaEventDestroy(m->ev_fork);
     if (m->ev_join) cudaEventDestroy(m->ev_join);
     cudaFree(m->rho);

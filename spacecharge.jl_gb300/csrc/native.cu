@@ -713,7 +713,13 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
     const int Hy = Ly / 2 + 1, Hz = Lz / 2 + 1;
     const int64_t gcs = (int64_t)nx * ny * (2 * nz - 1);
     const int64_t scs = (int64_t)Hx * Ly * Lz;
-    if (!w.goct) SC_CUDA(cudaMalloc(&w.goct, sizeof(float) * 3 * gcs));
+    // the free-space and image builds have their own scratch: they may run
+    // concurrently on two streams (native_green_async)
+    void*& goct = image ? w.goct_img : w.goct;
+    void*& gtmp = image ? w.gtmp_img : w.gtmp;
+    double*& fnear = image ? w.fnear_img : w.fnear;
+    int64_t& fnear_cap = image ? w.fnear_img_cap : w.fnear_cap;
+    if (!goct) SC_CUDA(cudaMalloc(&goct, sizeof(float) * 3 * gcs));
     if (image && !w.gimg) SC_CUDA(cudaMalloc(&w.gimg, sizeof(float2) * 3 * (int64_t)Hx * Hy * Lz));
     OctantGeom g;
     g.nx = nx;
@@ -747,32 +753,32 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
     // FP64 antiderivative terms on the near-box corners (3 terms x 3 comps)
     const bool has_near = g.nbx > 0 && g.nby > 0 && g.bz1 > g.bz0;
     const int64_t nterm = has_near ? 9 * (int64_t)(g.nbx + 1) * (g.nby + 1) * (g.bz1 - g.bz0 + 1) : 0;
-    if (w.fnear_cap < nterm) {
-        cudaFree(w.fnear);
-        w.fnear = nullptr;
-        SC_CUDA(cudaMalloc(&w.fnear, sizeof(double) * nterm));
-        w.fnear_cap = nterm;
+    if (fnear_cap < nterm) {
+        cudaFree(fnear);
+        fnear = nullptr;
+        SC_CUDA(cudaMalloc(&fnear, sizeof(double) * nterm));
+        fnear_cap = nterm;
     }
-    g.fnear = w.fnear;
+    g.fnear = fnear;
     const int zc = image ? 2 * nz - 1 : nz;
     const int64_t cells = (int64_t)nx * ny * zc;
     const int near_blocks = (int)((nterm + 63) / 64);
-    k_igf_split<<<(unsigned)(near_blocks + (cells + 63) / 64), 64, 0, s>>>((float*)w.goct, w.fnear, g, near_blocks);
+    k_igf_split<<<(unsigned)(near_blocks + (cells + 63) / 64), 64, 0, s>>>((float*)goct, fnear, g, near_blocks);
     SC_LAUNCH_CHECK("k_igf_split");
     if (has_near) {
         const int64_t box = (int64_t)g.nbx * g.nby * (g.bz1 - g.bz0);
-        k_igf_near_cells<<<(unsigned)((3 * box + 63) / 64), 64, 0, s>>>((float*)w.goct, w.fnear, g);
+        k_igf_near_cells<<<(unsigned)((3 * box + 63) / 64), 64, 0, s>>>((float*)goct, fnear, g);
         SC_LAUNCH_CHECK("k_igf_near_cells");
     }
     if (fft_engine() == 0 && w.log2L[0] <= 8 && w.log2L[1] <= 8 && w.log2L[2] <= 8) {
         // parity-reduced transform: real octant lines only (pipeline2.cuh)
         const int64_t t1max = (int64_t)Hx * ny * (2 * nz - 1), t2max = (int64_t)Hx * Hy * (2 * nz - 1);
-        if (!w.gtmp) SC_CUDA(cudaMalloc(&w.gtmp, sizeof(float) * 3 * (t1max + t2max)));
-        float* T1 = (float*)w.gtmp;
+        if (!gtmp) SC_CUDA(cudaMalloc(&gtmp, sizeof(float) * 3 * (t1max + t2max)));
+        float* T1 = (float*)gtmp;
         float* T2 = T1 + 3 * t1max;
         const int64_t t1cs = (int64_t)Hx * ny * zc, t2cs = (int64_t)Hx * Hy * zc;
         const int64_t plane = (int64_t)Hx * Hy;
-        if (launch3_green_x(w.log2L[0], (const float*)w.goct, T1, nx, ny * zc, Hx, gcs, t1cs, tw, s) &&
+        if (launch3_green_x(w.log2L[0], (const float*)goct, T1, nx, ny * zc, Hx, gcs, t1cs, tw, s) &&
             launch3_green_col(false, w.log2L[1], T1, T2, Hx, zc, ny, 1, Hx, (int64_t)Hx * ny, t1cs, Hx, plane, t2cs,
                               tw, s) &&
             launch3_green_col(image, w.log2L[2], T2, image ? w.gimg : w.gfree, (int)plane, 1, nz, 2, plane, 0, t2cs,
@@ -791,7 +797,7 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
         SC_TRY(set_smem(k_green_x, smem));
         const int rows = (2 * ny - 1) * (2 * nz - 1);
         dim3 grid(((rows + 1) / 2 + P - 1) / P, 3);
-        k_green_x<<<grid, 256, smem, s>>>((const float*)w.goct, S, nx, ny, nz, g.image, Lx, w.log2L[0], Ly, Lz, Hx,
+        k_green_x<<<grid, 256, smem, s>>>((const float*)goct, S, nx, ny, nz, g.image, Lx, w.log2L[0], Ly, Lz, Hx,
                                           lgP, gcs, scs, tw);
         SC_LAUNCH_CHECK("k_green_x");
     }
@@ -844,19 +850,24 @@ static void set_key(GreenKey& k, const sc_mesh* m, double offz) {
 }
 
 // Build (or reuse) the compressed Green spectra the solve needs.
+// Builds the free-space (image = false) or image spectrum unless the cached
+// one matches the geometry.
+template <typename T>
+static int ensure_green_part(sc_mesh* m, bool image, cudaStream_t s) {
+    NativeWork& w = m->nw;
+    const double offz = image ? 2 * m->lo[2] + (m->hi[2] - m->lo[2]) : 0.0;  // free_space.jl:39
+    GreenKey& key = image ? w.key_img : w.key_free;
+    if (m->green_cache && key_matches(key, m, offz)) return SC_OK;
+    StageScope st(m->timer, SC_STAGE_GREEN, s);
+    SC_TRY(build_green_any<T>(m, image, offz, s));
+    set_key(key, m, offz);
+    return SC_OK;
+}
+
 template <typename T>
 static int ensure_green_t(sc_mesh* m, int at_cathode, cudaStream_t s) {
-    NativeWork& w = m->nw;
-    const double offz = 2 * m->lo[2] + (m->hi[2] - m->lo[2]);  // free_space.jl:39
-    StageScope st(m->timer, SC_STAGE_GREEN, s);
-    if (!(m->green_cache && key_matches(w.key_free, m, 0.0))) {
-        SC_TRY(build_green_any<T>(m, false, 0.0, s));
-        set_key(w.key_free, m, 0.0);
-    }
-    if (at_cathode && !(m->green_cache && key_matches(w.key_img, m, offz))) {
-        SC_TRY(build_green_any<T>(m, true, offz, s));
-        set_key(w.key_img, m, offz);
-    }
+    SC_TRY(ensure_green_part<T>(m, false, s));
+    if (at_cathode) SC_TRY(ensure_green_part<T>(m, true, s));
     return SC_OK;
 }
 
@@ -1119,18 +1130,30 @@ int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green_r
 int native_green_async(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t* ready) {
     *ready = nullptr;
     if (!native_green_stale(m, at_cathode)) return SC_OK;
-    if (!m->side) {
-        // highest priority: the z pass waits for this build, the deposit on
-        // the caller's stream does not
-        int least = 0, greatest = 0;
-        SC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-        SC_CUDA(cudaStreamCreateWithPriority(&m->side, cudaStreamNonBlocking, greatest));
-    }
+    // highest priority: the z pass waits for these builds, the deposit on
+    // the caller's stream does not
+    int least = 0, greatest = 0;
+    SC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    if (!m->side) SC_CUDA(cudaStreamCreateWithPriority(&m->side, cudaStreamNonBlocking, greatest));
+    if (!m->side2) SC_CUDA(cudaStreamCreateWithPriority(&m->side2, cudaStreamNonBlocking, greatest));
     if (!m->ev_fork) SC_CUDA(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
     if (!m->ev_join) SC_CUDA(cudaEventCreateWithFlags(&m->ev_join, cudaEventDisableTiming));
+    if (!m->ev_join2) SC_CUDA(cudaEventCreateWithFlags(&m->ev_join2, cudaEventDisableTiming));
     SC_CUDA(cudaEventRecord(m->ev_fork, s));
     SC_CUDA(cudaStreamWaitEvent(m->side, m->ev_fork, 0));
-    const int st = native_ensure_green(m, at_cathode, m->side);
+    // the FP32 builds of the two spectra have separate scratch: run them side by side
+    int st = SC_OK;
+    if (at_cathode && m->precision == SC_PREC_MIXED) {
+        SC_TRY(alloc_work<float>(m));
+        SC_CUDA(cudaStreamWaitEvent(m->side2, m->ev_fork, 0));
+        st = ensure_green_part<float>(m, false, m->side);
+        if (st == SC_OK) st = ensure_green_part<float>(m, true, m->side2);
+        const cudaError_t e2 = cudaEventRecord(m->ev_join2, m->side2);
+        if (st == SC_OK && e2 != cudaSuccess) st = cuda_fail(e2, "cudaEventRecord");
+        cudaStreamWaitEvent(m->side, m->ev_join2, 0);
+    } else {
+        st = native_ensure_green(m, at_cathode, m->side);
+    }
     const cudaError_t e = cudaEventRecord(m->ev_join, m->side);
     if (st != SC_OK || e != cudaSuccess) {
         cudaStreamWaitEvent(s, m->ev_join, 0);
@@ -1142,8 +1165,8 @@ int native_green_async(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t* 
 
 int native_release(sc_mesh* m) {
     NativeWork& w = m->nw;
-    void* ptrs[] = {w.A,     w.B,     w.C,    w.D,     w.adjE,  w.adjcorner, w.fnear, w.fcorner,
-                    w.kgrid, w.kspec, w.goct, w.gspec, w.gtmp,  w.gfree,     w.gimg};
+    void* ptrs[] = {w.A,      w.B,     w.C,    w.D,        w.adjE,  w.adjcorner, w.fnear,    w.fnear_img, w.fcorner,
+                    w.kgrid,  w.kspec, w.goct, w.goct_img, w.gspec, w.gtmp,      w.gtmp_img, w.gfree,     w.gimg};
     for (void* p : ptrs) cudaFree(p);
     int L[3] = {w.L[0], w.L[1], w.L[2]};
     int lg[3] = {w.log2L[0], w.log2L[1], w.log2L[2]};

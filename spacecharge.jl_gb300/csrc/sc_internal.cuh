@@ -91,6 +91,10 @@ struct NativeWork {
     void* kgrid = nullptr;      // real kernel on the L grid (T)
     void* kspec = nullptr;      // its half spectrum (T2), Hx x Ly x Lz
     void* goct = nullptr;       // FP32 path: kernel values on the octant/quadrant, 3 comps
+    void* goct_img = nullptr;   //   the image build's own scratch (the two builds can run concurrently)
+    void* gtmp_img = nullptr;
+    double* fnear_img = nullptr;
+    int64_t fnear_img_cap = 0;
     void* gspec = nullptr;      // FP32 Stockham path: 3 half spectra Hx x Ly x Lz being transformed
     void* gtmp = nullptr;       // FP32 two-step path: parity-reduced x and y pass outputs (float)
     void* gfree = nullptr;      // compressed free-space spectra, 3 comps (T)
@@ -156,7 +160,8 @@ struct sc_mesh {
     void* tilework = nullptr; // tiled-deposit buffers (deposit_tiled.cu)
     void* corner = nullptr;   // vector-deposit per-cell corners, float[8N]
     cudaStream_t side = nullptr;  // Green build concurrent with the deposit (native_green_async)
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaStream_t side2 = nullptr; // the image build, beside the free-space one
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_join2 = nullptr;
     bool kick_graph = true;       // sc_kick replays a captured graph on repeated calls
     void* kickgraph = nullptr;    // its state (api.cu)
     void* hostpipe = nullptr;     // sc_kick_host staging buffers and copy streams (api.cu)
