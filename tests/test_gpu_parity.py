@@ -86,6 +86,23 @@ def test_kick_parity(sc, cuda, prec, grid, gamma):
 
 
 @pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("grid,cath", [((12, 12, 160), False), ((150, 10, 12), True), ((8, 140, 9), False)])
+def test_long_axis_parity(sc, cuda, prec, grid, cath):
+    """Axes of more than 128 nodes: transforms of 512 points, where the
+    mixed pipeline runs the shared-memory Stockham passes for that axis (and
+    the Green build and inverse passes fall back accordingly)."""
+    n = 8000
+    x, y, z = bunch(n, 17, sig=(1e-3, 0.8e-3, 2e-3))
+    if cath:
+        z = np.abs(z) + 0.2e-3
+    q = np.full(n, 1e-9 / n)
+    om, m, rho, oe, e = run_both(sc, grid, (x, y, z, q), prec, gamma=3.0, at_cathode=cath)
+    assert relerr(host(m.efield), om.efield) < TOL[prec]
+    for a, b in zip(e, oe):
+        assert relerr(a, b) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
 def test_cathode_parity(sc, cuda, prec):
     n = 5000
     x, y, z = bunch(n, 3, sig=(1e-3, 1e-3, 0.5e-3))
