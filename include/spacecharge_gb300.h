@@ -152,6 +152,14 @@ int sc_mesh_set_green_cache(sc_mesh* mesh, int enabled);
 #define SC_FFT_STOCKHAM 1
 int sc_set_fft_engine(int engine);
 
+/* Test hook for the error paths (no counterpart in the reference): after
+ * `after` more successful device allocations, every allocation the library
+ * makes fails with SC_ERR_OOM, without calling the runtime, until a negative
+ * `after` switches the injection off.  Process-wide.  A call that fails this
+ * way leaves its mesh usable: the next call with allocations allowed
+ * retries them. */
+int sc_test_fail_allocations(int64_t after);
+
 /* clear_mesh!(mesh), src/deposition.jl:10-12. */
 int sc_clear_mesh(sc_mesh* mesh, void* stream);
 

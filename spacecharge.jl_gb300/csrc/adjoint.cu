@@ -309,7 +309,7 @@ static int adjoint_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q,
     const int nx = m->n[0], ny = m->n[1], nz = m->n[2];
     const int Lx = w.L[0], Ly = w.L[1], Lz = w.L[2], Hx = w.Hx;
     const int64_t N = m->N;
-    if (!w.adjE) SC_CUDA(cudaMalloc(&w.adjE, sizeof(T) * 3 * N));
+    if (!w.adjE) SC_CUDA(dev_alloc(&w.adjE, sizeof(T) * 3 * N));
     T* adjE = (T*)w.adjE;
     const Axes ax = make_axes(m);
     k_adj_init<T><<<(N + 255) / 256, 256, 0, s>>>(adjE, (const typename Vec4<T>::V*)ggrid, N);
@@ -317,7 +317,7 @@ static int adjoint_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q,
     if ((gex || gey || gez) && n > 0) {
         if (std::is_same<T, float>::value) {
             const size_t slice = sizeof(float) * 8 * (size_t)N;
-            if (!w.adjcorner) SC_CUDA(cudaMalloc(&w.adjcorner, 3 * slice));
+            if (!w.adjcorner) SC_CUDA(dev_alloc(&w.adjcorner, 3 * slice));
             const P* g[3] = {gex, gey, gez};
             for (int c = 0; c < 3; ++c)
                 if (g[c]) SC_CUDA(cudaMemsetAsync((char*)w.adjcorner + c * slice, 0, slice, s));

@@ -36,21 +36,44 @@ int cuda_fail(cudaError_t e, const char* what) {
     return e == cudaErrorMemoryAllocation ? SC_ERR_OOM : SC_ERR_CUDA;
 }
 
+// ----------------------------------------------------- device allocation
+// Successful allocations still allowed before injected failures (< 0: none).
+static std::atomic<int64_t> g_alloc_allow{-1};
+static std::atomic<int64_t> g_alloc_gen{0};
+
+int64_t alloc_generation() { return g_alloc_gen.load(); }
+
+cudaError_t dev_alloc(void** p, size_t bytes) {
+    *p = nullptr;
+    int64_t left = g_alloc_allow.load();
+    while (left >= 0) {
+        if (left == 0) return cudaErrorMemoryAllocation;
+        if (g_alloc_allow.compare_exchange_weak(left, left - 1)) break;
+    }
+    const cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        (void)cudaGetLastError();
+        return e;
+    }
+    g_alloc_gen.fetch_add(1);
+    return e;
+}
+
+cudaError_t dev_realloc(void** p, size_t bytes) {
+    if (*p) {
+        cudaFree(*p);
+        *p = nullptr;
+        g_alloc_gen.fetch_add(1);
+    }
+    return dev_alloc(p, bytes);
+}
+
 // ------------------------------------------------------- per-device state
 static std::mutex g_ctx_mu;
 static std::vector<DeviceCtx*> g_ctx;
 
-int device_ctx(DeviceCtx** out) {
-    int dev = 0;
-    SC_CUDA(cudaGetDevice(&dev));
-    std::lock_guard<std::mutex> lk(g_ctx_mu);
-    if ((int)g_ctx.size() <= dev) g_ctx.resize(dev + 1, nullptr);
-    if (g_ctx[dev]) {
-        *out = g_ctx[dev];
-        return SC_OK;
-    }
-    DeviceCtx* c = new DeviceCtx();
-    c->device = dev;
+static int device_ctx_init(DeviceCtx* c, int dev) {
     SC_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, dev));
     // Twiddle table exp(-2 pi i k / kMaxL) built in FP64 from sin/cos of
     // exactly representable multiples of pi/2^kMaxLog: each FP32 entry is the
@@ -63,12 +86,34 @@ int device_ctx(DeviceCtx** out) {
         t64[k] = make_double2(c, s);
         t32[k] = make_float2((float)c, (float)s);
     }
-    SC_CUDA(cudaMalloc(&c->tw32, sizeof(float2) * kMaxL));
-    SC_CUDA(cudaMalloc(&c->tw64, sizeof(double2) * kMaxL));
+    SC_CUDA(dev_alloc(&c->tw32, sizeof(float2) * kMaxL));
+    SC_CUDA(dev_alloc(&c->tw64, sizeof(double2) * kMaxL));
     SC_CUDA(cudaMemcpy(c->tw32, t32.data(), sizeof(float2) * kMaxL, cudaMemcpyHostToDevice));
     SC_CUDA(cudaMemcpy(c->tw64, t64.data(), sizeof(double2) * kMaxL, cudaMemcpyHostToDevice));
     c->partial_blocks = 2 * c->sm_count;
-    SC_CUDA(cudaMalloc(&c->partials, sizeof(double) * 6 * (c->partial_blocks + 1)));
+    SC_CUDA(dev_alloc(&c->partials, sizeof(double) * 6 * (c->partial_blocks + 1)));
+    return SC_OK;
+}
+
+int device_ctx(DeviceCtx** out) {
+    int dev = 0;
+    SC_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    if ((int)g_ctx.size() <= dev) g_ctx.resize(dev + 1, nullptr);
+    if (g_ctx[dev]) {
+        *out = g_ctx[dev];
+        return SC_OK;
+    }
+    DeviceCtx* c = new DeviceCtx();
+    c->device = dev;
+    const int st = device_ctx_init(c, dev);
+    if (st != SC_OK) {
+        cudaFree(c->tw32);
+        cudaFree(c->tw64);
+        cudaFree(c->partials);
+        delete c;
+        return st;
+    }
     g_ctx[dev] = c;
     *out = c;
     return SC_OK;
@@ -86,6 +131,12 @@ Geom make_geom(const sc_mesh* m) {
         g.inv[d] = 1.0 / m->delta[d];
     }
     return g;
+}
+
+const char* stage_name(int stage) {
+    static const char* names[SC_NUM_STAGES] = {"sc:deposit", "sc:green", "sc:fwd_x", "sc:fwd_y", "sc:zpass",
+                                               "sc:inv_y",   "sc:inv_x", "sc:gather", "sc:plain_fft"};
+    return stage >= 0 && stage < SC_NUM_STAGES ? names[stage] : "sc:stage";
 }
 
 void StageTimer::begin(int stage, cudaStream_t s) {
@@ -169,9 +220,9 @@ static int mesh_alloc(const int32_t* g, const double* lo, const double* hi, cons
     }
     const size_t eb = field_elem_bytes(precision);
     const size_t ncomp = precision == SC_PREC_PLAIN64 ? 3 : 4;
-    e = cudaMalloc(&m->rho, eb * m->N);
-    if (e == cudaSuccess) e = cudaMalloc(&m->efield, eb * ncomp * m->N);
-    if (e == cudaSuccess) e = cudaMalloc(&m->oob, sizeof(unsigned long long));
+    e = dev_alloc(&m->rho, eb * m->N);
+    if (e == cudaSuccess) e = dev_alloc(&m->efield, eb * ncomp * m->N);
+    if (e == cudaSuccess) e = dev_alloc(&m->oob, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(m->rho, 0, eb * m->N);
     if (e == cudaSuccess) e = cudaMemset(m->efield, 0, eb * ncomp * m->N);
     if (e == cudaSuccess) e = cudaMemset(m->oob, 0, sizeof(unsigned long long));
@@ -218,12 +269,13 @@ int kick_issue(sc_mesh* m, const void* x, const void* y, const void* z, const vo
     // and the forward x and y transforms; the z pass waits for them.
     cudaEvent_t ready = nullptr;
     if (n > 0) SC_TRY(native_green_async(m, at_cathode, s, &ready));
-    const int st = sc_deposit(m, x, y, z, q, n, dtype, 1, mode, s);
+    int st = sc_deposit(m, x, y, z, q, n, dtype, 1, mode, s);
+    if (st == SC_OK) st = native_solve(m, at_cathode, s, ready);
     if (st != SC_OK) {
+        // the caller's stream still orders the Green build issued above
         if (ready) cudaStreamWaitEvent(s, ready, 0);
         return st;
     }
-    SC_TRY(native_solve(m, at_cathode, s, ready));
     if (n == 0) return SC_OK;
     StageScope sg(m->timer, SC_STAGE_GATHER, s);
     // the tiled deposit binned exactly these particles: gather through the tiles
@@ -245,13 +297,7 @@ struct KickGraph {
     int64_t launches = 0;  // kernels one replay runs
 };
 
-static std::vector<int64_t> kick_key(const sc_mesh* m, const void* const* ptr, int64_t n, int dtype,
-                                      int at_cathode) {
-    std::vector<int64_t> k;
-    for (int i = 0; i < 7; ++i) k.push_back((int64_t)(intptr_t)ptr[i]);
-    k.push_back(n);
-    k.push_back(dtype);
-    k.push_back(at_cathode);
+void mesh_state_key(const sc_mesh* m, std::vector<int64_t>& k) {
     k.push_back(m->green_cache);
     k.push_back(m->kick_mode);
     k.push_back(fft_engine());
@@ -264,6 +310,18 @@ static std::vector<int64_t> kick_key(const sc_mesh* m, const void* const* ptr, i
         memcpy(&b, &v, sizeof b);
         k.push_back(b);
     }
+    k.push_back(m->green_epoch);
+    k.push_back(alloc_generation());
+}
+
+static std::vector<int64_t> kick_key(const sc_mesh* m, const void* const* ptr, int64_t n, int dtype,
+                                      int at_cathode) {
+    std::vector<int64_t> k;
+    for (int i = 0; i < 7; ++i) k.push_back((int64_t)(intptr_t)ptr[i]);
+    k.push_back(n);
+    k.push_back(dtype);
+    k.push_back(at_cathode);
+    mesh_state_key(m, k);
     return k;
 }
 
@@ -286,7 +344,7 @@ static void kick_graph_drop(KickGraph* kg) {
 }
 
 static int kick_graph_capture(sc_mesh* m, KickGraph* kg, const void* const* p, int64_t n, int dtype,
-                              int at_cathode, std::vector<int64_t> key) {
+                              int at_cathode) {
     kick_graph_drop(kg);
     if (!kg->cap) SC_CUDA(cudaStreamCreateWithFlags(&kg->cap, cudaStreamNonBlocking));
     const int64_t l0 = m->launches;
@@ -309,7 +367,9 @@ static int kick_graph_capture(sc_mesh* m, KickGraph* kg, const void* const* p, i
         return cuda_fail(ei, "cudaGraphInstantiate");
     }
     kg->graph = g;
-    kg->key = std::move(key);
+    // keyed on the state after the capture (a capture that builds the Green
+    // spectra moves the epoch)
+    kg->key = kick_key(m, p, n, dtype, at_cathode);
     return SC_OK;
 }
 
@@ -358,25 +418,34 @@ void host_pipe_release(sc_mesh* m) {
     m->hostpipe = nullptr;
 }
 
+static int host_pipe_init(HostPipe* hp) {
+    SC_CUDA(cudaStreamCreateWithFlags(&hp->h2d, cudaStreamNonBlocking));
+    SC_CUDA(cudaStreamCreateWithFlags(&hp->d2h, cudaStreamNonBlocking));
+    SC_CUDA(cudaEventCreateWithFlags(&hp->fork, cudaEventDisableTiming));
+    SC_CUDA(cudaEventCreateWithFlags(&hp->done, cudaEventDisableTiming));
+    for (int c = 0; c < kHostChunks; ++c) {
+        SC_CUDA(cudaEventCreateWithFlags(&hp->in[c], cudaEventDisableTiming));
+        SC_CUDA(cudaEventCreateWithFlags(&hp->out[c], cudaEventDisableTiming));
+    }
+    return SC_OK;
+}
+
 static int host_pipe(sc_mesh* m, int64_t n, size_t elem, HostPipe** out) {
     HostPipe* hp = reinterpret_cast<HostPipe*>(m->hostpipe);
     if (!hp) {
         hp = new HostPipe();
         m->hostpipe = hp;
-        SC_CUDA(cudaStreamCreateWithFlags(&hp->h2d, cudaStreamNonBlocking));
-        SC_CUDA(cudaStreamCreateWithFlags(&hp->d2h, cudaStreamNonBlocking));
-        SC_CUDA(cudaEventCreateWithFlags(&hp->fork, cudaEventDisableTiming));
-        SC_CUDA(cudaEventCreateWithFlags(&hp->done, cudaEventDisableTiming));
-        for (int c = 0; c < kHostChunks; ++c) {
-            SC_CUDA(cudaEventCreateWithFlags(&hp->in[c], cudaEventDisableTiming));
-            SC_CUDA(cudaEventCreateWithFlags(&hp->out[c], cudaEventDisableTiming));
+        const int st = host_pipe_init(hp);
+        if (st != SC_OK) {
+            host_pipe_release(m);
+            return st;
         }
     }
     if (hp->cap < n || hp->elem != elem) {
         cudaFree(hp->stage);
         hp->stage = nullptr;
         hp->cap = 0;
-        SC_CUDA(cudaMalloc(&hp->stage, 7 * elem * (size_t)n));
+        SC_CUDA(dev_alloc(&hp->stage, 7 * elem * (size_t)n));
         hp->cap = n;
         hp->elem = elem;
     }
@@ -384,11 +453,9 @@ static int host_pipe(sc_mesh* m, int64_t n, size_t elem, HostPipe** out) {
     return SC_OK;
 }
 
-static int kick_host_issue(sc_mesh* m, const void* const* hin, int64_t n, int dtype, int at_cathode,
-                           void* const* hout, cudaStream_t s) {
+static int kick_host_run(sc_mesh* m, HostPipe* hp, const void* const* hin, int64_t n, int dtype, int at_cathode,
+                         void* const* hout, cudaStream_t s) {
     const size_t elem = dtype == SC_F64 ? 8 : 4;
-    HostPipe* hp = nullptr;
-    SC_TRY(host_pipe(m, n, elem, &hp));
     char* st = (char*)hp->stage;
     char* d[7];
     for (int i = 0; i < 7; ++i) d[i] = st + (size_t)i * elem * (size_t)hp->cap;
@@ -449,6 +516,19 @@ static int kick_host_issue(sc_mesh* m, const void* const* hin, int64_t n, int dt
     SC_CUDA(cudaEventRecord(hp->done, hp->d2h));
     SC_CUDA(cudaStreamWaitEvent(s, hp->done, 0));
     return SC_OK;
+}
+
+static int kick_host_issue(sc_mesh* m, const void* const* hin, int64_t n, int dtype, int at_cathode,
+                           void* const* hout, cudaStream_t s) {
+    HostPipe* hp = nullptr;
+    SC_TRY(host_pipe(m, n, dtype == SC_F64 ? 8 : 4, &hp));
+    const int st = kick_host_run(m, hp, hin, n, dtype, at_cathode, hout, s);
+    if (st != SC_OK) {
+        // an error returns with no copy of the caller's host buffers in flight
+        cudaStreamSynchronize(hp->h2d);
+        cudaStreamSynchronize(hp->d2h);
+    }
+    return st;
 }
 
 }  // namespace sc
@@ -618,6 +698,11 @@ int sc_set_fft_engine(int engine) {
     return SC_OK;
 }
 
+int sc_test_fail_allocations(int64_t after) {
+    g_alloc_allow.store(after < 0 ? -1 : after);
+    return SC_OK;
+}
+
 int sc_mesh_set_green_cache(sc_mesh* m, int enabled) {
     SC_TRY(check_mesh(m));
     m->green_cache = enabled != 0;
@@ -695,8 +780,7 @@ int sc_kick(sc_mesh* m, const void* x, const void* y, const void* z, const void*
         kg = new KickGraph();
         m->kickgraph = kg;
     }
-    // key again: the eager run may have autotuned or built cached spectra
-    return kick_graph_capture(m, kg, p, n, dtype, at_cathode, kick_key(m, p, n, dtype, at_cathode));
+    return kick_graph_capture(m, kg, p, n, dtype, at_cathode);
 }
 
 int sc_kick_host(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,

@@ -30,6 +30,7 @@ struct sc_batch {
     std::vector<const void*> key_ptr;
     std::vector<int64_t> key_n;
     int key_dtype = -1, key_cath = -1;
+    std::vector<int64_t> key_state;  // every mesh's mesh_state_key
 };
 
 namespace sc {
@@ -40,15 +41,24 @@ static int batch_issue(sc_batch* b, const void* const* x, const void* const* y, 
     SC_CUDA(cudaEventRecord(b->fork, s));
     for (cudaStream_t st : b->streams) SC_CUDA(cudaStreamWaitEvent(st, b->fork, 0));
     const int ns = (int)b->streams.size();
-    for (size_t i = 0; i < b->meshes.size(); ++i) {
-        cudaStream_t st = b->streams[i % ns];
-        SC_TRY(kick_issue(b->meshes[i], x[i], y[i], z[i], q[i], n[i], dtype, at_cathode, ex[i], ey[i], ez[i], st));
-    }
+    int st = SC_OK;
+    for (size_t i = 0; i < b->meshes.size() && st == SC_OK; ++i)
+        st = kick_issue(b->meshes[i], x[i], y[i], z[i], q[i], n[i], dtype, at_cathode, ex[i], ey[i], ez[i],
+                        b->streams[i % ns]);
+    // join every stream, also after a failed bunch: the caller's stream
+    // orders whatever was issued
     for (int k = 0; k < ns; ++k) {
-        SC_CUDA(cudaEventRecord(b->join[k], b->streams[k]));
-        SC_CUDA(cudaStreamWaitEvent(s, b->join[k], 0));
+        cudaError_t e = cudaEventRecord(b->join[k], b->streams[k]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, b->join[k], 0);
+        if (e != cudaSuccess && st == SC_OK) st = cuda_fail(e, "batch join");
     }
-    return SC_OK;
+    return st;
+}
+
+static std::vector<int64_t> batch_state(const sc_batch* b) {
+    std::vector<int64_t> k;
+    for (const sc_mesh* m : b->meshes) mesh_state_key(m, k);
+    return k;
 }
 
 static void batch_drop_graph(sc_batch* b) {
@@ -59,6 +69,7 @@ static void batch_drop_graph(sc_batch* b) {
     b->graph_nodes = 0;
     b->key_ptr.clear();
     b->key_n.clear();
+    b->key_state.clear();
 }
 
 }  // namespace sc
@@ -125,8 +136,10 @@ int sc_batch_kick(sc_batch* b, const void* const* x, const void* const* y, const
         key.insert(key.end(), p, p + 7);
     }
     std::vector<int64_t> kn(n, n + nb);
+    // the member meshes are the caller's: a refit, a rebuilt spectrum or a
+    // reallocated workspace of any of them forces a new capture
     if (b->graph_enabled && b->exec && key == b->key_ptr && kn == b->key_n && dtype == b->key_dtype &&
-        at_cathode == b->key_cath) {
+        at_cathode == b->key_cath && batch_state(b) == b->key_state) {
         SC_CUDA(cudaGraphLaunch(b->exec, s));
         return SC_OK;
     }
@@ -168,6 +181,7 @@ int sc_batch_kick(sc_batch* b, const void* const* x, const void* const* y, const
     b->key_n = kn;
     b->key_dtype = dtype;
     b->key_cath = at_cathode;
+    b->key_state = batch_state(b);
     return SC_OK;
 }
 

@@ -211,7 +211,7 @@ int corner_sum_launch(sc_mesh* m, const float* corner, float* out, cudaStream_t 
 
 static int corner_clear(sc_mesh* m, cudaStream_t s) {
     const size_t bytes = sizeof(float) * 8 * (size_t)m->N;
-    if (!m->corner) SC_CUDA(cudaMalloc(&m->corner, bytes));
+    if (!m->corner) SC_CUDA(dev_alloc(&m->corner, bytes));
     // Clearing here rather than in the node sum: the clear writes whole
     // sectors, so the atomics then find every line in L2 instead of
     // fetching it from DRAM.

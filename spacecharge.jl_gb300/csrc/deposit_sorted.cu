@@ -263,26 +263,25 @@ static int sorted_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q, 
         m->sortwork = w;
     }
     const int64_t N = m->N;
+    // capacity 0 until every buffer of the set is in place: a failed
+    // allocation leaves the set to be reallocated by the next call
     if (w->cap_n < n) {
-        cudaFree(w->key);
-        cudaFree(w->ticket);
-        cudaFree(w->skey);
-        cudaFree(w->pdat);
-        cudaFree(w->sdat);
-        SC_CUDA(cudaMalloc(&w->key, sizeof(int) * n));
-        SC_CUDA(cudaMalloc(&w->ticket, sizeof(int) * n));
-        SC_CUDA(cudaMalloc(&w->skey, sizeof(int) * n));
-        SC_CUDA(cudaMalloc(&w->pdat, sizeof(Pack4<double>) * n));
-        SC_CUDA(cudaMalloc(&w->sdat, sizeof(Pack4<double>) * n));
+        w->cap_n = 0;
+        SC_CUDA(dev_realloc(&w->key, sizeof(int) * n));
+        SC_CUDA(dev_realloc(&w->ticket, sizeof(int) * n));
+        SC_CUDA(dev_realloc(&w->skey, sizeof(int) * n));
+        SC_CUDA(dev_realloc(&w->pdat, sizeof(Pack4<double>) * n));
+        SC_CUDA(dev_realloc(&w->sdat, sizeof(Pack4<double>) * n));
         w->cap_n = n;
     }
     if (w->cap_N < N) {
         const int64_t nb = (N + 1023) / 1024;
-        SC_CUDA(cudaMalloc(&w->count, sizeof(int) * N));
-        SC_CUDA(cudaMalloc(&w->offset, sizeof(int) * N));
-        SC_CUDA(cudaMalloc(&w->sums, sizeof(int) * nb));
-        SC_CUDA(cudaMalloc(&w->fixed, sizeof(long long) * N));
-        SC_CUDA(cudaMalloc(&w->qsum, sizeof(double)));
+        w->cap_N = 0;
+        SC_CUDA(dev_realloc(&w->count, sizeof(int) * N));
+        SC_CUDA(dev_realloc(&w->offset, sizeof(int) * N));
+        SC_CUDA(dev_realloc(&w->sums, sizeof(int) * nb));
+        SC_CUDA(dev_realloc(&w->fixed, sizeof(long long) * N));
+        SC_CUDA(dev_realloc(&w->qsum, sizeof(double)));
         w->cap_N = N;
     }
     const Axes ax = make_axes(m);

@@ -321,24 +321,24 @@ static int tiled_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q, i
     }
     const TileGeom tg = tile_geom(m);
     if (tg.ntiles >= (1 << 22)) return fail(SC_ERR_UNSUPPORTED, "mesh too large for the tiled deposit");
+    w->src = nullptr;  // no binning for the gather until this one is issued
+    // capacity 0 until every buffer of the set is in place: a failed
+    // allocation leaves the set to be reallocated by the next call
     if (w->cap_n < n) {
-        void* ptrs[] = {w->key, w->ticket, w->skey, w->sidx, w->rec, w->srec};
-        for (void* p : ptrs) cudaFree(p);
-        SC_CUDA(cudaMalloc(&w->key, sizeof(int) * n));
-        SC_CUDA(cudaMalloc(&w->ticket, sizeof(int) * n));
-        SC_CUDA(cudaMalloc(&w->skey, sizeof(int) * n));
-        SC_CUDA(cudaMalloc(&w->sidx, sizeof(int) * n));
-        SC_CUDA(cudaMalloc(&w->rec, sizeof(TRec<double>) * n));
-        SC_CUDA(cudaMalloc(&w->srec, sizeof(TRec<double>) * n));
+        w->cap_n = 0;
+        SC_CUDA(dev_realloc(&w->key, sizeof(int) * n));
+        SC_CUDA(dev_realloc(&w->ticket, sizeof(int) * n));
+        SC_CUDA(dev_realloc(&w->skey, sizeof(int) * n));
+        SC_CUDA(dev_realloc(&w->sidx, sizeof(int) * n));
+        SC_CUDA(dev_realloc(&w->rec, sizeof(TRec<double>) * n));
+        SC_CUDA(dev_realloc(&w->srec, sizeof(TRec<double>) * n));
         w->cap_n = n;
     }
     if (w->cap_tiles < tg.ntiles) {
-        cudaFree(w->count);
-        cudaFree(w->offset);
-        cudaFree(w->woff);
-        SC_CUDA(cudaMalloc(&w->count, sizeof(int) * (tg.ntiles + 1)));
-        SC_CUDA(cudaMalloc(&w->offset, sizeof(int) * (tg.ntiles + 1)));
-        SC_CUDA(cudaMalloc(&w->woff, sizeof(int) * (tg.ntiles + 1)));
+        w->cap_tiles = 0;
+        SC_CUDA(dev_realloc(&w->count, sizeof(int) * (tg.ntiles + 1)));
+        SC_CUDA(dev_realloc(&w->offset, sizeof(int) * (tg.ntiles + 1)));
+        SC_CUDA(dev_realloc(&w->woff, sizeof(int) * (tg.ntiles + 1)));
         w->cap_tiles = tg.ntiles;
     }
     w->tg = tg;

@@ -647,10 +647,10 @@ static int alloc_green_tmp(sc_mesh* m, bool image) {
     const int64_t nx = m->n[0], ny = m->n[1], nz = m->n[2];
     const int64_t Lx = w.L[0], Ly = w.L[1], Lz = w.L[2], Hx = w.Hx;
     const int64_t Hy = Ly / 2 + 1;
-    if (!w.fcorner) SC_CUDA(cudaMalloc(&w.fcorner, sizeof(double) * (nx + 1) * (ny + 1) * (2 * nz)));
-    if (!w.kgrid) SC_CUDA(cudaMalloc(&w.kgrid, sizeof(T) * Lx * Ly * Lz));
-    if (!w.kspec) SC_CUDA(cudaMalloc(&w.kspec, sizeof(T2) * 2 * Hx * Ly * Lz));
-    if (image && !w.gimg) SC_CUDA(cudaMalloc(&w.gimg, sizeof(T2) * 3 * Hx * Hy * Lz));
+    if (!w.fcorner) SC_CUDA(dev_alloc(&w.fcorner, sizeof(double) * (nx + 1) * (ny + 1) * (2 * nz)));
+    if (!w.kgrid) SC_CUDA(dev_alloc(&w.kgrid, sizeof(T) * Lx * Ly * Lz));
+    if (!w.kspec) SC_CUDA(dev_alloc(&w.kspec, sizeof(T2) * 2 * Hx * Ly * Lz));
+    if (image && !w.gimg) SC_CUDA(dev_alloc(&w.gimg, sizeof(T2) * 3 * Hx * Hy * Lz));
     return SC_OK;
 }
 
@@ -719,8 +719,8 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
     void*& gtmp = image ? w.gtmp_img : w.gtmp;
     double*& fnear = image ? w.fnear_img : w.fnear;
     int64_t& fnear_cap = image ? w.fnear_img_cap : w.fnear_cap;
-    if (!goct) SC_CUDA(cudaMalloc(&goct, sizeof(float) * 3 * gcs));
-    if (image && !w.gimg) SC_CUDA(cudaMalloc(&w.gimg, sizeof(float2) * 3 * (int64_t)Hx * Hy * Lz));
+    if (!goct) SC_CUDA(dev_alloc(&goct, sizeof(float) * 3 * gcs));
+    if (image && !w.gimg) SC_CUDA(dev_alloc(&w.gimg, sizeof(float2) * 3 * (int64_t)Hx * Hy * Lz));
     OctantGeom g;
     g.nx = nx;
     g.ny = ny;
@@ -754,9 +754,8 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
     const bool has_near = g.nbx > 0 && g.nby > 0 && g.bz1 > g.bz0;
     const int64_t nterm = has_near ? 9 * (int64_t)(g.nbx + 1) * (g.nby + 1) * (g.bz1 - g.bz0 + 1) : 0;
     if (fnear_cap < nterm) {
-        cudaFree(fnear);
-        fnear = nullptr;
-        SC_CUDA(cudaMalloc(&fnear, sizeof(double) * nterm));
+        fnear_cap = 0;
+        SC_CUDA(dev_realloc(&fnear, sizeof(double) * nterm));
         fnear_cap = nterm;
     }
     g.fnear = fnear;
@@ -773,7 +772,7 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
     if (fft_engine() == 0 && w.log2L[0] <= 8 && w.log2L[1] <= 8 && w.log2L[2] <= 8) {
         // parity-reduced transform: real octant lines only (pipeline2.cuh)
         const int64_t t1max = (int64_t)Hx * ny * (2 * nz - 1), t2max = (int64_t)Hx * Hy * (2 * nz - 1);
-        if (!gtmp) SC_CUDA(cudaMalloc(&gtmp, sizeof(float) * 3 * (t1max + t2max)));
+        if (!gtmp) SC_CUDA(dev_alloc(&gtmp, sizeof(float) * 3 * (t1max + t2max)));
         float* T1 = (float*)gtmp;
         float* T2 = T1 + 3 * t1max;
         const int64_t t1cs = (int64_t)Hx * ny * zc, t2cs = (int64_t)Hx * Hy * zc;
@@ -788,7 +787,7 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
             return SC_OK;
         }
     }
-    if (!w.gspec) SC_CUDA(cudaMalloc(&w.gspec, sizeof(float2) * 3 * scs));
+    if (!w.gspec) SC_CUDA(dev_alloc(&w.gspec, sizeof(float2) * 3 * scs));
     float2* S = (float2*)w.gspec;
     {
         const int lgP = pick_rows(w.log2L[0]);
@@ -861,6 +860,7 @@ static int ensure_green_part(sc_mesh* m, bool image, cudaStream_t s) {
     StageScope st(m->timer, SC_STAGE_GREEN, s);
     SC_TRY(build_green_any<T>(m, image, offz, s));
     set_key(key, m, offz);
+    m->green_epoch++;
     return SC_OK;
 }
 

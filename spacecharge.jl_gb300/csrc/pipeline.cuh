@@ -237,15 +237,15 @@ template <typename T>
 static int alloc_work(sc_mesh* m) {
     using T2 = typename Cplx<T>::T2;
     NativeWork& w = m->nw;
-    if (w.A) return SC_OK;
     const int64_t ny = m->n[1], nz = m->n[2];
     const int64_t Hx = w.Hx, Ly = w.L[1], Lz = w.L[2];
     const int64_t Hy = Ly / 2 + 1, Hz = Lz / 2 + 1;
-    SC_CUDA(cudaMalloc(&w.A, sizeof(T2) * Hx * ny * nz));
-    SC_CUDA(cudaMalloc(&w.B, sizeof(T2) * Hx * Ly * nz));
-    SC_CUDA(cudaMalloc(&w.C, sizeof(T2) * 3 * Hx * Ly * nz));
-    SC_CUDA(cudaMalloc(&w.D, sizeof(T2) * 3 * Hx * ny * nz));
-    SC_CUDA(cudaMalloc(&w.gfree, sizeof(T) * 3 * Hx * Hy * Hz));
+    // each buffer on its own: a call after a failed allocation completes the set
+    if (!w.A) SC_CUDA(dev_alloc(&w.A, sizeof(T2) * Hx * ny * nz));
+    if (!w.B) SC_CUDA(dev_alloc(&w.B, sizeof(T2) * Hx * Ly * nz));
+    if (!w.C) SC_CUDA(dev_alloc(&w.C, sizeof(T2) * 3 * Hx * Ly * nz));
+    if (!w.D) SC_CUDA(dev_alloc(&w.D, sizeof(T2) * 3 * Hx * ny * nz));
+    if (!w.gfree) SC_CUDA(dev_alloc(&w.gfree, sizeof(T) * 3 * Hx * Hy * Hz));
     return SC_OK;
 }
 

@@ -133,9 +133,9 @@ static int plain_workspace(sc_mesh* m, cudaStream_t s) {
     PlainWork& w = m->pw;
     if (w.plan_ok) return SC_OK;
     const size_t total = (size_t)8 * m->N;
-    SC_CUDA(cudaMalloc(&w.crho, sizeof(double2) * total));
-    SC_CUDA(cudaMalloc(&w.cgrn, sizeof(double2) * total));
-    SC_CUDA(cudaMalloc(&w.tmp, sizeof(double2) * total));
+    if (!w.crho) SC_CUDA(dev_alloc(&w.crho, sizeof(double2) * total));
+    if (!w.cgrn) SC_CUDA(dev_alloc(&w.cgrn, sizeof(double2) * total));
+    if (!w.tmp) SC_CUDA(dev_alloc(&w.tmp, sizeof(double2) * total));
     // cuFFT dims are slowest-first: (2nz, 2ny, 2nx) for x-fastest storage.
     cufftResult r = cufftPlan3d(&w.plan, 2 * m->n[2], 2 * m->n[1], 2 * m->n[0], CUFFT_Z2Z);
     if (r != CUFFT_SUCCESS) return fail(SC_ERR_CUDA, "cufftPlan3d failed (%d)", (int)r);

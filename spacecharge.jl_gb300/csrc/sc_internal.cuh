@@ -2,6 +2,7 @@
 // libspacecharge_gb300.so.  Nothing here is part of the public C ABI.
 #pragma once
 
+#include <nvtx3/nvToolsExt.h>
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <stdint.h>
@@ -36,6 +37,22 @@ int cuda_fail(cudaError_t e, const char* what);
         cudaError_t _e = (call);                                 \
         if (_e != cudaSuccess) return ::sc::cuda_fail(_e, #call); \
     } while (0)
+
+// Every device buffer of the library comes from dev_alloc.  On failure *p is
+// null and the runtime's last-error slot is cleared, so the next launch check
+// does not report the failed allocation again.  sc_test_fail_allocations
+// makes it fail on demand, without calling the runtime.
+cudaError_t dev_alloc(void** p, size_t bytes);
+// Frees *p, then allocates `bytes` in its place (*p null on failure).
+cudaError_t dev_realloc(void** p, size_t bytes);
+template <typename T>
+inline cudaError_t dev_alloc(T** p, size_t bytes) {
+    return dev_alloc(reinterpret_cast<void**>(p), bytes);
+}
+template <typename T>
+inline cudaError_t dev_realloc(T** p, size_t bytes) {
+    return dev_realloc(reinterpret_cast<void**>(p), bytes);
+}
 
 #define SC_LAUNCH_CHECK(what)                                    \
     do {                                                         \
@@ -128,15 +145,21 @@ struct StageTimer {
     void end(cudaStream_t s);
     void release();
 };
-// RAII bracket: `StageScope t(m, SC_STAGE_X, s);`
+// NVTX range names of the stages (visible to nsys/ncu NVTX filters)
+const char* stage_name(int stage);
+
+// RAII bracket: `StageScope t(m, SC_STAGE_X, s);` -- an NVTX range on the
+// host always, CUDA events on the stream when the mesh's profiling is on.
 struct StageScope {
     StageTimer* t;
     cudaStream_t s;
     StageScope(StageTimer& tm, int stage, cudaStream_t st) : t(&tm), s(st) {
+        nvtxRangePushA(stage_name(stage));
         if (t->enabled) t->begin(stage, s);
     }
     ~StageScope() {
         if (t->enabled) t->end(s);
+        nvtxRangePop();
     }
 };
 }  // namespace sc
@@ -169,6 +192,7 @@ struct sc_mesh {
     int64_t track_cap = 0;
     size_t track_elem = 0;
     int kick_mode = SC_DEPOSIT_ATOMIC;  // deposit mode of sc_kick
+    int64_t green_epoch = 0;            // bumped by every Green spectrum build
 };
 
 namespace sc {
@@ -219,6 +243,13 @@ int deposit_chunk_finish(sc_mesh* m, int mode, cudaStream_t s);
 int kick_issue(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
                int at_cathode, void* ex, void* ey, void* ez, cudaStream_t s);
 void kick_graph_release(sc_mesh* m);
+// Appends what a captured kick of this mesh depends on besides its arguments:
+// flags, tuning choices, geometry (kernel arguments captured by value), the
+// Green epoch (cached spectra) and the allocation generation (workspace
+// addresses).  A graph replays only while this is unchanged.
+void mesh_state_key(const sc_mesh* m, std::vector<int64_t>& k);
+// Counts device allocations and frees made through dev_alloc / dev_realloc.
+int64_t alloc_generation();
 void host_pipe_release(sc_mesh* m);
 // new bounds for a mesh (sc_track's refit); cached spectra and graphs see the
 // change through their keys

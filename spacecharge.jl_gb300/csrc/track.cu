@@ -122,7 +122,7 @@ int sc_track(sc_mesh* m, void* x, void* y, void* z, void* ux, void* uy, void* uz
         cudaFree(m->trackE);
         m->trackE = nullptr;
         m->track_cap = 0;
-        SC_CUDA(cudaMalloc(&m->trackE, 3 * elem * (size_t)n));
+        SC_CUDA(dev_alloc(&m->trackE, 3 * elem * (size_t)n));
         m->track_cap = n;
         m->track_elem = elem;
     }

@@ -14,7 +14,8 @@ module SpaceChargeGB300
 using CUDA
 import ChainRulesCore
 
-export Mesh3D, deposit!, clear_mesh!, interpolate_field, solve!, kick, kick_host, track!, magnetic_field
+export Mesh3D, deposit!, clear_mesh!, interpolate_field, solve!, kick, kick_host, track!, magnetic_field,
+       set_kick_mode!
 
 const libsc = normpath(joinpath(@__DIR__, "..", "..", "..", "lib", "libspacecharge_gb300.so"))
 
@@ -127,12 +128,28 @@ function deposit!(mesh::Mesh3D, particles_x::CuArray{P}, particles_y::CuArray{P}
     if !(length(particles_x) == length(particles_y) == length(particles_z) == length(particles_q))
         error("Particle coordinate and charge arrays must have the same length.")
     end
-    m = mode === :atomic ? Cint(0) : mode === :sorted ? Cint(1) : Cint(2)
     check(ccall((:sc_deposit, libsc), Cint,
                 (Ptr{Cvoid}, CuPtr{P}, CuPtr{P}, CuPtr{P}, CuPtr{P}, Int64, Cint, Cint, Cint, Ptr{Cvoid}),
                 mesh.ptr, particles_x, particles_y, particles_z, particles_q, length(particles_x),
-                dtype_code(P), Cint(clear), m, stream_ptr()))
+                dtype_code(P), Cint(clear), deposit_mode_code(mode), stream_ptr()))
 end
+
+# include/spacecharge_gb300.h: SC_DEPOSIT_*
+const DEPOSIT_MODES = Dict(:atomic => Cint(0), :sorted => Cint(1), :deterministic => Cint(2),
+                           :tiled => Cint(3), :vector => Cint(4))
+deposit_mode_code(mode::Symbol) =
+    get(() -> error("unknown deposit mode $(repr(mode)); expected one of $(sort(collect(keys(DEPOSIT_MODES))))"),
+        DEPOSIT_MODES, mode)
+
+"""
+    set_kick_mode!(mesh, mode::Symbol)
+
+Deposit mode `kick` uses on this mesh: `:vector` (the default for mixed
+meshes), `:atomic` (the default otherwise), `:sorted`, `:deterministic`
+(bitwise reproducible) or `:tiled`.
+"""
+set_kick_mode!(mesh::Mesh3D, mode::Symbol) =
+    check(ccall((:sc_mesh_set_kick_mode, libsc), Cint, (Ptr{Cvoid}, Cint), mesh.ptr, deposit_mode_code(mode)))
 
 # solve!(mesh; at_cathode=false), src/solvers/free_space.jl:14-47
 solve!(mesh::Mesh3D; at_cathode::Bool=false) =

@@ -88,6 +88,7 @@ SIGNATURES = {
     "sc_mesh_set_kick_mode": [_vp, _int],
     "sc_mesh_set_kick_graph": [_vp, _int],
     "sc_set_fft_engine": [_int],
+    "sc_test_fail_allocations": [_i64],
     "sc_clear_mesh": [_vp, _vp],
     "sc_deposit": [_vp, _vp, _vp, _vp, _vp, _i64, _int, _int, _int, _vp],
     "sc_solve": [_vp, _int, _vp],

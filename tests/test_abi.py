@@ -38,6 +38,19 @@ def test_python_binding_covers_header(lib):
     assert set(declared_symbols()) <= set(L.SIGNATURES), set(declared_symbols()) - set(L.SIGNATURES)
 
 
+def test_julia_binding_calls_declared_symbols():
+    """Every ccall in the Julia package names an entry point of the header,
+    and its deposit-mode table matches the header's SC_DEPOSIT_* values."""
+    src = open(os.path.join(ROOT, "spacecharge.jl_gb300", "julia", "SpaceChargeGB300", "src",
+                            "SpaceChargeGB300.jl")).read()
+    called = set(re.findall(r"ccall\(\(:(sc_\w+),", src))
+    assert called and called <= set(declared_symbols()), called - set(declared_symbols())
+    hdr = open(os.path.join(ROOT, "include", "spacecharge_gb300.h")).read()
+    modes = {k.lower(): int(v) for k, v in re.findall(r"#define SC_DEPOSIT_(\w+)\s+(\d+)", hdr)}
+    jl = {k: int(v) for k, v in re.findall(r":(\w+) => Cint\((\d+)\)", src)}
+    assert jl == modes
+
+
 def test_version(lib):
     assert lib.sc_version() >= 10000
 
