@@ -3,6 +3,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -117,6 +118,14 @@ int device_ctx(DeviceCtx** out) {
     g_ctx[dev] = c;
     *out = c;
     return SC_OK;
+}
+
+bool pdl_enabled() {
+    static const bool on = [] {
+        const char* e = getenv("SC_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
 }
 
 static std::atomic<int> g_fft_engine{0};

@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(256) deposit_vector(const P* __restrict__ px, 
 
 __global__ void __launch_bounds__(256) k_corner_sum(const float* __restrict__ corner, int nx, int ny, int64_t N,
                                                     float* __restrict__ rho) {
+    pdl_wait();  // the corner slots come from the preceding deposit
     const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= N) return;
     const int i = (int)(node % nx);
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(256) k_corner_sum(const float* __restrict__ co
 }
 
 int corner_sum_launch(sc_mesh* m, const float* corner, float* out, cudaStream_t s) {
-    k_corner_sum<<<(m->N + 255) / 256, 256, 0, s>>>(corner, m->n[0], m->n[1], m->N, out);
+    launch_pdl(k_corner_sum, (unsigned)((m->N + 255) / 256), 256, 0, s, corner, m->n[0], m->n[1], m->N, out);
     SC_LAUNCH_CHECK("k_corner_sum");
     m->launches += 1;
     return SC_OK;

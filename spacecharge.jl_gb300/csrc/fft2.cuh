@@ -44,7 +44,12 @@ template <> struct Split<256> { static constexpr int R1 = 16, R2 = 16; };
 // twiddles there (a shared-memory load instead of a global one).
 template <int L, typename T2>
 __device__ __forceinline__ void stage_twiddles(T2* sw, const T2* __restrict__ tw) {
+    // The table is written once per device, before any transform: it is read
+    // ahead of the wait for the preceding grid (programmatic launch).  Every
+    // two-step kernel starts here, so the wait below orders all of its other
+    // global-memory accesses after the grids it follows.
     for (int j = threadIdx.x; j < L; j += blockDim.x) sw[j] = __ldg(tw + j * (kMaxL / L));
+    pdl_wait();
     __syncthreads();
 }
 

@@ -127,6 +127,7 @@ __global__ void __launch_bounds__(256, SC_GATH_MINB) gather_packed(const P* __re
                                                      P* __restrict__ ex, P* __restrict__ ey, P* __restrict__ ez,
                                                      unsigned long long* __restrict__ oob) {
     using V = typename Packed<A>::V;
+    pdl_wait();  // the field (and possibly the positions) come from preceding grids
     const int64_t base = (int64_t)blockIdx.x * (blockDim.x * kGathPerThread) + threadIdx.x;
     P x[kGathPerThread], y[kGathPerThread], z[kGathPerThread];
 #pragma unroll
@@ -207,20 +208,20 @@ int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64
     const int64_t gblocks = (n + 256 * kGathPerThread - 1) / (256 * kGathPerThread);
     if (m->precision == SC_PREC_MIXED) {
         if (dtype == SC_F64)
-            gather_packed<double, float><<<gblocks, 256, 0, s>>>((const double*)x, (const double*)y,
+            launch_pdl(gather_packed<double, float>, (unsigned)gblocks, 256, 0, s, (const double*)x, (const double*)y,
                                                                (const double*)z, n, ax, (const float4*)m->efield,
                                                                (double*)ex, (double*)ey, (double*)ez, m->oob);
         else
-            gather_packed<float, float><<<gblocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z, n,
+            launch_pdl(gather_packed<float, float>, (unsigned)gblocks, 256, 0, s, (const float*)x, (const float*)y, (const float*)z, n,
                                                               ax, (const float4*)m->efield, (float*)ex, (float*)ey,
                                                               (float*)ez, m->oob);
     } else {
         if (dtype == SC_F64)
-            gather_packed<double, double><<<gblocks, 256, 0, s>>>((const double*)x, (const double*)y,
+            launch_pdl(gather_packed<double, double>, (unsigned)gblocks, 256, 0, s, (const double*)x, (const double*)y,
                                                                 (const double*)z, n, ax, (const dnode4*)m->efield,
                                                                 (double*)ex, (double*)ey, (double*)ez, m->oob);
         else
-            gather_packed<float, double><<<gblocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z,
+            launch_pdl(gather_packed<float, double>, (unsigned)gblocks, 256, 0, s, (const float*)x, (const float*)y, (const float*)z,
                                                                n, ax, (const dnode4*)m->efield, (float*)ex,
                                                                (float*)ey, (float*)ez, m->oob);
     }

@@ -439,6 +439,7 @@ __global__ void __launch_bounds__(64) k_igf_split(float* __restrict__ G, double*
 // component) per thread.
 __global__ void __launch_bounds__(64) k_igf_near_cells(float* __restrict__ G, const double* __restrict__ T,
                                                        OctantGeom g) {
+    pdl_wait();  // the corner terms come from the preceding k_igf_split
     const int bz = g.bz1 - g.bz0;
     const int64_t box = (int64_t)g.nbx * g.nby * bz;
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -766,7 +767,7 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
     SC_LAUNCH_CHECK("k_igf_split");
     if (has_near) {
         const int64_t box = (int64_t)g.nbx * g.nby * (g.bz1 - g.bz0);
-        k_igf_near_cells<<<(unsigned)((3 * box + 63) / 64), 64, 0, s>>>((float*)goct, fnear, g);
+        launch_pdl(k_igf_near_cells, (unsigned)((3 * box + 63) / 64), 64, 0, s, (float*)goct, (const double*)fnear, g);
         SC_LAUNCH_CHECK("k_igf_near_cells");
     }
     if (fft_engine() == 0 && w.log2L[0] <= 8 && w.log2L[1] <= 8 && w.log2L[2] <= 8) {

@@ -672,11 +672,11 @@ static bool launch2_col(bool inv, int logL, const float2* in, float2* out, int n
     dim3 grid((unsigned)(((int64_t)ncols * nbatch + kColW - 1) / kColW), ncomp);
 #define SC_K2COL(LL)                                                                                            \
     if (inv)                                                                                                    \
-        k2_col<LL, true><<<grid, kColW * F2<LL>::NT, 0, s>>>(in, out, ncols, nbatch, n_valid, n_store, wrap, bwrap_n, \
+        launch_pdl(k2_col<LL, true>, grid, kColW * F2<LL>::NT, 0, s, in, out, ncols, nbatch, n_valid, n_store, wrap, bwrap_n, \
                                                               bwrap_L, as_in, bs_in, cs_in, as_out, bs_out,     \
                                                               cs_out, tw);                                      \
     else                                                                                                        \
-        k2_col<LL, false><<<grid, kColW * F2<LL>::NT, 0, s>>>(in, out, ncols, nbatch, n_valid, n_store, wrap, bwrap_n, \
+        launch_pdl(k2_col<LL, false>, grid, kColW * F2<LL>::NT, 0, s, in, out, ncols, nbatch, n_valid, n_store, wrap, bwrap_n, \
                                                                bwrap_L, as_in, bs_in, cs_in, as_out, bs_out,    \
                                                                cs_out, tw);
     SC_L_SWITCH(logL, SC_K2COL)
@@ -690,7 +690,7 @@ static bool launch2_fwd_x(int logL, const float* rho, float2* A, int nx, int row
     {                                                                        \
         constexpr int P = 256 / F2<LL>::NT;                                  \
         const int pairs = (rows + 1) / 2;                                    \
-        k2_fwd_x<LL><<<(pairs + P - 1) / P, 256, 0, s>>>(rho, A, nx, rows, Hx, tw); \
+        launch_pdl(k2_fwd_x<LL>, (pairs + P - 1) / P, 256, 0, s, rho, A, nx, rows, Hx, tw); \
     }
     SC_L_SWITCH(logL, SC_K2FX)
 #undef SC_K2FX
@@ -707,7 +707,7 @@ static bool launch2_inv_yx(int logLx, int logLy, const float2* C, float4* E4, in
         const size_t smem = sizeof(float2) * ((size_t)W * F2<LL>::S + (size_t)ny * Hx);               \
         if (smem > 100 * 1024) return false;                                                          \
         if (set_smem(k2_inv_yx<LL>, smem) != SC_OK) return false;                                     \
-        k2_inv_yx<LL><<<dim3(nz, 3), 256, smem, s>>>(C, reinterpret_cast<float*>(E4), nx, ny, nz, Hx, tw); \
+        launch_pdl(k2_inv_yx<LL>, dim3(nz, 3), 256, smem, s, C, reinterpret_cast<float*>(E4), nx, ny, nz, Hx, tw); \
     }
     SC_L_SWITCH(logLx, SC_K2YX)
 #undef SC_K2YX
@@ -722,7 +722,7 @@ static bool launch2_inv_x(int logL, const float2* D, float4* E4, int nx, int row
         const size_t smem = sizeof(float2) * (P * F2<LL>::S + 2 * P * LL);                  \
         if (set_smem(k2_inv_x<LL>, smem) != SC_OK) return false;                            \
         const int pairs = (rows + 1) / 2;                                                   \
-        k2_inv_x<LL><<<(pairs + P - 1) / P, 256, smem, s>>>(D, E4, nx, rows, Hx, cs, tw);   \
+        launch_pdl(k2_inv_x<LL>, (pairs + P - 1) / P, 256, smem, s, D, E4, nx, rows, Hx, cs, tw);   \
     }
     SC_L_SWITCH(logL, SC_K2IX)
 #undef SC_K2IX
@@ -737,7 +737,7 @@ static bool launch2_zpass(int logL, const float2* B, float2* C, int Hx, int Ly, 
                             sizeof(float) * 3 * (LL / 2 + 1) * kColW;                           \
         if (set_smem(k2_zpass<LL>, smem) != SC_OK) return false;                            \
         const int64_t ncol = (int64_t)Hx * Ly;                                              \
-        k2_zpass<LL><<<(unsigned)((ncol + kColW - 1) / kColW), kColW * F2<LL>::NT, smem, s>>>(B, C, Hx, Ly, nz, gv, tw); \
+        launch_pdl(k2_zpass<LL>, (unsigned)((ncol + kColW - 1) / kColW), kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz, gv, tw); \
     }
     SC_L_SWITCH(logL, SC_K2Z)
 #undef SC_K2Z
@@ -752,7 +752,7 @@ static bool launch2_adj_zpass(int logL, const float2* C, float2* B, int Hx, int 
                             sizeof(float) * 3 * (LL / 2 + 1) * kColW;                           \
         if (set_smem(k2_adj_zpass<LL>, smem) != SC_OK) return false;                        \
         const int64_t ncol = (int64_t)Hx * Ly;                                              \
-        k2_adj_zpass<LL><<<(unsigned)((ncol + kColW - 1) / kColW), kColW * F2<LL>::NT, smem, s>>>(C, B, Hx, Ly, nz, gv, tw); \
+        launch_pdl(k2_adj_zpass<LL>, (unsigned)((ncol + kColW - 1) / kColW), kColW * F2<LL>::NT, smem, s, C, B, Hx, Ly, nz, gv, tw); \
     }
     SC_L_SWITCH(logL, SC_K2AZ)
 #undef SC_K2AZ
@@ -765,7 +765,7 @@ static bool launch2_inv_x1(int logL, const float2* D, float* E4, int nx, int row
     {                                                                                 \
         constexpr int P = 256 / F2<LL>::NT;                                           \
         const int pairs = (rows + 1) / 2;                                             \
-        k2_inv_x1<LL><<<(pairs + P - 1) / P, 256, 0, s>>>(D, E4, nx, rows, Hx, tw);   \
+        launch_pdl(k2_inv_x1<LL>, (pairs + P - 1) / P, 256, 0, s, D, E4, nx, rows, Hx, tw);   \
     }
     SC_L_SWITCH(logL, SC_K2IX1)
 #undef SC_K2IX1
@@ -778,7 +778,7 @@ static bool launch3_green_x(int logL, const float* G, float* T, int nx, int rows
     {                                                                               \
         constexpr int P = 256 / F2<LL>::NT;                                         \
         dim3 grid(((rows + 1) / 2 + P - 1) / P, 3);                                 \
-        k3_green_x<LL><<<grid, 256, 0, s>>>(G, T, nx, rows, Hx, gcs, tcs, tw);      \
+        launch_pdl(k3_green_x<LL>, grid, 256, 0, s, G, T, nx, rows, Hx, gcs, tcs, tw);      \
     }
     SC_L_SWITCH(logL, SC_K3GX)
 #undef SC_K3GX
@@ -791,10 +791,10 @@ static bool launch3_green_col(bool img, int logL, const float* in, void* out, in
     dim3 grid((unsigned)(((int64_t)ncols * nbatch + 2 * kColW - 1) / (2 * kColW)), 3);
 #define SC_K3GC(LL)                                                                                           \
     if (img)                                                                                                  \
-        k3_green_col<LL, true><<<grid, kColW * F2<LL>::NT, 0, s>>>(in, out, ncols, nbatch, nh, odd_comp, as_in, \
+        launch_pdl(k3_green_col<LL, true>, grid, kColW * F2<LL>::NT, 0, s, in, out, ncols, nbatch, nh, odd_comp, as_in, \
                                                                    bs_in, cs_in, as_out, bs_out, cs_out, tw);   \
     else                                                                                                      \
-        k3_green_col<LL, false><<<grid, kColW * F2<LL>::NT, 0, s>>>(in, out, ncols, nbatch, nh, odd_comp,      \
+        launch_pdl(k3_green_col<LL, false>, grid, kColW * F2<LL>::NT, 0, s, in, out, ncols, nbatch, nh, odd_comp,      \
                                                                     as_in, bs_in, cs_in, as_out, bs_out, cs_out, tw);
     SC_L_SWITCH(logL, SC_K3GC)
 #undef SC_K3GC
