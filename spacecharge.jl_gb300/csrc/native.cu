@@ -260,6 +260,11 @@ __global__ void __launch_bounds__(256) k_green_compress(const typename Cplx<T>::
     }
 }
 
+// Green x and y passes as one (k3_green_xy) where it applies
+#ifndef SC_FUSED_GREEN_XY
+#define SC_FUSED_GREEN_XY 1
+#endif
+
 // ------------------------------------------- hybrid Green build (FP32 path)
 // One thread per displacement d of the stored region (octant in free space;
 // quadrant x all dz for the image) computes all three components.  Cells
@@ -778,6 +783,17 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
         float* T2 = T1 + 3 * t1max;
         const int64_t t1cs = (int64_t)Hx * ny * zc, t2cs = (int64_t)Hx * Hy * zc;
         const int64_t plane = (int64_t)Hx * Hy;
+        // x and y fused per z slice where the slice fits in shared memory
+        if (SC_FUSED_GREEN_XY &&
+            launch3_green_xy(w.log2L[0], w.log2L[1], (const float*)goct, T2, nx, ny, zc, Hx, gcs, t2cs, tw, s)) {
+            SC_LAUNCH_CHECK("k3_green_xy");
+            if (!launch3_green_col(image, w.log2L[2], T2, image ? w.gimg : w.gfree, (int)plane, 1, nz, 2, plane, 0,
+                                   t2cs, plane, 0, image ? plane * Lz : plane * Hz, tw, s))
+                return fail(SC_ERR_UNSUPPORTED, "Green z pass: transform length out of range");
+            SC_LAUNCH_CHECK("green z pass");
+            m->launches += has_near ? 4 : 3;
+            return SC_OK;
+        }
         if (launch3_green_x(w.log2L[0], (const float*)goct, T1, nx, ny * zc, Hx, gcs, t1cs, tw, s) &&
             launch3_green_col(false, w.log2L[1], T1, T2, Hx, zc, ny, 1, Hx, (int64_t)Hx * ny, t1cs, Hx, plane, t2cs,
                               tw, s) &&

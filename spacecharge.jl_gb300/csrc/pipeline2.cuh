@@ -651,6 +651,125 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(c
     }
 }
 
+// x and y passes of the Green transform fused, one CTA per (stored z slice,
+// component), Lx = Ly = L: the slice's ny rows are transformed along x (two
+// per complex FFT) into shared memory, then its Hx columns along y (two per
+// complex FFT) with the component's y parity, into T2[comp][iz][ky][kx].
+// The x-pass output (k3_green_x's T1) never goes to global memory.
+template <int L>
+__global__ void __launch_bounds__(256, 3) k3_green_xy(const float* __restrict__ G, float* __restrict__ T2, int nx,
+                                                   int ny, int Hx, int64_t gcs, int64_t t2cs,
+                                                   const float2* __restrict__ tw) {
+    using E = F2<L>;
+    constexpr int W = 256 / E::NT;  // row pairs (x pass) or columns (y pass) per round
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float2* xb = reinterpret_cast<float2*>(smraw);        // W exchange columns
+    float* ts = reinterpret_cast<float*>(xb + W * E::S);  // [ny][Hx]: the slice after the x pass
+    const int iz = blockIdx.x, comp = blockIdx.y;
+    float2 v[16];
+    // x pass: rows y0, y1 = y0 + 1 of slice iz; component 0 is odd along x
+    {
+        const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
+        float2* col = xb + p * E::S;
+        const float* gs = G + comp * gcs + (int64_t)nx * ny * iz;
+        for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
+            const int y0 = 2 * (q0 + p), y1 = y0 + 1;
+            const bool ok0 = y0 < ny, ok1 = y1 < ny;
+            const float* g0 = gs + (int64_t)nx * y0;
+            const float* g1 = g0 + nx;
+            if (t < E::R2) {
+#pragma unroll
+                for (int s = 0; s < E::R1; ++s) {
+                    const int x = t + E::R2 * s;
+                    const int dx = x < nx ? x : (x > L - nx ? x - L : L);
+                    float a = 0.f, b = 0.f;
+                    if (dx != L) {
+                        const int ax = dx < 0 ? -dx : dx;
+                        if (ok0) a = __ldg(g0 + ax);
+                        if (ok1) b = __ldg(g1 + ax);
+                        if (comp == 0 && dx < 0) a = -a, b = -b;
+                    }
+                    v[s] = make_float2(a, b);
+                }
+            }
+            E::template fwd<false>(v, col, t, swt);
+            if (t < E::R1) {
+#pragma unroll
+                for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+            }
+            __syncthreads();
+            if (ok0) {
+                for (int k = t; k <= L / 2; k += E::NT) {
+                    float2 xa, xbv;
+                    split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
+                    ts[y0 * Hx + k] = comp == 0 ? xa.y : xa.x;
+                    if (ok1) ts[y1 * Hx + k] = comp == 0 ? xbv.y : xbv.x;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // y pass: columns fa, fb = fa + W of the slice; component 1 is odd along y.
+    // Columns kx < L/2 go through the FFT two per round; the last one
+    // (kx = L/2, which would take a round of its own) by a direct sum.
+    {
+        const int c = threadIdx.x % W, t = threadIdx.x / W;
+        float2* col = xb + c * E::S;
+        const bool odd = comp == 1;
+        float* out = T2 + comp * t2cs + (int64_t)Hx * (L / 2 + 1) * iz;
+        for (int k = threadIdx.x; k <= L / 2; k += blockDim.x) {
+            // X(k) = sum_d x(d) w^(k d), d = -(ny-1)..ny-1, x(-d) = -x(d) when odd
+            float re = 0.f, im = 0.f;
+            for (int d = 0; d < ny; ++d) {
+                const float a = ts[d * Hx + L / 2];
+                const float2 wp = swt[(k * d) & (L - 1)];
+                if (d == 0) {
+                    re += a;
+                } else if (odd) {
+                    im += 2.f * a * wp.y;  // x(d) (w^kd - w^-kd) = 2i x(d) Im w^kd
+                } else {
+                    re += 2.f * a * wp.x;
+                }
+            }
+            out[(int64_t)k * Hx + L / 2] = odd ? im : re;
+        }
+        for (int k0 = 0; k0 < L / 2; k0 += 2 * W) {
+            const int fa = k0 + c, fb = fa + W;
+            const bool oka = fa < L / 2, okb = fb < L / 2;
+            if (t < E::R2) {
+#pragma unroll
+                for (int s = 0; s < E::R1; ++s) {
+                    const int n = t + E::R2 * s;
+                    const int d = n < ny ? n : (n > L - ny ? n - L : L);
+                    float a = 0.f, b = 0.f;
+                    if (d != L) {
+                        const int ad = d < 0 ? -d : d;
+                        if (oka) a = ts[ad * Hx + fa];
+                        if (okb) b = ts[ad * Hx + fb];
+                        if (odd && d < 0) a = -a, b = -b;
+                    }
+                    v[s] = make_float2(a, b);
+                }
+            }
+            E::template fwd<false>(v, col, t, swt);
+            if (t < E::R1) {
+#pragma unroll
+                for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+            }
+            __syncthreads();
+            for (int k = t; k <= L / 2; k += E::NT) {
+                float2 xa, xbv;
+                split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
+                if (oka) out[(int64_t)k * Hx + fa] = odd ? xa.y : xa.x;
+                if (okb) out[(int64_t)k * Hx + fb] = odd ? xbv.y : xbv.x;
+            }
+            __syncthreads();
+        }
+    }
+}
+
 // Launch helpers: run the two-step kernel when L <= 256, report false
 // otherwise (the caller falls back to the Stockham kernels).
 #define SC_L_SWITCH(logL, MACRO) \
@@ -782,6 +901,23 @@ static bool launch3_green_x(int logL, const float* G, float* T, int nx, int rows
     }
     SC_L_SWITCH(logL, SC_K3GX)
 #undef SC_K3GX
+    return true;
+}
+
+// The fused x+y Green pass needs Lx = Ly and the slice in shared memory.
+static bool launch3_green_xy(int logLx, int logLy, const float* G, float* T2, int nx, int ny, int zc, int Hx,
+                             int64_t gcs, int64_t t2cs, const float2* tw, cudaStream_t s) {
+    if (logLx != logLy) return false;
+#define SC_K3XY(LL)                                                                                 \
+    {                                                                                               \
+        constexpr int W = 256 / F2<LL>::NT;                                                         \
+        const size_t smem = sizeof(float2) * (size_t)W * F2<LL>::S + sizeof(float) * (size_t)ny * Hx; \
+        if (smem > 100 * 1024) return false;                                                        \
+        if (set_smem(k3_green_xy<LL>, smem) != SC_OK) return false;                                 \
+        launch_pdl(k3_green_xy<LL>, dim3(zc, 3), 256, smem, s, G, T2, nx, ny, Hx, gcs, t2cs, tw);    \
+    }
+    SC_L_SWITCH(logLx, SC_K3XY)
+#undef SC_K3XY
     return true;
 }
 
