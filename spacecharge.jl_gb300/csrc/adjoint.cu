@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(256) k_adj_zpass(const typename Cplx<T>::T2* _
             r.y -= p.x * g;
             if (gv.image) {
                 const int kzm = (Lz - kz) & (Lz - 1);
-                T2 gc = gic[kx + (int64_t)gv.Hx * gv.Hy * kzm];
+                T2 gc = img_at(gic + kx, (int64_t)gv.Hx * gv.Hy, kzm, gv, comp);
                 if (comp == 1) {
                     gc.x *= ysign;
                     gc.y *= ysign;

@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(256) k_zpass(const typename Cplx<T>::T2* __res
                 const T2 p = spec[it];
                 r = Cplx<T>::make(-p.y * g, p.x * g);  // p * (i g)
                 if (gv.image) {
-                    T2 gc = gic[kx + (int64_t)gv.Hx * gv.Hy * kz];
+                    T2 gc = img_at(gic + kx, (int64_t)gv.Hx * gv.Hy, kz, gv, comp);
                     if (comp == 1) {
                         gc.x *= ysign;
                         gc.y *= ysign;
@@ -698,6 +698,7 @@ static int build_green(sc_mesh* m, bool image, double offz, cudaStream_t s) {
         if (image) {
             cnt = (int64_t)Hx * Hy * Lz;
             dst = (T2*)w.gimg + (comp - 1) * cnt;
+            w.img_half = false;
         } else {
             cnt = (int64_t)Hx * Hy * Hz;
             dst = (T*)w.gfree + (comp - 1) * cnt;
@@ -788,9 +789,10 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
             launch3_green_xy(w.log2L[0], w.log2L[1], (const float*)goct, T2, nx, ny, zc, Hx, gcs, t2cs, tw, s)) {
             SC_LAUNCH_CHECK("k3_green_xy");
             if (!launch3_green_col(image, w.log2L[2], T2, image ? w.gimg : w.gfree, (int)plane, 1, nz, 2, plane, 0,
-                                   t2cs, plane, 0, image ? plane * Lz : plane * Hz, tw, s))
+                                   t2cs, plane, 0, plane * Hz, tw, s))
                 return fail(SC_ERR_UNSUPPORTED, "Green z pass: transform length out of range");
             SC_LAUNCH_CHECK("green z pass");
+            if (image) w.img_half = true;
             m->launches += has_near ? 4 : 3;
             return SC_OK;
         }
@@ -798,8 +800,9 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
             launch3_green_col(false, w.log2L[1], T1, T2, Hx, zc, ny, 1, Hx, (int64_t)Hx * ny, t1cs, Hx, plane, t2cs,
                               tw, s) &&
             launch3_green_col(image, w.log2L[2], T2, image ? w.gimg : w.gfree, (int)plane, 1, nz, 2, plane, 0, t2cs,
-                              plane, 0, image ? plane * Lz : plane * Hz, tw, s)) {
+                              plane, 0, plane * Hz, tw, s)) {
             SC_LAUNCH_CHECK("green two-step");
+            if (image) w.img_half = true;
             m->launches += has_near ? 5 : 4;
             return SC_OK;
         }
@@ -834,6 +837,7 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
         dim3 grid((Hx + W - 1) / W, Hy, 3);
         void* dst = image ? w.gimg : w.gfree;
         const int64_t dcs = image ? (int64_t)Hx * Hy * Lz : (int64_t)Hx * Hy * Hz;
+        if (image) w.img_half = false;
         k_green_z<<<grid, 256, smem, s>>>(S, dst, nz, g.image, Ly, Lz, w.log2L[2], Hx, lgW, scs, dcs, tw);
         SC_LAUNCH_CHECK("k_green_z");
     }

@@ -118,6 +118,7 @@ struct GreenView {
     int Hx, Hy, Hz, Ly, Lz;
     int64_t cs_free, cs_img;
     int image;
+    int img_half;  // image spectrum stored for kz <= Lz/2 only (img_at)
 };
 
 inline GreenView make_green_view(const NativeWork& w, int image) {
@@ -130,9 +131,27 @@ inline GreenView make_green_view(const NativeWork& w, int image) {
     gv.Ly = w.L[1];
     gv.Lz = w.L[2];
     gv.cs_free = (int64_t)w.Hx * gv.Hy * gv.Hz;
-    gv.cs_img = (int64_t)w.Hx * gv.Hy * w.L[2];
+    gv.img_half = w.img_half ? 1 : 0;
+    gv.cs_img = (int64_t)w.Hx * gv.Hy * (w.img_half ? gv.Hz : w.L[2]);
     gv.image = image;
     return gv;
+}
+
+// Image spectrum value at kz from a (kx, folded ky) column `gic` with kz
+// stride `gstep`.  Each stored column is the z transform of a real line
+// times -i^p and the phase of its offset start (p = 1 for components 0 and
+// 1), so S(Lz - kz) = eps conj S(kz) with eps = -1 for components 0 and 1,
+// +1 for component 2: half storage keeps kz <= Lz/2.
+template <typename T2>
+__device__ __forceinline__ T2 img_at(const T2* __restrict__ gic, int64_t gstep, int kz, const GreenView& gv,
+                                     int comp) {
+    if (!gv.img_half || kz <= gv.Lz / 2) return __ldg(gic + gstep * kz);
+    T2 v = __ldg(gic + gstep * (gv.Lz - kz));
+    if (comp < 2)
+        v.x = -v.x;  // -conj
+    else
+        v.y = -v.y;  // conj
+    return v;
 }
 
 template <typename T>

@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(con
                     const float2 X = sc[xsw(kz)];
                     out = make_float2(-X.y * g, X.x * g);  // X * (i g)
                     if (gv.image) {
-                        float2 gc = __ldg(gic + gstep * kz);
+                        float2 gc = img_at(gic, gstep, kz, gv, comp);
                         if (comp == 1) {
                             gc.x *= ysign;
                             gc.y *= ysign;
@@ -441,7 +441,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass
                 acc[r].y -= v[r].x * g;
                 if (gv.image) {
                     const int kzm = (L - kz) & (L - 1);
-                    float2 gc = __ldg(gic + gstep * kzm);
+                    float2 gc = img_at(gic, gstep, kzm, gv, comp);
                     if (comp == 1) {
                         gc.x *= ysign;
                         gc.y *= ysign;
@@ -572,7 +572,8 @@ __global__ void __launch_bounds__(256) k3_green_x(const float* __restrict__ G, f
 // d < nh; with `odd_comp` == comp the extension is odd.  IMG (image z pass):
 // the input holds the full line, d + nh - 1 for d = -(nh-1)..nh-1, and the
 // output is the complex image spectrum -i^p X(kz) e^{-2 pi i kz (nh-1)/L}
-// for all kz (p = 1 for components 0 and 1); otherwise k <= L/2 of the kept
+// for kz <= L/2 (p = 1 for components 0 and 1; img_at gives the other kz
+// from these); otherwise k <= L/2 of the kept
 // real part is stored at out + b*bs_out + col + k*as_out.
 template <int L, bool IMG>
 __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(const float* __restrict__ in, void* __restrict__ out,
@@ -625,27 +626,18 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(c
             if (oka) o[ba * bs_out + ca] = odd ? xa.y : xa.x;
             if (okb) o[bb * bs_out + cb] = odd ? xbv.y : xbv.x;
         } else {
-            // real line: X(L - k) = conj X(k)
-            const int k2 = (L - k) & (L - 1);
+            // the line is real, so X(L - k) = conj X(k): only k <= L/2 is
+            // stored, and img_at rebuilds the rest
             const float2 ph1 = tw[(int)(((int64_t)k * (nh - 1)) & (L - 1)) * (kMaxL / L)];
-            const float2 ph2 = tw[(int)(((int64_t)k2 * (nh - 1)) & (L - 1)) * (kMaxL / L)];
             float2* o = reinterpret_cast<float2*>(out) + comp * cs_out;
             for (int w = 0; w < 2; ++w) {
                 const bool okw = w == 0 ? oka : okb;
                 if (!okw) continue;
                 const float2 x = w == 0 ? xa : xbv;
-                float2 x1 = x, x2 = make_float2(x.x, -x.y);  // X(k), X(L - k)
-                if (comp < 2) {                               // times i
-                    x1 = make_float2(-x1.y, x1.x);
-                    x2 = make_float2(-x2.y, x2.x);
-                }
+                const float2 x1 = comp < 2 ? make_float2(-x.y, x.x) : x;  // times i for components 0 and 1
                 const int64_t base = w == 0 ? (ba * bs_out + ca) : (bb * bs_out + cb);
                 const float2 q1 = cmul(x1, ph1);
                 o[base + k * as_out] = make_float2(-q1.x, -q1.y);
-                if (k2 != k) {
-                    const float2 q2 = cmul(x2, ph2);
-                    o[base + k2 * as_out] = make_float2(-q2.x, -q2.y);
-                }
             }
         }
     }

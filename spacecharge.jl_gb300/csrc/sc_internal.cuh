@@ -151,6 +151,7 @@ struct NativeWork {
     void* gfree = nullptr;      // compressed free-space spectra, 3 comps (T)
     void* gimg = nullptr;       // compressed image spectra, 3 comps (T2)
     GreenKey key_free, key_img;
+    bool img_half = false;  // gimg holds kz <= Lz/2 only (the FP32 two-step build)
     int engine = -1;  // -1: process-wide setting; 0: two-step; 1: Stockham
     int lgW = -1;     // Stockham column tile (log2), -1: default
 };
