@@ -267,6 +267,10 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
@@ -293,6 +297,38 @@ __device__ __forceinline__ void prefetch_green(float* gsm, const GreenView& gv, 
     cp_async_commit();
 }
 
+// Copies one component's half-stored image spectrum for this CTA's kColW
+// columns, gim[kz][column] for kz <= L/2, to shared memory asynchronously
+// (img_half layout; img_smem_at rebuilds kz > L/2).
+template <int L>
+__device__ __forceinline__ void prefetch_img(float2* gim, const GreenView& gv, int comp, int Hx, int Ly) {
+    constexpr int HZ = L / 2 + 1;
+    const int64_t plane = (int64_t)Hx * Ly;
+    const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
+    const int cc = threadIdx.x % kColW;
+    const int ff = blockIdx.x * kColW + cc;
+    if (ff < plane) {
+        const int kyy = ff / Hx, kxx = ff - kyy * Hx;
+        const int kyf = kyy <= Ly / 2 ? kyy : Ly - kyy;
+        const float2* src = reinterpret_cast<const float2*>(gv.gimg) + comp * gv.cs_img + kxx + (int64_t)gv.Hx * kyf;
+        for (int kz = threadIdx.x / kColW; kz < HZ; kz += blockDim.x / kColW)
+            cp_async8(gim + kz * kColW + cc, src + gstep * kz);
+    }
+    cp_async_commit();
+}
+
+// img_at on the shared-memory copy of prefetch_img
+template <int L>
+__device__ __forceinline__ float2 img_smem_at(const float2* gim, int kz, int c, int comp) {
+    if (kz <= L / 2) return gim[kz * kColW + c];
+    float2 v = gim[(L - kz) * kColW + c];
+    if (comp < 2)
+        v.x = -v.x;
+    else
+        v.y = -v.y;
+    return v;
+}
+
 // z pass: forward z transform of rho^(kx, ky, .), products with the three
 // Green spectra (image: rho^ at -kz times the image spectrum), three inverse
 // transforms, z < nz stored.  The tile's free-space Green values (3 x
@@ -310,10 +346,15 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(con
     float2* spec = xb + kColW * E::S;  // natural-order spectrum of this tile's columns
     constexpr int HZ = L / 2 + 1;
     float* gsm = reinterpret_cast<float*>(spec + kColW * E::S);  // [3][HZ][kColW]
+    // image, half-stored: one component's spectrum at a time, [HZ][kColW],
+    // the next one copied in during the current one's inverse transform
+    float2* gim = reinterpret_cast<float2*>(gsm + 3 * HZ * kColW);
+    const bool img_smem = gv.image && gv.img_half;
     // columns are the (kx, ky) plane flattened: f = kx + Hx*ky is contiguous
     const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
     const int64_t plane = (int64_t)Hx * Ly;
     prefetch_green<L>(gsm, gv, Hx, Ly);
+    if (img_smem) prefetch_img<L>(gim, gv, 0, Hx, Ly);
     const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
     const int f = blockIdx.x * kColW + c;
     const bool cok = f < plane;
@@ -339,6 +380,10 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(con
     const int kyf = ky <= Ly / 2 ? ky : Ly - ky;
     const float ysign = ky <= Ly / 2 ? 1.f : -1.f;
     for (int comp = 0; comp < 3; ++comp) {
+        if (img_smem && comp > 0) {
+            cp_async_wait_all();
+            __syncthreads();
+        }
         if (t < E::R1) {
             const float* gfc = gsm + comp * HZ * kColW + c;
             const float2* gic = reinterpret_cast<const float2*>(gv.gimg) + comp * gv.cs_img + kx + gv.Hx * kyf;
@@ -355,7 +400,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(con
                     const float2 X = sc[xsw(kz)];
                     out = make_float2(-X.y * g, X.x * g);  // X * (i g)
                     if (gv.image) {
-                        float2 gc = img_at(gic, gstep, kz, gv, comp);
+                        float2 gc = img_smem ? img_smem_at<L>(gim, kz, c, comp) : img_at(gic, gstep, kz, gv, comp);
                         if (comp == 1) {
                             gc.x *= ysign;
                             gc.y *= ysign;
@@ -365,6 +410,10 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(con
                 }
                 v[r] = out;
             }
+        }
+        if (img_smem && comp < 2) {
+            __syncthreads();  // every thread is done with this component's copy
+            prefetch_img<L>(gim, gv, comp + 1, Hx, Ly);
         }
         E::template inv<true>(v, col, t, swt);
         if (t < E::R2 && cok) {
@@ -845,7 +894,8 @@ static bool launch2_zpass(int logL, const float2* B, float2* C, int Hx, int Ly, 
 #define SC_K2Z(LL)                                                                          \
     {                                                                                       \
         const size_t smem = sizeof(float2) * kColW * F2<LL>::S * 2 +                        \
-                            sizeof(float) * 3 * (LL / 2 + 1) * kColW;                           \
+                            sizeof(float) * 3 * (LL / 2 + 1) * kColW +                          \
+                            (gv.image && gv.img_half ? sizeof(float2) * (LL / 2 + 1) * kColW : 0); \
         if (set_smem(k2_zpass<LL>, smem) != SC_OK) return false;                            \
         const int64_t ncol = (int64_t)Hx * Ly;                                              \
         launch_pdl(k2_zpass<LL>, (unsigned)((ncol + kColW - 1) / kColW), kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz, gv, tw); \
