@@ -132,6 +132,18 @@ int sc_mesh_create_from_particles(const int32_t grid_size[3], const void* x,
 /* Frees the mesh, its fields and its workspace. */
 int sc_mesh_destroy(sc_mesh* mesh);
 
+/* New bounds for an existing mesh, keeping its grid, fields and workspaces
+ * (no counterpart in the reference, whose Mesh3D geometry is set once; a
+ * tracking code there builds a new mesh per step).  The validation and delta
+ * of the manual constructor (src/mesh.jl:233-247).  Cached Green spectra and
+ * captured kick graphs follow the new geometry on the next call. */
+int sc_mesh_set_bounds(sc_mesh* mesh, const double min_bounds[3], const double max_bounds[3]);
+
+/* The same with the particle constructor's bounds for x, y, z (sc_auto_bounds,
+ * src/mesh.jl:122-201).  Synchronises `stream`. */
+int sc_mesh_refit(sc_mesh* mesh, const void* x, const void* y, const void* z, int64_t n, int dtype,
+                  void* stream);
+
 /* Mesh properties (the fields of Mesh3D, src/mesh.jl:19-34). */
 int sc_mesh_get_info(const sc_mesh* mesh, sc_mesh_info* info);
 

@@ -605,6 +605,26 @@ int sc_mesh_create_from_particles(const int32_t grid_size[3], const void* x, con
     return mesh_alloc(grid_size, lo, hi, dl, gamma, total_charge, precision, out);
 }
 
+int sc_mesh_set_bounds(sc_mesh* m, const double min_bounds[3], const double max_bounds[3]) {
+    SC_TRY(check_mesh(m));
+    if (!min_bounds || !max_bounds) return fail(SC_ERR_INVALID, "bounds are NULL");
+    double delta[3];
+    for (int d = 0; d < 3; ++d) {
+        if (!(max_bounds[d] > min_bounds[d]))  // src/mesh.jl:236-238
+            return fail(SC_ERR_INVALID, "max_bounds must be strictly greater than min_bounds for all dimensions.");
+        delta[d] = (max_bounds[d] - min_bounds[d]) / (double)(m->n[d] - 1);  // :247
+    }
+    return mesh_set_geometry(m, min_bounds, max_bounds, delta);
+}
+
+int sc_mesh_refit(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n, int dtype, void* stream) {
+    SC_TRY(check_mesh(m));
+    DeviceGuard g(m->device);
+    double lo[3], hi[3], dl[3];
+    SC_TRY(sc_auto_bounds(m->n, x, y, z, n, dtype, lo, hi, dl, stream));
+    return mesh_set_geometry(m, lo, hi, dl);
+}
+
 int sc_mesh_destroy(sc_mesh* m) {
     if (!m) return SC_OK;
     DeviceGuard g(m->device);

@@ -15,7 +15,7 @@ using CUDA
 import ChainRulesCore
 
 export Mesh3D, deposit!, clear_mesh!, interpolate_field, solve!, kick, kick_host, track!, magnetic_field,
-       set_kick_mode!
+       set_kick_mode!, set_bounds!, refit!
 
 const libsc = normpath(joinpath(@__DIR__, "..", "..", "..", "lib", "libspacecharge_gb300.so"))
 
@@ -116,6 +116,42 @@ function Mesh3D(grid_size::NTuple{3,Int}, min_bounds::NTuple{3,Real}, max_bounds
                 Int32[grid_size...], Float64[min_bounds...], Float64[max_bounds...], Float64(gamma),
                 Float64(total_charge), code, out))
     return _wrap(out[], storage_type(code))
+end
+
+# the mesh's bounds after the library changed them
+function _sync_bounds!(mesh::Mesh3D)
+    info = Ref{MeshInfo}()
+    check(ccall((:sc_mesh_get_info, libsc), Cint, (Ptr{Cvoid}, Ref{MeshInfo}), mesh.ptr, info))
+    mesh.min_bounds = info[].min_bounds
+    mesh.max_bounds = info[].max_bounds
+    mesh.delta = info[].delta
+    return mesh
+end
+
+"""
+    set_bounds!(mesh, min_bounds, max_bounds)
+
+New bounds for `mesh`, keeping its grid, fields and workspaces
+(sc_mesh_set_bounds; the manual constructor's validation and delta,
+src/mesh.jl:233-247).
+"""
+function set_bounds!(mesh::Mesh3D, min_bounds::NTuple{3,Real}, max_bounds::NTuple{3,Real})
+    check(ccall((:sc_mesh_set_bounds, libsc), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}), mesh.ptr,
+                Float64[min_bounds...], Float64[max_bounds...]))
+    return _sync_bounds!(mesh)
+end
+
+"""
+    refit!(mesh, px, py, pz)
+
+The particle constructor's bounds for these particles (sc_mesh_refit,
+src/mesh.jl:122-201).
+"""
+function refit!(mesh::Mesh3D, px::CuArray{P}, py::CuArray{P}, pz::CuArray{P}) where {P<:Union{Float32,Float64}}
+    length(px) == length(py) == length(pz) || error("Particle coordinate arrays must have the same length.")
+    check(ccall((:sc_mesh_refit, libsc), Cint, (Ptr{Cvoid}, CuPtr{P}, CuPtr{P}, CuPtr{P}, Int64, Cint, Ptr{Cvoid}),
+                mesh.ptr, px, py, pz, length(px), dtype_code(P), stream_ptr()))
+    return _sync_bounds!(mesh)
 end
 
 # clear_mesh!(mesh), src/deposition.jl:10-12
@@ -235,6 +271,7 @@ function track!(mesh::Mesh3D, x::CuArray{P}, y::CuArray{P}, z::CuArray{P}, ux::C
                  Cdouble, Cdouble, Cint, Cint, Cint, Ptr{Cvoid}),
                 mesh.ptr, x, y, z, ux, uy, uz, q, length(x), dtype_code(P), Float64(dt), Float64(qm), Cint(steps),
                 Cint(refit), Cint(at_cathode), stream_ptr()))
+    refit && _sync_bounds!(mesh)
     return nothing
 end
 

@@ -81,6 +81,8 @@ SIGNATURES = {
     "sc_mesh_create_from_particles": [_i32p, _vp, _vp, _vp, _i64, _int, C.c_double, C.c_double, _int, _vp,
                                       C.POINTER(_vp)],
     "sc_mesh_destroy": [_vp],
+    "sc_mesh_set_bounds": [_vp, _dp, _dp],
+    "sc_mesh_refit": [_vp, _vp, _vp, _vp, _i64, _int, _vp],
     "sc_mesh_get_info": [_vp, C.POINTER(MeshInfo)],
     "sc_mesh_rho": [_vp, C.POINTER(_vp)],
     "sc_mesh_efield": [_vp, C.POINTER(_vp)],

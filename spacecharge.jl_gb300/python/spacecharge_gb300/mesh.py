@@ -124,6 +124,12 @@ class Mesh3D:
         else:
             raise SpaceChargeError("Mesh3D(grid_size, px, py, pz) or Mesh3D(grid_size, min_bounds, max_bounds)")
         self._h = _Handle(out)
+        self._refresh()
+        self._rho = None
+        self._efield = None
+
+    def _refresh(self) -> None:
+        """Re-read the mesh's properties (after a change of bounds)."""
         info = L.MeshInfo()
         L.call("sc_mesh_get_info", self._h.ptr, C.byref(info))
         self.grid_size = tuple(int(v) for v in info.grid_size)
@@ -135,8 +141,27 @@ class Mesh3D:
         self.fft_shape = tuple(int(v) for v in info.fft_shape)
         self.efield_layout = int(info.efield_layout)
         self.T = np.float32 if info.elem_bytes == 4 else np.float64
-        self._rho = None
-        self._efield = None
+
+    def set_bounds(self, min_bounds, max_bounds) -> None:
+        """New bounds for this mesh, keeping its grid, fields and workspaces
+        (sc_mesh_set_bounds; the manual constructor's validation and delta)."""
+        lo = (C.c_double * 3)(*[float(v) for v in min_bounds])
+        hi = (C.c_double * 3)(*[float(v) for v in max_bounds])
+        L.call("sc_mesh_set_bounds", self._h.ptr, lo, hi)
+        self._refresh()
+
+    def refit(self, particles_x, particles_y, particles_z) -> None:
+        """The particle constructor's bounds for these particles
+        (sc_mesh_refit, src/mesh.jl:122-201)."""
+        lens = [_length(a) for a in (particles_x, particles_y, particles_z)]
+        if min(lens) == 0:
+            raise SpaceChargeError("Particle arrays cannot be empty.")
+        if not (lens[0] == lens[1] == lens[2]):
+            raise SpaceChargeError("Particle coordinate arrays must have the same length.")
+        (x, y, z), dt = _as_device((particles_x, particles_y, particles_z))
+        L.call("sc_mesh_refit", self._h.ptr, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
+               C.c_void_p(z.data_ptr()), lens[0], dt, _stream())
+        self._refresh()
 
     # --- field access (mesh.rho / mesh.efield in the reference) -----------
     @property
@@ -333,6 +358,8 @@ def track(mesh: Mesh3D, x, y, z, ux, uy, uz, q, dt: float, qm: float, steps: int
         raise SpaceChargeError("Particle coordinate and charge arrays must have the same length.")
     L.call("sc_track", mesh.ptr, *[_ptr(t) for t in ts], x.numel(), L.SC_F64 if x.dtype == torch.float64 else L.SC_F32,
            float(dt), float(qm), int(steps), 1 if refit else 0, 1 if at_cathode else 0, _stream())
+    if refit:
+        mesh._refresh()
 
 
 def magnetic_field(mesh: Mesh3D, ex, ey):

@@ -104,3 +104,6 @@ def test_python_host_validation(sc):
 def test_null_mesh(lib):
     assert lib.sc_solve(None, 0, None) == 1
     assert lib.sc_deposit(None, None, None, None, None, 0, 1, 1, 0, None) == 1
+    assert lib.sc_mesh_set_bounds(None, _d3(0, 0, 0), _d3(1, 1, 1)) == 1
+    assert lib.sc_last_error() == b"mesh is NULL"
+    assert lib.sc_mesh_refit(None, None, None, None, 1, 1, None) == 1
