@@ -42,9 +42,17 @@ static int batch_issue(sc_batch* b, const void* const* x, const void* const* y, 
     for (cudaStream_t st : b->streams) SC_CUDA(cudaStreamWaitEvent(st, b->fork, 0));
     const int ns = (int)b->streams.size();
     int st = SC_OK;
-    for (size_t i = 0; i < b->meshes.size() && st == SC_OK; ++i)
-        st = kick_issue(b->meshes[i], x[i], y[i], z[i], q[i], n[i], dtype, at_cathode, ex[i], ey[i], ez[i],
-                        b->streams[i % ns]);
+    for (size_t i = 0; i < b->meshes.size() && st == SC_OK; ++i) {
+        // With other bunches on the other streams, a fused inverse pass that
+        // takes a whole SM per CTA still pays (64 uneven bunches: 7.07 ->
+        // 6.22 ms); alone on the GPU it does not (the 128^3 cathode kick:
+        // 0.712 -> 0.724 ms).
+        sc_mesh* m = b->meshes[i];
+        const size_t cap = m->fused_smem_cap;
+        m->fused_smem_cap = ns > 1 ? 210 * 1024 : cap;
+        st = kick_issue(m, x[i], y[i], z[i], q[i], n[i], dtype, at_cathode, ex[i], ey[i], ez[i], b->streams[i % ns]);
+        m->fused_smem_cap = cap;
+    }
     // join every stream, also after a failed bunch: the caller's stream
     // orders whatever was issued
     for (int k = 0; k < ns; ++k) {

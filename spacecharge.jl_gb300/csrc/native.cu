@@ -978,7 +978,7 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
         StageScope st(m->timer, SC_STAGE_INV_Y, s);
         if (two && SC_FUSED_INV_YX &&
             launch2_inv_yx(w.log2L[0], w.log2L[1], (const float2*)C, (float4*)m->efield, nx, ny, nz, Hx,
-                           (const float2*)tw, s)) {
+                           (const float2*)tw, s, m->fused_smem_cap)) {
             SC_LAUNCH_CHECK("k2_inv_yx");
             m->launches -= 1;  // one launch for the two passes
             return SC_OK;

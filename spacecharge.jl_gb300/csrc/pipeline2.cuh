@@ -858,14 +858,17 @@ static bool launch2_fwd_x(int logL, const float* rho, float2* A, int nx, int row
 }
 
 // The fused inverse y+x pass needs Lx = Ly and the plane in shared memory.
+// `cap`: the largest plane (bytes of shared memory) to fuse; above about
+// 100 KB a CTA has an SM to itself, which pays only when other streams' work
+// fills the rest (batch_issue).
 static bool launch2_inv_yx(int logLx, int logLy, const float2* C, float4* E4, int nx, int ny, int nz, int Hx,
-                           const float2* tw, cudaStream_t s) {
+                           const float2* tw, cudaStream_t s, size_t cap) {
     if (logLx != logLy) return false;
 #define SC_K2YX(LL)                                                                                   \
     {                                                                                                 \
         constexpr int W = 256 / F2<LL>::NT;                                                           \
         const size_t smem = sizeof(float2) * ((size_t)W * F2<LL>::S + (size_t)ny * Hx);               \
-        if (smem > 100 * 1024) return false;                                                          \
+        if (smem > cap) return false;                                                                 \
         if (set_smem(k2_inv_yx<LL>, smem) != SC_OK) return false;                                     \
         launch_pdl(k2_inv_yx<LL>, dim3(nz, 3), 256, smem, s, C, reinterpret_cast<float*>(E4), nx, ny, nz, Hx, tw); \
     }

@@ -228,6 +228,9 @@ struct sc_mesh {
     size_t track_elem = 0;
     int kick_mode = SC_DEPOSIT_ATOMIC;  // deposit mode of sc_kick
     int64_t green_epoch = 0;            // bumped by every Green spectrum build
+    // largest shared-memory plane of the fused inverse y+x pass: 100 KB keeps
+    // two CTAs per SM; batch_issue raises it while other bunches run beside
+    size_t fused_smem_cap = 100 * 1024;
 };
 
 namespace sc {
