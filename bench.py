@@ -452,6 +452,22 @@ def main():
     ms_grad = max_over_ranks(timed(grad_step, args.steps, args.warmup), ws)
     clocks = sampler.stop()
 
+    # ---- tracking (the kick's caller): per step a kick, B from E and a
+    #      relativistic Boris push of the device-resident bunch (sc_track),
+    #      with the bounds refitted to the bunch every step (one extrema
+    #      reduction and host read per step) or held; Green rebuilt as needed
+    nstep = 10
+    state = [t.clone() for t in dev[:3]] + [torch.zeros_like(dev[0]) for _ in range(3)]
+    mt = sc.Mesh3D(GRID, dev[0], dev[1], dev[2], precision="mixed", gamma=GAMMA, total_charge=QTOT)
+
+    def track(refit):
+        return lambda: sc.track(mt, *state, dev[3], dt=1e-13, qm=-1.75882001076e11, steps=nstep, refit=refit)
+
+    track_res = {"steps_per_call": nstep, "workload": WORKLOAD + ", bunch at rest, dt = 0.1 ps",
+                 "ms_per_step_refit": round(max_over_ranks(timed(track(True), 3, 1), ws) / nstep, 4),
+                 "ms_per_step_fixed_bounds": round(max_over_ranks(timed(track(False), 3, 1), ws) / nstep, 4)}
+    del mt, state
+
     # ---- deposit alone in each mode (same particles, mixed mesh)
     dep_ms = {}
     for name, mode in (("atomic", L.SC_DEPOSIT_ATOMIC), ("sorted", L.SC_DEPOSIT_SORTED),
@@ -542,6 +558,7 @@ def main():
         "e2e": {"value": round(ms_e2e, 4), "unit": "ms", "h2d_bytes_per_step": 4 * NP * 8,
                 "d2h_bytes_per_step": 3 * NP * 8},
         "deposit_modes_ms": dep_ms,
+        "track": track_res,
         "cathode_128": cath_res,
         "batch": batch_res,
         "gpu_launches": int(round(launches_per_kick * args.steps)),
