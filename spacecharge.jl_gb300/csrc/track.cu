@@ -8,11 +8,17 @@
 //   u' = u- + u- x t,  u+ = u- + u' x s,  u_new = u+ + a E
 //   x += c dt u_new / gamma(u_new)
 // FP64 meshes push in FP64 throughout.  Mixed meshes keep u and x in the
-// particle type and form the increments (half kicks, rotation, drift) in
-// FP32: each is small next to the value it is added to, so FP32 keeps it to
-// ~1e-7 of itself, and the FP64 adds keep a relativistic u exact to the step.
+// particle type and form the increments (both half kicks with the rotation,
+// and the drift) in FP32: each is small next to the value it is added to, so
+// FP32 keeps it to ~1e-7 of itself, and one FP64 add per coordinate keeps a
+// relativistic u exact to the step.  FP64 arithmetic, conversions included,
+// runs at 1/64 of the FP32 rate on this GPU: the mixed push converts between
+// FP64 and FP32 with integer operations (f64_to_f32, f32_to_f64) and issues
+// only the two FP64 adds per coordinate that the FP64 state needs.
 #include <algorithm>
+#include <type_traits>
 
+#include "cells.cuh"
 #include "sc_internal.cuh"
 
 namespace sc {
@@ -52,27 +58,36 @@ __global__ void __launch_bounds__(256) k_boris_mixed(P* __restrict__ x, P* __res
                                                      float kb, float cdt) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float Ex = (float)ex[i], Ey = (float)ey[i], Ez = (float)ez[i];
+    const float Ex = f64_to_f32(ex[i]), Ey = f64_to_f32(ey[i]), Ez = f64_to_f32(ez[i]);
     const float bx = -kb * Ey, by = kb * Ex;
     const float hx = a * Ex, hy = a * Ey, hz = a * Ez;  // half electric kick
-    const double umx = (double)ux[i] + hx, umy = (double)uy[i] + hy, umz = (double)uz[i] + hz;
-    const float fx = (float)umx, fy = (float)umy, fz = (float)umz;
+    const P ux0 = ux[i], uy0 = uy[i], uz0 = uz[i];
+    const float wx = f64_to_f32(ux0), wy = f64_to_f32(uy0), wz = f64_to_f32(uz0);
+    const float fx = wx + hx, fy = wy + hy, fz = wz + hz;  // u-
     const float tb = qmdt2 / sqrtf(1.0f + fx * fx + fy * fy + fz * fz);
     const float tx = tb * bx, ty = tb * by;
     const float px = fx - fz * ty, py = fy + fz * tx, pz = fz + (fx * ty - fy * tx);  // u'
     const float s = 2.0f / (1.0f + tx * tx + ty * ty);
     const float sx = s * tx, sy = s * ty;
-    // u_new = u- + (u' x s) + a E
-    const double nx = umx + (double)(-pz * sy + hx), ny = umy + (double)(pz * sx + hy),
-                 nz = umz + (double)((px * sy - py * sx) + hz);
-    const float gx = (float)nx, gy = (float)ny, gz = (float)nz;
+    // u_new - u = 2 a E + (u' x s)
+    const float dx = hx + (-pz * sy + hx), dy = hy + (pz * sx + hy), dz = hz + ((px * sy - py * sx) + hz);
+    const float gx = wx + dx, gy = wy + dy, gz = wz + dz;  // u_new to FP32 rounding, for the drift
     const float f = cdt / sqrtf(1.0f + gx * gx + gy * gy + gz * gz);
-    x[i] = (P)((double)x[i] + (double)(f * gx));
-    y[i] = (P)((double)y[i] + (double)(f * gy));
-    z[i] = (P)((double)z[i] + (double)(f * gz));
-    ux[i] = (P)nx;
-    uy[i] = (P)ny;
-    uz[i] = (P)nz;
+    if (std::is_same<P, double>::value) {
+        x[i] = (P)((double)x[i] + f32_to_f64(f * gx));
+        y[i] = (P)((double)y[i] + f32_to_f64(f * gy));
+        z[i] = (P)((double)z[i] + f32_to_f64(f * gz));
+        ux[i] = (P)((double)ux0 + f32_to_f64(dx));
+        uy[i] = (P)((double)uy0 + f32_to_f64(dy));
+        uz[i] = (P)((double)uz0 + f32_to_f64(dz));
+    } else {  // FP32 state: the FP32 add rounds as the FP64 add then FP32 store would
+        x[i] = (P)((float)x[i] + f * gx);
+        y[i] = (P)((float)y[i] + f * gy);
+        z[i] = (P)((float)z[i] + f * gz);
+        ux[i] = (P)((float)ux0 + dx);
+        uy[i] = (P)((float)uy0 + dy);
+        uz[i] = (P)((float)uz0 + dz);
+    }
 }
 
 static int push_launch(sc_mesh* m, void* x, void* y, void* z, void* ux, void* uy, void* uz, const void* ex,
