@@ -40,7 +40,7 @@ extern "C" {
 #define SC_ERR_OOM          3  /* device allocation failed */
 #define SC_ERR_OUT_OF_RANGE 4  /* particles outside the mesh were skipped */
 #define SC_ERR_TIMEOUT      5  /* a bounded device-side wait gave up */
-#define SC_ERR_UNSUPPORTED  6  /* size or option this build does not handle */
+#define SC_ERR_UNSUPPORTED  6  /* size or option the library does not handle */
 
 /* particle / output element types */
 #define SC_F32 0
