@@ -74,11 +74,11 @@ struct Packed<double> {
     using V = dnode4;
 };
 
+// One 32-byte load (sm_100+) of a 32-byte aligned FP64 node, read-only path.
 __device__ __forceinline__ dnode4 ldg4(const dnode4* p) {
-    // two 16-byte loads (sm_100+ also has 32-byte loads; keep it portable)
-    const double2* q = reinterpret_cast<const double2*>(p);
-    const double2 a = __ldg(q), b = __ldg(q + 1);
-    return dnode4{a.x, a.y, b.x, b.y};
+    dnode4 r;
+    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];" : "=d"(r.x), "=d"(r.y), "=d"(r.z), "=d"(r.w) : "l"(p));
+    return r;
 }
 __device__ __forceinline__ float4 ldg4(const float4* p) { return __ldg(p); }
 
