@@ -153,17 +153,41 @@ struct Acc;
 template <typename A>
 struct Acc<A, false> {
     using V = A;
-    __device__ __forceinline__ static V from(A v, double) { return v; }
+    __device__ __forceinline__ static V from(A v, int) { return v; }
     __device__ __forceinline__ static void add(A* rho, long long*, int64_t i, V v) { atomicAdd(rho + i, v); }
 };
+// round(v * 2^k) to nearest, ties to even, for FP32 v with |v| 2^k < 2^62,
+// with integer operations only (the FP64 route costs three instructions on
+// the slow FP64 pipe per corner); equal to __double2ll_rn((double)v * 2^k).
+__device__ __forceinline__ long long f32_to_fixed(float v, int k) {
+    const unsigned u = __float_as_uint(v);
+    const int be = (int)((u >> 23) & 0xFF);
+    const long long m = be ? (long long)((u & 0x7FFFFFu) | 0x800000u) : (long long)(u & 0x7FFFFFu);
+    const int sh = (be ? be : 1) - 150 + k;  // |v| 2^k = m 2^sh
+    long long r;
+    if (sh >= 0) {
+        r = m << sh;  // sh < 38 since m 2^sh < 2^62
+    } else if (sh > -40) {
+        const int s = -sh;
+        r = m >> s;
+        const long long rem = m & ((1LL << s) - 1), half = 1LL << (s - 1);
+        if (rem > half || (rem == half && (r & 1))) r += 1;
+    } else {
+        r = 0;  // m < 2^24: below half a unit
+    }
+    return (u >> 31) ? -r : r;
+}
+
 template <typename A>
 struct Acc<A, true> {
     using V = long long;
-    __device__ __forceinline__ static V from(A v, double scale) { return __double2ll_rn((double)v * scale); }
+    __device__ __forceinline__ static V from(A v, int k) { return __double2ll_rn(ldexp((double)v, k)); }
     __device__ __forceinline__ static void add(A*, long long* fx, int64_t i, V v) {
         atomicAdd(reinterpret_cast<unsigned long long*>(fx + i), (unsigned long long)v);
     }
 };
+template <>
+__device__ __forceinline__ long long Acc<float, true>::from(float v, int k) { return f32_to_fixed(v, k); }
 
 // fixed-point exponent: sum|q| * 2^k lies in [2^61, 2^62)
 __device__ __forceinline__ int fixed_exponent(double qsum) { return qsum > 0 ? 61 - ilogb(qsum) : 0; }
@@ -177,7 +201,7 @@ __global__ void __launch_bounds__(256) k_dep_seg(const int* __restrict__ skey, c
     // particles skipped as out of range are not in the sorted array: it is
     // dense in [0, offset[N-1] + count[N-1])
     const int64_t nsorted = (int64_t)*last_off + *last_cnt;
-    const double scale = DET ? ldexp(1.0, fixed_exponent(*qsum)) : 0.0;
+    const int scale = DET ? fixed_exponent(*qsum) : 0;  // the fixed-point exponent k
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const bool in = i < nsorted;
@@ -219,7 +243,13 @@ __global__ void __launch_bounds__(256) k_dep_seg(const int* __restrict__ skey, c
     for (int j = 0; j < 8; ++j) Acc<A, DET>::add(rho, fixed, k + off[j], c[j]);
 }
 
-// sum |q| in FP64 (the fixed-point scale of the deterministic deposit)
+// sum |q| in FP64 (the fixed-point scale of the deterministic deposit), in
+// a fixed order: each block's partial to out[1 + block], then k_abs_final
+// adds the partials in block order into out[0].  A floating-point atomic
+// here would make the sum, and with it the exponent near a power of two,
+// depend on the block order.
+constexpr int kAbsBlocks = 2 * 152;
+
 template <typename P>
 __global__ void __launch_bounds__(256) k_abs_sum(const P* __restrict__ q, int64_t n, double* __restrict__ out) {
     double s = 0;
@@ -232,8 +262,15 @@ __global__ void __launch_bounds__(256) k_abs_sum(const P* __restrict__ q, int64_
     if (threadIdx.x == 0) {
         double t = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
-        atomicAdd(out, t);
+        out[1 + blockIdx.x] = t;
     }
+}
+
+__global__ void k_abs_final(double* __restrict__ out, int nblocks) {
+    if (threadIdx.x != 0) return;
+    double t = 0;
+    for (int b = 0; b < nblocks; ++b) t += out[1 + b];
+    out[0] = t;
 }
 
 // fixed point -> rho (adds to the existing rho, which `clear` has zeroed or
@@ -281,7 +318,7 @@ static int sorted_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q, 
         SC_CUDA(dev_realloc(&w->offset, sizeof(int) * N));
         SC_CUDA(dev_realloc(&w->sums, sizeof(int) * nb));
         SC_CUDA(dev_realloc(&w->fixed, sizeof(long long) * N));
-        SC_CUDA(dev_realloc(&w->qsum, sizeof(double)));
+        SC_CUDA(dev_realloc(&w->qsum, sizeof(double) * (1 + kAbsBlocks)));
         w->cap_N = N;
     }
     const Axes ax = make_axes(m);
@@ -308,16 +345,17 @@ static int sorted_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q, 
         m->launches += 6;
         return SC_OK;
     }
-    SC_CUDA(cudaMemsetAsync(w->qsum, 0, sizeof(double), s));
-    k_abs_sum<P><<<2 * 152, 256, 0, s>>>(q, n, w->qsum);
+    k_abs_sum<P><<<kAbsBlocks, 256, 0, s>>>(q, n, w->qsum);
     SC_LAUNCH_CHECK("k_abs_sum");
+    k_abs_final<<<1, 32, 0, s>>>(w->qsum, kAbsBlocks);
+    SC_LAUNCH_CHECK("k_abs_final");
     SC_CUDA(cudaMemsetAsync(w->fixed, 0, sizeof(long long) * N, s));
     k_dep_seg<A, true><<<blocks, 256, 0, s>>>(w->skey, (const Pack4<A>*)w->sdat, last_off, last_cnt, m->n[0], m->n[1],
                                                (A*)m->rho, w->fixed, w->qsum);
     SC_LAUNCH_CHECK("k_dep_seg");
     k_fixed_to_rho<A><<<(N + 255) / 256, 256, 0, s>>>(w->fixed, w->qsum, (A*)m->rho, N);
     SC_LAUNCH_CHECK("k_fixed_to_rho");
-    m->launches += 8;
+    m->launches += 9;
     return SC_OK;
 }
 
