@@ -1,38 +1,71 @@
 // extrema(particles_x/y/z) for the particle-bounds Mesh3D constructor
 // (src/mesh.jl:147-149): one device reduction, then a 48-byte copy to the
 // host (CUDA.jl's `extrema` on CuArrays does the same round trip).
-#include <float.h>
-
 #include <mutex>
 
+#include "cells.cuh"
 #include "sc_internal.cuh"
 
 namespace sc {
 
+// FP64 min/max run on the slow FP64 pipe (1/64 of the FP32 rate here): the
+// reduction compares order keys instead, 64-bit integers that sort as the
+// doubles do (-0 just below +0).  A NaN (either sign) lands beyond +-inf, so
+// any NaN makes the maximum or the minimum non-finite, which the host check
+// rejects, as the explicit NaN flag of an FP64 reduction would.
+__device__ __forceinline__ unsigned long long order_key(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double from_order_key(unsigned long long k) {
+    const unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+    return __longlong_as_double((long long)b);
+}
+__device__ __forceinline__ double widen(double v) { return v; }
+__device__ __forceinline__ double widen(float v) { return f32_to_f64(v); }
+
 template <typename P>
 __global__ void __launch_bounds__(256) minmax_partials(const P* __restrict__ x, const P* __restrict__ y,
                                                        const P* __restrict__ z, int64_t n,
-                                                       double* __restrict__ partials) {
-    double mn[3] = {DBL_MAX, DBL_MAX, DBL_MAX};
-    double mx[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
-    // NaN is carried as "not finite" by the host check; fmin/fmax skip it,
-    // so flag it explicitly through +inf.
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double v[3] = {(double)x[i], (double)y[i], (double)z[i]};
+                                                       unsigned long long* __restrict__ partials) {
+    unsigned long long mn[3] = {~0ull, ~0ull, ~0ull};
+    unsigned long long mx[3] = {0ull, 0ull, 0ull};
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    // four elements per coordinate in flight per thread: the loop is bound by
+    // load latency, not by the integer compares
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        P v[3][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            v[0][u] = __ldg(x + i + u * stride);
+            v[1][u] = __ldg(y + i + u * stride);
+            v[2][u] = __ldg(z + i + u * stride);
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const unsigned long long k = order_key(widen(v[d][u]));
+                mn[d] = min(mn[d], k);
+                mx[d] = max(mx[d], k);
+            }
+    }
+    for (; i < n; i += stride) {
+        const unsigned long long k[3] = {order_key(widen(x[i])), order_key(widen(y[i])), order_key(widen(z[i]))};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const double a = v[d] == v[d] ? v[d] : __longlong_as_double(0x7ff0000000000000LL);
-            mn[d] = fmin(mn[d], a);
-            mx[d] = fmax(mx[d], a);
+            mn[d] = min(mn[d], k[d]);
+            mx[d] = max(mx[d], k[d]);
         }
     }
-    __shared__ double red[6][8];
+    __shared__ unsigned long long red[6][8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         for (int o = 16; o > 0; o >>= 1) {
-            mn[d] = fmin(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
-            mx[d] = fmax(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+            mn[d] = min(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+            mx[d] = max(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
         }
         if (lane == 0) {
             red[d][warp] = mn[d];
@@ -42,18 +75,24 @@ __global__ void __launch_bounds__(256) minmax_partials(const P* __restrict__ x, 
     __syncthreads();
     if (threadIdx.x < 6) {
         const int k = threadIdx.x;
-        double r = red[k][0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = k < 3 ? fmin(r, red[k][w]) : fmax(r, red[k][w]);
+        unsigned long long r = red[k][0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = k < 3 ? min(r, red[k][w]) : max(r, red[k][w]);
         partials[blockIdx.x * 6 + k] = r;
     }
 }
 
-__global__ void minmax_final(const double* __restrict__ partials, int nblocks, double* __restrict__ out) {
-    const int k = threadIdx.x;
-    if (k >= 6) return;
-    double r = partials[k];
-    for (int b = 1; b < nblocks; ++b) r = k < 3 ? fmin(r, partials[b * 6 + k]) : fmax(r, partials[b * 6 + k]);
-    out[k] = r;
+// One warp per extremum (6 warps): each lane reduces a stride of the block
+// partials, then the warp reduces its lanes.
+__global__ void __launch_bounds__(192) minmax_final(const unsigned long long* __restrict__ partials, int nblocks,
+                                                    double* __restrict__ out) {
+    const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned long long r = k < 3 ? ~0ull : 0ull;
+    for (int b = lane; b < nblocks; b += 32) r = k < 3 ? min(r, partials[b * 6 + k]) : max(r, partials[b * 6 + k]);
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long v = __shfl_xor_sync(0xffffffffu, r, o);
+        r = k < 3 ? min(r, v) : max(r, v);
+    }
+    if (lane == 0) out[k] = from_order_key(r);
 }
 
 int bounds_reduce(const void* x, const void* y, const void* z, int64_t n, int dtype, double mins[3],
@@ -69,13 +108,13 @@ int bounds_reduce(const void* x, const void* y, const void* z, int64_t n, int dt
     if (blocks < 1) blocks = 1;
     if (dtype == SC_F64)
         minmax_partials<double><<<blocks, 256, 0, s>>>((const double*)x, (const double*)y, (const double*)z, n,
-                                                      ctx->partials);
+                                                      reinterpret_cast<unsigned long long*>(ctx->partials));
     else
         minmax_partials<float><<<blocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z, n,
-                                                     ctx->partials);
+                                                     reinterpret_cast<unsigned long long*>(ctx->partials));
     SC_LAUNCH_CHECK("minmax_partials");
     double* out = ctx->partials + 6 * ctx->partial_blocks;
-    minmax_final<<<1, 32, 0, s>>>(ctx->partials, blocks, out);
+    minmax_final<<<1, 192, 0, s>>>(reinterpret_cast<const unsigned long long*>(ctx->partials), blocks, out);
     SC_LAUNCH_CHECK("minmax_final");
     double h[6];
     SC_CUDA(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, s));

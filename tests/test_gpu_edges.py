@@ -126,3 +126,28 @@ def test_kick_gather_copy_matches_interpolate_field(sc, cuda, grid):
     host = sc.kick_host(m, *[t.cpu() for t in dev], q.cpu())
     want = [t.cpu() for t in sc.interpolate_field(m, *dev)]
     assert all(torch.equal(a, b) for a, b in zip(host, want))
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_auto_bounds_extrema_and_non_finite(sc, cuda, dtype):
+    """The particle constructor's extrema (an integer order-key reduction on
+    the device) equal numpy's, across signs and -0.0, and a NaN of either
+    sign or an infinity is rejected, as the reference's bounds would be
+    unusable."""
+    import torch
+
+    rng = np.random.default_rng(17)
+    n = 300_001
+    pts = [(rng.standard_normal(n) * s + o).astype(dtype) for s, o in ((1e-3, -2e-3), (5.0, 0.0), (1e-9, 1e-9))]
+    pts[1][7] = -0.0
+    m = sc.Mesh3D((8, 8, 8), *pts, precision="mixed")
+    ref = sc.Mesh3D((8, 8, 8), *[torch.from_numpy(p).cuda() for p in pts], precision="mixed")
+    assert (m.min_bounds, m.max_bounds) == (ref.min_bounds, ref.max_bounds)
+    om = O.mesh_auto((8, 8, 8), *pts)  # numpy extrema, the reference's FP64 padding
+    assert m.min_bounds == tuple(om.min_bounds) and m.max_bounds == tuple(om.max_bounds)
+    assert m.delta == tuple(om.delta)
+    for bad in (np.nan, -np.nan, np.inf, -np.inf):
+        q = [p.copy() for p in pts]
+        q[1][n // 2] = bad
+        with pytest.raises(sc.SpaceChargeError, match="finite"):
+            sc.Mesh3D((8, 8, 8), *q, precision="mixed")
