@@ -32,6 +32,8 @@ struct ACell<float> {
     }
     template <typename P>
     __device__ __forceinline__ static float cvt(P v) { return f64_to_f32(v); }
+    // 1/delta in FP32 (precomputed: no FP64 conversion per thread)
+    __device__ __forceinline__ static float inv(const AxisP& a) { return a.invf; }
 };
 template <>
 struct ACell<double> {
@@ -41,6 +43,7 @@ struct ACell<double> {
     }
     template <typename P>
     __device__ __forceinline__ static double cvt(P v) { return (double)v; }
+    __device__ __forceinline__ static double inv(const AxisP& a) { return a.inv; }
 };
 
 template <typename T>
@@ -278,9 +281,9 @@ __global__ void __launch_bounds__(256) k_adj_particles(const P* __restrict__ px,
         gzs += (c0 ? T(1) : T(-1)) * wx[a0] * wy[b0] * S;
     }
     dq[p] = out_cast<P, T>(sq);
-    dx[p] = out_cast<P, T>(gxs * (T)ax.a[0].inv);
-    dy[p] = out_cast<P, T>(gys * (T)ax.a[1].inv);
-    dz[p] = out_cast<P, T>(gzs * (T)ax.a[2].inv);
+    dx[p] = out_cast<P, T>(gxs * ACell<T>::inv(ax.a[0]));
+    dy[p] = out_cast<P, T>(gys * ACell<T>::inv(ax.a[1]));
+    dz[p] = out_cast<P, T>(gzs * ACell<T>::inv(ax.a[2]));
 }
 
 template <typename P, typename T>
