@@ -266,11 +266,14 @@ __global__ void __launch_bounds__(256) k_abs_sum(const P* __restrict__ q, int64_
     }
 }
 
+// One warp: lane l adds partials l, l + 32, ... in order, then a fixed
+// butterfly combines the lanes, so the order never depends on scheduling.
 __global__ void k_abs_final(double* __restrict__ out, int nblocks) {
-    if (threadIdx.x != 0) return;
+    const int lane = threadIdx.x & 31;
     double t = 0;
-    for (int b = 0; b < nblocks; ++b) t += out[1 + b];
-    out[0] = t;
+    for (int b = lane; b < nblocks; b += 32) t += out[1 + b];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) out[0] = t;
 }
 
 // fixed point -> rho (adds to the existing rho, which `clear` has zeroed or
