@@ -294,16 +294,19 @@ int kick_issue(sc_mesh* m, const void* x, const void* y, const void* z, const vo
 
 // ------------------------------------------------------------ kick graph
 // A repeated sc_kick with the same arguments and mesh state replays a CUDA
-// graph of the kick instead of issuing its ~15 launches from the host.  The
-// first call with new arguments runs eagerly (it also allocates workspaces and
-// builds cached Green spectra) and then captures the same work; the graph is
-// launched on the caller's stream.
+// graph of the kick instead of issuing its ~15 launches from the host.  A call
+// with new arguments runs eagerly (it also allocates workspaces and builds
+// cached Green spectra); when the next call brings the same arguments back, it
+// runs eagerly again and captures the same work, and later calls replay the
+// graph on the caller's stream.  A caller that passes new arrays every call
+// (allocating its outputs, say) never pays for a capture.
 struct KickGraph {
     cudaStream_t cap = nullptr;  // capture origin (the caller's stream may be the legacy stream)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::vector<int64_t> key;
-    int64_t launches = 0;  // kernels one replay runs
+    std::vector<int64_t> seen;  // arguments of the last eager call (kick_key without epoch and generation)
+    int64_t launches = 0;       // kernels one replay runs
 };
 
 void mesh_state_key(const sc_mesh* m, std::vector<int64_t>& k) {
@@ -808,6 +811,13 @@ int sc_kick(sc_mesh* m, const void* x, const void* y, const void* z, const void*
     if (!kg) {
         kg = new KickGraph();
         m->kickgraph = kg;
+    }
+    // the Green epoch and the allocation generation close mesh_state_key: an
+    // eager kick may move them, the arguments it was called with stay
+    key.resize(key.size() - 2);
+    if (key != kg->seen) {
+        kg->seen = std::move(key);
+        return SC_OK;
     }
     return kick_graph_capture(m, kg, p, n, dtype, at_cathode);
 }

@@ -14,7 +14,7 @@ module SpaceChargeGB300
 using CUDA
 import ChainRulesCore
 
-export Mesh3D, deposit!, clear_mesh!, interpolate_field, solve!, kick, kick_host, track!, magnetic_field,
+export Mesh3D, deposit!, clear_mesh!, interpolate_field, solve!, kick, kick!, kick_host, track!, magnetic_field,
        set_kick_mode!, set_bounds!, refit!
 
 const libsc = normpath(joinpath(@__DIR__, "..", "..", "..", "lib", "libspacecharge_gb300.so"))
@@ -213,6 +213,20 @@ d(loss)/d(px, py, pz, pq) with the mesh geometry held fixed.
 function kick(mesh::Mesh3D, px::CuArray{P}, py::CuArray{P}, pz::CuArray{P}, pq::CuArray{P};
               at_cathode::Bool=false) where {P<:Union{Float32,Float64}}
     Ex = similar(px); Ey = similar(px); Ez = similar(px)
+    return kick!(Ex, Ey, Ez, mesh, px, py, pz, pq; at_cathode=at_cathode)
+end
+
+"""
+    kick!(Ex, Ey, Ez, mesh, px, py, pz, pq; at_cathode=false) -> (Ex, Ey, Ez)
+
+`kick` into caller-owned field arrays.  Repeated calls with the same arrays
+replay a CUDA graph of the kick (sc_kick), which `kick`'s fresh outputs
+rule out.
+"""
+function kick!(Ex::CuArray{P}, Ey::CuArray{P}, Ez::CuArray{P}, mesh::Mesh3D, px::CuArray{P}, py::CuArray{P},
+               pz::CuArray{P}, pq::CuArray{P}; at_cathode::Bool=false) where {P<:Union{Float32,Float64}}
+    length(px) == length(py) == length(pz) == length(pq) == length(Ex) == length(Ey) == length(Ez) ||
+        error("Particle coordinate and charge arrays must have the same length.")
     check(ccall((:sc_kick, libsc), Cint,
                 (Ptr{Cvoid}, CuPtr{P}, CuPtr{P}, CuPtr{P}, CuPtr{P}, Int64, Cint, Cint, CuPtr{P}, CuPtr{P},
                  CuPtr{P}, Ptr{Cvoid}),

@@ -291,16 +291,27 @@ def interpolate_field(mesh: Mesh3D, particles_x, particles_y, particles_z):
     return _return_like(particles_x, (ex, ey, ez))
 
 
-def kick(mesh: Mesh3D, particles_x, particles_y, particles_z, particles_q, at_cathode: bool = False):
-    """deposit! -> solve! -> interpolate_field in one library call."""
+def kick(mesh: Mesh3D, particles_x, particles_y, particles_z, particles_q, at_cathode: bool = False, out=None):
+    """deposit! -> solve! -> interpolate_field in one library call.  `out`:
+    three contiguous CUDA tensors of the particle dtype to write the field
+    into (repeated calls with the same particle tensors and `out` replay a
+    captured CUDA graph)."""
     lens = [_length(a) for a in (particles_x, particles_y, particles_z, particles_q)]
     if not (lens[0] == lens[1] == lens[2] == lens[3]):
         raise SpaceChargeError("Particle coordinate and charge arrays must have the same length.")
     (x, y, z, q), dt = _as_device((particles_x, particles_y, particles_z, particles_q))
-    ex, ey, ez = _similar_out(particles_x, (x, y, z))
+    if out is not None:
+        ex, ey, ez = out
+        for t in out:
+            if not (_is_device_tensor(t) and t.is_contiguous() and t.dtype == x.dtype and t.numel() == lens[0]):
+                raise SpaceChargeError("out must be three contiguous CUDA tensors of the particle dtype and count")
+    else:
+        ex, ey, ez = _similar_out(particles_x, (x, y, z))
     L.call("sc_kick", mesh.ptr, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), C.c_void_p(z.data_ptr()),
            C.c_void_p(q.data_ptr()), lens[0], dt, 1 if at_cathode else 0, C.c_void_p(ex.data_ptr()),
            C.c_void_p(ey.data_ptr()), C.c_void_p(ez.data_ptr()), _stream())
+    if out is not None:
+        return tuple(out)
     return _return_like(particles_x, (ex, ey, ez))
 
 

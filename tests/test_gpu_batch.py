@@ -112,7 +112,7 @@ def test_kick_graph_replay_matches_eager(sc, cuda, cache):
 
     n0 = m.launch_count()
     for step in range(4):
-        kick()  # eager + capture on the first call, replays after
+        kick()  # eager, then eager + capture, then replays
         e = sc.kick(ref, *dev)
         for a, b in zip(out, e):
             assert rel(a.cpu().numpy(), b.cpu().numpy()) < 1e-5
