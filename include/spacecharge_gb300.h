@@ -23,6 +23,9 @@
  *    efield is (nx,ny,nz,3) component-planar for SC_PREC_PLAIN64 meshes and
  *    packed (4,nx,ny,nz) = (Ex,Ey,Ez,0) per node for the hand-written
  *    pipelines (sc_mesh_info.efield_layout says which).
+ *  - Threads: different meshes (and batches) may be used from different
+ *    host threads at once; one mesh is used by one thread at a time, as a
+ *    Julia Mesh3D is (its fields and workspace are mutated in place).
  */
 #ifndef SPACECHARGE_GB300_H
 #define SPACECHARGE_GB300_H
