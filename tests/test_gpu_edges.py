@@ -176,3 +176,45 @@ def test_kick_out_argument_replays(sc, cuda):
         dev[1].mul_(1.02)
     with pytest.raises(sc.SpaceChargeError, match="out must be"):
         sc.kick(m, *dev, q, out=[t.float() for t in out])
+
+
+def test_meshes_kicked_from_two_host_threads(sc, cuda):
+    """Different meshes kicked concurrently from two host threads, each on
+    its own stream (graph captures are thread-local), give the results of
+    kicking them one after the other."""
+    import threading
+
+    import torch
+
+    rng = np.random.default_rng(23)
+    n = 100_000
+    bunches = []
+    for k in range(2):
+        dev = [torch.from_numpy(v).cuda() for v in rng.standard_normal((3, n)) * (1e-3 * (k + 1))]
+        dev.append(torch.full((n,), 1e-9 / n, dtype=torch.float64, device="cuda"))
+        bunches.append(dev)
+    meshes = [sc.Mesh3D((32, 32, 32), b[0], b[1], b[2], precision="mixed") for b in bunches]
+    for m in meshes:
+        m.set_kick_mode("deterministic")
+    want = [[t.clone() for t in sc.kick(m, *b)] for m, b in zip(meshes, bunches)]
+    outs = [[torch.empty_like(b[0]) for _ in range(3)] for b in bunches]
+    errors = []
+
+    def work(k):
+        try:
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                for _ in range(5):  # eager, capture, replays
+                    sc.kick(meshes[k], *bunches[k], out=outs[k])
+            s.synchronize()
+        except Exception as e:  # reported below
+            errors.append(e)
+
+    th = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    assert not errors, errors
+    for got, ref in zip(outs, want):
+        assert all(torch.equal(a, b) for a, b in zip(got, ref))
