@@ -302,6 +302,22 @@ function magnetic_field(mesh::Mesh3D, Ex::CuArray{P}, Ey::CuArray{P}) where {P<:
     return Bx, By
 end
 
+# Host arrays (where the reference would run on its CPU backend): the
+# particles are copied to the device, the work runs there, and field outputs
+# come back as host arrays.
+Mesh3D(grid_size::NTuple{3,Int}, px::Vector{P}, py::Vector{P}, pz::Vector{P};
+       kw...) where {P<:Union{Float32,Float64}} = Mesh3D(grid_size, CuArray(px), CuArray(py), CuArray(pz); kw...)
+
+deposit!(mesh::Mesh3D, px::Vector{P}, py::Vector{P}, pz::Vector{P}, pq::Vector{P};
+         kw...) where {P<:Union{Float32,Float64}} =
+    deposit!(mesh, CuArray(px), CuArray(py), CuArray(pz), CuArray(pq); kw...)
+
+interpolate_field(mesh::Mesh3D, px::Vector{P}, py::Vector{P}, pz::Vector{P}) where {P<:Union{Float32,Float64}} =
+    map(Array, interpolate_field(mesh, CuArray(px), CuArray(py), CuArray(pz)))
+
+kick(mesh::Mesh3D, px::Vector{P}, py::Vector{P}, pz::Vector{P}, pq::Vector{P};
+     at_cathode::Bool=false) where {P<:Union{Float32,Float64}} = kick_host(mesh, px, py, pz, pq; at_cathode=at_cathode)
+
 function Base.show(io::IO, mesh::Mesh3D{T}) where {T}  # src/mesh.jl:267-273
     nx, ny, nz = mesh.grid_size
     lo, hi = mesh.min_bounds, mesh.max_bounds
