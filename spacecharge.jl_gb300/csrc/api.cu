@@ -401,8 +401,11 @@ int mesh_set_geometry(sc_mesh* m, const double lo[3], const double hi[3], const 
 // device staging buffers in chunks on an H2D copy stream and each chunk is
 // deposited as soon as it has arrived; after the solve, each chunk is
 // gathered and copied back on a D2H copy stream while the next is gathered.
-// The Green build runs on the side stream from the start.
-constexpr int kHostChunks = 4;
+// The Green build runs on the side stream from the start.  Two chunks: each
+// chunk costs seven copies and their events, and with 1M FP64 particles the
+// kick took 0.401 ms with 2 chunks, 0.431 with 3, 0.421 with 4 and 0.489
+// with 8.
+constexpr int kHostChunks = 2;
 
 struct HostPipe {
     void* stage = nullptr;  // x, y, z, q, ex, ey, ez, each cap particles
