@@ -468,6 +468,31 @@ static int host_pipe(sc_mesh* m, int64_t n, size_t elem, HostPipe** out) {
     return SC_OK;
 }
 
+// Chunk boundaries of the two halves of the host kick, in multiples of 256
+// particles.  The H2D side and the D2H side split the particles
+// independently.  The deposit runs about three times faster than the H2D
+// link and the gather about four times faster than the D2H link, so the last
+// H2D chunk is small (its deposit is the only one not hidden under a copy)
+// and so is the first gather chunk (the D2H waits for it).  With 1M FP64
+// particles the kick took 0.400 ms with halves on both sides, 0.390 with
+// 75/25 in and 25/75 out and 0.387 with 65/35 in and 15/85 out.
+constexpr double kHostFirstIn = 0.65, kHostFirstOut = 0.15;
+
+static void host_splits(int64_t n, int K, int64_t* cin, int64_t* cout) {
+    const double fin = K == 2 ? kHostFirstIn : 1.0 / K, fout = K == 2 ? kHostFirstOut : 1.0 / K;
+    auto fill = [&](int64_t* c, double first) {
+        c[0] = 0;
+        for (int k = 1; k < K; ++k) {
+            const double f = first + (1.0 - first) * (k - 1) / std::max(1, K - 1);
+            c[k] = std::min<int64_t>(n, ((int64_t)(f * (double)n) + 255) / 256 * 256);
+            c[k] = std::max(c[k], c[k - 1]);
+        }
+        c[K] = n;
+    };
+    fill(cin, fin);
+    fill(cout, fout);
+}
+
 static int kick_host_run(sc_mesh* m, HostPipe* hp, const void* const* hin, int64_t n, int dtype, int at_cathode,
                          void* const* hout, cudaStream_t s) {
     const size_t elem = dtype == SC_F64 ? 8 : 4;
@@ -477,7 +502,8 @@ static int kick_host_run(sc_mesh* m, HostPipe* hp, const void* const* hin, int64
     const int mode = m->precision == SC_PREC_PLAIN64 ? SC_DEPOSIT_ATOMIC : m->kick_mode;
     const bool chunked = deposit_chunkable(m, mode);
     const int K = chunked ? (int)std::min<int64_t>(kHostChunks, std::max<int64_t>(1, n / 65536)) : 1;
-    const int64_t per = (n + K - 1) / K;
+    int64_t cin[kHostChunks + 1], cout[kHostChunks + 1];
+    host_splits(n, K, cin, cout);
     SC_CUDA(cudaEventRecord(hp->fork, s));
     SC_CUDA(cudaStreamWaitEvent(hp->h2d, hp->fork, 0));
     SC_CUDA(cudaStreamWaitEvent(hp->d2h, hp->fork, 0));
@@ -499,8 +525,8 @@ static int kick_host_run(sc_mesh* m, HostPipe* hp, const void* const* hin, int64
             StageScope sd(m->timer, SC_STAGE_DEPOSIT, s);
             SC_TRY(deposit_chunk_begin(m, mode, s));
             for (int c = 0; c < K; ++c) {
-                const int64_t off = c * per, cnt = std::min<int64_t>(per, n - off);
-                if (cnt <= 0) break;
+                const int64_t off = cin[c], cnt = cin[c + 1] - cin[c];
+                if (cnt <= 0) continue;
                 for (int i = 0; i < 4; ++i)
                     SC_CUDA(cudaMemcpyAsync(d[i] + off * elem, (const char*)hin[i] + off * elem, elem * (size_t)cnt,
                                             cudaMemcpyHostToDevice, hp->h2d));
@@ -517,8 +543,8 @@ static int kick_host_run(sc_mesh* m, HostPipe* hp, const void* const* hin, int64
             SC_TRY(native_solve(m, at_cathode, s, ready));
         StageScope sg(m->timer, SC_STAGE_GATHER, s);
         for (int c = 0; c < K; ++c) {
-            const int64_t off = c * per, cnt = std::min<int64_t>(per, n - off);
-            if (cnt <= 0) break;
+            const int64_t off = cout[c], cnt = cout[c + 1] - cout[c];
+            if (cnt <= 0) continue;
             SC_TRY(gather_launch(m, d[0] + off * elem, d[1] + off * elem, d[2] + off * elem, cnt, dtype,
                                  d[4] + off * elem, d[5] + off * elem, d[6] + off * elem, s));
             SC_CUDA(cudaEventRecord(hp->out[c], s));
