@@ -93,6 +93,8 @@ static int device_ctx_init(DeviceCtx* c, int dev) {
     SC_CUDA(cudaMemcpy(c->tw64, t64.data(), sizeof(double2) * kMaxL, cudaMemcpyHostToDevice));
     c->partial_blocks = 2 * c->sm_count;
     SC_CUDA(dev_alloc(&c->partials, sizeof(double) * 6 * (c->partial_blocks + 1)));
+    SC_CUDA(cudaHostAlloc((void**)&c->ext_host, sizeof(double) * 8, cudaHostAllocMapped));
+    SC_CUDA(cudaHostGetDevicePointer((void**)&c->ext_dev, c->ext_host, 0));
     return SC_OK;
 }
 
@@ -112,6 +114,7 @@ int device_ctx(DeviceCtx** out) {
         cudaFree(c->tw32);
         cudaFree(c->tw64);
         cudaFree(c->partials);
+        if (c->ext_host) cudaFreeHost(c->ext_host);
         delete c;
         return st;
     }

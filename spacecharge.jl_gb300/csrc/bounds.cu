@@ -113,12 +113,13 @@ int bounds_reduce(const void* x, const void* y, const void* z, int64_t n, int dt
         minmax_partials<float><<<blocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z, n,
                                                      reinterpret_cast<unsigned long long*>(ctx->partials));
     SC_LAUNCH_CHECK("minmax_partials");
-    double* out = ctx->partials + 6 * ctx->partial_blocks;
-    minmax_final<<<1, 192, 0, s>>>(reinterpret_cast<const unsigned long long*>(ctx->partials), blocks, out);
+    // the final kernel writes the extrema straight into page-locked host
+    // memory: the host waits for the stream and reads them, with no copy
+    minmax_final<<<1, 192, 0, s>>>(reinterpret_cast<const unsigned long long*>(ctx->partials), blocks,
+                                   ctx->ext_dev);
     SC_LAUNCH_CHECK("minmax_final");
-    double h[6];
-    SC_CUDA(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, s));
     SC_CUDA(cudaStreamSynchronize(s));
+    const volatile double* h = ctx->ext_host;
     for (int d = 0; d < 3; ++d) {
         mins[d] = h[d];
         maxs[d] = h[3 + d];

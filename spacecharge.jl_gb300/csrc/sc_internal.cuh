@@ -107,6 +107,8 @@ struct DeviceCtx {
     double2* tw64 = nullptr;  // the same in FP64
     double* partials = nullptr;  // bounds reduction partials
     int partial_blocks = 0;
+    double* ext_host = nullptr;  // the reduction's 6 extrema: page-locked, mapped,
+    double* ext_dev = nullptr;   // written by the final kernel through ext_dev
     int sm_count = 0;
 };
 int device_ctx(DeviceCtx** out);  // for the current device
