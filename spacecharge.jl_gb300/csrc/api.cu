@@ -402,9 +402,12 @@ int mesh_set_geometry(sc_mesh* m, const double lo[3], const double hi[3], const 
 // ------------------------------------------------------ host-buffer kick
 // sc_kick_host: particles and outputs in host memory.  The particles go to
 // device staging buffers in chunks on an H2D copy stream and each chunk is
-// deposited as soon as it has arrived; after the solve, each chunk is
-// gathered and copied back on a D2H copy stream while the next is gathered.
-// The Green build runs on the side stream from the start.  Two chunks: each
+// deposited as soon as it has arrived (atomic and vector deposits; the
+// sorted, deterministic and tiled deposits wait for all of them); after the
+// solve, each chunk is gathered and copied back on a D2H copy stream while
+// the next is gathered (every mode but the tiled one, whose gather reads its
+// binning of all particles).  The Green build runs on the side stream from
+// the start, beside the copies.  Two chunks: each
 // chunk costs seven copies and their events, and with 1M FP64 particles the
 // kick took 0.401 ms with 2 chunks, 0.431 with 3, 0.421 with 4 and 0.489
 // with 8.
@@ -481,81 +484,81 @@ static int host_pipe(sc_mesh* m, int64_t n, size_t elem, HostPipe** out) {
 // 75/25 in and 25/75 out and 0.387 with 65/35 in and 15/85 out.
 constexpr double kHostFirstIn = 0.65, kHostFirstOut = 0.15;
 
-static void host_splits(int64_t n, int K, int64_t* cin, int64_t* cout) {
-    const double fin = K == 2 ? kHostFirstIn : 1.0 / K, fout = K == 2 ? kHostFirstOut : 1.0 / K;
-    auto fill = [&](int64_t* c, double first) {
-        c[0] = 0;
-        for (int k = 1; k < K; ++k) {
-            const double f = first + (1.0 - first) * (k - 1) / std::max(1, K - 1);
-            c[k] = std::min<int64_t>(n, ((int64_t)(f * (double)n) + 255) / 256 * 256);
-            c[k] = std::max(c[k], c[k - 1]);
-        }
-        c[K] = n;
-    };
-    fill(cin, fin);
-    fill(cout, fout);
+// c[0..K]: K chunks of the n particles, the first one a fraction `first` of
+// them and the rest equal
+static void host_split(int64_t n, int K, double first, int64_t* c) {
+    c[0] = 0;
+    for (int k = 1; k < K; ++k) {
+        const double f = first + (1.0 - first) * (k - 1) / std::max(1, K - 1);
+        c[k] = std::min<int64_t>(n, ((int64_t)(f * (double)n) + 255) / 256 * 256);
+        c[k] = std::max(c[k], c[k - 1]);
+    }
+    c[K] = n;
 }
 
 static int kick_host_run(sc_mesh* m, HostPipe* hp, const void* const* hin, int64_t n, int dtype, int at_cathode,
-                         void* const* hout, cudaStream_t s) {
+                         void* const* hout, cudaStream_t s, cudaEvent_t* ready) {
     const size_t elem = dtype == SC_F64 ? 8 : 4;
     char* st = (char*)hp->stage;
     char* d[7];
     for (int i = 0; i < 7; ++i) d[i] = st + (size_t)i * elem * (size_t)hp->cap;
-    const int mode = m->precision == SC_PREC_PLAIN64 ? SC_DEPOSIT_ATOMIC : m->kick_mode;
-    const bool chunked = deposit_chunkable(m, mode);
-    const int K = chunked ? (int)std::min<int64_t>(kHostChunks, std::max<int64_t>(1, n / 65536)) : 1;
+    const bool plain = m->precision == SC_PREC_PLAIN64;
+    const int mode = plain ? SC_DEPOSIT_ATOMIC : m->kick_mode;
+    // sorted, deterministic and tiled deposits need every particle at once;
+    // the tiled deposit's gather reads its binning of all of them
+    const bool chunk_in = deposit_chunkable(m, mode);
+    const bool chunk_out = plain || mode != SC_DEPOSIT_TILED;
+    const int K = (int)std::min<int64_t>(kHostChunks, std::max<int64_t>(1, n / 65536));
+    const int Kin = chunk_in ? K : 1, Kout = chunk_out ? K : 1;
     int64_t cin[kHostChunks + 1], cout[kHostChunks + 1];
-    host_splits(n, K, cin, cout);
+    host_split(n, Kin, Kin == 2 ? kHostFirstIn : 1.0 / Kin, cin);
+    host_split(n, Kout, Kout == 2 ? kHostFirstOut : 1.0 / Kout, cout);
     SC_CUDA(cudaEventRecord(hp->fork, s));
     SC_CUDA(cudaStreamWaitEvent(hp->h2d, hp->fork, 0));
     SC_CUDA(cudaStreamWaitEvent(hp->d2h, hp->fork, 0));
-    if (!chunked) {
-        // sorted, deterministic and tiled deposits need every particle at once
+    if (!plain) SC_TRY(native_green_async(m, at_cathode, s, ready));
+    auto h2d = [&](int c) -> int {
+        const int64_t off = cin[c], cnt = cin[c + 1] - cin[c];
         for (int i = 0; i < 4; ++i)
-            SC_CUDA(cudaMemcpyAsync(d[i], hin[i], elem * (size_t)n, cudaMemcpyHostToDevice, hp->h2d));
-        SC_CUDA(cudaEventRecord(hp->in[0], hp->h2d));
-        SC_CUDA(cudaStreamWaitEvent(s, hp->in[0], 0));
-        SC_TRY(kick_issue(m, d[0], d[1], d[2], d[3], n, dtype, at_cathode, d[4], d[5], d[6], s));
-        SC_CUDA(cudaEventRecord(hp->out[0], s));
-        SC_CUDA(cudaStreamWaitEvent(hp->d2h, hp->out[0], 0));
-        for (int i = 0; i < 3; ++i)
-            SC_CUDA(cudaMemcpyAsync(hout[i], d[4 + i], elem * (size_t)n, cudaMemcpyDeviceToHost, hp->d2h));
-    } else {
-        cudaEvent_t ready = nullptr;
-        if (m->precision != SC_PREC_PLAIN64) SC_TRY(native_green_async(m, at_cathode, s, &ready));
-        {
-            StageScope sd(m->timer, SC_STAGE_DEPOSIT, s);
-            SC_TRY(deposit_chunk_begin(m, mode, s));
-            for (int c = 0; c < K; ++c) {
-                const int64_t off = cin[c], cnt = cin[c + 1] - cin[c];
-                if (cnt <= 0) continue;
-                for (int i = 0; i < 4; ++i)
-                    SC_CUDA(cudaMemcpyAsync(d[i] + off * elem, (const char*)hin[i] + off * elem, elem * (size_t)cnt,
-                                            cudaMemcpyHostToDevice, hp->h2d));
-                SC_CUDA(cudaEventRecord(hp->in[c], hp->h2d));
-                SC_CUDA(cudaStreamWaitEvent(s, hp->in[c], 0));
-                SC_TRY(deposit_chunk_add(m, d[0] + off * elem, d[1] + off * elem, d[2] + off * elem,
-                                         d[3] + off * elem, cnt, dtype, mode, s));
-            }
-            SC_TRY(deposit_chunk_finish(m, mode, s));
-        }
-        if (m->precision == SC_PREC_PLAIN64)
-            SC_TRY(plain_solve(m, at_cathode, s));
-        else
-            SC_TRY(native_solve(m, at_cathode, s, ready));
-        StageScope sg(m->timer, SC_STAGE_GATHER, s);
-        for (int c = 0; c < K; ++c) {
-            const int64_t off = cout[c], cnt = cout[c + 1] - cout[c];
+            SC_CUDA(cudaMemcpyAsync(d[i] + off * elem, (const char*)hin[i] + off * elem, elem * (size_t)cnt,
+                                    cudaMemcpyHostToDevice, hp->h2d));
+        SC_CUDA(cudaEventRecord(hp->in[c], hp->h2d));
+        SC_CUDA(cudaStreamWaitEvent(s, hp->in[c], 0));
+        return SC_OK;
+    };
+    if (chunk_in) {
+        StageScope sd(m->timer, SC_STAGE_DEPOSIT, s);
+        SC_TRY(deposit_chunk_begin(m, mode, s));
+        for (int c = 0; c < Kin; ++c) {
+            const int64_t off = cin[c], cnt = cin[c + 1] - cin[c];
             if (cnt <= 0) continue;
+            SC_TRY(h2d(c));
+            SC_TRY(deposit_chunk_add(m, d[0] + off * elem, d[1] + off * elem, d[2] + off * elem,
+                                     d[3] + off * elem, cnt, dtype, mode, s));
+        }
+        SC_TRY(deposit_chunk_finish(m, mode, s));
+    } else {
+        SC_TRY(h2d(0));
+        SC_TRY(sc_deposit(m, d[0], d[1], d[2], d[3], n, dtype, 1, mode, s));
+    }
+    if (plain)
+        SC_TRY(plain_solve(m, at_cathode, s));
+    else
+        SC_TRY(native_solve(m, at_cathode, s, *ready));
+    StageScope sg(m->timer, SC_STAGE_GATHER, s);
+    for (int c = 0; c < Kout; ++c) {
+        const int64_t off = cout[c], cnt = cout[c + 1] - cout[c];
+        if (cnt <= 0) continue;
+        if (chunk_out)
             SC_TRY(gather_launch(m, d[0] + off * elem, d[1] + off * elem, d[2] + off * elem, cnt, dtype,
                                  d[4] + off * elem, d[5] + off * elem, d[6] + off * elem, s));
-            SC_CUDA(cudaEventRecord(hp->out[c], s));
-            SC_CUDA(cudaStreamWaitEvent(hp->d2h, hp->out[c], 0));
-            for (int i = 0; i < 3; ++i)
-                SC_CUDA(cudaMemcpyAsync((char*)hout[i] + off * elem, d[4 + i] + off * elem, elem * (size_t)cnt,
-                                        cudaMemcpyDeviceToHost, hp->d2h));
-        }
+        else
+            SC_TRY(gather_tiled_launch(m, d[0], n, dtype, d[4], d[5], d[6], s));
+        SC_CUDA(cudaEventRecord(hp->out[c], s));
+        SC_CUDA(cudaStreamWaitEvent(hp->d2h, hp->out[c], 0));
+        for (int i = 0; i < 3; ++i)
+            SC_CUDA(cudaMemcpyAsync((char*)hout[i] + off * elem, d[4 + i] + off * elem, elem * (size_t)cnt,
+                                    cudaMemcpyDeviceToHost, hp->d2h));
     }
     SC_CUDA(cudaEventRecord(hp->done, hp->d2h));
     SC_CUDA(cudaStreamWaitEvent(s, hp->done, 0));
@@ -566,9 +569,12 @@ static int kick_host_issue(sc_mesh* m, const void* const* hin, int64_t n, int dt
                            void* const* hout, cudaStream_t s) {
     HostPipe* hp = nullptr;
     SC_TRY(host_pipe(m, n, dtype == SC_F64 ? 8 : 4, &hp));
-    const int st = kick_host_run(m, hp, hin, n, dtype, at_cathode, hout, s);
+    cudaEvent_t ready = nullptr;
+    const int st = kick_host_run(m, hp, hin, n, dtype, at_cathode, hout, s, &ready);
     if (st != SC_OK) {
-        // an error returns with no copy of the caller's host buffers in flight
+        // an error returns with no copy of the caller's host buffers in flight,
+        // and with the caller's stream ordered after the Green build
+        if (ready) cudaStreamWaitEvent(s, ready, 0);
         cudaStreamSynchronize(hp->h2d);
         cudaStreamSynchronize(hp->d2h);
     }
