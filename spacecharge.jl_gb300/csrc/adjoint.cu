@@ -298,11 +298,12 @@ static int adjoint_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q,
     // needed, overlaps the deposit on the mesh's side stream)
     cudaEvent_t ready = nullptr;
     if (n > 0) SC_TRY(native_green_async(m, at_cathode, s, &ready));
-    int st = cudaMemsetAsync(m->rho, 0, sizeof(T) * m->N, s) == cudaSuccess ? SC_OK
-                                                                             : cuda_fail(cudaGetLastError(), "memset");
-    if (st == SC_OK)
-        st = deposit_launch(m, x, y, z, q, n, sizeof(P) == 8 ? SC_F64 : SC_F32,
-                            m->precision == SC_PREC_MIXED ? SC_DEPOSIT_VECTOR : SC_DEPOSIT_ATOMIC, s);
+    const int dmode = m->precision == SC_PREC_MIXED ? SC_DEPOSIT_VECTOR : SC_DEPOSIT_ATOMIC;
+    const bool assign = deposit_assigns(m, dmode);
+    int st = assign || cudaMemsetAsync(m->rho, 0, sizeof(T) * m->N, s) == cudaSuccess
+                 ? SC_OK
+                 : cuda_fail(cudaGetLastError(), "memset");
+    if (st == SC_OK) st = deposit_launch(m, x, y, z, q, n, sizeof(P) == 8 ? SC_F64 : SC_F32, dmode, s, assign);
     if (st != SC_OK) {
         if (ready) cudaStreamWaitEvent(s, ready, 0);
         return st;

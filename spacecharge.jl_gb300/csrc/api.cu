@@ -799,9 +799,11 @@ int sc_deposit(sc_mesh* m, const void* x, const void* y, const void* z, const vo
     if (!valid_deposit_mode(mode)) return fail(SC_ERR_INVALID, "unknown deposit mode %d", mode);
     DeviceGuard g(m->device);
     StageScope st(m->timer, SC_STAGE_DEPOSIT, (cudaStream_t)stream);
-    if (clear) SC_TRY(sc_clear_mesh(m, stream));
+    // a clearing vector deposit writes rho whole in its node sum
+    const bool assign = clear && n > 0 && deposit_assigns(m, mode);
+    if (clear && !assign) SC_TRY(sc_clear_mesh(m, stream));
     if (n == 0) return SC_OK;
-    return deposit_launch(m, x, y, z, q, n, dtype, mode, (cudaStream_t)stream);
+    return deposit_launch(m, x, y, z, q, n, dtype, mode, (cudaStream_t)stream, assign);
 }
 
 int sc_solve(sc_mesh* m, int at_cathode, void* stream) {

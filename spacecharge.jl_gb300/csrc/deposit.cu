@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(256) deposit_vector(const P* __restrict__ px, 
 }
 
 __global__ void __launch_bounds__(256) k_corner_sum(const float* __restrict__ corner, int nx, int ny, int64_t N,
-                                                    float* __restrict__ rho) {
+                                                    float* __restrict__ rho, int assign) {
     pdl_wait();  // the corner slots come from the preceding deposit
     const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= N) return;
@@ -200,11 +200,15 @@ __global__ void __launch_bounds__(256) k_corner_sum(const float* __restrict__ co
             }
         }
     }
-    rho[node] += s;
+    if (assign)
+        rho[node] = s;
+    else
+        rho[node] += s;
 }
 
-int corner_sum_launch(sc_mesh* m, const float* corner, float* out, cudaStream_t s) {
-    launch_pdl(k_corner_sum, (unsigned)((m->N + 255) / 256), 256, 0, s, corner, m->n[0], m->n[1], m->N, out);
+int corner_sum_launch(sc_mesh* m, const float* corner, float* out, cudaStream_t s, bool assign) {
+    launch_pdl(k_corner_sum, (unsigned)((m->N + 255) / 256), 256, 0, s, corner, m->n[0], m->n[1], m->N, out,
+               assign ? 1 : 0);
     SC_LAUNCH_CHECK("k_corner_sum");
     m->launches += 1;
     return SC_OK;
@@ -235,10 +239,14 @@ static int deposit_vector_add(sc_mesh* m, const Axes& ax, const void* x, const v
 }
 
 static int deposit_vector_launch(sc_mesh* m, const Axes& ax, const void* x, const void* y, const void* z,
-                                 const void* q, int64_t n, int dtype, cudaStream_t s) {
+                                 const void* q, int64_t n, int dtype, cudaStream_t s, bool assign) {
     SC_TRY(corner_clear(m, s));
     SC_TRY(deposit_vector_add(m, ax, x, y, z, q, n, dtype, s));
-    return corner_sum_launch(m, (const float*)m->corner, (float*)m->rho, s);
+    return corner_sum_launch(m, (const float*)m->corner, (float*)m->rho, s, assign);
+}
+
+bool deposit_assigns(const sc_mesh* m, int mode) {
+    return mode == SC_DEPOSIT_VECTOR && m->precision == SC_PREC_MIXED;
 }
 
 // Deposit in chunks (sc_kick_host): the atomic and vector modes accumulate,
@@ -248,8 +256,8 @@ bool deposit_chunkable(const sc_mesh* m, int mode) {
 }
 
 int deposit_chunk_begin(sc_mesh* m, int mode, cudaStream_t s) {
+    if (deposit_assigns(m, mode)) return corner_clear(m, s);  // the node sum assigns rho
     SC_CUDA(cudaMemsetAsync(m->rho, 0, field_elem_bytes(m->precision) * m->N, s));
-    if (mode == SC_DEPOSIT_VECTOR && m->precision == SC_PREC_MIXED) SC_TRY(corner_clear(m, s));
     return SC_OK;
 }
 
@@ -262,8 +270,7 @@ int deposit_chunk_add(sc_mesh* m, const void* x, const void* y, const void* z, c
 }
 
 int deposit_chunk_finish(sc_mesh* m, int mode, cudaStream_t s) {
-    if (mode == SC_DEPOSIT_VECTOR && m->precision == SC_PREC_MIXED)
-        return corner_sum_launch(m, (const float*)m->corner, (float*)m->rho, s);
+    if (deposit_assigns(m, mode)) return corner_sum_launch(m, (const float*)m->corner, (float*)m->rho, s, true);
     return SC_OK;
 }
 
@@ -323,7 +330,7 @@ int deposit_sorted_launch(sc_mesh* m, const void* x, const void* y, const void* 
                           int dtype, int mode, cudaStream_t s);
 
 int deposit_launch(sc_mesh* m, const void* x, const void* y, const void* z, const void* q, int64_t n, int dtype,
-                   int mode, cudaStream_t s) {
+                   int mode, cudaStream_t s, bool assign) {
     const Axes ax = make_axes(m);
     const int64_t blocks = (n + 255) / 256;
     if (m->precision == SC_PREC_PLAIN64) {
@@ -339,7 +346,7 @@ int deposit_launch(sc_mesh* m, const void* x, const void* y, const void* z, cons
     }
     if (mode == SC_DEPOSIT_TILED) return deposit_tiled_launch(m, x, y, z, q, n, dtype, s);
     if (mode == SC_DEPOSIT_VECTOR && m->precision == SC_PREC_MIXED)
-        return deposit_vector_launch(m, ax, x, y, z, q, n, dtype, s);
+        return deposit_vector_launch(m, ax, x, y, z, q, n, dtype, s, assign);
     if (mode == SC_DEPOSIT_SORTED || mode == SC_DEPOSIT_DETERMINISTIC)
         return deposit_sorted_launch(m, x, y, z, q, n, dtype, mode, s);
     const int64_t ablocks = (n + 256 * kDepPerThread - 1) / (256 * kDepPerThread);

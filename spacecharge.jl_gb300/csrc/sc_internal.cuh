@@ -268,11 +268,15 @@ Geom make_geom(const sc_mesh* m);
 int bounds_reduce(const void* x, const void* y, const void* z, int64_t n, int dtype,
                   double mins[3], double maxs[3], cudaStream_t s);
 
+// assign: the deposit writes rho instead of adding to it, where
+// deposit_assigns(m, mode) (the vector deposit's node sum); rho is then not
+// cleared beforehand
 int deposit_launch(sc_mesh* m, const void* x, const void* y, const void* z, const void* q,
-                   int64_t n, int dtype, int mode, cudaStream_t s);
+                   int64_t n, int dtype, int mode, cudaStream_t s, bool assign = false);
+bool deposit_assigns(const sc_mesh* m, int mode);
 // out[node] += sum of the node's entries in the 8 cells around it (float[8N]
 // per-cell corner slots, the vector deposit's layout)
-int corner_sum_launch(sc_mesh* m, const float* corner, float* out, cudaStream_t s);
+int corner_sum_launch(sc_mesh* m, const float* corner, float* out, cudaStream_t s, bool assign = false);
 // chunked deposit of sc_kick_host (deposit.cu)
 bool deposit_chunkable(const sc_mesh* m, int mode);
 int deposit_chunk_begin(sc_mesh* m, int mode, cudaStream_t s);
