@@ -50,8 +50,10 @@ static int batch_issue(sc_batch* b, const void* const* x, const void* const* y, 
         sc_mesh* m = b->meshes[i];
         const size_t cap = m->fused_smem_cap;
         m->fused_smem_cap = ns > 1 ? 210 * 1024 : cap;
+        m->beside_others = ns > 1;
         st = kick_issue(m, x[i], y[i], z[i], q[i], n[i], dtype, at_cathode, ex[i], ey[i], ez[i], b->streams[i % ns]);
         m->fused_smem_cap = cap;
+        m->beside_others = false;
     }
     // join every stream, also after a failed bunch: the caller's stream
     // orders whatever was issued

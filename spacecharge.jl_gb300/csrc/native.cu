@@ -909,6 +909,9 @@ int native_ensure_green(sc_mesh* m, int at_cathode, cudaStream_t s) {
 }
 
 // inverse y and x as one pass (k2_inv_yx) where it applies
+#ifndef SC_FUSED_FWD_XY
+#define SC_FUSED_FWD_XY 1
+#endif
 #ifndef SC_FUSED_INV_YX
 #define SC_FUSED_INV_YX 1
 #endif
@@ -937,13 +940,28 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
     const int eng = w.engine >= 0 ? w.engine : fft_engine();
     const bool two = std::is_same<T, float>::value && eng == 0;
     const int lgWy = w.lgW >= 0 ? w.lgW : pick_cols(w.log2L[1]);
-    {
+    // The fused forward pass runs one CTA per z plane, each a long chain of
+    // FFT rounds: it pays only with the GPU to itself.  Beside a concurrent
+    // Green build the kick went from 0.138 to 0.145 ms, and inside a batch
+    // from 6.10 to 6.43 ms; alone, the Green-cached kick went from 0.110 to
+    // 0.108 ms and the tracking step from 0.134 to 0.131 ms.
+    bool fwd_fused = false;
+    if (two && SC_FUSED_FWD_XY && !green_ready && !m->beside_others) {
+        StageScope st(m->timer, SC_STAGE_FWD_X, s);
+        fwd_fused = launch2_fwd_xy(w.log2L[0], w.log2L[1], (const float*)m->rho, (float2*)B, nx, ny, nz, Hx,
+                                   (const float2*)tw, s, m->fused_smem_cap);
+        if (fwd_fused) {
+            SC_LAUNCH_CHECK("k2_fwd_xy");
+            m->launches -= 1;  // one launch for the two passes
+        }
+    }
+    if (!fwd_fused) {
         StageScope st(m->timer, SC_STAGE_FWD_X, s);
         if (!(two && launch2_fwd_x(w.log2L[0], (const float*)m->rho, (float2*)A, nx, rows, Hx, (const float2*)tw, s)))
             SC_TRY(run_fwd_x<T>((const T*)m->rho, A, nx, rows, w, tw, s));
         SC_LAUNCH_CHECK("fwd_x");
     }
-    {
+    if (!fwd_fused) {
         // y: A (Hx x ny x nz) -> B (Hx x Ly x nz)
         StageScope st(m->timer, SC_STAGE_FWD_Y, s);
         if (!(two && launch2_col(false, w.log2L[1], (const float2*)A, (float2*)B, Hx, ny, Ly, Hx, (int64_t)Hx * ny,

@@ -206,6 +206,84 @@ __global__ void __launch_bounds__(256) k2_fwd_x(const float* __restrict__ rho, f
     }
 }
 
+// Forward x and y fused, one CTA per z plane, Lx = Ly = L: the plane's rows,
+// two per complex FFT, into their half spectra in shared memory (as
+// k2_fwd_x), then the Hx columns along y (as the forward k2_col: inputs
+// y < ny, all L outputs) into B[kx + Hx*(ky + L*z)].  Replaces those two
+// passes when the plane fits in shared memory; the x pass's output never
+// goes to global memory.
+template <int L>
+__global__ void __launch_bounds__(256) k2_fwd_xy(const float* __restrict__ rho, float2* __restrict__ B, int nx,
+                                                 int ny, int Hx, const float2* __restrict__ tw) {
+    using E = F2<L>;
+    constexpr int W = 256 / E::NT;  // row pairs (x pass) or columns (y pass) per round
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float2* xb = reinterpret_cast<float2*>(smraw);  // W exchange columns
+    float2* ds = xb + W * E::S;                     // [ny][Hx]: the plane after the x pass
+    const int z = blockIdx.x;
+    float2 v[16];
+    // x pass: rows y0, y1 = y0 + 1 (row-pair-fastest thread map)
+    {
+        const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
+        float2* col = xb + p * E::S;
+        const float* rz = rho + (int64_t)nx * ny * z;
+        for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
+            const int y0 = 2 * (q0 + p), y1 = y0 + 1;
+            if (t < E::R2) {
+#pragma unroll
+                for (int s = 0; s < E::R1; ++s) {
+                    const int x = t + E::R2 * s;
+                    float re = 0.f, im = 0.f;
+                    if (x < nx) {
+                        if (y0 < ny) re = rz[(int64_t)y0 * nx + x];
+                        if (y1 < ny) im = rz[(int64_t)y1 * nx + x];
+                    }
+                    v[s] = make_float2(re, im);
+                }
+            }
+            E::template fwd<false>(v, col, t, swt);
+            if (t < E::R1) {
+#pragma unroll
+                for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+            }
+            __syncthreads();
+            if (y0 < ny) {
+                for (int k = t; k <= L / 2; k += E::NT) {
+                    float2 xa, xbv;
+                    split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
+                    ds[y0 * Hx + k] = xa;
+                    if (y1 < ny) ds[y1 * Hx + k] = xbv;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    // y pass: the Hx columns (column-fastest thread map), zero beyond y = ny
+    {
+        const int c = threadIdx.x % W, t = threadIdx.x / W;
+        float2* col = xb + c * E::S;
+        float2* Bz = B + (int64_t)Hx * L * z;
+        for (int k0 = 0; k0 < Hx; k0 += W) {
+            const int kx = k0 + c;
+            const bool ok = kx < Hx;
+            if (t < E::R2) {
+#pragma unroll
+                for (int s = 0; s < E::R1; ++s) {
+                    const int n = t + E::R2 * s;
+                    v[s] = (ok && n < ny) ? ds[n * Hx + kx] : make_float2(0.f, 0.f);
+                }
+            }
+            E::template fwd<false>(v, col, t, swt);
+            if (t < E::R1 && ok) {
+#pragma unroll
+                for (int r = 0; r < E::R2; ++r) Bz[kx + (int64_t)Hx * (t + E::R1 * r)] = v[r];
+            }
+        }
+    }
+}
+
 // Inverse x pass of the three components, two rows per complex IFFT, packed
 // float4 output nodes.
 template <int L>
@@ -854,6 +932,24 @@ static bool launch2_fwd_x(int logL, const float* rho, float2* A, int nx, int row
     }
     SC_L_SWITCH(logL, SC_K2FX)
 #undef SC_K2FX
+    return true;
+}
+
+// The fused forward x+y pass: Lx = Ly and the plane in shared memory, at
+// most `cap` bytes (as launch2_inv_yx).
+static bool launch2_fwd_xy(int logLx, int logLy, const float* rho, float2* B, int nx, int ny, int nz, int Hx,
+                           const float2* tw, cudaStream_t s, size_t cap) {
+    if (logLx != logLy) return false;
+#define SC_K2XY(LL)                                                                     \
+    {                                                                                   \
+        constexpr int W = 256 / F2<LL>::NT;                                             \
+        const size_t smem = sizeof(float2) * ((size_t)W * F2<LL>::S + (size_t)ny * Hx); \
+        if (smem > cap) return false;                                                   \
+        if (set_smem(k2_fwd_xy<LL>, smem) != SC_OK) return false;                       \
+        launch_pdl(k2_fwd_xy<LL>, dim3(nz), 256, smem, s, rho, B, nx, ny, Hx, tw);      \
+    }
+    SC_L_SWITCH(logLx, SC_K2XY)
+#undef SC_K2XY
     return true;
 }
 

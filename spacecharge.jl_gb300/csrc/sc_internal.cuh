@@ -233,6 +233,8 @@ struct sc_mesh {
     // largest shared-memory plane of the fused inverse y+x pass: 100 KB keeps
     // two CTAs per SM; batch_issue raises it while other bunches run beside
     size_t fused_smem_cap = 100 * 1024;
+    // set by batch_issue while other bunches' kernels run beside this mesh's
+    bool beside_others = false;
 };
 
 namespace sc {
