@@ -345,14 +345,22 @@ static int adjoint_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q,
     const int rows = ny * nz;
     const int64_t dcs = (int64_t)Hx * ny * nz;
     const bool two = std::is_same<T, float>::value && fft_engine() == 0;
-    for (int c = 0; c < 3; ++c)
-        if (!(two && launch2_fwd_x(w.log2L[0], (const float*)(adjE + c * N), (float2*)(D + c * dcs), nx, rows, Hx,
-                                   (const float2*)tw, s)))
-            SC_TRY(run_fwd_x<T>(adjE + c * N, D + c * dcs, nx, rows, w, tw, s));
-    if (!(two && launch2_col(false, w.log2L[1], (const float2*)D, (float2*)C, Hx, ny, Ly, Hx, (int64_t)Hx * ny, dcs,
-                             Hx, (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, nz, 3, (const float2*)tw, s)))
-        SC_TRY(run_col<false, T>(D, C, Hx, Ly, w.log2L[1], ny, Ly, Hx, (int64_t)Hx * ny, dcs, Hx, (int64_t)Hx * Ly,
-                                 (int64_t)Hx * Ly * nz, nz, 3, tw, s));
+    // forward x and y of the three components: fused per (z plane,
+    // component) where the plane fits (3 nz CTAs), else the separate passes
+    if (two && launch2_fwd_xy(w.log2L[0], w.log2L[1], (const float*)adjE, (float2*)C, nx, ny, nz, Hx,
+                              (const float2*)tw, s, m->fused_smem_cap, 3, N, (int64_t)Hx * Ly * nz)) {
+        SC_LAUNCH_CHECK("k2_fwd_xy");
+        m->launches -= 3;  // one launch for the four below
+    } else {
+        for (int c = 0; c < 3; ++c)
+            if (!(two && launch2_fwd_x(w.log2L[0], (const float*)(adjE + c * N), (float2*)(D + c * dcs), nx, rows,
+                                       Hx, (const float2*)tw, s)))
+                SC_TRY(run_fwd_x<T>(adjE + c * N, D + c * dcs, nx, rows, w, tw, s));
+        if (!(two && launch2_col(false, w.log2L[1], (const float2*)D, (float2*)C, Hx, ny, Ly, Hx, (int64_t)Hx * ny,
+                                 dcs, Hx, (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, nz, 3, (const float2*)tw, s)))
+            SC_TRY(run_col<false, T>(D, C, Hx, Ly, w.log2L[1], ny, Ly, Hx, (int64_t)Hx * ny, dcs, Hx,
+                                     (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, nz, 3, tw, s));
+    }
     if (two && launch2_adj_zpass(w.log2L[2], (const float2*)C, (float2*)B, Hx, Ly, nz,
                                  make_green_view(w, at_cathode ? 1 : 0), (const float2*)tw, s)) {
         SC_LAUNCH_CHECK("k2_adj_zpass");

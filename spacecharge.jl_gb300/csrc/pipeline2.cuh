@@ -211,10 +211,12 @@ __global__ void __launch_bounds__(256) k2_fwd_x(const float* __restrict__ rho, f
 // k2_fwd_x), then the Hx columns along y (as the forward k2_col: inputs
 // y < ny, all L outputs) into B[kx + Hx*(ky + L*z)].  Replaces those two
 // passes when the plane fits in shared memory; the x pass's output never
-// goes to global memory.
+// goes to global memory.  blockIdx.y selects a component: input rho + y *
+// in_cs, output B + y * out_cs.
 template <int L>
 __global__ void __launch_bounds__(256) k2_fwd_xy(const float* __restrict__ rho, float2* __restrict__ B, int nx,
-                                                 int ny, int Hx, const float2* __restrict__ tw) {
+                                                 int ny, int Hx, int64_t in_cs, int64_t out_cs,
+                                                 const float2* __restrict__ tw) {
     using E = F2<L>;
     constexpr int W = 256 / E::NT;  // row pairs (x pass) or columns (y pass) per round
     __shared__ float2 swt[L];
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(256) k2_fwd_xy(const float* __restrict__ rho, 
     {
         const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
         float2* col = xb + p * E::S;
-        const float* rz = rho + (int64_t)nx * ny * z;
+        const float* rz = rho + blockIdx.y * in_cs + (int64_t)nx * ny * z;
         for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
             const int y0 = 2 * (q0 + p), y1 = y0 + 1;
             if (t < E::R2) {
@@ -264,7 +266,7 @@ __global__ void __launch_bounds__(256) k2_fwd_xy(const float* __restrict__ rho, 
     {
         const int c = threadIdx.x % W, t = threadIdx.x / W;
         float2* col = xb + c * E::S;
-        float2* Bz = B + (int64_t)Hx * L * z;
+        float2* Bz = B + blockIdx.y * out_cs + (int64_t)Hx * L * z;
         for (int k0 = 0; k0 < Hx; k0 += W) {
             const int kx = k0 + c;
             const bool ok = kx < Hx;
@@ -938,7 +940,8 @@ static bool launch2_fwd_x(int logL, const float* rho, float2* A, int nx, int row
 // The fused forward x+y pass: Lx = Ly and the plane in shared memory, at
 // most `cap` bytes (as launch2_inv_yx).
 static bool launch2_fwd_xy(int logLx, int logLy, const float* rho, float2* B, int nx, int ny, int nz, int Hx,
-                           const float2* tw, cudaStream_t s, size_t cap) {
+                           const float2* tw, cudaStream_t s, size_t cap, int ncomp = 1, int64_t in_cs = 0,
+                           int64_t out_cs = 0) {
     if (logLx != logLy) return false;
 #define SC_K2XY(LL)                                                                     \
     {                                                                                   \
@@ -946,7 +949,7 @@ static bool launch2_fwd_xy(int logLx, int logLy, const float* rho, float2* B, in
         const size_t smem = sizeof(float2) * ((size_t)W * F2<LL>::S + (size_t)ny * Hx); \
         if (smem > cap) return false;                                                   \
         if (set_smem(k2_fwd_xy<LL>, smem) != SC_OK) return false;                       \
-        launch_pdl(k2_fwd_xy<LL>, dim3(nz), 256, smem, s, rho, B, nx, ny, Hx, tw);      \
+        launch_pdl(k2_fwd_xy<LL>, dim3(nz, ncomp), 256, smem, s, rho, B, nx, ny, Hx, in_cs, out_cs, tw); \
     }
     SC_L_SWITCH(logLx, SC_K2XY)
 #undef SC_K2XY
