@@ -374,20 +374,30 @@ static int adjoint_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q,
         k_adj_zpass<T><<<grid, 256, smem, s>>>(C, B, Hx, Ly, nz, Lz, w.log2L[2], lgW, gv, tw);
         SC_LAUNCH_CHECK("k_adj_zpass");
     }
-    if (!(two && launch2_col(true, w.log2L[1], (const float2*)B, (float2*)A, Hx, Ly, ny, Hx, (int64_t)Hx * Ly, 0, Hx,
-                             (int64_t)Hx * ny, 0, nz, 1, (const float2*)tw, s)))
-        SC_TRY(run_col<true, T>(B, A, Hx, Ly, w.log2L[1], Ly, ny, Hx, (int64_t)Hx * Ly, 0, Hx, (int64_t)Hx * ny, 0, nz,
-                                1, tw, s));
-    if (two && launch2_inv_x1(w.log2L[0], (const float2*)A, (float*)m->efield, nx, rows, Hx, (const float2*)tw, s)) {
-        SC_LAUNCH_CHECK("k2_inv_x1");
+    // inverse y and x of rhobar^ into lane 3 of the packed nodes: fused per z
+    // plane where the plane fits, else the separate passes
+    if (two && launch2_inv_yx(w.log2L[0], w.log2L[1], (const float2*)B, (float4*)m->efield, nx, ny, nz, Hx,
+                              (const float2*)tw, s, m->fused_smem_cap, 1, 3)) {
+        SC_LAUNCH_CHECK("k2_inv_yx");
+        m->launches -= 1;  // one launch for the two passes
     } else {
-        const int lgP = pick_rows(w.log2L[0]);
-        const int P_ = 1 << lgP;
-        const size_t smem = sizeof(T2) * 2 * P_ * Lx;
-        SC_TRY(set_smem(k_inv_x1<T>, smem));
-        const int pairs = (rows + 1) / 2;
-        k_inv_x1<T><<<(pairs + P_ - 1) / P_, 256, smem, s>>>(A, (T*)m->efield, nx, rows, Lx, w.log2L[0], Hx, lgP, tw);
-        SC_LAUNCH_CHECK("k_inv_x1");
+        if (!(two && launch2_col(true, w.log2L[1], (const float2*)B, (float2*)A, Hx, Ly, ny, Hx, (int64_t)Hx * Ly,
+                                 0, Hx, (int64_t)Hx * ny, 0, nz, 1, (const float2*)tw, s)))
+            SC_TRY(run_col<true, T>(B, A, Hx, Ly, w.log2L[1], Ly, ny, Hx, (int64_t)Hx * Ly, 0, Hx, (int64_t)Hx * ny, 0,
+                                    nz, 1, tw, s));
+        if (two &&
+            launch2_inv_x1(w.log2L[0], (const float2*)A, (float*)m->efield, nx, rows, Hx, (const float2*)tw, s)) {
+            SC_LAUNCH_CHECK("k2_inv_x1");
+        } else {
+            const int lgP = pick_rows(w.log2L[0]);
+            const int P_ = 1 << lgP;
+            const size_t smem = sizeof(T2) * 2 * P_ * Lx;
+            SC_TRY(set_smem(k_inv_x1<T>, smem));
+            const int pairs = (rows + 1) / 2;
+            k_inv_x1<T><<<(pairs + P_ - 1) / P_, 256, smem, s>>>(A, (T*)m->efield, nx, rows, Lx, w.log2L[0], Hx, lgP,
+                                                                tw);
+            SC_LAUNCH_CHECK("k_inv_x1");
+        }
     }
     k_adj_particles<P, T><<<(n + 255) / 256, 256, 0, s>>>(x, y, z, q, gex, gey, gez, n, ax, (const T*)m->efield, dx,
                                                          dy, dz, dq);

@@ -91,9 +91,11 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k2_col(const f
 // component's lane of the packed float4 nodes.  Replaces inverse y + inverse
 // x when the plane fits in shared memory; the intermediate D never goes to
 // global memory.
+// blockIdx.y = c reads component c of C and writes lane lane0 + c of the
+// nodes (the adjoint's rhobar: one component into lane 3).
 template <int L>
 __global__ void __launch_bounds__(256) k2_inv_yx(const float2* __restrict__ C, float* __restrict__ E4, int nx,
-                                                 int ny, int nz, int Hx, const float2* __restrict__ tw) {
+                                                 int ny, int nz, int Hx, int lane0, const float2* __restrict__ tw) {
     using E = F2<L>;
     constexpr int W = 256 / E::NT;  // columns (phase 1) or row pairs (phase 2) per round
     __shared__ float2 swt[L];
@@ -131,7 +133,7 @@ __global__ void __launch_bounds__(256) k2_inv_yx(const float2* __restrict__ C, f
     {
         const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
         float2* col = xb + p * E::S;
-        float* out = E4 + comp;
+        float* out = E4 + lane0 + comp;
         for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
             const int y0 = 2 * (q0 + p), y1 = y0 + 1;
             if (t < E::R1) {
@@ -961,7 +963,7 @@ static bool launch2_fwd_xy(int logLx, int logLy, const float* rho, float2* B, in
 // 100 KB a CTA has an SM to itself, which pays only when other streams' work
 // fills the rest (batch_issue).
 static bool launch2_inv_yx(int logLx, int logLy, const float2* C, float4* E4, int nx, int ny, int nz, int Hx,
-                           const float2* tw, cudaStream_t s, size_t cap) {
+                           const float2* tw, cudaStream_t s, size_t cap, int ncomp = 3, int lane0 = 0) {
     if (logLx != logLy) return false;
 #define SC_K2YX(LL)                                                                                   \
     {                                                                                                 \
@@ -969,7 +971,8 @@ static bool launch2_inv_yx(int logLx, int logLy, const float2* C, float4* E4, in
         const size_t smem = sizeof(float2) * ((size_t)W * F2<LL>::S + (size_t)ny * Hx);               \
         if (smem > cap) return false;                                                                 \
         if (set_smem(k2_inv_yx<LL>, smem) != SC_OK) return false;                                     \
-        launch_pdl(k2_inv_yx<LL>, dim3(nz, 3), 256, smem, s, C, reinterpret_cast<float*>(E4), nx, ny, nz, Hx, tw); \
+        launch_pdl(k2_inv_yx<LL>, dim3(nz, ncomp), 256, smem, s, C, reinterpret_cast<float*>(E4), nx, ny, nz, Hx, \
+                   lane0, tw);                                                                                 \
     }
     SC_L_SWITCH(logLx, SC_K2YX)
 #undef SC_K2YX
