@@ -1,6 +1,8 @@
 // extrema(particles_x/y/z) for the particle-bounds Mesh3D constructor
 // (src/mesh.jl:147-149): one device reduction, then a 48-byte copy to the
 // host (CUDA.jl's `extrema` on CuArrays does the same round trip).
+#include <atomic>
+#include <chrono>
 #include <mutex>
 
 #include "cells.cuh"
@@ -83,8 +85,10 @@ __global__ void __launch_bounds__(256) minmax_partials(const P* __restrict__ x, 
 
 // One warp per extremum (6 warps): each lane reduces a stride of the block
 // partials, then the warp reduces its lanes.
+// out[6], read as an unsigned 64-bit word, is set to `seq` once the six
+// extrema are visible to the host.
 __global__ void __launch_bounds__(192) minmax_final(const unsigned long long* __restrict__ partials, int nblocks,
-                                                    double* __restrict__ out) {
+                                                    double* __restrict__ out, unsigned long long seq) {
     const int k = threadIdx.x >> 5, lane = threadIdx.x & 31;
     unsigned long long r = k < 3 ? ~0ull : 0ull;
     for (int b = lane; b < nblocks; b += 32) r = k < 3 ? min(r, partials[b * 6 + k]) : max(r, partials[b * 6 + k]);
@@ -92,7 +96,15 @@ __global__ void __launch_bounds__(192) minmax_final(const unsigned long long* __
         const unsigned long long v = __shfl_xor_sync(0xffffffffu, r, o);
         r = k < 3 ? min(r, v) : max(r, v);
     }
-    if (lane == 0) out[k] = from_order_key(r);
+    if (lane == 0) {
+        out[k] = from_order_key(r);
+        __threadfence_system();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence_system();
+        *reinterpret_cast<volatile unsigned long long*>(out + 6) = seq;
+    }
 }
 
 int bounds_reduce(const void* x, const void* y, const void* z, int64_t n, int dtype, double mins[3],
@@ -113,12 +125,22 @@ int bounds_reduce(const void* x, const void* y, const void* z, int64_t n, int dt
         minmax_partials<float><<<blocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z, n,
                                                      reinterpret_cast<unsigned long long*>(ctx->partials));
     SC_LAUNCH_CHECK("minmax_partials");
-    // the final kernel writes the extrema straight into page-locked host
-    // memory: the host waits for the stream and reads them, with no copy
+    // The final kernel writes the extrema straight into page-locked host
+    // memory, then a sequence number after them.  The host spins on that
+    // word for up to 20 ms (it returns as soon as the kernel has written it,
+    // without the latency of a stream synchronisation), and otherwise
+    // synchronises the stream, which also reports any error.
+    const unsigned long long seq = ++ctx->ext_seq;
     minmax_final<<<1, 192, 0, s>>>(reinterpret_cast<const unsigned long long*>(ctx->partials), blocks,
-                                   ctx->ext_dev);
+                                   ctx->ext_dev, seq);
     SC_LAUNCH_CHECK("minmax_final");
-    SC_CUDA(cudaStreamSynchronize(s));
+    const volatile unsigned long long* flag = reinterpret_cast<volatile unsigned long long*>(ctx->ext_host + 6);
+    const auto t0 = std::chrono::steady_clock::now();
+    while (*flag != seq && std::chrono::steady_clock::now() - t0 < std::chrono::milliseconds(20)) {
+    }
+    std::atomic_thread_fence(std::memory_order_acquire);
+    if (*flag != seq) SC_CUDA(cudaStreamSynchronize(s));
+    if (*flag != seq) return fail(SC_ERR_CUDA, "bounds reduction: extrema not written");
     const volatile double* h = ctx->ext_host;
     for (int d = 0; d < 3; ++d) {
         mins[d] = h[d];

@@ -109,6 +109,7 @@ struct DeviceCtx {
     int partial_blocks = 0;
     double* ext_host = nullptr;  // the reduction's 6 extrema: page-locked, mapped,
     double* ext_dev = nullptr;   // written by the final kernel through ext_dev
+    unsigned long long ext_seq = 0;  // sequence number the final kernel writes after them
     int sm_count = 0;
 };
 int device_ctx(DeviceCtx** out);  // for the current device
