@@ -541,10 +541,14 @@ static int kick_host_run(sc_mesh* m, HostPipe* hp, const void* const* hin, int64
         SC_TRY(h2d(0));
         SC_TRY(sc_deposit(m, d[0], d[1], d[2], d[3], n, dtype, 1, mode, s));
     }
-    if (plain)
+    if (plain) {
         SC_TRY(plain_solve(m, at_cathode, s));
-    else
-        SC_TRY(native_solve(m, at_cathode, s, *ready));
+    } else {
+        m->green_ahead = true;
+        const int st = native_solve(m, at_cathode, s, *ready);
+        m->green_ahead = false;
+        SC_TRY(st);
+    }
     StageScope sg(m->timer, SC_STAGE_GATHER, s);
     for (int c = 0; c < Kout; ++c) {
         const int64_t off = cout[c], cnt = cout[c + 1] - cout[c];

@@ -236,6 +236,9 @@ struct sc_mesh {
     size_t fused_smem_cap = 100 * 1024;
     // set by batch_issue while other bunches' kernels run beside this mesh's
     bool beside_others = false;
+    // set by the host-buffer kick: its Green build, started beside the H2D
+    // copies, has finished before the solve's forward passes run
+    bool green_ahead = false;
 };
 
 namespace sc {
