@@ -3,7 +3,7 @@
  * (libspacecharge_gb300.so).
  *
  * The library replaces the hot path of SpaceCharge.jl v1.2.0:
- *   Mesh3D (src/mesh.jl:122-265) -> deposit! (src/deposition.jl:218)
+ *   Mesh3D (src/mesh.jl:95-238) -> deposit! (src/deposition.jl:218)
  *   -> solve! (src/solvers/free_space.jl:14) -> interpolate_field
  *   (src/interpolation.jl:100).
  * A Julia host binds these functions with `ccall`; the Python host in
@@ -104,15 +104,15 @@ int sc_version(void);
 const char* sc_last_error(void);
 
 /* Manual-bounds constructor: Mesh3D(grid_size, min_bounds, max_bounds;
- * T, gamma, total_charge), src/mesh.jl:223-265.  Validates grid >= 2 and
- * max > min (mesh.jl:233-238); delta = (max-min)/(n-1) (mesh.jl:247).
+ * T, gamma, total_charge), src/mesh.jl:196-238.  Validates grid >= 2 and
+ * max > min (mesh.jl:206-211); delta = (max-min)/(n-1) (mesh.jl:220).
  * Allocates rho and efield (zeroed) on the current CUDA device. */
 int sc_mesh_create(const int32_t grid_size[3], const double min_bounds[3],
                    const double max_bounds[3], double gamma, double total_charge,
                    int precision, sc_mesh** out);
 
 /* The bounds arithmetic of the particle-bounds constructor, src/mesh.jl:
- * 133-177: validation, extrema (one device reduction + a 48-byte copy to
+ * 106-150: validation, extrema (one device reduction + a 48-byte copy to
  * the host, which synchronises `stream`), 1e-6*delta padding, delta
  * recomputation and the delta == 0 -> 1e-6 patch, all in FP64. */
 int sc_auto_bounds(const int32_t grid_size[3], const void* x, const void* y,
@@ -121,12 +121,12 @@ int sc_auto_bounds(const int32_t grid_size[3], const void* x, const void* y,
 
 /* The same bounds from extrema the caller already has (for instance reduced
  * over the ranks that each hold part of a bunch): the padding and delta
- * arithmetic of mesh.jl:152-177 on mins[3], maxs[3].  Host only. */
+ * arithmetic of mesh.jl:125-150 on mins[3], maxs[3].  Host only. */
 int sc_bounds_from_extrema(const int32_t grid_size[3], const double mins[3], const double maxs[3],
                            double min_bounds[3], double max_bounds[3], double delta[3]);
 
 /* Particle-bounds constructor: Mesh3D(grid_size, px, py, pz; T, gamma,
- * total_charge), src/mesh.jl:122-201.  Synchronises `stream`. */
+ * total_charge), src/mesh.jl:95-174.  Synchronises `stream`. */
 int sc_mesh_create_from_particles(const int32_t grid_size[3], const void* x,
                                   const void* y, const void* z, int64_t n, int dtype,
                                   double gamma, double total_charge, int precision,
@@ -138,12 +138,12 @@ int sc_mesh_destroy(sc_mesh* mesh);
 /* New bounds for an existing mesh, keeping its grid, fields and workspaces
  * (no counterpart in the reference, whose Mesh3D geometry is set once; a
  * tracking code there builds a new mesh per step).  The validation and delta
- * of the manual constructor (src/mesh.jl:233-247).  Cached Green spectra and
+ * of the manual constructor (src/mesh.jl:206-220).  Cached Green spectra and
  * captured kick graphs follow the new geometry on the next call. */
 int sc_mesh_set_bounds(sc_mesh* mesh, const double min_bounds[3], const double max_bounds[3]);
 
 /* The same with the particle constructor's bounds for x, y, z (sc_auto_bounds,
- * src/mesh.jl:122-201).  Synchronises `stream`. */
+ * src/mesh.jl:95-174).  Synchronises `stream`. */
 int sc_mesh_refit(sc_mesh* mesh, const void* x, const void* y, const void* z, int64_t n, int dtype,
                   void* stream);
 
@@ -272,13 +272,17 @@ int sc_kick_adjoint(sc_mesh* mesh, const void* x, const void* y, const void* z, 
  * the caller's rho (FP32, nx*ny*nz, x fastest) into the caller's efield
  * (FP32, packed (4, nx, ny, nz) = (Ex, Ey, Ez, 0) per node).  It calls no
  * cudaMalloc, cudaFree or allocating library routine: its workspace is one
- * file-scope device array of about 8.6 MB, which every GPU that loads the
- * library holds until exit.
+ * file-scope device array of about 8.6 MB.  The array is committed on a
+ * device when the library's kernels are loaded there (under CUDA's lazy
+ * module loading, the default, at the library's first call on that device)
+ * and is held until that device's context is destroyed.
  *  - Grids are limited to 32 nodes per axis; larger ones return
  *    SC_ERR_UNSUPPORTED with a message naming the limit.
- *  - The first call on a device looks up the array's device address and
- *    uploads an 8 KB twiddle table (synchronous); make that first call
- *    before any stream capture.
+ *  - The first call on a device uploads an 8 KB twiddle table into the
+ *    array (a synchronous copy); make that first call before any stream
+ *    capture.  Every call looks up the array's device address; after a
+ *    device reset the array has a new one and the next call uploads the
+ *    table again.
  *  - All calls on a device share the array and it keeps the last call's
  *    contents; calls that overlap on the GPU (other streams, other host
  *    threads) race and must be serialised by the caller. */
@@ -346,7 +350,7 @@ int sc_relative_to_absolute(const float* rx, const float* ry, const float* rz, i
 /* `steps` tracking steps of the bunch in its own field (the kick's caller
  * in a tracking code; no counterpart in the reference).  Each step: when
  * `refit`, new mesh bounds from the particles (the particle constructor's
- * arithmetic, mesh.jl:122-201; this synchronises), the kick, B = (beta/c)
+ * arithmetic, mesh.jl:95-174; this synchronises), the kick, B = (beta/c)
  * z x E, and one relativistic Boris step of the dimensionless momenta
  * u = gamma*beta and the positions over `dt` seconds for a species of
  * charge/mass `qm` [C/kg].  x, y, z, ux, uy, uz are updated in place on the

@@ -48,20 +48,20 @@ class OMesh:
 
 
 def _check_grid(grid_size):
-    # src/mesh.jl:133-135 and :233-235
+    # src/mesh.jl:106-108 and :206-208
     if any(int(g) <= 1 for g in grid_size):
         raise ValueError("All elements of grid_size must be at least 2.")
 
 
 def mesh_auto(grid_size, px, py, pz, T=np.float64, gamma=1.0, total_charge=0.0):
-    """Particle-bounds constructor, src/mesh.jl:122-201 (Float64 arithmetic)."""
+    """Particle-bounds constructor, src/mesh.jl:95-174 (Float64 arithmetic)."""
     _check_grid(grid_size)
     px, py, pz = (np.asarray(a) for a in (px, py, pz))
-    if px.size == 0 or py.size == 0 or pz.size == 0:  # :137-139
+    if px.size == 0 or py.size == 0 or pz.size == 0:  # :110-112
         raise ValueError("Particle arrays cannot be empty.")
-    if not (px.size == py.size == pz.size):  # :141-143
+    if not (px.size == py.size == pz.size):  # :114-116
         raise ValueError("Particle coordinate arrays must have the same length.")
-    # :147-149 extrema, then :152-169 in Float64 (the particle eltype promotes)
+    # :120-122 extrema, then :125-142 in Float64 (the particle eltype promotes)
     mins = [float(a.min()) for a in (px, py, pz)]
     maxs = [float(a.max()) for a in (px, py, pz)]
     n = [int(g) for g in grid_size]
@@ -69,19 +69,19 @@ def mesh_auto(grid_size, px, py, pz, T=np.float64, gamma=1.0, total_charge=0.0):
     lo = [mins[d] - 1e-6 * delta[d] for d in range(3)]
     hi = [maxs[d] + 1e-6 * delta[d] for d in range(3)]
     delta = [(hi[d] - lo[d]) / (n[d] - 1) for d in range(3)]
-    delta = [1e-6 if d == 0 else d for d in delta]  # :172-176
+    delta = [1e-6 if d == 0 else d for d in delta]  # :145-149
     return OMesh(grid_size, lo, hi, delta, gamma, total_charge, T)
 
 
 def mesh_manual(grid_size, min_bounds, max_bounds, T=np.float64, gamma=1.0, total_charge=0.0):
-    """Manual-bounds constructor, src/mesh.jl:223-265."""
+    """Manual-bounds constructor, src/mesh.jl:196-238."""
     _check_grid(grid_size)
-    if any(float(h) <= float(l) for l, h in zip(min_bounds, max_bounds)):  # :236-238
+    if any(float(h) <= float(l) for l, h in zip(min_bounds, max_bounds)):  # :209-211
         raise ValueError("max_bounds must be strictly greater than min_bounds for all dimensions.")
     Tt = np.dtype(T).type
     lo = [Tt(v) for v in min_bounds]
     hi = [Tt(v) for v in max_bounds]
-    delta = [(hi[d] - lo[d]) / Tt(int(grid_size[d]) - 1) for d in range(3)]  # :247
+    delta = [(hi[d] - lo[d]) / Tt(int(grid_size[d]) - 1) for d in range(3)]  # :220
     return OMesh(grid_size, lo, hi, delta, gamma, total_charge, T)
 
 
@@ -318,7 +318,7 @@ def boris_push(x, y, z, ux, uy, uz, ex, ey, ez, bx, by, dt, qm):
 
 def track(grid_size, x, y, z, ux, uy, uz, q, dt, qm, steps, gamma=1.0, at_cathode=False):
     """`steps` tracking steps of a bunch in its own field: refit a mesh to
-    the particles (the particle constructor, mesh.jl:122-201), kick, B from
+    the particles (the particle constructor, mesh.jl:95-174), kick, B from
     E, one Boris step.  Returns the final (x, y, z, ux, uy, uz)."""
     state = [np.array(a, dtype=np.float64) for a in (x, y, z, ux, uy, uz)]
     for _ in range(steps):

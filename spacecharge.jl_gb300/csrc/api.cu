@@ -182,7 +182,7 @@ void StageTimer::release() {
 
 static int check_grid(const int32_t* g) {
     if (!g) return fail(SC_ERR_INVALID, "grid_size is NULL");
-    // src/mesh.jl:133-135
+    // src/mesh.jl:106-108
     for (int d = 0; d < 3; ++d)
         if (g[d] <= 1) return fail(SC_ERR_INVALID, "All elements of grid_size must be at least 2.");
     return SC_OK;
@@ -599,12 +599,12 @@ int sc_mesh_create(const int32_t grid_size[3], const double min_bounds[3], const
                    double gamma, double total_charge, int precision, sc_mesh** out) {
     SC_TRY(check_grid(grid_size));
     if (!min_bounds || !max_bounds) return fail(SC_ERR_INVALID, "bounds are NULL");
-    // src/mesh.jl:236-238
+    // src/mesh.jl:209-211
     for (int d = 0; d < 3; ++d)
         if (!(max_bounds[d] > min_bounds[d]))
             return fail(SC_ERR_INVALID, "max_bounds must be strictly greater than min_bounds for all dimensions.");
     double delta[3];
-    for (int d = 0; d < 3; ++d) delta[d] = (max_bounds[d] - min_bounds[d]) / (double)(grid_size[d] - 1);  // :247
+    for (int d = 0; d < 3; ++d) delta[d] = (max_bounds[d] - min_bounds[d]) / (double)(grid_size[d] - 1);  // :220
     return mesh_alloc(grid_size, min_bounds, max_bounds, delta, gamma, total_charge, precision, out);
 }
 
@@ -612,7 +612,7 @@ int sc_auto_bounds(const int32_t grid_size[3], const void* x, const void* y, con
                    int dtype, double min_bounds[3], double max_bounds[3], double delta[3], void* stream) {
     SC_TRY(check_grid(grid_size));
     SC_TRY(check_dtype(dtype));
-    if (n <= 0 || !x || !y || !z) return fail(SC_ERR_INVALID, "Particle arrays cannot be empty.");  // :137-139
+    if (n <= 0 || !x || !y || !z) return fail(SC_ERR_INVALID, "Particle arrays cannot be empty.");  // :110-112
     double mins[3], maxs[3];
     SC_TRY(bounds_reduce(x, y, z, n, dtype, mins, maxs, (cudaStream_t)stream));
     return sc_bounds_from_extrema(grid_size, mins, maxs, min_bounds, max_bounds, delta);
@@ -625,7 +625,7 @@ int sc_bounds_from_extrema(const int32_t grid_size[3], const double mins[3], con
     for (int d = 0; d < 3; ++d)
         if (!isfinite(mins[d]) || !isfinite(maxs[d]))
             return fail(SC_ERR_INVALID, "particle coordinates must be finite");
-    // src/mesh.jl:152-177, Float64 throughout
+    // src/mesh.jl:125-150, Float64 throughout
     double dl[3], lo[3], hi[3];
     for (int d = 0; d < 3; ++d) dl[d] = (maxs[d] - mins[d]) / (double)(grid_size[d] - 1);
     for (int d = 0; d < 3; ++d) {
@@ -655,9 +655,9 @@ int sc_mesh_set_bounds(sc_mesh* m, const double min_bounds[3], const double max_
     if (!min_bounds || !max_bounds) return fail(SC_ERR_INVALID, "bounds are NULL");
     double delta[3];
     for (int d = 0; d < 3; ++d) {
-        if (!(max_bounds[d] > min_bounds[d]))  // src/mesh.jl:236-238
+        if (!(max_bounds[d] > min_bounds[d]))  // src/mesh.jl:209-211
             return fail(SC_ERR_INVALID, "max_bounds must be strictly greater than min_bounds for all dimensions.");
-        delta[d] = (max_bounds[d] - min_bounds[d]) / (double)(m->n[d] - 1);  // :247
+        delta[d] = (max_bounds[d] - min_bounds[d]) / (double)(m->n[d] - 1);  // :220
     }
     return mesh_set_geometry(m, min_bounds, max_bounds, delta);
 }

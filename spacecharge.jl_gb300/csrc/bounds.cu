@@ -1,5 +1,5 @@
 // extrema(particles_x/y/z) for the particle-bounds Mesh3D constructor
-// (src/mesh.jl:147-149): one device reduction, then a 48-byte copy to the
+// (src/mesh.jl:120-122): one device reduction, then a 48-byte copy to the
 // host (CUDA.jl's `extrema` on CuArrays does the same round trip).
 #include <atomic>
 #include <chrono>

@@ -1251,8 +1251,12 @@ constexpr size_t kNaBytes = kNaA + kNaB + kNaC + kNaD + kNaGoct + kNaGspec + kNa
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
-// Device address of the array for the current device, looked up (and the
-// twiddle table uploaded) on the first call on that device.
+// Device address of the array on the current device.  It is looked up on
+// every call (cheap once the module is loaded on the device) and compared
+// with the one seen last on that device: a new address means the array was
+// loaded again (a new primary context after cudaDeviceReset), so the
+// twiddle table is uploaded again.  The upload is a synchronous copy; it
+// happens on the first call on a device and after such a reload only.
 static std::mutex g_na_mu;
 static void* g_na_base[256] = {};
 
@@ -1260,11 +1264,11 @@ static int noalloc_base(unsigned char** out) {
     int dev = 0;
     SC_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 256) return fail(SC_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
     std::lock_guard<std::mutex> lk(g_na_mu);
-    if (!g_na_base[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    if (g_na_base[dev] != p) {
         float2 tw[kMaxL];
         for (int k = 0; k < kMaxL; ++k) {
             long double a = -2.0L * 3.141592653589793238462643383279502884L * (long double)k / (long double)kMaxL;
@@ -1275,7 +1279,7 @@ static int noalloc_base(unsigned char** out) {
         if (e != cudaSuccess) return cuda_fail(e, "twiddle upload");
         g_na_base[dev] = p;
     }
-    *out = (unsigned char*)g_na_base[dev];
+    *out = (unsigned char*)p;
     return SC_OK;
 }
 
@@ -1392,7 +1396,7 @@ int native_solve_noalloc(const int32_t* grid, const double* delta, double gamma,
         SC_LAUNCH_CHECK("k_col_fft");
     }
     {
-        GreenView gv;
+        GreenView gv{};
         gv.gfree = gfree;
         gv.gimg = nullptr;
         gv.Hx = Hx;

@@ -1,7 +1,7 @@
 // Tracking steps of a bunch in its own field (sc_track; no counterpart in the
 // reference, which stops at the kick).  Each step: optionally refit the mesh
 // bounds to the particles (the particle constructor's arithmetic,
-// mesh.jl:122-201), kick, B = (beta/c) z x E, and one relativistic Boris step
+// mesh.jl:95-174), kick, B = (beta/c) z x E, and one relativistic Boris step
 // (J. P. Boris 1970; Birdsall & Langdon section 15-4) of u = gamma*beta:
 //   u- = u + a E,  a = qm dt / (2c)
 //   t = qm dt / (2 gamma(u-)) B,  s = 2 t / (1 + |t|^2)

@@ -88,7 +88,7 @@ precision_code(::Type{Float64}, p) = p === :plain64 ? SC_PREC_PLAIN64 : SC_PREC_
 precision_code(::Type{Float32}, p) = SC_PREC_MIXED
 storage_type(code) = code == SC_PREC_MIXED ? Float32 : Float64
 
-# Mesh3D(grid_size, px, py, pz; T, gamma, total_charge), src/mesh.jl:122-201
+# Mesh3D(grid_size, px, py, pz; T, gamma, total_charge), src/mesh.jl:95-174
 function Mesh3D(grid_size::NTuple{3,Int}, particles_x::CuArray{P}, particles_y::CuArray{P},
                 particles_z::CuArray{P}; T::Type{<:AbstractFloat}=Float64, precision::Symbol=:native,
                 gamma::Real=1.0, total_charge::Real=0.0) where {P<:Union{Float32,Float64}}
@@ -105,7 +105,7 @@ function Mesh3D(grid_size::NTuple{3,Int}, particles_x::CuArray{P}, particles_y::
     return _wrap(out[], storage_type(code))
 end
 
-# Mesh3D(grid_size, min_bounds, max_bounds; T, gamma, total_charge), src/mesh.jl:223-265
+# Mesh3D(grid_size, min_bounds, max_bounds; T, gamma, total_charge), src/mesh.jl:196-238
 function Mesh3D(grid_size::NTuple{3,Int}, min_bounds::NTuple{3,Real}, max_bounds::NTuple{3,Real};
                 T::Type{<:AbstractFloat}=Float64, precision::Symbol=:native, gamma::Real=1.0,
                 total_charge::Real=0.0)
@@ -133,7 +133,7 @@ end
 
 New bounds for `mesh`, keeping its grid, fields and workspaces
 (sc_mesh_set_bounds; the manual constructor's validation and delta,
-src/mesh.jl:233-247).
+src/mesh.jl:206-220).
 """
 function set_bounds!(mesh::Mesh3D, min_bounds::NTuple{3,Real}, max_bounds::NTuple{3,Real})
     check(ccall((:sc_mesh_set_bounds, libsc), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}), mesh.ptr,
@@ -145,7 +145,7 @@ end
     refit!(mesh, px, py, pz)
 
 The particle constructor's bounds for these particles (sc_mesh_refit,
-src/mesh.jl:122-201).
+src/mesh.jl:95-174).
 """
 function refit!(mesh::Mesh3D, px::CuArray{P}, py::CuArray{P}, pz::CuArray{P}) where {P<:Union{Float32,Float64}}
     length(px) == length(py) == length(pz) || error("Particle coordinate arrays must have the same length.")
@@ -318,7 +318,7 @@ interpolate_field(mesh::Mesh3D, px::Vector{P}, py::Vector{P}, pz::Vector{P}) whe
 kick(mesh::Mesh3D, px::Vector{P}, py::Vector{P}, pz::Vector{P}, pq::Vector{P};
      at_cathode::Bool=false) where {P<:Union{Float32,Float64}} = kick_host(mesh, px, py, pz, pq; at_cathode=at_cathode)
 
-function Base.show(io::IO, mesh::Mesh3D{T}) where {T}  # src/mesh.jl:267-273
+function Base.show(io::IO, mesh::Mesh3D{T}) where {T}  # src/mesh.jl:240-246
     nx, ny, nz = mesh.grid_size
     lo, hi = mesh.min_bounds, mesh.max_bounds
     print(io, "Mesh3D{$T, CuArray} ($(nx)x$(ny)x$(nz)) bounds=[($(lo[1]),$(lo[2]),$(lo[3])), " *

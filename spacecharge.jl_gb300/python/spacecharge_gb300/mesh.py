@@ -86,7 +86,7 @@ class _Handle:
 
 class Mesh3D:
     """Mesh3D(grid_size, particles_x, particles_y, particles_z; ...) or
-    Mesh3D(grid_size, min_bounds, max_bounds; ...), src/mesh.jl:122-265.
+    Mesh3D(grid_size, min_bounds, max_bounds; ...), src/mesh.jl:95-238.
 
     Keywords: T (np.float64 -> precision "fp64", np.float32 -> "mixed"),
     precision ("plain64" = the reference algorithm in FP64 with cuFFT,
@@ -105,17 +105,17 @@ class Mesh3D:
         g = (C.c_int32 * 3)(*[int(v) for v in grid_size])
         out = C.c_void_p()
         prec = _PRECISIONS[precision]
-        if len(args) == 2:  # manual bounds, mesh.jl:223-265
+        if len(args) == 2:  # manual bounds, mesh.jl:196-238
             lo = (C.c_double * 3)(*[float(v) for v in args[0]])
             hi = (C.c_double * 3)(*[float(v) for v in args[1]])
             L.call("sc_mesh_create", g, lo, hi, float(gamma), float(total_charge), prec, C.byref(out))
-        elif len(args) == 3:  # particle bounds, mesh.jl:122-201
-            if any(int(v) <= 1 for v in grid_size):  # :133-135
+        elif len(args) == 3:  # particle bounds, mesh.jl:95-174
+            if any(int(v) <= 1 for v in grid_size):  # :106-108
                 raise SpaceChargeError("All elements of grid_size must be at least 2.")
             lens = [_length(a) for a in args]
-            if min(lens) == 0:  # :137-139
+            if min(lens) == 0:  # :110-112
                 raise SpaceChargeError("Particle arrays cannot be empty.")
-            if not (lens[0] == lens[1] == lens[2]):  # :141-143
+            if not (lens[0] == lens[1] == lens[2]):  # :114-116
                 raise SpaceChargeError("Particle coordinate arrays must have the same length.")
             (x, y, z), dt = _as_device(args)
             L.call("sc_mesh_create_from_particles", g, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
@@ -152,7 +152,7 @@ class Mesh3D:
 
     def refit(self, particles_x, particles_y, particles_z) -> None:
         """The particle constructor's bounds for these particles
-        (sc_mesh_refit, src/mesh.jl:122-201)."""
+        (sc_mesh_refit, src/mesh.jl:95-174)."""
         lens = [_length(a) for a in (particles_x, particles_y, particles_z)]
         if min(lens) == 0:
             raise SpaceChargeError("Particle arrays cannot be empty.")
@@ -226,7 +226,7 @@ class Mesh3D:
         L.call("sc_mesh_out_of_range", self._h.ptr, C.byref(n), _stream())
         return int(n.value)
 
-    def __repr__(self):  # mesh.jl:267-273
+    def __repr__(self):  # mesh.jl:240-246
         nx, ny, nz = self.grid_size
         lo, hi = self.min_bounds, self.max_bounds
         T = "Float32" if self.T == np.float32 else "Float64"

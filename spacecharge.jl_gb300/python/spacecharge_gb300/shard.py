@@ -33,7 +33,7 @@ def shard_bunches(counts: Sequence[int], world_size: int, rank: int) -> list[int
 
 
 def global_bounds(grid_size, x, y, z, group=None):
-    """Bounds of the particle constructor (mesh.jl:152-177) for a bunch whose
+    """Bounds of the particle constructor (mesh.jl:125-150) for a bunch whose
     particles are split over the ranks of `group`: this rank's extrema (its
     share may be empty), MIN/MAX all-reduced, then sc_bounds_from_extrema.
     Returns (min_bounds, max_bounds) as tuples."""
@@ -49,8 +49,10 @@ def global_bounds(grid_size, x, y, z, group=None):
             ext.append((float("inf"), float("-inf")))
         else:
             ext.append((float(t.min()), float(t.max())))
-    dev = x.device if isinstance(x, torch.Tensor) and dist.is_initialized() and \
-        dist.get_backend(group) == "nccl" else "cpu"
+    # NCCL reduces device tensors only, whatever container the particles came in
+    dev = "cpu"
+    if dist.is_initialized() and dist.get_backend(group) == "nccl":
+        dev = torch.device("cuda", torch.cuda.current_device())
     red = torch.tensor([e[0] for e in ext] + [-e[1] for e in ext], dtype=torch.float64, device=dev)
     if dist.is_initialized() and dist.get_world_size(group) > 1:
         dist.all_reduce(red, op=dist.ReduceOp.MIN, group=group)

@@ -43,7 +43,7 @@ def test_validation():  # test_mesh.jl:76-94
 def test_physics_params():  # test_mesh.jl:97-108
     m = O.mesh_auto((5, 5, 5), [0.0], [0.0], [0.0], gamma=2.0, total_charge=1.0)
     assert m.gamma == 2.0 and m.total_charge == 1.0
-    # single particle: span 0 -> delta patched to 1e-6 (mesh.jl:172-176)
+    # single particle: span 0 -> delta patched to 1e-6 (mesh.jl:145-149)
     assert m.delta == (1e-6, 1e-6, 1e-6) and m.min_bounds == (0.0, 0.0, 0.0)
 
 
