@@ -196,6 +196,9 @@ def bench_batch(sc, L, C, torch, flush, stream, ws, rank, steps, warmup):
     torch.cuda.synchronize()
     ms_batch = max_over_ranks(ev_time(lambda: batch.kick(xs, ys, zs, qs), steps), ws)
     nodes = batch.graph_nodes
+    # the batch's fields, kept for the comparison with the plain FP64 kicks below
+    bout = [[t.double().cpu() for t in o] for o in batch.kick(xs, ys, zs, qs)]
+    bmesh = [m.efield.double().cpu() for m in meshes]
 
     outs = [[torch.empty_like(d[0]) for _ in range(3)] for d in dev]
 
@@ -208,12 +211,21 @@ def bench_batch(sc, L, C, torch, flush, stream, ws, rank, steps, warmup):
     ms_seq = max_over_ranks(ev_time(seq_mixed, max(2, steps // 4)), ws)
     # plain FP64 path, one bunch at a time (meshes created and freed outside the timed region)
     ms_plain = 0.0
-    for (g, gm, *_), d, o in zip(spec, dev, outs):
+    err = {"mesh": [0.0, 0.0], "particles": [0.0, 0.0]}  # worst bunch: [max rel, RMS rel]
+
+    def worse(key, a, r):
+        e = (a - r).abs()
+        err[key][0] = max(err[key][0], float(e.max() / r.abs().max()))
+        err[key][1] = max(err[key][1], float(e.norm() / r.norm()))
+
+    for (g, gm, *_), d, o, bo, bm in zip(spec, dev, outs, bout, bmesh):
         mp = sc.Mesh3D(g, d[0], d[1], d[2], precision="plain64", gamma=gm)
         k = lambda: L.call("sc_kick", mp.ptr, *[C.c_void_p(t.data_ptr()) for t in d], d[0].numel(), L.SC_F64, 0,
                            *[C.c_void_p(t.data_ptr()) for t in o], C.c_void_p(stream.cuda_stream))
         k()
         ms_plain += ev_time(k, 1)
+        worse("mesh", bm, mp.efield.double().cpu())
+        worse("particles", torch.stack(bo), torch.stack([t.cpu() for t in o]))
         del mp
     ms_plain = max_over_ranks(ms_plain, ws)
     npart = sum(len(s[2]) for s in spec)
@@ -222,6 +234,8 @@ def bench_batch(sc, L, C, torch, flush, stream, ws, rank, steps, warmup):
             "grids": sorted({str(s[0]) for s in spec}), "ms_batched_graph": round(ms_batch, 3),
             "ms_sequential_mixed": round(ms_seq, 3), "ms_sequential_fp64_plain": round(ms_plain, 3),
             "speedup_vs_fp64_plain": round(ms_plain / ms_batch, 2), "graph_nodes": nodes,
+            "max_rel_err_vs_fp64": {k: v[0] for k, v in err.items()},
+            "rms_rel_err_vs_fp64": {k: v[1] for k, v in err.items()},
             "green": "cached per bunch (fixed geometry)", "l2": "flushed between calls"}
 
 

@@ -31,13 +31,15 @@ def rel(a, b):
     return np.abs(a - b).max() / np.abs(b).max()
 
 
+# the second size is the differentiation workload's own autograd check:
+# 10,000 particles on a 16^3 mesh
+@pytest.mark.parametrize("n,grid", [(2000, (12, 10, 14)), (10000, (16, 16, 16))])
 @pytest.mark.parametrize("at_cathode", [False, True])
-def test_adjoint_vs_torch_autograd(sc, cuda, at_cathode):
+def test_adjoint_vs_torch_autograd(sc, cuda, at_cathode, n, grid):
     import torch
 
     from oracle import torch_twin
 
-    n, grid = 2000, (12, 10, 14)
     x, y, z = bunch(n, 1)
     if at_cathode:
         z = np.abs(z) + 0.3e-3

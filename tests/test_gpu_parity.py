@@ -86,6 +86,70 @@ def test_kick_parity(sc, cuda, prec, grid, gamma):
 
 
 @pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("grid,gamma,sig,cath", [
+    ((16, 16, 24), 50.0, (0.4e-3, 0.4e-3, 2e-3), False),    # boosted cells ~160 x longer than wide
+    ((32, 32, 32), 50.0, (0.2e-3, 0.2e-3, 2e-3), False),    # ~500: the most elongated bunch of 64 uneven ones
+    ((16, 16, 24), 50.0, (0.3e-3, 0.3e-3, 2e-3), True),     # ~110, with the cathode image
+    ((16, 16, 24), 1.0, (2e-3, 2e-3, 0.02e-3), False),      # flat cells, ~1/150
+])
+def test_kick_parity_elongated_cells(sc, cuda, prec, grid, gamma, sig, cath):
+    """Cells far from cubic in the rest frame (dz_boosted / dx = gamma *
+    delta_z / delta_x), where the mixed Green build's near box and its
+    quadrature orders see the most stretched cells (the gamma-stretched dz of
+    green_functions.jl:73).
+
+    The reference's own FP64 arithmetic is noisy here: its corner
+    differences of the antiderivative cancel catastrophically on needle-like
+    cells, so one ulp in F moves the field by up to ~2e-9 of its maximum
+    (measured below against a long-double Green function).  The FP64 paths
+    (plain64 is the reference algorithm) evaluate the same expressions with
+    the GPU's libm, so they are held to 3x that floor where it exceeds 1e-10;
+    the mixed path keeps 1e-5."""
+    n = 6000
+    x, y, z = bunch(n, 13, sig=sig)
+    if cath:
+        z = np.abs(z) + 0.2e-3
+    q = np.full(n, 1e-9 / n)
+    om, m, rho, oe, e = run_both(sc, grid, (x, y, z, q), prec, gamma=gamma, at_cathode=cath)
+    ratio = gamma * m.delta[2] / m.delta[0]
+    assert ratio > 90 or ratio < 0.01
+    tol = TOL[prec]
+    if prec != "mixed":
+        tol = max(tol, 3 * fp64_rounding_floor(om, cath))
+    assert relerr(host(m.efield), om.efield) < tol
+    for a, b in zip(e, oe):
+        assert relerr(a, b) < tol
+
+
+def fp64_rounding_floor(om, at_cathode):
+    """max |dE| / max |E| where dE is the change of the oracle's mesh field
+    when its Green function (src/green_functions.jl:69-112) is evaluated in
+    long double instead of FP64: the FP64 rounding noise of the reference
+    algorithm on this geometry (the convolution is linear, so dE is the
+    field of rho convolved with G64 - Glong)."""
+    import scipy.fft as sfft
+
+    nx, ny, nz = om.grid_size
+    shape = (2 * nx, 2 * ny, 2 * nz)
+    dE = np.zeros(om.grid_size + (3,))
+    passes = [((0.0, 0.0, 0.0), om.rho)]
+    if at_cathode:  # src/solvers/free_space.jl:34-45
+        offz = 2 * om.min_bounds[2] + (om.max_bounds[2] - om.min_bounds[2])
+        passes.append(((0.0, 0.0, offz), -om.rho[:, :, ::-1]))
+    for off, rho in passes:
+        crho = np.zeros(shape, complex)
+        crho[:nx, :ny, :nz] = rho
+        crho = sfft.fftn(crho)
+        for c in (1, 2, 3):
+            with np.errstate(all="ignore"):
+                g64 = O.green_function(shape, om.delta, om.gamma, c, off, np.float64)
+                glong = O.green_function(shape, om.delta, om.gamma, c, off, np.longdouble).astype(np.float64)
+            t = sfft.ifftn(crho * sfft.fftn(np.nan_to_num(g64 - glong)))
+            dE[..., c - 1] += O.FPEI * np.real(t[nx - 1:2 * nx - 1, ny - 1:2 * ny - 1, nz - 1:2 * nz - 1])
+    return np.abs(dE).max() / np.abs(om.efield).max()
+
+
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("grid,cath", [((12, 12, 160), False), ((150, 10, 12), True), ((8, 140, 9), False)])
 def test_long_axis_parity(sc, cuda, prec, grid, cath):
     """Axes of more than 128 nodes: transforms of 512 points, where the
