@@ -31,26 +31,24 @@ constexpr int kColW = 16;  // columns per CTA of the column passes
 // out may alias (each CTA reads all of its columns before writing them).
 __device__ __forceinline__ int wrap_row2(int c, int n, int L) { return c < n ? c : L - (2 * n - 1) + c; }
 
+// Body of one CTA: column tile `tile` of component `comp`; xb holds kColW
+// exchange columns.
 template <int L, bool INV>
-__global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k2_col(const float2* in, float2* out, int ncols, int nbatch,
-                                                            int n_valid, int n_store, int wrap, int bwrap_n, int bwrap_L,
-                                                            int64_t as_in, int64_t bs_in, int64_t cs_in,
-                                                            int64_t as_out, int64_t bs_out, int64_t cs_out,
-                                                            const float2* __restrict__ tw) {
+__device__ __forceinline__ void col_body(const float2* in, float2* out, int ncols, int nbatch, int n_valid,
+                                         int n_store, int wrap, int bwrap_n, int bwrap_L, int64_t as_in,
+                                         int64_t bs_in, int64_t cs_in, int64_t as_out, int64_t bs_out,
+                                         int64_t cs_out, int64_t tile, int comp, const float2* swt, float2* xb) {
     using E = F2<L>;
-    __shared__ float2 swt[L];
-    stage_twiddles<L>(swt, tw);
-    __shared__ float2 xb[kColW * E::S];
     // columns of all batches flattened: f = col + ncols * batch (a tile may
     // straddle two batches: two contiguous segments)
     const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
-    const int64_t f = (int64_t)blockIdx.x * kColW + c;
+    const int64_t f = tile * kColW + c;
     const bool cok = f < (int64_t)ncols * nbatch;
     const int bb = cok ? (int)(f / ncols) : 0;
     const int col = (int)(f - (int64_t)bb * ncols);
     const int b = bwrap_n > 0 ? wrap_row2(bb, bwrap_n, bwrap_L) : bb;
-    const float2* src = in + b * bs_in + blockIdx.y * cs_in + col;
-    float2* dst = out + b * bs_out + blockIdx.y * cs_out + col;
+    const float2* src = in + b * bs_in + comp * cs_in + col;
+    float2* dst = out + b * bs_out + comp * cs_out + col;
     float2 v[16];
     if (!INV) {
         if (t < E::R2) {
@@ -85,27 +83,34 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k2_col(const f
     }
 }
 
+template <int L, bool INV>
+__global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k2_col(const float2* in, float2* out, int ncols, int nbatch,
+                                                            int n_valid, int n_store, int wrap, int bwrap_n, int bwrap_L,
+                                                            int64_t as_in, int64_t bs_in, int64_t cs_in,
+                                                            int64_t as_out, int64_t bs_out, int64_t cs_out,
+                                                            const float2* __restrict__ tw) {
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
+    __shared__ float2 xb[kColW * F2<L>::S];
+    col_body<L, INV>(in, out, ncols, nbatch, n_valid, n_store, wrap, bwrap_n, bwrap_L, as_in, bs_in, cs_in, as_out,
+                     bs_out, cs_out, blockIdx.x, blockIdx.y, swt, xb);
+}
+
 // Inverse y and x fused, one CTA per (z plane, component), Lx = Ly = L: the
 // plane's Hx columns are inverse-transformed along y (the outputs y < ny stay
 // in shared memory), then its rows, two per complex IFFT, along x into the
 // component's lane of the packed float4 nodes.  Replaces inverse y + inverse
 // x when the plane fits in shared memory; the intermediate D never goes to
 // global memory.
-// blockIdx.y = c reads component c of C and writes lane lane0 + c of the
-// nodes (the adjoint's rhobar: one component into lane 3).
+// Body of one CTA: Cp is the (component, z plane) of C, `out` the plane's
+// first node lane to write (stride 4 floats per node).
 template <int L>
-__global__ void __launch_bounds__(256) k2_inv_yx(const float2* __restrict__ C, float* __restrict__ E4, int nx,
-                                                 int ny, int nz, int Hx, int lane0, const float2* __restrict__ tw) {
+__device__ __forceinline__ void inv_yx_body(const float2* __restrict__ Cp, float* __restrict__ out, int nx, int ny,
+                                            int Hx, const float2* swt, unsigned char* smraw) {
     using E = F2<L>;
     constexpr int W = 256 / E::NT;  // columns (phase 1) or row pairs (phase 2) per round
-    __shared__ float2 swt[L];
-    stage_twiddles<L>(swt, tw);
-    extern __shared__ __align__(16) unsigned char smraw[];
     float2* xb = reinterpret_cast<float2*>(smraw);  // W exchange columns
     float2* ds = xb + W * E::S;                     // [ny][Hx]: the plane after inverse y
-    const int z = blockIdx.x, comp = blockIdx.y;
-    const int64_t plane = (int64_t)Hx * L;
-    const float2* Cp = C + (int64_t)comp * plane * nz + plane * z;
     float2 v[16];
     // phase 1: inverse y of the Hx columns (column-fastest thread map)
     {
@@ -133,7 +138,6 @@ __global__ void __launch_bounds__(256) k2_inv_yx(const float2* __restrict__ C, f
     {
         const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
         float2* col = xb + p * E::S;
-        float* out = E4 + lane0 + comp;
         for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
             const int y0 = 2 * (q0 + p), y1 = y0 + 1;
             if (t < E::R1) {
@@ -158,7 +162,7 @@ __global__ void __launch_bounds__(256) k2_inv_yx(const float2* __restrict__ C, f
                 for (int s = 0; s < E::R1; ++s) {
                     const int x = t + E::R2 * s;
                     if (x >= nx) continue;
-                    const int64_t node = x + (int64_t)nx * (y0 + (int64_t)ny * z);
+                    const int64_t node = x + (int64_t)nx * y0;
                     if (y0 < ny) out[4 * node] = v[s].x;
                     if (y1 < ny) out[4 * (node + nx)] = v[s].y;
                 }
@@ -167,17 +171,30 @@ __global__ void __launch_bounds__(256) k2_inv_yx(const float2* __restrict__ C, f
     }
 }
 
-// x pass: two real rows per complex FFT -> their half spectra.
+// blockIdx.x = z plane; blockIdx.y = c reads component c of C and writes
+// lane lane0 + c of the nodes (the adjoint's rhobar: one component into
+// lane 3).
 template <int L>
-__global__ void __launch_bounds__(256) k2_fwd_x(const float* __restrict__ rho, float2* __restrict__ A, int nx,
-                                                int rows, int Hx, const float2* __restrict__ tw) {
-    using E = F2<L>;
+__global__ void __launch_bounds__(256) k2_inv_yx(const float2* __restrict__ C, float* __restrict__ E4, int nx,
+                                                 int ny, int nz, int Hx, int lane0, const float2* __restrict__ tw) {
     __shared__ float2 swt[L];
     stage_twiddles<L>(swt, tw);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int z = blockIdx.x, comp = blockIdx.y;
+    const int64_t plane = (int64_t)Hx * L;
+    inv_yx_body<L>(C + (int64_t)comp * plane * nz + plane * z, E4 + lane0 + comp + 4 * (int64_t)nx * ny * z, nx, ny,
+                   Hx, swt, smraw);
+}
+
+// x pass: two real rows per complex FFT -> their half spectra.
+// Body of one CTA: row pairs blk * P + ...; xb holds P exchange columns.
+template <int L>
+__device__ __forceinline__ void fwd_x_body(const float* __restrict__ rho, float2* __restrict__ A, int nx, int rows,
+                                           int Hx, int blk, const float2* swt, float2* xb) {
+    using E = F2<L>;
     constexpr int P = 256 / E::NT;  // row pairs per CTA
-    __shared__ float2 xb[P * E::S];
     const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
-    const int r0 = 2 * (blockIdx.x * P + p), r1 = r0 + 1;
+    const int r0 = 2 * (blk * P + p), r1 = r0 + 1;
     float2* col = xb + p * E::S;
     float2 v[16];
     if (t < E::R2) {
@@ -208,31 +225,35 @@ __global__ void __launch_bounds__(256) k2_fwd_x(const float* __restrict__ rho, f
     }
 }
 
+template <int L>
+__global__ void __launch_bounds__(256) k2_fwd_x(const float* __restrict__ rho, float2* __restrict__ A, int nx,
+                                                int rows, int Hx, const float2* __restrict__ tw) {
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
+    __shared__ float2 xb[(256 / F2<L>::NT) * F2<L>::S];
+    fwd_x_body<L>(rho, A, nx, rows, Hx, blockIdx.x, swt, xb);
+}
+
 // Forward x and y fused, one CTA per z plane, Lx = Ly = L: the plane's rows,
 // two per complex FFT, into their half spectra in shared memory (as
 // k2_fwd_x), then the Hx columns along y (as the forward k2_col: inputs
 // y < ny, all L outputs) into B[kx + Hx*(ky + L*z)].  Replaces those two
 // passes when the plane fits in shared memory; the x pass's output never
-// goes to global memory.  blockIdx.y selects a component: input rho + y *
-// in_cs, output B + y * out_cs.
+// goes to global memory.
+// Body of one CTA: rz is the z plane of rho (ny rows of nx), Bz the plane
+// of B (L rows of Hx).
 template <int L>
-__global__ void __launch_bounds__(256) k2_fwd_xy(const float* __restrict__ rho, float2* __restrict__ B, int nx,
-                                                 int ny, int Hx, int64_t in_cs, int64_t out_cs,
-                                                 const float2* __restrict__ tw) {
+__device__ __forceinline__ void fwd_xy_body(const float* __restrict__ rz, float2* __restrict__ Bz, int nx, int ny,
+                                            int Hx, const float2* swt, unsigned char* smraw) {
     using E = F2<L>;
     constexpr int W = 256 / E::NT;  // row pairs (x pass) or columns (y pass) per round
-    __shared__ float2 swt[L];
-    stage_twiddles<L>(swt, tw);
-    extern __shared__ __align__(16) unsigned char smraw[];
     float2* xb = reinterpret_cast<float2*>(smraw);  // W exchange columns
     float2* ds = xb + W * E::S;                     // [ny][Hx]: the plane after the x pass
-    const int z = blockIdx.x;
     float2 v[16];
     // x pass: rows y0, y1 = y0 + 1 (row-pair-fastest thread map)
     {
         const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
         float2* col = xb + p * E::S;
-        const float* rz = rho + blockIdx.y * in_cs + (int64_t)nx * ny * z;
         for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
             const int y0 = 2 * (q0 + p), y1 = y0 + 1;
             if (t < E::R2) {
@@ -268,7 +289,6 @@ __global__ void __launch_bounds__(256) k2_fwd_xy(const float* __restrict__ rho, 
     {
         const int c = threadIdx.x % W, t = threadIdx.x / W;
         float2* col = xb + c * E::S;
-        float2* Bz = B + blockIdx.y * out_cs + (int64_t)Hx * L * z;
         for (int k0 = 0; k0 < Hx; k0 += W) {
             const int kx = k0 + c;
             const bool ok = kx < Hx;
@@ -286,6 +306,20 @@ __global__ void __launch_bounds__(256) k2_fwd_xy(const float* __restrict__ rho, 
             }
         }
     }
+}
+
+// blockIdx.x = z plane; blockIdx.y selects a component: input rho + y *
+// in_cs, output B + y * out_cs.
+template <int L>
+__global__ void __launch_bounds__(256) k2_fwd_xy(const float* __restrict__ rho, float2* __restrict__ B, int nx,
+                                                 int ny, int Hx, int64_t in_cs, int64_t out_cs,
+                                                 const float2* __restrict__ tw) {
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int z = blockIdx.x;
+    fwd_xy_body<L>(rho + blockIdx.y * in_cs + (int64_t)nx * ny * z, B + blockIdx.y * out_cs + (int64_t)Hx * L * z,
+                   nx, ny, Hx, swt, smraw);
 }
 
 // Inverse x pass of the three components, two rows per complex IFFT, packed
@@ -361,12 +395,12 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // shared memory asynchronously; cp_async_wait_all + a barrier before use.
 // blockDim.x is a multiple of kColW, so each thread keeps one column.
 template <int L>
-__device__ __forceinline__ void prefetch_green(float* gsm, const GreenView& gv, int Hx, int Ly) {
+__device__ __forceinline__ void prefetch_green(float* gsm, const GreenView& gv, int Hx, int Ly, int tile) {
     constexpr int HZ = L / 2 + 1;
     const int64_t plane = (int64_t)Hx * Ly;
     const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
     const int cc = threadIdx.x % kColW;
-    const int ff = blockIdx.x * kColW + cc;
+    const int ff = tile * kColW + cc;
     if (ff < plane) {
         const int kyy = ff / Hx, kxx = ff - kyy * Hx;
         const int kyf = kyy <= Ly / 2 ? kyy : Ly - kyy;
@@ -383,12 +417,12 @@ __device__ __forceinline__ void prefetch_green(float* gsm, const GreenView& gv, 
 // columns, gim[kz][column] for kz <= L/2, to shared memory asynchronously
 // (img_half layout; img_smem_at rebuilds kz > L/2).
 template <int L>
-__device__ __forceinline__ void prefetch_img(float2* gim, const GreenView& gv, int comp, int Hx, int Ly) {
+__device__ __forceinline__ void prefetch_img(float2* gim, const GreenView& gv, int comp, int Hx, int Ly, int tile) {
     constexpr int HZ = L / 2 + 1;
     const int64_t plane = (int64_t)Hx * Ly;
     const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
     const int cc = threadIdx.x % kColW;
-    const int ff = blockIdx.x * kColW + cc;
+    const int ff = tile * kColW + cc;
     if (ff < plane) {
         const int kyy = ff / Hx, kxx = ff - kyy * Hx;
         const int kyf = kyy <= Ly / 2 ? kyy : Ly - kyy;
@@ -416,14 +450,13 @@ __device__ __forceinline__ float2 img_smem_at(const float2* gim, int kz, int c, 
 // transforms, z < nz stored.  The tile's free-space Green values (3 x
 // (L/2+1) x kColW floats) are copied to shared memory asynchronously at the
 // start, so their L2 latency overlaps the forward transform.
+// Body of one CTA: `tile` is the CTA's column tile (kColW consecutive
+// columns of the flattened (kx, ky) plane).
 template <int L>
-__global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(const float2* __restrict__ B,
-                                                                 float2* __restrict__ C, int Hx, int Ly, int nz,
-                                                                 GreenView gv, const float2* __restrict__ tw) {
+__device__ __forceinline__ void zpass_body(const float2* __restrict__ B, float2* __restrict__ C, int Hx, int Ly,
+                                           int nz, const GreenView& gv, int tile, const float2* swt,
+                                           unsigned char* smraw) {
     using E = F2<L>;
-    __shared__ float2 swt[L];
-    stage_twiddles<L>(swt, tw);
-    extern __shared__ __align__(16) unsigned char smraw[];
     float2* xb = reinterpret_cast<float2*>(smraw);
     float2* spec = xb + kColW * E::S;  // natural-order spectrum of this tile's columns
     constexpr int HZ = L / 2 + 1;
@@ -435,10 +468,10 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(con
     // columns are the (kx, ky) plane flattened: f = kx + Hx*ky is contiguous
     const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
     const int64_t plane = (int64_t)Hx * Ly;
-    prefetch_green<L>(gsm, gv, Hx, Ly);
-    if (img_smem) prefetch_img<L>(gim, gv, 0, Hx, Ly);
+    prefetch_green<L>(gsm, gv, Hx, Ly, tile);
+    if (img_smem) prefetch_img<L>(gim, gv, 0, Hx, Ly, tile);
     const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
-    const int f = blockIdx.x * kColW + c;
+    const int f = tile * kColW + c;
     const bool cok = f < plane;
     const int ky = cok ? f / Hx : 0;
     const int kx = f - ky * Hx;
@@ -495,7 +528,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(con
         }
         if (img_smem && comp < 2) {
             __syncthreads();  // every thread is done with this component's copy
-            prefetch_img<L>(gim, gv, comp + 1, Hx, Ly);
+            prefetch_img<L>(gim, gv, comp + 1, Hx, Ly, tile);
         }
         E::template inv<true>(v, col, t, swt);
         if (t < E::R2 && cok) {
@@ -507,6 +540,16 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(con
             }
         }
     }
+}
+
+template <int L>
+__global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(const float2* __restrict__ B,
+                                                                 float2* __restrict__ C, int Hx, int Ly, int nz,
+                                                                 GreenView gv, const float2* __restrict__ tw) {
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    zpass_body<L>(B, C, Hx, Ly, nz, gv, blockIdx.x, swt, smraw);
 }
 
 // Adjoint z pass: three forward z transforms of Ebar_c, correlation with the
@@ -531,7 +574,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass
     float2* sc = spec + c * E::S;
     constexpr int HZ = L / 2 + 1;
     float* gsm = reinterpret_cast<float*>(spec + kColW * E::S);  // [3][HZ][kColW]
-    prefetch_green<L>(gsm, gv, Hx, Ly);
+    prefetch_green<L>(gsm, gv, Hx, Ly, blockIdx.x);
     const int kyf = ky <= Ly / 2 ? ky : Ly - ky;
     const float ysign = ky <= Ly / 2 ? 1.f : -1.f;
     const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
