@@ -291,21 +291,59 @@ int sc_solve_noalloc(const int32_t grid_size[3], const double delta[3], double g
 
 /* ---- many bunches: one call for their kicks, replayed as a CUDA graph ----
  * No counterpart in the reference (a tracking code calls its kick once per
- * bunch).  A batch references caller-owned meshes (SC_PREC_FP64 or MIXED,
- * all on the current device; each with its own grid, bounds and gamma).
- * sc_batch_kick runs every bunch's deposit -> solve -> interpolate with
- * bunch i on internal stream i % nstreams, forked from and joined back into
- * `stream`.  The first call with a given set of pointers, counts, dtype,
- * at_cathode and stream runs eagerly (allocating workspaces and building
- * Green spectra) and captures the same work into a CUDA graph; later calls
- * with identical arguments replay the graph in one launch.  Meshes must not
- * be destroyed while their batch exists. */
+ * bunch: benchmark/full_pipeline_benchmark.jl:64-71 times one at a time).
+ * A batch references caller-owned meshes (SC_PREC_FP64 or MIXED, all on
+ * the current device; each with its own grid, bounds and gamma).
+ *  - Staged engine (default).  Bunches on SC_PREC_MIXED meshes with
+ *    transforms of at most 256 points, Lx = Ly, and deposit mode
+ *    SC_DEPOSIT_VECTOR or SC_DEPOSIT_ATOMIC are kicked stage by stage in
+ *    groups (sc_batch_set_group_bytes): per group, on one internal stream,
+ *    one launch clears its bunches' charge buffers, one deposits them, one
+ *    sums the corner slots, one or two run the forward x+y transforms
+ *    (sc_batch_set_fused_forward), one the z pass with the Green multiply,
+ *    one the inverse y+x pass and one the gather.  A vector-mode bunch with
+ *    fewer particles than a quarter of its nodes deposits with scalar
+ *    atomics instead.
+ *  - The other bunches run their whole kick on internal stream
+ *    i % nstreams, beside the groups.
+ *  - The first call with a given set of pointers, counts, dtype and
+ *    at_cathode plans the groups (synchronising `stream` once, allocating
+ *    workspaces, building Green spectra, uploading the per-bunch tables),
+ *    runs eagerly, and captures the same work into a CUDA graph; later
+ *    calls with identical arguments replay the graph in one launch.  A
+ *    planning call must not be issued while `stream` is being captured.
+ *  - Meshes must not be destroyed while their batch exists. */
 typedef struct sc_batch sc_batch;
 int sc_batch_create(sc_mesh* const* meshes, int nbunch, int nstreams, sc_batch** out);
 int sc_batch_kick(sc_batch* batch, const void* const* x, const void* const* y, const void* const* z,
                   const void* const* q, const int64_t* n, int dtype, int at_cathode, void* const* ex,
                   void* const* ey, void* const* ez, void* stream);
 int sc_batch_set_graph(sc_batch* batch, int enabled); /* default 1 */
+/* 0: every bunch on the per-bunch stream path (the staged engine off);
+ * default 1. */
+int sc_batch_set_staged(sc_batch* batch, int enabled);
+/* Staged bunches are kicked in groups: consecutive bunches of one grid
+ * class whose fields, charge buffers and transform intermediates together
+ * take at most `bytes` (0: every bunch on its own, INT64_MAX: one group per
+ * class).  Group g is one chain of stage launches on internal stream
+ * g % nstreams, so a small budget keeps a group's data in L2 between its
+ * stages and a large one saves launches.  The next kick plans anew. */
+int sc_batch_set_group_bytes(sc_batch* batch, int64_t bytes);
+/* 1: the staged forward x and y transforms as one fused pass per z plane;
+ * 0: as an x pass and a y pass. */
+int sc_batch_set_fused_forward(sc_batch* batch, int enabled);
+/* Times graph replays of these kick arguments for group budgets of 0,
+ * 48 MB, 128 MB, 512 MB and unbounded, each with the fused and the two-pass
+ * forward transform, keeps the fastest for this batch and returns it in
+ * *group_bytes and *fused_forward (either may be NULL).  Synchronising; the
+ * arguments are sc_batch_kick's and are kicked 50 times. */
+int sc_batch_autotune(sc_batch* batch, const void* const* x, const void* const* y, const void* const* z,
+                      const void* const* q, const int64_t* n, int dtype, int at_cathode, void* const* ex,
+                      void* const* ey, void* const* ez, void* stream, int64_t* group_bytes,
+                      int* fused_forward);
+/* Bunches the current plan kicks stage by stage, and the kernel launches
+ * of those stages per kick (0 before the first kick). */
+int sc_batch_staged_count(const sc_batch* batch, int* staged, int64_t* launches);
 int sc_batch_graph_nodes(const sc_batch* batch, int64_t* count);
 int sc_batch_destroy(sc_batch* batch);
 

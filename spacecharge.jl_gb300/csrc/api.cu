@@ -312,7 +312,7 @@ struct KickGraph {
     int64_t launches = 0;       // kernels one replay runs
 };
 
-void mesh_state_key(const sc_mesh* m, std::vector<int64_t>& k) {
+void mesh_state_key(const sc_mesh* m, std::vector<int64_t>& k, bool with_epoch) {
     k.push_back(m->green_cache);
     k.push_back(m->kick_mode);
     k.push_back(fft_engine());
@@ -325,7 +325,7 @@ void mesh_state_key(const sc_mesh* m, std::vector<int64_t>& k) {
         memcpy(&b, &v, sizeof b);
         k.push_back(b);
     }
-    k.push_back(m->green_epoch);
+    if (with_epoch) k.push_back(m->green_epoch);
     k.push_back(alloc_generation());
 }
 

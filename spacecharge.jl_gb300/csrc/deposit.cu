@@ -8,6 +8,7 @@
 //   particles per thread with their loads in flight together, 8 atomics each.
 // deposit_vector: mixed meshes; 2 vector atomics per particle into per-cell
 //   corner slots, then a pass that sums each node's 8 slots.
+#include "batch.cuh"
 #include "cells.cuh"
 #include "sc_internal.cuh"
 
@@ -83,12 +84,13 @@ struct CellCalc<double> {
 #endif
 constexpr int kDepPerThread = SC_DEP_PT;
 
+// Body of one CTA: particles blk * 256 * kDepPerThread + ... of the bunch.
 template <typename P, typename A>
-__global__ void __launch_bounds__(256) deposit_atomic(const P* __restrict__ px, const P* __restrict__ py,
-                                                      const P* __restrict__ pz, const P* __restrict__ pq,
-                                                      int64_t n, Axes ax, A* __restrict__ rho,
-                                                      unsigned long long* __restrict__ oob) {
-    const int64_t base = (int64_t)blockIdx.x * (blockDim.x * kDepPerThread) + threadIdx.x;
+__device__ __forceinline__ void deposit_atomic_body(const P* __restrict__ px, const P* __restrict__ py,
+                                                    const P* __restrict__ pz, const P* __restrict__ pq, int64_t n,
+                                                    const Axes& ax, A* __restrict__ rho,
+                                                    unsigned long long* __restrict__ oob, int64_t blk) {
+    const int64_t base = blk * (blockDim.x * kDepPerThread) + threadIdx.x;
     P x[kDepPerThread], y[kDepPerThread], z[kDepPerThread], qq[kDepPerThread];
 #pragma unroll
     for (int k = 0; k < kDepPerThread; ++k) {
@@ -130,6 +132,14 @@ __global__ void __launch_bounds__(256) deposit_atomic(const P* __restrict__ px, 
     if (skipped) atomicAdd(oob, (unsigned long long)skipped);
 }
 
+template <typename P, typename A>
+__global__ void __launch_bounds__(256) deposit_atomic(const P* __restrict__ px, const P* __restrict__ py,
+                                                      const P* __restrict__ pz, const P* __restrict__ pq,
+                                                      int64_t n, Axes ax, A* __restrict__ rho,
+                                                      unsigned long long* __restrict__ oob) {
+    deposit_atomic_body<P, A>(px, py, pz, pq, n, ax, rho, oob, blockIdx.x);
+}
+
 // ------------------------------------------------ vector (mixed meshes)
 // The 8 CIC weights of a particle in cell c = (ix, iy, iz) go with two 16-byte
 // vector atomics into corner[8c .. 8c+7]: the 4 nodes of the cell's lower z
@@ -139,11 +149,11 @@ __global__ void __launch_bounds__(256) deposit_atomic(const P* __restrict__ px, 
 // around it hold for it.  Cells with an index n-1 are never written and stay
 // zero from the clear.
 template <typename P>
-__global__ void __launch_bounds__(256) deposit_vector(const P* __restrict__ px, const P* __restrict__ py,
-                                                      const P* __restrict__ pz, const P* __restrict__ pq,
-                                                      int64_t n, Axes ax, float4* __restrict__ corner,
-                                                      unsigned long long* __restrict__ oob) {
-    const int64_t base = (int64_t)blockIdx.x * (blockDim.x * kDepPerThread) + threadIdx.x;
+__device__ __forceinline__ void deposit_vector_body(const P* __restrict__ px, const P* __restrict__ py,
+                                                    const P* __restrict__ pz, const P* __restrict__ pq, int64_t n,
+                                                    const Axes& ax, float4* __restrict__ corner,
+                                                    unsigned long long* __restrict__ oob, int64_t blk) {
+    const int64_t base = blk * (blockDim.x * kDepPerThread) + threadIdx.x;
     P x[kDepPerThread], y[kDepPerThread], z[kDepPerThread], qq[kDepPerThread];
 #pragma unroll
     for (int k = 0; k < kDepPerThread; ++k) {
@@ -179,10 +189,17 @@ __global__ void __launch_bounds__(256) deposit_vector(const P* __restrict__ px, 
     if (skipped) atomicAdd(oob, (unsigned long long)skipped);
 }
 
-__global__ void __launch_bounds__(256) k_corner_sum(const float* __restrict__ corner, int nx, int ny, int64_t N,
-                                                    float* __restrict__ rho, int assign) {
-    pdl_wait();  // the corner slots come from the preceding deposit
-    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+template <typename P>
+__global__ void __launch_bounds__(256) deposit_vector(const P* __restrict__ px, const P* __restrict__ py,
+                                                      const P* __restrict__ pz, const P* __restrict__ pq,
+                                                      int64_t n, Axes ax, float4* __restrict__ corner,
+                                                      unsigned long long* __restrict__ oob) {
+    deposit_vector_body<P>(px, py, pz, pq, n, ax, corner, oob, blockIdx.x);
+}
+
+__device__ __forceinline__ void corner_sum_body(const float* __restrict__ corner, int nx, int ny, int64_t N,
+                                                float* __restrict__ rho, int assign, int64_t blk) {
+    const int64_t node = blk * blockDim.x + threadIdx.x;
     if (node >= N) return;
     const int i = (int)(node % nx);
     const int64_t r = node / nx;
@@ -204,6 +221,12 @@ __global__ void __launch_bounds__(256) k_corner_sum(const float* __restrict__ co
         rho[node] = s;
     else
         rho[node] += s;
+}
+
+__global__ void __launch_bounds__(256) k_corner_sum(const float* __restrict__ corner, int nx, int ny, int64_t N,
+                                                    float* __restrict__ rho, int assign) {
+    pdl_wait();  // the corner slots come from the preceding deposit
+    corner_sum_body(corner, nx, ny, N, rho, assign, blockIdx.x);
 }
 
 int corner_sum_launch(sc_mesh* m, const float* corner, float* out, cudaStream_t s, bool assign) {
@@ -370,6 +393,79 @@ int deposit_launch(sc_mesh* m, const void* x, const void* y, const void* z, cons
     }
     SC_LAUNCH_CHECK("deposit_atomic");
     m->launches += 1;
+    return SC_OK;
+}
+
+
+// ------------------------------------------------------- staged batch kick
+// One launch per stage over a group of bunches (batch.cuh): each CTA finds
+// its bunch and its CTA index within the bunch in the launch's CtaRef table
+// and runs the single-mesh kernel's body on that bunch.
+__global__ void __launch_bounds__(256) kb_clear(const ClearSeg* __restrict__ segs, const CtaRef* __restrict__ map) {
+    const CtaRef r = map[blockIdx.x];
+    const ClearSeg g = segs[r.item];
+    const int64_t lo = (int64_t)r.local * kClearChunk;
+    const int64_t hi = lo + kClearChunk < g.n ? lo + kClearChunk : g.n;
+    pdl_wait();  // the previous call's readers of these buffers came before
+    // the buffers come from cudaMalloc (256-byte aligned) and chunks are
+    // multiples of 4 floats, so whole float4 groups start aligned
+    const int64_t nv = (hi - lo) / 4;
+    float4* p4 = reinterpret_cast<float4*>(g.p + lo);
+    for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) p4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t i = lo + 4 * nv + threadIdx.x; i < hi; i += blockDim.x) g.p[i] = 0.f;
+}
+
+template <typename P>
+__global__ void __launch_bounds__(256) kb_deposit(const BunchDesc* __restrict__ tab, const CtaRef* __restrict__ map) {
+    const CtaRef r = map[blockIdx.x];
+    const BunchDesc& b = tab[r.item];
+    const Axes ax = b.ax;
+    pdl_wait();  // rho or the corner slots were cleared by the preceding launch
+    if (b.corner)
+        deposit_vector_body<P>((const P*)b.x, (const P*)b.y, (const P*)b.z, (const P*)b.q, b.n, ax, b.corner, b.oob,
+                               r.local);
+    else
+        deposit_atomic_body<P, float>((const P*)b.x, (const P*)b.y, (const P*)b.z, (const P*)b.q, b.n, ax, b.rho,
+                                      b.oob, r.local);
+}
+
+__global__ void __launch_bounds__(256) kb_corner_sum(const BunchDesc* __restrict__ tab,
+                                                     const CtaRef* __restrict__ map) {
+    const CtaRef r = map[blockIdx.x];
+    const BunchDesc& b = tab[r.item];
+    pdl_wait();
+    corner_sum_body(reinterpret_cast<const float*>(b.corner), b.nx, b.ny, (int64_t)b.nx * b.ny * b.nz, b.rho, 1,
+                    r.local);
+}
+
+int batch_clear_launch(const ClearSeg* segs, const CtaRef* map, int64_t ctas, cudaStream_t s) {
+    if (ctas == 0) return SC_OK;
+    launch_pdl(kb_clear, (unsigned)ctas, 256, 0, s, segs, map);
+    SC_LAUNCH_CHECK("kb_clear");
+    return SC_OK;
+}
+
+int batch_deposit_particles_per_cta() { return 256 * kDepPerThread; }
+
+int batch_deposit_launch(const BunchDesc* tab, const CtaRef* map, int64_t ctas, int dtype, cudaStream_t s) {
+    if (ctas == 0) return SC_OK;
+    if (dtype == SC_F64)
+        launch_pdl(kb_deposit<double>, (unsigned)ctas, 256, 0, s, tab, map);
+    else
+        launch_pdl(kb_deposit<float>, (unsigned)ctas, 256, 0, s, tab, map);
+    SC_LAUNCH_CHECK("kb_deposit");
+    return SC_OK;
+}
+
+int batch_corner_sum_launch(const BunchDesc* tab, const CtaRef* map, int64_t ctas, cudaStream_t s) {
+    if (ctas == 0) return SC_OK;
+    launch_pdl(kb_corner_sum, (unsigned)ctas, 256, 0, s, tab, map);
+    SC_LAUNCH_CHECK("kb_corner_sum");
+    return SC_OK;
+}
+
+int corner_alloc(sc_mesh* m) {
+    if (!m->corner) SC_CUDA(dev_alloc(&m->corner, sizeof(float) * 8 * (size_t)m->N));
     return SC_OK;
 }
 

@@ -7,6 +7,7 @@
 //   node as one 16-byte (FP32) or 32-byte (FP64) load, 8 loads per particle.
 // Out-of-range particles get E = 0 and are counted (the reference reads out
 // of bounds there).
+#include "batch.cuh"
 #include "cells.cuh"
 #include "sc_internal.cuh"
 
@@ -120,15 +121,15 @@ struct GCell<double> {
 #endif
 constexpr int kGathPerThread = SC_GATH_PT;
 
+// Body of one CTA: particles blk * 256 * kGathPerThread + ... of the bunch.
 template <typename P, typename A>
-__global__ void __launch_bounds__(256, SC_GATH_MINB) gather_packed(const P* __restrict__ px, const P* __restrict__ py,
-                                                     const P* __restrict__ pz, int64_t n, Axes ax,
-                                                     const typename Packed<A>::V* __restrict__ ef,
-                                                     P* __restrict__ ex, P* __restrict__ ey, P* __restrict__ ez,
-                                                     unsigned long long* __restrict__ oob) {
+__device__ __forceinline__ void gather_packed_body(const P* __restrict__ px, const P* __restrict__ py,
+                                                   const P* __restrict__ pz, int64_t n, const Axes& ax,
+                                                   const typename Packed<A>::V* __restrict__ ef, P* __restrict__ ex,
+                                                   P* __restrict__ ey, P* __restrict__ ez,
+                                                   unsigned long long* __restrict__ oob, int64_t blk) {
     using V = typename Packed<A>::V;
-    pdl_wait();  // the field (and possibly the positions) come from preceding grids
-    const int64_t base = (int64_t)blockIdx.x * (blockDim.x * kGathPerThread) + threadIdx.x;
+    const int64_t base = blk * (blockDim.x * kGathPerThread) + threadIdx.x;
     P x[kGathPerThread], y[kGathPerThread], z[kGathPerThread];
 #pragma unroll
     for (int k = 0; k < kGathPerThread; ++k) {
@@ -186,6 +187,40 @@ __global__ void __launch_bounds__(256, SC_GATH_MINB) gather_packed(const P* __re
         ez[p] = to_out<P, A>(sz_);
     }
     if (skipped) atomicAdd(oob, (unsigned long long)skipped);
+}
+
+template <typename P, typename A>
+__global__ void __launch_bounds__(256, SC_GATH_MINB) gather_packed(const P* __restrict__ px, const P* __restrict__ py,
+                                                     const P* __restrict__ pz, int64_t n, Axes ax,
+                                                     const typename Packed<A>::V* __restrict__ ef,
+                                                     P* __restrict__ ex, P* __restrict__ ey, P* __restrict__ ez,
+                                                     unsigned long long* __restrict__ oob) {
+    pdl_wait();  // the field (and possibly the positions) come from preceding grids
+    gather_packed_body<P, A>(px, py, pz, n, ax, ef, ex, ey, ez, oob, blockIdx.x);
+}
+
+// Staged batch kick (batch.cuh): the gather of a group of bunches in one launch.
+template <typename P>
+__global__ void __launch_bounds__(256, SC_GATH_MINB) kb_gather(const BunchDesc* __restrict__ tab,
+                                                               const CtaRef* __restrict__ map) {
+    const CtaRef r = map[blockIdx.x];
+    const BunchDesc& b = tab[r.item];
+    const Axes ax = b.ax;
+    pdl_wait();
+    gather_packed_body<P, float>((const P*)b.x, (const P*)b.y, (const P*)b.z, b.n, ax, b.efield, (P*)b.ex, (P*)b.ey,
+                                 (P*)b.ez, b.oob, r.local);
+}
+
+int batch_gather_particles_per_cta() { return 256 * kGathPerThread; }
+
+int batch_gather_launch(const BunchDesc* tab, const CtaRef* map, int64_t ctas, int dtype, cudaStream_t s) {
+    if (ctas == 0) return SC_OK;
+    if (dtype == SC_F64)
+        launch_pdl(kb_gather<double>, (unsigned)ctas, 256, 0, s, tab, map);
+    else
+        launch_pdl(kb_gather<float>, (unsigned)ctas, 256, 0, s, tab, map);
+    SC_LAUNCH_CHECK("kb_gather");
+    return SC_OK;
 }
 
 int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n, int dtype, void* ex,

@@ -296,8 +296,9 @@ void kick_graph_release(sc_mesh* m);
 // Appends what a captured kick of this mesh depends on besides its arguments:
 // flags, tuning choices, geometry (kernel arguments captured by value), the
 // Green epoch (cached spectra) and the allocation generation (workspace
-// addresses).  A graph replays only while this is unchanged.
-void mesh_state_key(const sc_mesh* m, std::vector<int64_t>& k);
+// addresses).  A graph replays only while this is unchanged.  Without the
+// epoch (with_epoch = false) it keys what a batch's stage plan depends on.
+void mesh_state_key(const sc_mesh* m, std::vector<int64_t>& k, bool with_epoch = true);
 // Counts device allocations and frees made through dev_alloc / dev_realloc.
 int64_t alloc_generation();
 void host_pipe_release(sc_mesh* m);

@@ -113,6 +113,13 @@ SIGNATURES = {
     "sc_batch_kick": [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_i64), _int,
                       _int, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), _vp],
     "sc_batch_set_graph": [_vp, _int],
+    "sc_batch_set_staged": [_vp, _int],
+    "sc_batch_set_group_bytes": [_vp, _i64],
+    "sc_batch_set_fused_forward": [_vp, _int],
+    "sc_batch_autotune": [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_i64), _int,
+                          _int, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), _vp, C.POINTER(_i64),
+                          C.POINTER(_int)],
+    "sc_batch_staged_count": [_vp, C.POINTER(_int), C.POINTER(_i64)],
     "sc_batch_graph_nodes": [_vp, C.POINTER(_i64)],
     "sc_batch_destroy": [_vp],
     "sc_autotune": [_vp, _vp, C.POINTER(_int)],

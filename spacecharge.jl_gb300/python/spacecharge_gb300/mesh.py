@@ -538,13 +538,39 @@ class Batch:
     def set_graph(self, enabled: bool) -> None:
         L.call("sc_batch_set_graph", self._ptr, 1 if enabled else 0)
 
+    def set_staged(self, enabled: bool) -> None:
+        """Staged engine on (default) or every bunch on the per-bunch streams."""
+        L.call("sc_batch_set_staged", self._ptr, 1 if enabled else 0)
+
+    def set_group_bytes(self, nbytes: int) -> None:
+        """Working-set budget of a group of staged bunches (0: one bunch per
+        group; a huge value: one group per grid class)."""
+        L.call("sc_batch_set_group_bytes", self._ptr, int(nbytes))
+
+    def set_fused_forward(self, enabled: bool) -> None:
+        """Staged forward x+y transforms as one fused pass (True) or two."""
+        L.call("sc_batch_set_fused_forward", self._ptr, 1 if enabled else 0)
+
+    def autotune(self, xs, ys, zs, qs, at_cathode: bool = False) -> tuple[int, bool]:
+        """Times the kick of these bunches for several group budgets and both
+        forward-pass forms, keeps the fastest and returns it as
+        (group_bytes, fused_forward)."""
+        return self.kick(xs, ys, zs, qs, at_cathode=at_cathode, _tune=True)
+
     @property
     def graph_nodes(self) -> int:
         n = C.c_int64()
         L.call("sc_batch_graph_nodes", self._ptr, C.byref(n))
         return int(n.value)
 
-    def kick(self, xs, ys, zs, qs, at_cathode: bool = False):
+    @property
+    def staged(self) -> tuple[int, int]:
+        """(bunches kicked stage by stage, kernel launches of those stages)."""
+        k, n = C.c_int(), C.c_int64()
+        L.call("sc_batch_staged_count", self._ptr, C.byref(k), C.byref(n))
+        return int(k.value), int(n.value)
+
+    def kick(self, xs, ys, zs, qs, at_cathode: bool = False, _tune: bool = False):
         torch = _torch()
         nb = len(self.meshes)
         if not (len(xs) == len(ys) == len(zs) == len(qs) == nb):
@@ -571,6 +597,11 @@ class Batch:
             return (C.c_void_p * nb)(*[src[i][k].data_ptr() for i in range(nb)])
 
         n = (C.c_int64 * nb)(*[int(b[0].numel()) for b in dev])
-        L.call("sc_batch_kick", self._ptr, ptrs(0, dev), ptrs(1, dev), ptrs(2, dev), ptrs(3, dev), n, dt,
-               1 if at_cathode else 0, ptrs(0, self._outs), ptrs(1, self._outs), ptrs(2, self._outs), _stream())
+        args = (ptrs(0, dev), ptrs(1, dev), ptrs(2, dev), ptrs(3, dev), n, dt, 1 if at_cathode else 0,
+                ptrs(0, self._outs), ptrs(1, self._outs), ptrs(2, self._outs), _stream())
+        if _tune:
+            g, f = C.c_int64(), C.c_int()
+            L.call("sc_batch_autotune", self._ptr, *args, C.byref(g), C.byref(f))
+            return int(g.value), bool(f.value)
+        L.call("sc_batch_kick", self._ptr, *args)
         return [tuple(o) for o in self._outs]

@@ -118,3 +118,83 @@ def test_kick_graph_replay_matches_eager(sc, cuda, cache):
             assert rel(a.cpu().numpy(), b.cpu().numpy()) < 1e-5
         dev[0].mul_(1.01)  # move the particles in place
     assert m.launch_count() > n0
+
+
+@pytest.mark.parametrize("at_cathode", [False, True])
+@pytest.mark.parametrize("group_bytes,fused", [(0, False), (2**62, True), (64 << 20, False)])
+def test_staged_engine_mixed_members(sc, cuda, at_cathode, group_bytes, fused):
+    """The staged engine (one launch per stage over a group of bunches)
+    beside the per-bunch streams: dense bunches (vector deposit), sparse
+    ones (scalar atomics), a mesh with the Green cache off (its spectrum
+    rebuilt inside the graph), and members the stages do not take (an FP64
+    mesh, a sorted deposit, Lx != Ly) kicked on the streams.  Every bunch
+    equals its own kick, for per-bunch and whole-class groups, fused and
+    two-pass forward transforms, eager and replayed, and with the engine
+    off."""
+    import torch
+
+    rng = np.random.default_rng(21)
+    plan = [((16, 16, 16), 40000, "mixed", None), ((32, 32, 32), 2000, "mixed", None),
+            ((12, 12, 20), 30000, "mixed", "nocache"), ((16, 16, 16), 10000, "fp64", None),
+            ((24, 24, 24), 20000, "mixed", "sorted"), ((24, 16, 32), 15000, "mixed", None),
+            ((32, 32, 64), 300000, "mixed", None), ((20, 20, 20), 500, "mixed", None),
+            ((16, 16, 16), 5000, "mixed", None)]
+    meshes, singles, dev = [], [], []
+    for g, n, prec, opt in plan:
+        sig = rng.uniform(0.3e-3, 1.5e-3, 3)
+        x, y, z = rng.standard_normal((3, n)).clip(-4.5, 4.5) * sig[:, None]
+        if at_cathode:
+            z = np.abs(z) + 0.1e-3
+        q = np.full(n, rng.uniform(1e-11, 1e-9) / n)
+        gm = float(rng.uniform(1, 20))
+        m = sc.Mesh3D(g, x, y, z, precision=prec, gamma=gm)
+        r = sc.Mesh3D(g, x, y, z, precision=prec, gamma=gm)
+        if opt == "nocache":
+            m.set_green_cache(False)
+        if opt == "sorted":
+            m.set_kick_mode("sorted")
+        meshes.append(m)
+        singles.append(r)
+        dev.append([torch.from_numpy(a).cuda() for a in (x, y, z, q)])
+    b = sc.Batch(meshes, nstreams=3)
+    b.set_group_bytes(group_bytes)
+    b.set_fused_forward(fused)
+
+    def check(out):
+        for r, d, o in zip(singles, dev, out):
+            ref = sc.kick(r, *d, at_cathode=at_cathode)
+            for a, c in zip(o, ref):
+                assert rel(a.cpu().numpy(), c.cpu().numpy()) < 1e-5
+
+    out = [tuple(t.clone() for t in o) for o in b.kick(*zip(*dev), at_cathode=at_cathode)]
+    staged, launches = b.staged
+    # all but the FP64 mesh, the sorted deposit and the Lx != Ly mesh
+    assert staged == 6 and launches >= 6
+    check(out)
+    for step in range(2):  # replays follow particles moved in place
+        for d in dev:
+            d[0].mul_(1.02)
+        check(b.kick(*zip(*dev), at_cathode=at_cathode))
+    assert b.graph_nodes > 0
+    b.set_staged(False)
+    check(b.kick(*zip(*dev), at_cathode=at_cathode))
+    assert b.staged == (0, 0)
+
+
+def test_batch_autotune_keeps_results(sc, cuda):
+    """sc_batch_autotune picks a group budget and forward form; kicks after
+    it equal single kicks."""
+    import torch
+
+    spec = bunches(6, 4)
+    meshes = [sc.Mesh3D(g, x, y, z, precision="mixed", gamma=gm) for g, gm, x, y, z, q in spec]
+    dev = [[torch.from_numpy(a).cuda() for a in (x, y, z, q)] for _, _, x, y, z, q in spec]
+    b = sc.Batch(meshes)
+    gb, fused = b.autotune(*zip(*dev))
+    assert gb in (0, 48 << 20, 128 << 20, 512 << 20, 2**63 - 1) and fused in (False, True)
+    out = b.kick(*zip(*dev))
+    for m, d, o in zip(meshes, dev, out):
+        o = [t.clone() for t in o]
+        r = sc.kick(m, *d)
+        for a, c in zip(o, r):
+            assert rel(a.cpu().numpy(), c.cpu().numpy()) < 1e-5
