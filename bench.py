@@ -453,6 +453,15 @@ def main():
     mm.set_green_cache(True)
     ms_cached = max_over_ranks(timed(kick(mm), args.steps, args.warmup), ws)
 
+    # ---- the hand-written FP64 pipeline (the Julia host's T=Float64), Green
+    #      function rebuilt every kick and cached
+    m64 = sc.Mesh3D(GRID, *BOUNDS, precision="fp64", gamma=GAMMA, total_charge=QTOT)
+    m64.set_green_cache(False)
+    ms_fp64 = max_over_ranks(timed(kick(m64), max(3, args.steps // 2), 3), ws)
+    m64.set_green_cache(True)
+    ms_fp64_cached = max_over_ranks(timed(kick(m64), max(3, args.steps // 2), 3), ws)
+    del m64
+
     # ---- plain FP64 path (reference algorithm, cuFFT Z2Z)
     mp = sc.Mesh3D(GRID, *BOUNDS, precision="plain64", gamma=GAMMA, total_charge=QTOT)
     ms_plain = max_over_ranks(timed(kick(mp), max(3, args.steps // 4), 3), ws)
@@ -587,6 +596,8 @@ def main():
                    "precision": "mixed", "green": "rebuilt every kick", "l2": "flushed (256 MB) between kicks",
                    "parallelism": f"replicas x{ws}"},
         "ms_fp64_plain": round(ms_plain, 4),
+        "ms_fp64_native": round(ms_fp64, 4),
+        "ms_fp64_native_green_cached": round(ms_fp64_cached, 4),
         "speedup_vs_fp64_plain": round(ms_plain / ms_mixed, 3),
         "ms_green_cached": round(ms_cached, 4),
         "max_rel_err_vs_fp64": {"mesh": err_grid[0], "particles": err_part[0]},

@@ -195,6 +195,64 @@ __global__ void __launch_bounds__(256) k_igf_corners(double* __restrict__ F, int
     F[t] = val;
 }
 
+// The same corners for all three components in one launch, one (corner,
+// component) per thread (the FP64 antiderivative's FP64 issue time spread
+// over many warps): F[c][ez - ez0][ey][ex].
+__global__ void __launch_bounds__(128) k_igf_corners3(double* __restrict__ F, int nx, int ny, int nz, int ez0,
+                                                      double dx, double dy, double dz_lab, double gamma,
+                                                      double offz) {
+    const int cx = nx + 1, cy = ny + 1, cz = nz + 1 - ez0;
+    const int64_t per = (int64_t)cx * cy * cz;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= 3 * per) return;
+    const int icomp = (int)(t / per) + 1;
+    const int64_t e = t - (icomp - 1) * per;
+    const int ex = (int)(e % cx);
+    const int ey = (int)((e / cx) % cy);
+    const int ez = (int)(e / ((int64_t)cx * cy)) + ez0;
+    const int isize = 2 * nx, jsize = 2 * ny, ksize = 2 * nz;
+    const double dz = dz_lab * gamma;
+    const double factor = (icomp == 1 || icomp == 2) ? gamma / (dx * dy * dz) : 1.0 / (dx * dy * dz);
+    const double umin = (double)(1 - isize) * dx / 2;
+    const double vmin = (double)(1 - jsize) * dy / 2;
+    const double wmin = (double)(1 - ksize) * dz / 2 + offz * gamma;
+    const double u = (double)(ex + nx - 1) * dx + umin;
+    const double v = (double)(ey + ny - 1) * dy + vmin;
+    const double w = (double)(ez + nz - 1) * dz + wmin;
+    double val;
+    if (icomp == 1)
+        val = field_green_n(u, v, w) * factor;
+    else if (icomp == 2)
+        val = field_green_n(v, w, u) * factor;
+    else
+        val = field_green_n(w, u, v) * factor;
+    F[t] = val;
+}
+
+// 8-point difference (green_functions.jl:108-111) of every stored cell of
+// the three components, scaled by FPEI/(Lx Ly Lz), into the octant array
+// G[c][dz - ez0][dy][dx] that the parity-reduced transform reads.
+__global__ void __launch_bounds__(128) k_igf_place_oct(const double* __restrict__ F, double* __restrict__ G, int nx,
+                                                       int ny, int nz, int ez0, double scale) {
+    const int cx = nx + 1, cy = ny + 1, cz = nz + 1 - ez0;
+    const int64_t per = (int64_t)cx * cy * cz;
+    const int64_t cells = (int64_t)nx * ny * (nz - ez0);
+    pdl_wait();  // the corners come from the preceding k_igf_corners3
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= 3 * cells) return;
+    const int c = (int)(t / cells);
+    const int64_t e = t - c * cells;
+    const int dx = (int)(e % nx);
+    const int dy = (int)((e / nx) % ny);
+    const int dzi = (int)(e / ((int64_t)nx * ny));
+    const int64_t sy = cx, sz = (int64_t)cx * cy;
+    const double* f = F + c * per + dx + sy * dy + sz * dzi;
+    auto Fv = [&](int a, int b, int d) { return f[a + sy * b + sz * d]; };
+    const double g = Fv(1, 1, 1) - Fv(0, 1, 1) - Fv(1, 0, 1) - Fv(1, 1, 0) - Fv(0, 0, 0) + Fv(0, 0, 1) +
+                     Fv(0, 1, 0) + Fv(1, 0, 0);
+    G[t] = g * scale;
+}
+
 // 8-point difference (green_functions.jl:108-111) for displacements
 // d in [0,nx-1] x [0,ny-1] x [dz0, nz-1], scaled by FPEI/(Lx Ly Lz) and
 // written with the component's parity to every mirrored index mod L.
@@ -851,8 +909,77 @@ template <>
 int build_green_any<float>(sc_mesh* m, bool image, double offz, cudaStream_t s) {
     return build_green_mixed(m, image, offz, s);
 }
+// FP64 pipeline: the reference's FP64 corner differences on the stored
+// octant (free space) or quadrant (image) of all three components, then the
+// parity-reduced transform of pipeline2.cuh in FP64 (real octant lines, two
+// per complex FFT, about 8x less transform work than the full L grid).
+// Returns false (nothing issued) where that transform does not apply
+// (transform lengths above 256).
+static int build_green_fp64_reduced(sc_mesh* m, bool image, double offz, cudaStream_t s, bool* done) {
+    *done = false;
+    NativeWork& w = m->nw;
+    // (the process-wide Stockham-only setting keeps the full-grid build too)
+    if (fft_engine() != 0 || w.log2L[0] > 8 || w.log2L[1] > 8 || w.log2L[2] > 8) return SC_OK;
+    DeviceCtx* ctx = nullptr;
+    SC_TRY(device_ctx(&ctx));
+    const double2* tw = ctx->tw64;
+    const int nx = m->n[0], ny = m->n[1], nz = m->n[2];
+    const int Lx = w.L[0], Ly = w.L[1], Lz = w.L[2], Hx = w.Hx;
+    const int Hy = Ly / 2 + 1, Hz = Lz / 2 + 1;
+    const int ez0 = image ? -(nz - 1) : 0;
+    const int zc = nz - ez0;
+    const int64_t ncorner = (int64_t)(nx + 1) * (ny + 1) * (zc + 1);
+    const int64_t gcs = (int64_t)nx * ny * zc;
+    const int64_t t1max = (int64_t)Hx * ny * (2 * nz - 1), t2max = (int64_t)Hx * Hy * (2 * nz - 1);
+    // scratch (shared by the free-space and image builds, which run one
+    // after the other on one stream in FP64): corners | octant | x, y outputs
+    const int64_t need = 3 * ((int64_t)(nx + 1) * (ny + 1) * 2 * nz) + 3 * (int64_t)nx * ny * (2 * nz - 1) +
+                         3 * (t1max + t2max);
+    if (w.fnear_cap < need) {
+        w.fnear_cap = 0;
+        SC_CUDA(dev_realloc(&w.fnear, sizeof(double) * need));
+        w.fnear_cap = need;
+    }
+    if (image && !w.gimg) SC_CUDA(dev_alloc(&w.gimg, sizeof(double2) * 3 * (int64_t)Hx * Hy * Lz));
+    double* F = w.fnear;
+    double* G = F + 3 * ((int64_t)(nx + 1) * (ny + 1) * 2 * nz);
+    double* T1 = G + 3 * (int64_t)nx * ny * (2 * nz - 1);
+    double* T2 = T1 + 3 * t1max;
+    k_igf_corners3<<<(unsigned)((3 * ncorner + 127) / 128), 128, 0, s>>>(F, nx, ny, nz, ez0, m->delta[0], m->delta[1],
+                                                                        m->delta[2], m->gamma, image ? offz : 0.0);
+    SC_LAUNCH_CHECK("k_igf_corners3");
+    launch_pdl(k_igf_place_oct, (unsigned)((3 * gcs + 127) / 128), 128, 0, s, (const double*)F, G, nx, ny, nz, ez0,
+               kFpei / ((double)Lx * Ly * Lz));
+    SC_LAUNCH_CHECK("k_igf_place_oct");
+    const int64_t t1cs = (int64_t)Hx * ny * zc, t2cs = (int64_t)Hx * Hy * zc;
+    const int64_t plane = (int64_t)Hx * Hy;
+    void* dst = image ? w.gimg : w.gfree;
+    bool ok = launch3_green_xy<double>(w.log2L[0], w.log2L[1], G, T2, nx, ny, zc, Hx, gcs, t2cs, tw, s);
+    if (ok) {
+        SC_LAUNCH_CHECK("k3_green_xy");
+        m->launches += 3;
+    } else {
+        ok = launch3_green_x<double>(w.log2L[0], G, T1, nx, ny * zc, Hx, gcs, t1cs, tw, s) &&
+             launch3_green_col<double>(false, w.log2L[1], T1, T2, Hx, zc, ny, 1, Hx, (int64_t)Hx * ny, t1cs, Hx,
+                                       plane, t2cs, tw, s);
+        if (!ok) return fail(SC_ERR_UNSUPPORTED, "FP64 Green x/y pass: transform length out of range");
+        SC_LAUNCH_CHECK("green x/y passes");
+        m->launches += 4;
+    }
+    if (!launch3_green_col<double>(image, w.log2L[2], T2, dst, (int)plane, 1, nz, 2, plane, 0, t2cs, plane, 0,
+                                   plane * Hz, tw, s))
+        return fail(SC_ERR_UNSUPPORTED, "FP64 Green z pass: transform length out of range");
+    SC_LAUNCH_CHECK("green z pass");
+    if (image) w.img_half = true;
+    *done = true;
+    return SC_OK;
+}
+
 template <>
 int build_green_any<double>(sc_mesh* m, bool image, double offz, cudaStream_t s) {
+    bool done = false;
+    SC_TRY(build_green_fp64_reduced(m, image, offz, s, &done));
+    if (done) return SC_OK;
     SC_TRY(build_green<double>(m, image, offz, s));
     m->launches += 18;
     return SC_OK;

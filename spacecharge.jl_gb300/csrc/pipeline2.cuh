@@ -689,38 +689,43 @@ __global__ void __launch_bounds__(256) k2_inv_x1(const float2* __restrict__ D, f
 // pass leaves Im(K^), the compressed spectrum.  The image kernel has no parity
 // in z: its z pass transforms the full line and forms the complex spectrum.
 //
+// The kernels run in FP32 (the mixed pipeline) or FP64 (the FP64 pipeline),
+// Tr the real type.  Their exchange columns are in dynamic shared memory.
+//
 // x pass: rows r = ay + ny*iz of the stored octant G (iz = |dz| in free space,
 // dz + nz - 1 for the image), out T[comp][r][kx], kx <= L/2.
-template <int L>
-__global__ void __launch_bounds__(256) k3_green_x(const float* __restrict__ G, float* __restrict__ T, int nx,
+template <int L, typename Tr>
+__global__ void __launch_bounds__(256) k3_green_x(const Tr* __restrict__ G, Tr* __restrict__ T, int nx,
                                                   int rows, int Hx, int64_t gcs, int64_t tcs,
-                                                  const float2* __restrict__ tw) {
+                                                  const typename Cplx<Tr>::T2* __restrict__ tw) {
     using E = F2<L>;
-    __shared__ float2 swt[L];
+    using T2 = typename Cplx<Tr>::T2;
+    __shared__ T2 swt[L];
     stage_twiddles<L>(swt, tw);
     constexpr int P = 256 / E::NT;
-    __shared__ float2 xb[P * E::S];
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T2* xb = reinterpret_cast<T2*>(smraw);  // P exchange columns
     const int comp = blockIdx.y;
     const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
     const int r0 = 2 * (blockIdx.x * P + p), r1 = r0 + 1;
     const bool ok0 = r0 < rows, ok1 = r1 < rows;
-    const float* g0 = G + comp * gcs + (int64_t)nx * r0;
-    const float* g1 = g0 + nx;
-    float2* col = xb + p * E::S;
-    float2 v[16];
+    const Tr* g0 = G + comp * gcs + (int64_t)nx * r0;
+    const Tr* g1 = g0 + nx;
+    T2* col = xb + p * E::S;
+    T2 v[16];
     if (t < E::R2) {
 #pragma unroll
         for (int s = 0; s < E::R1; ++s) {
             const int x = t + E::R2 * s;
             const int dx = x < nx ? x : (x > L - nx ? x - L : L);
-            float a = 0.f, b = 0.f;
+            Tr a = 0, b = 0;
             if (dx != L) {
                 const int ax = dx < 0 ? -dx : dx;
                 if (ok0) a = __ldg(g0 + ax);
                 if (ok1) b = __ldg(g1 + ax);
                 if (comp == 0 && dx < 0) a = -a, b = -b;
             }
-            v[s] = make_float2(a, b);
+            v[s] = Cplx<Tr>::make(a, b);
         }
     }
     E::template fwd<false>(v, col, t, swt);
@@ -730,9 +735,9 @@ __global__ void __launch_bounds__(256) k3_green_x(const float* __restrict__ G, f
     }
     __syncthreads();
     if (ok0) {
-        float* T0 = T + comp * tcs + (int64_t)Hx * r0;
+        Tr* T0 = T + comp * tcs + (int64_t)Hx * r0;
         for (int k = t; k <= L / 2; k += E::NT) {
-            float2 xa, xbv;
+            T2 xa, xbv;
             split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
             T0[k] = comp == 0 ? xa.y : xa.x;
             if (ok1) T0[Hx + k] = comp == 0 ? xbv.y : xbv.x;
@@ -749,16 +754,18 @@ __global__ void __launch_bounds__(256) k3_green_x(const float* __restrict__ G, f
 // for kz <= L/2 (p = 1 for components 0 and 1; img_at gives the other kz
 // from these); otherwise k <= L/2 of the kept
 // real part is stored at out + b*bs_out + col + k*as_out.
-template <int L, bool IMG>
-__global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(const float* __restrict__ in, void* __restrict__ out,
+template <int L, bool IMG, typename Tr>
+__global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(const Tr* __restrict__ in, void* __restrict__ out,
                                                                   int ncols, int nbatch, int nh, int odd_comp,
                                                                   int64_t as_in, int64_t bs_in, int64_t cs_in,
                                                                   int64_t as_out, int64_t bs_out, int64_t cs_out,
-                                                                  const float2* __restrict__ tw) {
+                                                                  const typename Cplx<Tr>::T2* __restrict__ tw) {
     using E = F2<L>;
-    __shared__ float2 swt[L];
+    using T2 = typename Cplx<Tr>::T2;
+    __shared__ T2 swt[L];
     stage_twiddles<L>(swt, tw);
-    __shared__ float2 xb[kColW * E::S];
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T2* xb = reinterpret_cast<T2*>(smraw);  // kColW exchange columns
     const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
     const int comp = blockIdx.y;
     const int64_t total = (int64_t)ncols * nbatch;
@@ -766,24 +773,24 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(c
     const bool oka = fa < total, okb = fb < total;
     const int ba = oka ? (int)(fa / ncols) : 0, bb = okb ? (int)(fb / ncols) : 0;
     const int ca = (int)(fa - (int64_t)ba * ncols), cb = (int)(fb - (int64_t)bb * ncols);
-    const float* sa = in + comp * cs_in + ba * bs_in + ca;
-    const float* sb = in + comp * cs_in + bb * bs_in + cb;
+    const Tr* sa = in + comp * cs_in + ba * bs_in + ca;
+    const Tr* sb = in + comp * cs_in + bb * bs_in + cb;
     const bool odd = comp == odd_comp;
-    float2* col = xb + c * E::S;
-    float2 v[16];
+    T2* col = xb + c * E::S;
+    T2 v[16];
     if (t < E::R2) {
 #pragma unroll
         for (int s = 0; s < E::R1; ++s) {
             const int n = t + E::R2 * s;
             const int d = n < nh ? n : (n > L - nh ? n - L : L);
-            float a = 0.f, b = 0.f;
+            Tr a = 0, b = 0;
             if (d != L) {
                 const int64_t o = (IMG ? d + nh - 1 : (d < 0 ? -d : d)) * as_in;
                 if (oka) a = __ldg(sa + o);
                 if (okb) b = __ldg(sb + o);
                 if (!IMG && odd && d < 0) a = -a, b = -b;
             }
-            v[s] = make_float2(a, b);
+            v[s] = Cplx<Tr>::make(a, b);
         }
     }
     E::template fwd<false>(v, col, t, swt);
@@ -793,25 +800,25 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(c
     }
     __syncthreads();
     for (int k = t; k <= L / 2; k += E::NT) {
-        float2 xa, xbv;
+        T2 xa, xbv;
         split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
         if (!IMG) {
-            float* o = reinterpret_cast<float*>(out) + comp * cs_out + k * as_out;
+            Tr* o = reinterpret_cast<Tr*>(out) + comp * cs_out + k * as_out;
             if (oka) o[ba * bs_out + ca] = odd ? xa.y : xa.x;
             if (okb) o[bb * bs_out + cb] = odd ? xbv.y : xbv.x;
         } else {
             // the line is real, so X(L - k) = conj X(k): only k <= L/2 is
             // stored, and img_at rebuilds the rest
-            const float2 ph1 = tw[(int)(((int64_t)k * (nh - 1)) & (L - 1)) * (kMaxL / L)];
-            float2* o = reinterpret_cast<float2*>(out) + comp * cs_out;
+            const T2 ph1 = tw[(int)(((int64_t)k * (nh - 1)) & (L - 1)) * (kMaxL / L)];
+            T2* o = reinterpret_cast<T2*>(out) + comp * cs_out;
             for (int w = 0; w < 2; ++w) {
                 const bool okw = w == 0 ? oka : okb;
                 if (!okw) continue;
-                const float2 x = w == 0 ? xa : xbv;
-                const float2 x1 = comp < 2 ? make_float2(-x.y, x.x) : x;  // times i for components 0 and 1
+                const T2 x = w == 0 ? xa : xbv;
+                const T2 x1 = comp < 2 ? Cplx<Tr>::make(-x.y, x.x) : x;  // times i for components 0 and 1
                 const int64_t base = w == 0 ? (ba * bs_out + ca) : (bb * bs_out + cb);
-                const float2 q1 = cmul(x1, ph1);
-                o[base + k * as_out] = make_float2(-q1.x, -q1.y);
+                const T2 q1 = cmul(x1, ph1);
+                o[base + k * as_out] = Cplx<Tr>::make(-q1.x, -q1.y);
             }
         }
     }
@@ -822,42 +829,45 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(c
 // per complex FFT) into shared memory, then its Hx columns along y (two per
 // complex FFT) with the component's y parity, into T2[comp][iz][ky][kx].
 // The x-pass output (k3_green_x's T1) never goes to global memory.
-template <int L>
-__global__ void __launch_bounds__(256, 3) k3_green_xy(const float* __restrict__ G, float* __restrict__ T2, int nx,
+// FP32: three CTAs per SM at 80 registers; FP64: one, its slice takes up to
+// 202 KB of shared memory
+template <int L, typename Tr>
+__global__ void __launch_bounds__(256, sizeof(Tr) == 4 ? 3 : 1) k3_green_xy(const Tr* __restrict__ G, Tr* __restrict__ T2out, int nx,
                                                    int ny, int Hx, int64_t gcs, int64_t t2cs,
-                                                   const float2* __restrict__ tw) {
+                                                   const typename Cplx<Tr>::T2* __restrict__ tw) {
     using E = F2<L>;
+    using T2 = typename Cplx<Tr>::T2;
     constexpr int W = 256 / E::NT;  // row pairs (x pass) or columns (y pass) per round
-    __shared__ float2 swt[L];
+    __shared__ T2 swt[L];
     stage_twiddles<L>(swt, tw);
     extern __shared__ __align__(16) unsigned char smraw[];
-    float2* xb = reinterpret_cast<float2*>(smraw);        // W exchange columns
-    float* ts = reinterpret_cast<float*>(xb + W * E::S);  // [ny][Hx]: the slice after the x pass
+    T2* xb = reinterpret_cast<T2*>(smraw);        // W exchange columns
+    Tr* ts = reinterpret_cast<Tr*>(xb + W * E::S);  // [ny][Hx]: the slice after the x pass
     const int iz = blockIdx.x, comp = blockIdx.y;
-    float2 v[16];
+    T2 v[16];
     // x pass: rows y0, y1 = y0 + 1 of slice iz; component 0 is odd along x
     {
         const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
-        float2* col = xb + p * E::S;
-        const float* gs = G + comp * gcs + (int64_t)nx * ny * iz;
+        T2* col = xb + p * E::S;
+        const Tr* gs = G + comp * gcs + (int64_t)nx * ny * iz;
         for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
             const int y0 = 2 * (q0 + p), y1 = y0 + 1;
             const bool ok0 = y0 < ny, ok1 = y1 < ny;
-            const float* g0 = gs + (int64_t)nx * y0;
-            const float* g1 = g0 + nx;
+            const Tr* g0 = gs + (int64_t)nx * y0;
+            const Tr* g1 = g0 + nx;
             if (t < E::R2) {
 #pragma unroll
                 for (int s = 0; s < E::R1; ++s) {
                     const int x = t + E::R2 * s;
                     const int dx = x < nx ? x : (x > L - nx ? x - L : L);
-                    float a = 0.f, b = 0.f;
+                    Tr a = 0, b = 0;
                     if (dx != L) {
                         const int ax = dx < 0 ? -dx : dx;
                         if (ok0) a = __ldg(g0 + ax);
                         if (ok1) b = __ldg(g1 + ax);
                         if (comp == 0 && dx < 0) a = -a, b = -b;
                     }
-                    v[s] = make_float2(a, b);
+                    v[s] = Cplx<Tr>::make(a, b);
                 }
             }
             E::template fwd<false>(v, col, t, swt);
@@ -868,7 +878,7 @@ __global__ void __launch_bounds__(256, 3) k3_green_xy(const float* __restrict__ 
             __syncthreads();
             if (ok0) {
                 for (int k = t; k <= L / 2; k += E::NT) {
-                    float2 xa, xbv;
+                    T2 xa, xbv;
                     split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
                     ts[y0 * Hx + k] = comp == 0 ? xa.y : xa.x;
                     if (ok1) ts[y1 * Hx + k] = comp == 0 ? xbv.y : xbv.x;
@@ -882,21 +892,21 @@ __global__ void __launch_bounds__(256, 3) k3_green_xy(const float* __restrict__ 
     // (kx = L/2, which would take a round of its own) by a direct sum.
     {
         const int c = threadIdx.x % W, t = threadIdx.x / W;
-        float2* col = xb + c * E::S;
+        T2* col = xb + c * E::S;
         const bool odd = comp == 1;
-        float* out = T2 + comp * t2cs + (int64_t)Hx * (L / 2 + 1) * iz;
+        Tr* out = T2out + comp * t2cs + (int64_t)Hx * (L / 2 + 1) * iz;
         for (int k = threadIdx.x; k <= L / 2; k += blockDim.x) {
             // X(k) = sum_d x(d) w^(k d), d = -(ny-1)..ny-1, x(-d) = -x(d) when odd
-            float re = 0.f, im = 0.f;
+            Tr re = 0, im = 0;
             for (int d = 0; d < ny; ++d) {
-                const float a = ts[d * Hx + L / 2];
-                const float2 wp = swt[(k * d) & (L - 1)];
+                const Tr a = ts[d * Hx + L / 2];
+                const T2 wp = swt[(k * d) & (L - 1)];
                 if (d == 0) {
                     re += a;
                 } else if (odd) {
-                    im += 2.f * a * wp.y;  // x(d) (w^kd - w^-kd) = 2i x(d) Im w^kd
+                    im += Tr(2) * a * wp.y;  // x(d) (w^kd - w^-kd) = 2i x(d) Im w^kd
                 } else {
-                    re += 2.f * a * wp.x;
+                    re += Tr(2) * a * wp.x;
                 }
             }
             out[(int64_t)k * Hx + L / 2] = odd ? im : re;
@@ -909,14 +919,14 @@ __global__ void __launch_bounds__(256, 3) k3_green_xy(const float* __restrict__ 
                 for (int s = 0; s < E::R1; ++s) {
                     const int n = t + E::R2 * s;
                     const int d = n < ny ? n : (n > L - ny ? n - L : L);
-                    float a = 0.f, b = 0.f;
+                    Tr a = 0, b = 0;
                     if (d != L) {
                         const int ad = d < 0 ? -d : d;
                         if (oka) a = ts[ad * Hx + fa];
                         if (okb) b = ts[ad * Hx + fb];
                         if (odd && d < 0) a = -a, b = -b;
                     }
-                    v[s] = make_float2(a, b);
+                    v[s] = Cplx<Tr>::make(a, b);
                 }
             }
             E::template fwd<false>(v, col, t, swt);
@@ -926,7 +936,7 @@ __global__ void __launch_bounds__(256, 3) k3_green_xy(const float* __restrict__ 
             }
             __syncthreads();
             for (int k = t; k <= L / 2; k += E::NT) {
-                float2 xa, xbv;
+                T2 xa, xbv;
                 split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
                 if (oka) out[(int64_t)k * Hx + fa] = odd ? xa.y : xa.x;
                 if (okb) out[(int64_t)k * Hx + fb] = odd ? xbv.y : xbv.x;
@@ -1081,47 +1091,64 @@ static bool launch2_inv_x1(int logL, const float2* D, float* E4, int nx, int row
     return true;
 }
 
-static bool launch3_green_x(int logL, const float* G, float* T, int nx, int rows, int Hx, int64_t gcs, int64_t tcs,
-                            const float2* tw, cudaStream_t s) {
+template <typename Tr>
+static bool launch3_green_x(int logL, const Tr* G, Tr* T, int nx, int rows, int Hx, int64_t gcs, int64_t tcs,
+                            const typename Cplx<Tr>::T2* tw, cudaStream_t s) {
+    using T2 = typename Cplx<Tr>::T2;
 #define SC_K3GX(LL)                                                                 \
     {                                                                               \
         constexpr int P = 256 / F2<LL>::NT;                                         \
+        const size_t smem = sizeof(T2) * P * F2<LL>::S;                             \
+        if (set_smem(k3_green_x<LL, Tr>, smem) != SC_OK) return false;              \
         dim3 grid(((rows + 1) / 2 + P - 1) / P, 3);                                 \
-        launch_pdl(k3_green_x<LL>, grid, 256, 0, s, G, T, nx, rows, Hx, gcs, tcs, tw);      \
+        launch_pdl(k3_green_x<LL, Tr>, grid, 256, smem, s, G, T, nx, rows, Hx, gcs, tcs, tw); \
     }
     SC_L_SWITCH(logL, SC_K3GX)
 #undef SC_K3GX
     return true;
 }
 
-// The fused x+y Green pass needs Lx = Ly and the slice in shared memory.
-static bool launch3_green_xy(int logLx, int logLy, const float* G, float* T2, int nx, int ny, int zc, int Hx,
-                             int64_t gcs, int64_t t2cs, const float2* tw, cudaStream_t s) {
+// The fused x+y Green pass needs Lx = Ly and the slice in shared memory
+// (100 KB in FP32, where three CTAs share an SM; the FP64 slice of a
+// 128 x 128 plane takes 202 KB).
+template <typename Tr>
+static bool launch3_green_xy(int logLx, int logLy, const Tr* G, Tr* T2, int nx, int ny, int zc, int Hx,
+                             int64_t gcs, int64_t t2cs, const typename Cplx<Tr>::T2* tw, cudaStream_t s) {
+    using C2 = typename Cplx<Tr>::T2;
     if (logLx != logLy) return false;
+    const size_t cap = sizeof(Tr) == 4 ? 100 * 1024 : 210 * 1024;
 #define SC_K3XY(LL)                                                                                 \
     {                                                                                               \
         constexpr int W = 256 / F2<LL>::NT;                                                         \
-        const size_t smem = sizeof(float2) * (size_t)W * F2<LL>::S + sizeof(float) * (size_t)ny * Hx; \
-        if (smem > 100 * 1024) return false;                                                        \
-        if (set_smem(k3_green_xy<LL>, smem) != SC_OK) return false;                                 \
-        launch_pdl(k3_green_xy<LL>, dim3(zc, 3), 256, smem, s, G, T2, nx, ny, Hx, gcs, t2cs, tw);    \
+        const size_t smem = sizeof(C2) * (size_t)W * F2<LL>::S + sizeof(Tr) * (size_t)ny * Hx;     \
+        if (smem > cap) return false;                                                               \
+        if (set_smem(k3_green_xy<LL, Tr>, smem) != SC_OK) return false;                             \
+        launch_pdl(k3_green_xy<LL, Tr>, dim3(zc, 3), 256, smem, s, G, T2, nx, ny, Hx, gcs, t2cs, tw); \
     }
     SC_L_SWITCH(logLx, SC_K3XY)
 #undef SC_K3XY
     return true;
 }
 
-static bool launch3_green_col(bool img, int logL, const float* in, void* out, int ncols, int nbatch, int nh,
+template <typename Tr>
+static bool launch3_green_col(bool img, int logL, const Tr* in, void* out, int ncols, int nbatch, int nh,
                               int odd_comp, int64_t as_in, int64_t bs_in, int64_t cs_in, int64_t as_out,
-                              int64_t bs_out, int64_t cs_out, const float2* tw, cudaStream_t s) {
+                              int64_t bs_out, int64_t cs_out, const typename Cplx<Tr>::T2* tw, cudaStream_t s) {
+    using T2 = typename Cplx<Tr>::T2;
     dim3 grid((unsigned)(((int64_t)ncols * nbatch + 2 * kColW - 1) / (2 * kColW)), 3);
 #define SC_K3GC(LL)                                                                                           \
-    if (img)                                                                                                  \
-        launch_pdl(k3_green_col<LL, true>, grid, kColW * F2<LL>::NT, 0, s, in, out, ncols, nbatch, nh, odd_comp, as_in, \
-                                                                   bs_in, cs_in, as_out, bs_out, cs_out, tw);   \
-    else                                                                                                      \
-        launch_pdl(k3_green_col<LL, false>, grid, kColW * F2<LL>::NT, 0, s, in, out, ncols, nbatch, nh, odd_comp,      \
-                                                                    as_in, bs_in, cs_in, as_out, bs_out, cs_out, tw);
+    {                                                                                                         \
+        const size_t smem = sizeof(T2) * kColW * F2<LL>::S;                                                   \
+        if (img) {                                                                                            \
+            if (set_smem(k3_green_col<LL, true, Tr>, smem) != SC_OK) return false;                           \
+            launch_pdl(k3_green_col<LL, true, Tr>, grid, kColW * F2<LL>::NT, smem, s, in, out, ncols, nbatch, nh, \
+                       odd_comp, as_in, bs_in, cs_in, as_out, bs_out, cs_out, tw);                           \
+        } else {                                                                                              \
+            if (set_smem(k3_green_col<LL, false, Tr>, smem) != SC_OK) return false;                          \
+            launch_pdl(k3_green_col<LL, false, Tr>, grid, kColW * F2<LL>::NT, smem, s, in, out, ncols, nbatch, nh, \
+                       odd_comp, as_in, bs_in, cs_in, as_out, bs_out, cs_out, tw);                           \
+        }                                                                                                     \
+    }
     SC_L_SWITCH(logL, SC_K3GC)
 #undef SC_K3GC
     return true;
