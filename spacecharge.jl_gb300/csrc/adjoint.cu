@@ -192,46 +192,6 @@ __global__ void __launch_bounds__(256) k_adj_zpass(const typename Cplx<T>::T2* _
     }
 }
 
-// Inverse x pass of one component into the spare fourth lane of the packed
-// field nodes (the adjoint charge density rhobar).
-template <typename T>
-__global__ void __launch_bounds__(256) k_inv_x1(const typename Cplx<T>::T2* __restrict__ D, T* __restrict__ E4,
-                                                int nx, int rows, int Lx, int logLx, int Hx, int lgP,
-                                                const typename Cplx<T>::T2* __restrict__ tw) {
-    using T2 = typename Cplx<T>::T2;
-    extern __shared__ __align__(16) unsigned char smraw[];
-    const int P = 1 << lgP;
-    const int n = P << logLx;
-    T2* a = reinterpret_cast<T2*>(smraw);
-    T2* b = a + n;
-    const int pair0 = blockIdx.x << lgP;
-    for (int it = threadIdx.x; it < n; it += blockDim.x) {
-        const int p = it >> logLx, k = it & (Lx - 1);
-        const int r0 = 2 * (pair0 + p), r1 = r0 + 1;
-        T2 xa = Cplx<T>::make(0, 0), xb = Cplx<T>::make(0, 0);
-        const bool cj = k >= Hx;
-        const int kk = cj ? Lx - k : k;
-        if (r0 < rows) xa = D[(int64_t)r0 * Hx + kk];
-        if (r1 < rows) xb = D[(int64_t)r1 * Hx + kk];
-        if (cj) {
-            xa.y = -xa.y;
-            xb.y = -xb.y;
-        }
-        a[(k << lgP) + p] = Cplx<T>::make(xa.x - xb.y, xa.y + xb.x);
-    }
-    __syncthreads();
-    const T2* res = smem_fft<true>(a, b, Lx, logLx, lgP, tw);
-    for (int it = threadIdx.x; it < 2 * n; it += blockDim.x) {
-        const int rp = it >> logLx, x = it & (Lx - 1);
-        if (x >= nx) continue;
-        const int p = rp >> 1, half = rp & 1;
-        const int row = 2 * (pair0 + p) + half;
-        if (row >= rows) continue;
-        const T2 v = res[(x << lgP) + p];
-        E4[4 * ((int64_t)row * nx + x) + 3] = half ? v.y : v.x;
-    }
-}
-
 template <typename P, typename T>
 __device__ __forceinline__ P out_cast(T v) {
     return (P)v;

@@ -885,6 +885,12 @@ int sc_solve_potential(sc_mesh* m, int at_cathode, void* phi, void* stream) {
     SC_TRY(check_mesh(m));
     if (!phi) return fail(SC_ERR_INVALID, "phi is NULL");
     DeviceGuard g(m->device);
+    // the hand-written pipelines take transforms of up to 256 points (axes
+    // of up to 128 nodes); longer ones and plain64 meshes use the FP64 cuFFT
+    // schedule of the reference
+    const NativeWork& w = m->nw;
+    if (m->precision != SC_PREC_PLAIN64 && w.log2L[0] <= 8 && w.log2L[1] <= 8 && w.log2L[2] <= 8)
+        return native_potential(m, at_cathode, phi, (cudaStream_t)stream);
     return plain_potential(m, at_cathode, phi, (cudaStream_t)stream);
 }
 

@@ -1329,10 +1329,50 @@ int native_green_async(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t* 
     return SC_OK;
 }
 
+template <typename T>
+static int forward_t(sc_mesh* m, cudaStream_t s) {
+    using T2 = typename Cplx<T>::T2;
+    DeviceCtx* ctx = nullptr;
+    SC_TRY(device_ctx(&ctx));
+    const T2* tw = twiddles<T>(ctx);
+    SC_TRY(alloc_work<T>(m));
+    NativeWork& w = m->nw;
+    const int nx = m->n[0], ny = m->n[1], nz = m->n[2];
+    const int Ly = w.L[1], Hx = w.Hx;
+    const int rows = ny * nz;
+    const int eng = w.engine >= 0 ? w.engine : fft_engine();
+    const bool two = std::is_same<T, float>::value && eng == 0;
+    const int lgWy = w.lgW >= 0 ? w.lgW : pick_cols(w.log2L[1]);
+    if (two && SC_FUSED_FWD_XY &&
+        launch2_fwd_xy(w.log2L[0], w.log2L[1], (const float*)m->rho, (float2*)w.B, nx, ny, nz, Hx, (const float2*)tw,
+                       s, m->fused_smem_cap)) {
+        SC_LAUNCH_CHECK("k2_fwd_xy");
+        m->launches += 1;
+        return SC_OK;
+    }
+    T2* A = (T2*)w.A;
+    if (!(two && launch2_fwd_x(w.log2L[0], (const float*)m->rho, (float2*)A, nx, rows, Hx, (const float2*)tw, s)))
+        SC_TRY(run_fwd_x<T>((const T*)m->rho, A, nx, rows, w, tw, s));
+    SC_LAUNCH_CHECK("fwd_x");
+    if (!(two && launch2_col(false, w.log2L[1], (const float2*)A, (float2*)w.B, Hx, ny, Ly, Hx, (int64_t)Hx * ny, 0,
+                             Hx, (int64_t)Hx * Ly, 0, nz, 1, (const float2*)tw, s)))
+        SC_TRY(run_col<false, T>(A, (T2*)w.B, Hx, Ly, w.log2L[1], ny, Ly, Hx, (int64_t)Hx * ny, 0, Hx,
+                                 (int64_t)Hx * Ly, 0, nz, 1, tw, s, lgWy));
+    SC_LAUNCH_CHECK("fwd_y");
+    m->launches += 2;
+    return SC_OK;
+}
+
+int native_forward(sc_mesh* m, cudaStream_t s) {
+    if (m->precision == SC_PREC_MIXED) return forward_t<float>(m, s);
+    return forward_t<double>(m, s);
+}
+
 int native_release(sc_mesh* m) {
     NativeWork& w = m->nw;
     void* ptrs[] = {w.A,      w.B,     w.C,    w.D,        w.adjE,  w.adjcorner, w.fnear,    w.fnear_img, w.fcorner,
-                    w.kgrid,  w.kspec, w.goct, w.goct_img, w.gspec, w.gtmp,      w.gtmp_img, w.gfree,     w.gimg};
+                    w.kgrid,  w.kspec, w.goct, w.goct_img, w.gspec, w.gtmp,      w.gtmp_img, w.gfree,     w.gimg,
+                    w.pfree,  w.pimg,  w.pscratch};
     for (void* p : ptrs) cudaFree(p);
     int L[3] = {w.L[0], w.L[1], w.L[2]};
     int lg[3] = {w.log2L[0], w.log2L[1], w.log2L[2]};

@@ -694,9 +694,11 @@ __global__ void __launch_bounds__(256) k2_inv_x1(const float2* __restrict__ D, f
 //
 // x pass: rows r = ay + ny*iz of the stored octant G (iz = |dz| in free space,
 // dz + nz - 1 for the image), out T[comp][r][kx], kx <= L/2.
+// odd_x: the component that is odd along x (0 for the field; -1 for the
+// potential kernel, which is even along every axis).
 template <int L, typename Tr>
 __global__ void __launch_bounds__(256) k3_green_x(const Tr* __restrict__ G, Tr* __restrict__ T, int nx,
-                                                  int rows, int Hx, int64_t gcs, int64_t tcs,
+                                                  int rows, int Hx, int64_t gcs, int64_t tcs, int odd_x,
                                                   const typename Cplx<Tr>::T2* __restrict__ tw) {
     using E = F2<L>;
     using T2 = typename Cplx<Tr>::T2;
@@ -723,7 +725,7 @@ __global__ void __launch_bounds__(256) k3_green_x(const Tr* __restrict__ G, Tr* 
                 const int ax = dx < 0 ? -dx : dx;
                 if (ok0) a = __ldg(g0 + ax);
                 if (ok1) b = __ldg(g1 + ax);
-                if (comp == 0 && dx < 0) a = -a, b = -b;
+                if (comp == odd_x && dx < 0) a = -a, b = -b;
             }
             v[s] = Cplx<Tr>::make(a, b);
         }
@@ -739,8 +741,8 @@ __global__ void __launch_bounds__(256) k3_green_x(const Tr* __restrict__ G, Tr* 
         for (int k = t; k <= L / 2; k += E::NT) {
             T2 xa, xbv;
             split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
-            T0[k] = comp == 0 ? xa.y : xa.x;
-            if (ok1) T0[Hx + k] = comp == 0 ? xbv.y : xbv.x;
+            T0[k] = comp == odd_x ? xa.y : xa.x;
+            if (ok1) T0[Hx + k] = comp == odd_x ? xbv.y : xbv.x;
         }
     }
 }
@@ -754,11 +756,15 @@ __global__ void __launch_bounds__(256) k3_green_x(const Tr* __restrict__ G, Tr* 
 // for kz <= L/2 (p = 1 for components 0 and 1; img_at gives the other kz
 // from these); otherwise k <= L/2 of the kept
 // real part is stored at out + b*bs_out + col + k*as_out.
+// imask (image z pass): bit c set when component c was stored as the
+// imaginary part along an odd axis, so its spectrum takes a factor i (3 for
+// the field's x and y components; 0 for the potential).
 template <int L, bool IMG, typename Tr>
 __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(const Tr* __restrict__ in, void* __restrict__ out,
                                                                   int ncols, int nbatch, int nh, int odd_comp,
                                                                   int64_t as_in, int64_t bs_in, int64_t cs_in,
                                                                   int64_t as_out, int64_t bs_out, int64_t cs_out,
+                                                                  int imask,
                                                                   const typename Cplx<Tr>::T2* __restrict__ tw) {
     using E = F2<L>;
     using T2 = typename Cplx<Tr>::T2;
@@ -815,7 +821,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(c
                 const bool okw = w == 0 ? oka : okb;
                 if (!okw) continue;
                 const T2 x = w == 0 ? xa : xbv;
-                const T2 x1 = comp < 2 ? Cplx<Tr>::make(-x.y, x.x) : x;  // times i for components 0 and 1
+                const T2 x1 = ((imask >> comp) & 1) ? Cplx<Tr>::make(-x.y, x.x) : x;  // times i
                 const int64_t base = w == 0 ? (ba * bs_out + ca) : (bb * bs_out + cb);
                 const T2 q1 = cmul(x1, ph1);
                 o[base + k * as_out] = Cplx<Tr>::make(-q1.x, -q1.y);
@@ -831,9 +837,11 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(c
 // The x-pass output (k3_green_x's T1) never goes to global memory.
 // FP32: three CTAs per SM at 80 registers; FP64: one, its slice takes up to
 // 202 KB of shared memory
+// odd_x, odd_y: the components odd along x and y (0 and 1 for the field;
+// -1 for the potential kernel)
 template <int L, typename Tr>
 __global__ void __launch_bounds__(256, sizeof(Tr) == 4 ? 3 : 1) k3_green_xy(const Tr* __restrict__ G, Tr* __restrict__ T2out, int nx,
-                                                   int ny, int Hx, int64_t gcs, int64_t t2cs,
+                                                   int ny, int Hx, int64_t gcs, int64_t t2cs, int odd_x, int odd_y,
                                                    const typename Cplx<Tr>::T2* __restrict__ tw) {
     using E = F2<L>;
     using T2 = typename Cplx<Tr>::T2;
@@ -865,7 +873,7 @@ __global__ void __launch_bounds__(256, sizeof(Tr) == 4 ? 3 : 1) k3_green_xy(cons
                         const int ax = dx < 0 ? -dx : dx;
                         if (ok0) a = __ldg(g0 + ax);
                         if (ok1) b = __ldg(g1 + ax);
-                        if (comp == 0 && dx < 0) a = -a, b = -b;
+                        if (comp == odd_x && dx < 0) a = -a, b = -b;
                     }
                     v[s] = Cplx<Tr>::make(a, b);
                 }
@@ -880,8 +888,8 @@ __global__ void __launch_bounds__(256, sizeof(Tr) == 4 ? 3 : 1) k3_green_xy(cons
                 for (int k = t; k <= L / 2; k += E::NT) {
                     T2 xa, xbv;
                     split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
-                    ts[y0 * Hx + k] = comp == 0 ? xa.y : xa.x;
-                    if (ok1) ts[y1 * Hx + k] = comp == 0 ? xbv.y : xbv.x;
+                    ts[y0 * Hx + k] = comp == odd_x ? xa.y : xa.x;
+                    if (ok1) ts[y1 * Hx + k] = comp == odd_x ? xbv.y : xbv.x;
                 }
             }
             __syncthreads();
@@ -893,7 +901,7 @@ __global__ void __launch_bounds__(256, sizeof(Tr) == 4 ? 3 : 1) k3_green_xy(cons
     {
         const int c = threadIdx.x % W, t = threadIdx.x / W;
         T2* col = xb + c * E::S;
-        const bool odd = comp == 1;
+        const bool odd = comp == odd_y;
         Tr* out = T2out + comp * t2cs + (int64_t)Hx * (L / 2 + 1) * iz;
         for (int k = threadIdx.x; k <= L / 2; k += blockDim.x) {
             // X(k) = sum_d x(d) w^(k d), d = -(ny-1)..ny-1, x(-d) = -x(d) when odd
@@ -1091,17 +1099,19 @@ static bool launch2_inv_x1(int logL, const float2* D, float* E4, int nx, int row
     return true;
 }
 
+// ncomp kernel components (blockIdx.y); odd_x, odd_y, imask as in the
+// kernels (the field's defaults: 3 components, 0, 1, 3).
 template <typename Tr>
 static bool launch3_green_x(int logL, const Tr* G, Tr* T, int nx, int rows, int Hx, int64_t gcs, int64_t tcs,
-                            const typename Cplx<Tr>::T2* tw, cudaStream_t s) {
+                            const typename Cplx<Tr>::T2* tw, cudaStream_t s, int ncomp = 3, int odd_x = 0) {
     using T2 = typename Cplx<Tr>::T2;
 #define SC_K3GX(LL)                                                                 \
     {                                                                               \
         constexpr int P = 256 / F2<LL>::NT;                                         \
         const size_t smem = sizeof(T2) * P * F2<LL>::S;                             \
         if (set_smem(k3_green_x<LL, Tr>, smem) != SC_OK) return false;              \
-        dim3 grid(((rows + 1) / 2 + P - 1) / P, 3);                                 \
-        launch_pdl(k3_green_x<LL, Tr>, grid, 256, smem, s, G, T, nx, rows, Hx, gcs, tcs, tw); \
+        dim3 grid(((rows + 1) / 2 + P - 1) / P, ncomp);                             \
+        launch_pdl(k3_green_x<LL, Tr>, grid, 256, smem, s, G, T, nx, rows, Hx, gcs, tcs, odd_x, tw); \
     }
     SC_L_SWITCH(logL, SC_K3GX)
 #undef SC_K3GX
@@ -1113,7 +1123,8 @@ static bool launch3_green_x(int logL, const Tr* G, Tr* T, int nx, int rows, int 
 // 128 x 128 plane takes 202 KB).
 template <typename Tr>
 static bool launch3_green_xy(int logLx, int logLy, const Tr* G, Tr* T2, int nx, int ny, int zc, int Hx,
-                             int64_t gcs, int64_t t2cs, const typename Cplx<Tr>::T2* tw, cudaStream_t s) {
+                             int64_t gcs, int64_t t2cs, const typename Cplx<Tr>::T2* tw, cudaStream_t s,
+                             int ncomp = 3, int odd_x = 0, int odd_y = 1) {
     using C2 = typename Cplx<Tr>::T2;
     if (logLx != logLy) return false;
     const size_t cap = sizeof(Tr) == 4 ? 100 * 1024 : 210 * 1024;
@@ -1123,7 +1134,7 @@ static bool launch3_green_xy(int logLx, int logLy, const Tr* G, Tr* T2, int nx, 
         const size_t smem = sizeof(C2) * (size_t)W * F2<LL>::S + sizeof(Tr) * (size_t)ny * Hx;     \
         if (smem > cap) return false;                                                               \
         if (set_smem(k3_green_xy<LL, Tr>, smem) != SC_OK) return false;                             \
-        launch_pdl(k3_green_xy<LL, Tr>, dim3(zc, 3), 256, smem, s, G, T2, nx, ny, Hx, gcs, t2cs, tw); \
+        launch_pdl(k3_green_xy<LL, Tr>, dim3(zc, ncomp), 256, smem, s, G, T2, nx, ny, Hx, gcs, t2cs, odd_x, odd_y, tw); \
     }
     SC_L_SWITCH(logLx, SC_K3XY)
 #undef SC_K3XY
@@ -1133,20 +1144,21 @@ static bool launch3_green_xy(int logLx, int logLy, const Tr* G, Tr* T2, int nx, 
 template <typename Tr>
 static bool launch3_green_col(bool img, int logL, const Tr* in, void* out, int ncols, int nbatch, int nh,
                               int odd_comp, int64_t as_in, int64_t bs_in, int64_t cs_in, int64_t as_out,
-                              int64_t bs_out, int64_t cs_out, const typename Cplx<Tr>::T2* tw, cudaStream_t s) {
+                              int64_t bs_out, int64_t cs_out, const typename Cplx<Tr>::T2* tw, cudaStream_t s,
+                              int ncomp = 3, int imask = 3) {
     using T2 = typename Cplx<Tr>::T2;
-    dim3 grid((unsigned)(((int64_t)ncols * nbatch + 2 * kColW - 1) / (2 * kColW)), 3);
+    dim3 grid((unsigned)(((int64_t)ncols * nbatch + 2 * kColW - 1) / (2 * kColW)), ncomp);
 #define SC_K3GC(LL)                                                                                           \
     {                                                                                                         \
         const size_t smem = sizeof(T2) * kColW * F2<LL>::S;                                                   \
         if (img) {                                                                                            \
             if (set_smem(k3_green_col<LL, true, Tr>, smem) != SC_OK) return false;                           \
             launch_pdl(k3_green_col<LL, true, Tr>, grid, kColW * F2<LL>::NT, smem, s, in, out, ncols, nbatch, nh, \
-                       odd_comp, as_in, bs_in, cs_in, as_out, bs_out, cs_out, tw);                           \
+                       odd_comp, as_in, bs_in, cs_in, as_out, bs_out, cs_out, imask, tw);                    \
         } else {                                                                                              \
             if (set_smem(k3_green_col<LL, false, Tr>, smem) != SC_OK) return false;                          \
             launch_pdl(k3_green_col<LL, false, Tr>, grid, kColW * F2<LL>::NT, smem, s, in, out, ncols, nbatch, nh, \
-                       odd_comp, as_in, bs_in, cs_in, as_out, bs_out, cs_out, tw);                           \
+                       odd_comp, as_in, bs_in, cs_in, as_out, bs_out, cs_out, imask, tw);                    \
         }                                                                                                     \
     }
     SC_L_SWITCH(logL, SC_K3GC)

@@ -19,13 +19,7 @@ __device__ __forceinline__ double field_green(double x, double y, double z) {
 
 // src/green_functions.jl:13-22 (the reference defines it and never calls it):
 // the antiderivative of 1/r, zero at r = 0.
-__device__ __forceinline__ double potential_green(double x, double y, double z) {
-    const double r = sqrt(x * x + y * y + z * z);
-    if (r == 0.0) return 0.0;
-    const double half = 0.5;
-    return -half * z * z * atan(x * y / (z * r)) - half * y * y * atan(x * z / (y * r)) -
-           half * x * x * atan(y * z / (x * r)) + y * z * log(x + r) + x * z * log(y + r) + x * y * log(z + r);
-}
+__device__ __forceinline__ double potential_green(double x, double y, double z) { return potential_green_n(x, y, z); }
 
 // green_functions.jl:69-101: F * factor at every point of the doubled grid.
 // icomp 4 is the scalar potential: potential_green with the transverse

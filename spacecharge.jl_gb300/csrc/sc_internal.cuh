@@ -19,6 +19,17 @@ namespace sc {
 constexpr double kClight = 299792458.0;
 constexpr double kFpei = kClight * kClight * 1.0e-7;
 
+// Antiderivative of 1/r, potential_green_function of
+// src/green_functions.jl:13-22 (defined in the reference, not called there):
+// zero at r = 0, the same expression and order.
+__device__ __forceinline__ double potential_green_n(double x, double y, double z) {
+    const double r = sqrt(x * x + y * y + z * z);
+    if (r == 0.0) return 0.0;
+    const double half = 0.5;
+    return -half * z * z * atan(x * y / (z * r)) - half * y * y * atan(x * z / (y * r)) -
+           half * x * x * atan(y * z / (x * r)) + y * z * log(x + r) + x * z * log(y + r) + x * y * log(z + r);
+}
+
 // Packed FP64 field node (Ex, Ey, Ez, 0); 32-byte aligned.
 struct __align__(32) dnode4 {
     double x, y, z, w;
@@ -157,6 +168,14 @@ struct NativeWork {
     bool img_half = false;  // gimg holds kz <= Lz/2 only (the FP32 two-step build)
     int engine = -1;  // -1: process-wide setting; 0: two-step; 1: Stockham
     int lgW = -1;     // Stockham column tile (log2), -1: default
+    // scalar potential (potential.cu): compressed spectra of the potential
+    // kernel (free space: real, T, Hx x Hy x Hz; image: complex, T2, kz <= Lz/2)
+    // and the scratch of their build
+    void* pfree = nullptr;
+    void* pimg = nullptr;
+    void* pscratch = nullptr;
+    int64_t pscratch_cap = 0;
+    GreenKey key_pfree, key_pimg;
 };
 
 struct PlainWork {
@@ -341,5 +360,11 @@ int adjoint_launch(sc_mesh* m, const void* x, const void* y, const void* z, cons
                    int at_cathode, const void* gex, const void* gey, const void* gez, const void* ggrid, void* dx,
                    void* dy, void* dz, void* dq, cudaStream_t s);
 int native_release(sc_mesh* m);
+// the forward x and y transforms of the mesh's rho into the workspace's B
+// (the field solve's, alone on the GPU: fused where the plane fits)
+int native_forward(sc_mesh* m, cudaStream_t s);
+// scalar potential of the mesh's rho on the hand-written pipeline (T phi[N],
+// x fastest); SC_ERR_UNSUPPORTED where a transform is longer than 256
+int native_potential(sc_mesh* m, int at_cathode, void* phi, cudaStream_t s);
 
 }  // namespace sc

@@ -1,5 +1,7 @@
 """sc_solve_potential (the scalar potential beside the field solve) against
-the oracle's restatement, and against -grad(phi) = E."""
+the oracle's restatement, and against -grad(phi) = E.  Mixed and FP64 meshes
+run the hand-written pipeline (axes up to 128 nodes); plain64 meshes and
+longer axes run the FP64 cuFFT schedule."""
 import numpy as np
 import pytest
 
@@ -50,3 +52,28 @@ def test_minus_grad_phi_is_e(sc, cuda):
     ex = -(phi[2:, 1:-1, 1:-1] - phi[:-2, 1:-1, 1:-1]) / (2 * d[0])
     core = E[8:24, 8:24, 8:24, 0]
     assert np.abs(ex[7:23, 7:23, 7:23] - core).max() < 0.03 * np.abs(core).max()
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("mixed", 1e-5)])
+@pytest.mark.parametrize("grid,gamma,cath", [((40, 36, 64), 10.0, False), ((32, 32, 48), 3.0, True),
+                                             ((12, 10, 150), 2.0, False)])
+def test_potential_larger_grids(sc, cuda, prec, tol, grid, gamma, cath):
+    """Grids where most cells are far from the origin (the mixed build's
+    quadrature), boosted cells, the image, and an axis of 150 nodes (a
+    512-point transform: the cuFFT schedule)."""
+    rng = np.random.default_rng(8)
+    n = 40_000
+    x, y, z = rng.standard_normal((3, n)).clip(-4.5, 4.5) * np.array([[1e-3], [0.8e-3], [0.3e-3]])
+    if cath:
+        z = np.abs(z) + 0.1e-3
+    q = np.full(n, 1e-9 / n)
+    om = O.mesh_auto(grid, x, y, z, gamma=gamma)
+    O.deposit(om, x, y, z, q)
+    ref = O.solve_potential(om, at_cathode=cath)
+    m = sc.Mesh3D(grid, x, y, z, precision=prec, gamma=gamma)
+    sc.deposit(m, x, y, z, q)
+    phi = sc.solve_potential(m, at_cathode=cath)
+    assert rel(phi.cpu().numpy(), ref) < tol
+    # a second solve reuses the cached potential spectrum
+    phi2 = sc.solve_potential(m, at_cathode=cath)
+    assert rel(phi2.cpu().numpy(), ref) < tol
