@@ -255,6 +255,31 @@ def bench_batch(sc, L, C, torch, flush, stream, ws, rank, steps, warmup):
             "green": "cached per bunch (fixed geometry)", "l2": "flushed between calls"}
 
 
+def bench_potential(sc, torch, dev, flush, stream, steps, warmup):
+    """Scalar potential of the headline bunch's charge (sc_solve_potential),
+    mixed and FP64 meshes, the potential Green function rebuilt every solve."""
+    res = {"workload": WORKLOAD + ", scalar potential of the deposited charge", "green": "rebuilt every solve"}
+    for prec in ("mixed", "fp64", "plain64"):
+        m = sc.Mesh3D(GRID, *BOUNDS, precision=prec, gamma=GAMMA, total_charge=QTOT)
+        sc.deposit(m, *dev)
+        m.set_green_cache(False)
+        for _ in range(warmup):
+            sc.solve_potential(m)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(steps if prec != "plain64" else max(2, steps // 4)):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            sc.solve_potential(m)
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        res["ms_" + prec] = round(float(np.mean(ts)), 4)
+        del m
+    return res
+
+
 def flat_top_cylinder(n, seed=3):
     """Uniform cylinder of radius 1 mm and length 2 mm with a 0.05 mm Gaussian
     edge per transverse axis, z in [0.1, 2.1] mm above the cathode plane."""
@@ -363,6 +388,8 @@ def main():
                     help="time only the 4M-particle cathode workload (128^3, image on) and print its JSON object")
     ap.add_argument("--batch-only", action="store_true",
                     help="time only the 64-bunch batch workload and print its JSON object")
+    ap.add_argument("--potential-only", action="store_true",
+                    help="time only the scalar potential of the headline bunch and print its JSON object")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -390,6 +417,11 @@ def main():
 
     if args.cathode_only:
         res = bench_cathode(sc, L, C, torch, flush, stream, ws, args.steps, args.warmup)
+        if rank == 0:
+            print(json.dumps(res), flush=True)
+        return 0
+    if args.potential_only:
+        res = bench_potential(sc, torch, dev, flush, stream, args.steps, args.warmup)
         if rank == 0:
             print(json.dumps(res), flush=True)
         return 0
@@ -531,6 +563,9 @@ def main():
                              mode, C.c_void_p(stream.cuda_stream))
         dep_ms[name] = round(max_over_ranks(timed(dep, max(3, args.steps // 2), args.warmup), ws), 4)
 
+    # ---- scalar potential of the same charge (mixed, FP64, plain FP64)
+    pot_res = bench_potential(sc, torch, dev, flush, stream, max(3, args.steps // 2), args.warmup)
+
     # ---- cathode workload: 4M-particle flat-top cylinder on the cathode, 128^3
     cath_res = None
     if not args.no_cathode:
@@ -615,6 +650,7 @@ def main():
                 "d2h_bytes_per_step": 3 * NP * 8},
         "deposit_modes_ms": dep_ms,
         "track": track_res,
+        "potential": pot_res,
         "cathode_128": cath_res,
         "batch": batch_res,
         "gpu_launches": int(round(launches_per_kick * args.steps)),

@@ -404,8 +404,14 @@ int sc_track(sc_mesh* mesh, void* x, void* y, void* z, void* ux, void* uy, void*
  * that antiderivative and the transverse factor gamma/(dx dy dz): the
  * lab-frame potential gamma*phi' of the bunch's rest-frame potential.
  * `phi` is a device array of nx*ny*nz elements of the mesh type, x fastest;
- * `at_cathode` adds the image charge's potential.  Computed in FP64 with
- * cuFFT for every mesh precision. */
+ * `at_cathode` adds the image charge's potential.
+ *  - SC_PREC_MIXED and SC_PREC_FP64 meshes with at most 128 nodes per axis:
+ *    the hand-written pipeline in the mesh's precision, with its own cached
+ *    potential Green spectrum (parity-reduced: even along every axis).  It
+ *    uses the spare fourth lane of the mesh's packed field nodes as scratch
+ *    (Ex, Ey, Ez are left as they are).
+ *  - SC_PREC_PLAIN64 meshes and longer axes: the reference's schedule in
+ *    FP64 with cuFFT. */
 int sc_solve_potential(sc_mesh* mesh, int at_cathode, void* phi, void* stream);
 
 #ifdef __cplusplus

@@ -15,7 +15,7 @@ using CUDA
 import ChainRulesCore
 
 export Mesh3D, deposit!, clear_mesh!, interpolate_field, solve!, kick, kick!, kick_host, track!, magnetic_field,
-       set_kick_mode!, set_bounds!, refit!
+       set_kick_mode!, set_bounds!, refit!, solve_potential
 
 const libsc = normpath(joinpath(@__DIR__, "..", "..", "..", "lib", "libspacecharge_gb300.so"))
 
@@ -191,6 +191,16 @@ set_kick_mode!(mesh::Mesh3D, mode::Symbol) =
 solve!(mesh::Mesh3D; at_cathode::Bool=false) =
     check(ccall((:sc_solve, libsc), Cint, (Ptr{Cvoid}, Cint, Ptr{Cvoid}), mesh.ptr, Cint(at_cathode),
                 stream_ptr()))
+
+# solve_potential(mesh; at_cathode=false) -> phi::CuArray{T,3}: the scalar
+# potential of the deposited charge with potential_green_function
+# (src/green_functions.jl:13-22, defined but not called by the reference)
+function solve_potential(mesh::Mesh3D{T}; at_cathode::Bool=false) where {T}
+    phi = CuArray{T}(undef, mesh.grid_size...)
+    check(ccall((:sc_solve_potential, libsc), Cint, (Ptr{Cvoid}, Cint, CuPtr{T}, Ptr{Cvoid}), mesh.ptr,
+                Cint(at_cathode), pointer(phi), stream_ptr()))
+    return phi
+end
 
 # interpolate_field(mesh, px, py, pz) -> (Ex, Ey, Ez), src/interpolation.jl:100-128
 function interpolate_field(mesh::Mesh3D, particles_x::CuArray{P}, particles_y::CuArray{P},
