@@ -392,12 +392,27 @@ def main():
                     help="time only the scalar potential of the headline bunch and print its JSON object")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # N ranks requested without a launcher: start them under torchrun,
+        # one process per GPU, and pass its exit status on
+        import socket
+        import subprocess
+
+        sock = socket.socket()
+        sock.bind(("127.0.0.1", 0))
+        port = sock.getsockname()[1]
+        sock.close()
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr", "127.0.0.1", f"--master-port={port}", os.path.abspath(__file__)] + sys.argv[1:]
+        return subprocess.call(cmd)
     if args.impl == "reference":
         return run_reference(args)
 
     import torch
 
     ws, rank, local = dist_env()
+    if local >= torch.cuda.device_count():
+        raise SystemExit(f"rank {rank} needs GPU {local}, but only {torch.cuda.device_count()} are visible")
     torch.cuda.set_device(local)
     if ws > 1:
         import torch.distributed as dist
