@@ -292,7 +292,12 @@ int kick_issue(sc_mesh* m, const void* x, const void* y, const void* z, const vo
     StageScope sg(m->timer, SC_STAGE_GATHER, s);
     // the tiled deposit binned exactly these particles: gather through the tiles
     if (mode == SC_DEPOSIT_TILED) return gather_tiled_launch(m, x, n, dtype, ex, ey, ez, s);
-    return gather_launch(m, x, y, z, n, dtype, ex, ey, ez, s);
+#ifndef SC_GATHER_EARLY
+#define SC_GATHER_EARLY 0
+#endif
+    // the positions are the caller's, read by the deposit before the solve's
+    // passes: no grid of this kick writes them
+    return gather_launch(m, x, y, z, n, dtype, ex, ey, ez, s, SC_GATHER_EARLY != 0);
 }
 
 // ------------------------------------------------------------ kick graph

@@ -122,12 +122,16 @@ struct GCell<double> {
 constexpr int kGathPerThread = SC_GATH_PT;
 
 // Body of one CTA: particles blk * 256 * kGathPerThread + ... of the bunch.
+// wait_after_positions: wait for the preceding grid (programmatic launch)
+// after the position loads rather than before the body; for callers whose
+// positions no preceding grid writes.
 template <typename P, typename A>
 __device__ __forceinline__ void gather_packed_body(const P* __restrict__ px, const P* __restrict__ py,
                                                    const P* __restrict__ pz, int64_t n, const Axes& ax,
                                                    const typename Packed<A>::V* __restrict__ ef, P* __restrict__ ex,
                                                    P* __restrict__ ey, P* __restrict__ ez,
-                                                   unsigned long long* __restrict__ oob, int64_t blk) {
+                                                   unsigned long long* __restrict__ oob, int64_t blk,
+                                                   bool wait_after_positions = false) {
     using V = typename Packed<A>::V;
     const int64_t base = blk * (blockDim.x * kGathPerThread) + threadIdx.x;
     P x[kGathPerThread], y[kGathPerThread], z[kGathPerThread];
@@ -139,6 +143,7 @@ __device__ __forceinline__ void gather_packed_body(const P* __restrict__ px, con
         y[k] = in ? __ldg(py + p) : P(0);
         z[k] = in ? __ldg(pz + p) : P(0);
     }
+    if (wait_after_positions) pdl_wait();
     const int nx = ax.a[0].n, ny = ax.a[1].n;
     const int64_t sy = nx, sz = (int64_t)nx * ny;
     const int64_t off[8] = {0, 1, sy, 1 + sy, sz, 1 + sz, sy + sz, 1 + sy + sz};
@@ -194,9 +199,10 @@ __global__ void __launch_bounds__(256, SC_GATH_MINB) gather_packed(const P* __re
                                                      const P* __restrict__ pz, int64_t n, Axes ax,
                                                      const typename Packed<A>::V* __restrict__ ef,
                                                      P* __restrict__ ex, P* __restrict__ ey, P* __restrict__ ez,
-                                                     unsigned long long* __restrict__ oob) {
-    pdl_wait();  // the field (and possibly the positions) come from preceding grids
-    gather_packed_body<P, A>(px, py, pz, n, ax, ef, ex, ey, ez, oob, blockIdx.x);
+                                                     unsigned long long* __restrict__ oob, int early) {
+    // the field (and, unless `early`, possibly the positions) come from preceding grids
+    if (!early) pdl_wait();
+    gather_packed_body<P, A>(px, py, pz, n, ax, ef, ex, ey, ez, oob, blockIdx.x, early != 0);
 }
 
 // Staged batch kick (batch.cuh): the gather of a group of bunches in one launch.
@@ -224,7 +230,8 @@ int batch_gather_launch(const BunchDesc* tab, const CtaRef* map, int64_t ctas, i
 }
 
 int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n, int dtype, void* ex,
-                  void* ey, void* ez, cudaStream_t s) {
+                  void* ey, void* ez, cudaStream_t s, bool early) {
+    const int e = early ? 1 : 0;
     const Axes ax = make_axes(m);
     const int64_t blocks = (n + 255) / 256;
     if (m->precision == SC_PREC_PLAIN64) {
@@ -245,20 +252,20 @@ int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64
         if (dtype == SC_F64)
             launch_pdl(gather_packed<double, float>, (unsigned)gblocks, 256, 0, s, (const double*)x, (const double*)y,
                                                                (const double*)z, n, ax, (const float4*)m->efield,
-                                                               (double*)ex, (double*)ey, (double*)ez, m->oob);
+                                                               (double*)ex, (double*)ey, (double*)ez, m->oob, e);
         else
             launch_pdl(gather_packed<float, float>, (unsigned)gblocks, 256, 0, s, (const float*)x, (const float*)y, (const float*)z, n,
                                                               ax, (const float4*)m->efield, (float*)ex, (float*)ey,
-                                                              (float*)ez, m->oob);
+                                                              (float*)ez, m->oob, e);
     } else {
         if (dtype == SC_F64)
             launch_pdl(gather_packed<double, double>, (unsigned)gblocks, 256, 0, s, (const double*)x, (const double*)y,
                                                                 (const double*)z, n, ax, (const dnode4*)m->efield,
-                                                                (double*)ex, (double*)ey, (double*)ez, m->oob);
+                                                                (double*)ex, (double*)ey, (double*)ez, m->oob, e);
         else
             launch_pdl(gather_packed<float, double>, (unsigned)gblocks, 256, 0, s, (const float*)x, (const float*)y, (const float*)z,
                                                                n, ax, (const dnode4*)m->efield, (float*)ex,
-                                                               (float*)ey, (float*)ez, m->oob);
+                                                               (float*)ey, (float*)ez, m->oob, e);
     }
     SC_LAUNCH_CHECK("gather_packed");
     m->launches += 1;

@@ -1300,8 +1300,12 @@ int native_green_async(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t* 
     // the caller's stream does not
     int least = 0, greatest = 0;
     SC_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-    if (!m->side) SC_CUDA(cudaStreamCreateWithPriority(&m->side, cudaStreamNonBlocking, greatest));
-    if (!m->side2) SC_CUDA(cudaStreamCreateWithPriority(&m->side2, cudaStreamNonBlocking, greatest));
+#ifndef SC_GREEN_LOW_PRIORITY
+#define SC_GREEN_LOW_PRIORITY 0
+#endif
+    const int prio = SC_GREEN_LOW_PRIORITY ? least : greatest;
+    if (!m->side) SC_CUDA(cudaStreamCreateWithPriority(&m->side, cudaStreamNonBlocking, prio));
+    if (!m->side2) SC_CUDA(cudaStreamCreateWithPriority(&m->side2, cudaStreamNonBlocking, prio));
     if (!m->ev_fork) SC_CUDA(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
     if (!m->ev_join) SC_CUDA(cudaEventCreateWithFlags(&m->ev_join, cudaEventDisableTiming));
     if (!m->ev_join2) SC_CUDA(cudaEventCreateWithFlags(&m->ev_join2, cudaEventDisableTiming));

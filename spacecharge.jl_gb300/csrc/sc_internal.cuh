@@ -326,8 +326,10 @@ void host_pipe_release(sc_mesh* m);
 int mesh_set_geometry(sc_mesh* m, const double lo[3], const double hi[3], const double delta[3]);
 // true when the next solve would (re)build a Green spectrum
 bool native_green_stale(const sc_mesh* m, int at_cathode);
+// early: load the positions before waiting for the preceding grid (only
+// where no preceding grid writes them: the kick, after its own passes)
 int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n,
-                  int dtype, void* ex, void* ey, void* ez, cudaStream_t s);
+                  int dtype, void* ex, void* ey, void* ez, cudaStream_t s, bool early = false);
 
 int cell_index_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n, int dtype,
                       int32_t* idx, double* frac, cudaStream_t s);
