@@ -322,6 +322,11 @@ __global__ void __launch_bounds__(256) k_green_compress(const typename Cplx<T>::
 #ifndef SC_FUSED_GREEN_XY
 #define SC_FUSED_GREEN_XY 1
 #endif
+// the field kernel's components paired, four real lines per FFT
+// (k4_green_xy, k4_green_col) where they apply
+#ifndef SC_PAIRED_GREEN
+#define SC_PAIRED_GREEN 1
+#endif
 
 // ------------------------------------------- hybrid Green build (FP32 path)
 // One thread per displacement d of the stored region (octant in free space;
@@ -842,16 +847,35 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
         float* T2 = T1 + 3 * t1max;
         const int64_t t1cs = (int64_t)Hx * ny * zc, t2cs = (int64_t)Hx * Hy * zc;
         const int64_t plane = (int64_t)Hx * Hy;
-        // x and y fused per z slice where the slice fits in shared memory
-        if (SC_FUSED_GREEN_XY &&
-            launch3_green_xy(w.log2L[0], w.log2L[1], (const float*)goct, T2, nx, ny, zc, Hx, gcs, t2cs, tw, s)) {
-            SC_LAUNCH_CHECK("k3_green_xy");
-            if (!launch3_green_col(image, w.log2L[2], T2, image ? w.gimg : w.gfree, (int)plane, 1, nz, 2, plane, 0,
-                                   t2cs, plane, 0, plane * Hz, tw, s))
-                return fail(SC_ERR_UNSUPPORTED, "Green z pass: transform length out of range");
+        // x and y fused per z slice where the slice fits in shared memory:
+        // components 0 and 1 paired (four real lines per FFT), 2 alone
+        bool xy = false;
+        int nl = 0;
+        if (SC_PAIRED_GREEN &&
+            launch_green_xy_field(w.log2L[0], w.log2L[1], (const float*)goct, T2, nx, ny, zc, Hx, gcs, t2cs, tw, s)) {
+            xy = true;
+            nl = 1;
+        } else if (SC_FUSED_GREEN_XY &&
+                   launch3_green_xy(w.log2L[0], w.log2L[1], (const float*)goct, T2, nx, ny, zc, Hx, gcs, t2cs, tw, s)) {
+            xy = true;
+            nl = 1;
+        }
+        if (xy) {
+            SC_LAUNCH_CHECK("green x+y pass");
+            bool zok;
+            if (!image && SC_PAIRED_GREEN) {
+                zok = launch_green_z_field(w.log2L[2], (const float*)T2, (float*)w.gfree, (int)plane, nz, plane, t2cs,
+                                           plane, plane * Hz, m->gamma, tw, s);
+                nl += 1;
+            } else {
+                zok = launch3_green_col(image, w.log2L[2], T2, image ? w.gimg : w.gfree, (int)plane, 1, nz, 2, plane, 0,
+                                        t2cs, plane, 0, plane * Hz, tw, s);
+                nl += 1;
+            }
+            if (!zok) return fail(SC_ERR_UNSUPPORTED, "Green z pass: transform length out of range");
             SC_LAUNCH_CHECK("green z pass");
             if (image) w.img_half = true;
-            m->launches += has_near ? 4 : 3;
+            m->launches += nl + (has_near ? 2 : 1);
             return SC_OK;
         }
         if (launch3_green_x(w.log2L[0], (const float*)goct, T1, nx, ny * zc, Hx, gcs, t1cs, tw, s) &&
@@ -954,8 +978,12 @@ static int build_green_fp64_reduced(sc_mesh* m, bool image, double offz, cudaStr
     const int64_t t1cs = (int64_t)Hx * ny * zc, t2cs = (int64_t)Hx * Hy * zc;
     const int64_t plane = (int64_t)Hx * Hy;
     void* dst = image ? w.gimg : w.gfree;
-    bool ok = launch3_green_xy<double>(w.log2L[0], w.log2L[1], G, T2, nx, ny, zc, Hx, gcs, t2cs, tw, s);
+    bool ok = SC_PAIRED_GREEN &&
+              launch_green_xy_field<double>(w.log2L[0], w.log2L[1], G, T2, nx, ny, zc, Hx, gcs, t2cs, tw, s);
     if (ok) {
+        SC_LAUNCH_CHECK("k4_green_xy");
+        m->launches += 3;
+    } else if ((ok = launch3_green_xy<double>(w.log2L[0], w.log2L[1], G, T2, nx, ny, zc, Hx, gcs, t2cs, tw, s))) {
         SC_LAUNCH_CHECK("k3_green_xy");
         m->launches += 3;
     } else {
@@ -966,9 +994,12 @@ static int build_green_fp64_reduced(sc_mesh* m, bool image, double offz, cudaStr
         SC_LAUNCH_CHECK("green x/y passes");
         m->launches += 4;
     }
-    if (!launch3_green_col<double>(image, w.log2L[2], T2, dst, (int)plane, 1, nz, 2, plane, 0, t2cs, plane, 0,
-                                   plane * Hz, tw, s))
-        return fail(SC_ERR_UNSUPPORTED, "FP64 Green z pass: transform length out of range");
+    const bool zok = (!image && SC_PAIRED_GREEN)
+                         ? launch_green_z_field<double>(w.log2L[2], T2, (double*)dst, (int)plane, nz, plane, t2cs, plane,
+                                                        plane * Hz, m->gamma, tw, s)
+                         : launch3_green_col<double>(image, w.log2L[2], T2, dst, (int)plane, 1, nz, 2, plane, 0, t2cs,
+                                                     plane, 0, plane * Hz, tw, s);
+    if (!zok) return fail(SC_ERR_UNSUPPORTED, "FP64 Green z pass: transform length out of range");
     SC_LAUNCH_CHECK("green z pass");
     if (image) w.img_half = true;
     *done = true;

@@ -954,6 +954,234 @@ __global__ void __launch_bounds__(256, sizeof(Tr) == 4 ? 3 : 1) k3_green_xy(cons
     }
 }
 
+// Paired Green transform of the field kernel: four real lines per complex
+// FFT.  An even real line has a real spectrum E, an odd one an imaginary
+// spectrum i P; for z = e1 + i e2 + o1 + i o2 (e even, o odd),
+//   Z(k) = (E1 - P2) + i (E2 + P1),  Z(L - k) = (E1 + P2) + i (E2 - P1),
+// so E1, E2, P1, P2 follow from Z(k) and Z(L - k).  The field kernel's
+// components have that mix: along x component 0 is odd and 1 even, along y
+// component 1 odd and 0 even, along z (free space) component 2 odd and 0, 1
+// even.  Pairing components 0 and 1 in the x and y passes and 0 and 2 in the
+// z pass does their transforms with half the FFTs of k3_green_xy and
+// k3_green_col; the remaining component runs through those kernels alone.
+template <typename T2, typename Tr>
+__device__ __forceinline__ void unpack4(T2 Zk, T2 Zm, Tr& e1, Tr& e2, Tr& p1, Tr& p2) {
+    e1 = Tr(0.5) * (Zk.x + Zm.x);
+    p2 = Tr(0.5) * (Zm.x - Zk.x);
+    e2 = Tr(0.5) * (Zk.y + Zm.y);
+    p1 = Tr(0.5) * (Zk.y - Zm.y);
+}
+
+// x and y passes of the field kernel's three components, Lx = Ly = L, NTH
+// threads, one stored z slice per blockIdx.x and two CTA roles
+// (blockIdx.y): role 0 transforms components 0 (odd along x, even along y)
+// and 1 (even along x, odd along y) together, four lines per FFT; role 1
+// transforms component 2 (even along both) with two lines per FFT through
+// the same code, its odd partner zero.  The rows go along x into shared
+// memory, then the columns along y into T2out[comp][iz][ky][kx].
+template <int L, typename Tr, int NTH>
+__global__ void __launch_bounds__(NTH, 1) k4_green_xy(const Tr* __restrict__ G, Tr* __restrict__ T2out, int nx,
+                                                      int ny, int Hx, int64_t gcs, int64_t t2cs,
+                                                      const typename Cplx<Tr>::T2* __restrict__ tw) {
+    using E = F2<L>;
+    using T2 = typename Cplx<Tr>::T2;
+    constexpr int W = NTH / E::NT;  // row pairs (x pass) or column pairs (y pass) per round
+    __shared__ T2 swt[L];
+    stage_twiddles<L>(swt, tw);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T2* xb = reinterpret_cast<T2*>(smraw);             // W exchange columns
+    Tr* ts0 = reinterpret_cast<Tr*>(xb + W * E::S);  // [ny][Hx]: the lines even along y, after the x pass
+    Tr* ts1 = ts0 + (int64_t)ny * Hx;                 // the lines odd along y (role 0)
+    const int iz = blockIdx.x;
+    const bool pair = blockIdx.y == 0;
+    T2 v[16];
+    {
+        const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
+        T2* col = xb + p * E::S;
+        // even along x: component 1 (role 0) or 2 (role 1); odd: component 0
+        const Tr* ge = G + (pair ? 1 : 2) * gcs + (int64_t)nx * ny * iz;
+        const Tr* go = G + (int64_t)nx * ny * iz;
+        Tr* dst_e = pair ? ts1 : ts0;
+        for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
+            const int y0 = 2 * (q0 + p), y1 = y0 + 1;
+            const bool ok0 = y0 < ny, ok1 = y1 < ny;
+            if (t < E::R2) {
+#pragma unroll
+                for (int s = 0; s < E::R1; ++s) {
+                    const int x = t + E::R2 * s;
+                    const int dx = x < nx ? x : (x > L - nx ? x - L : L);
+                    Tr e1 = 0, e2 = 0, o1 = 0, o2 = 0;
+                    if (dx != L) {
+                        const int ax = dx < 0 ? -dx : dx;
+                        if (ok0) e1 = __ldg(ge + (int64_t)nx * y0 + ax);
+                        if (ok1) e2 = __ldg(ge + (int64_t)nx * y1 + ax);
+                        // an odd line vanishes at d = 0 (the stored sample there is rounding)
+                        if (pair && dx != 0) {
+                            if (ok0) o1 = __ldg(go + (int64_t)nx * y0 + ax);
+                            if (ok1) o2 = __ldg(go + (int64_t)nx * y1 + ax);
+                            if (dx < 0) o1 = -o1, o2 = -o2;
+                        }
+                    }
+                    v[s] = Cplx<Tr>::make(e1 + o1, e2 + o2);
+                }
+            }
+            E::template fwd<false>(v, col, t, swt);
+            if (t < E::R1) {
+#pragma unroll
+                for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+            }
+            __syncthreads();
+            if (ok0) {
+                for (int k = t; k <= L / 2; k += E::NT) {
+                    Tr e1, e2, p1, p2;
+                    unpack4(col[xsw(k)], col[xsw((L - k) & (L - 1))], e1, e2, p1, p2);
+                    dst_e[y0 * Hx + k] = e1;
+                    if (ok1) dst_e[y1 * Hx + k] = e2;
+                    if (pair) {
+                        ts0[y0 * Hx + k] = p1;
+                        if (ok1) ts0[y1 * Hx + k] = p2;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    {
+        const int c = threadIdx.x % W, t = threadIdx.x / W;
+        T2* col = xb + c * E::S;
+        // even along y: component 0 (role 0) or 2 (role 1); odd: component 1
+        Tr* out_e = T2out + (pair ? 0 : 2) * t2cs + (int64_t)Hx * (L / 2 + 1) * iz;
+        Tr* out_o = T2out + t2cs + (int64_t)Hx * (L / 2 + 1) * iz;
+        // the Nyquist column kx = L/2 by direct sums:
+        // X(k) = sum_d x(d) w^(k d), d = -(ny-1)..ny-1
+        for (int k = threadIdx.x; k <= L / 2; k += NTH) {
+            Tr re = 0, im = 0;
+            for (int d = 0; d < ny; ++d) {
+                const T2 wp = swt[(k * d) & (L - 1)];
+                if (d == 0) {
+                    re += ts0[L / 2];
+                } else {
+                    re += Tr(2) * ts0[d * Hx + L / 2] * wp.x;                   // even: 2 x(d) Re w^kd
+                    if (pair) im += Tr(2) * ts1[d * Hx + L / 2] * wp.y;        // odd: 2i x(d) Im w^kd
+                }
+            }
+            out_e[(int64_t)k * Hx + L / 2] = re;
+            if (pair) out_o[(int64_t)k * Hx + L / 2] = im;
+        }
+        for (int k0 = 0; k0 < L / 2; k0 += 2 * W) {
+            const int fa = k0 + c, fb = fa + W;
+            const bool oka = fa < L / 2, okb = fb < L / 2;
+            if (t < E::R2) {
+#pragma unroll
+                for (int s = 0; s < E::R1; ++s) {
+                    const int n = t + E::R2 * s;
+                    const int d = n < ny ? n : (n > L - ny ? n - L : L);
+                    Tr e1 = 0, e2 = 0, o1 = 0, o2 = 0;
+                    if (d != L) {
+                        const int ad = d < 0 ? -d : d;
+                        if (oka) e1 = ts0[ad * Hx + fa];
+                        if (okb) e2 = ts0[ad * Hx + fb];
+                        if (pair && d != 0) {
+                            if (oka) o1 = ts1[ad * Hx + fa];
+                            if (okb) o2 = ts1[ad * Hx + fb];
+                            if (d < 0) o1 = -o1, o2 = -o2;
+                        }
+                    }
+                    v[s] = Cplx<Tr>::make(e1 + o1, e2 + o2);
+                }
+            }
+            E::template fwd<false>(v, col, t, swt);
+            if (t < E::R1) {
+#pragma unroll
+                for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+            }
+            __syncthreads();
+            for (int k = t; k <= L / 2; k += E::NT) {
+                Tr e1, e2, p1, p2;
+                unpack4(col[xsw(k)], col[xsw((L - k) & (L - 1))], e1, e2, p1, p2);
+                if (oka) out_e[(int64_t)k * Hx + fa] = e1;
+                if (okb) out_e[(int64_t)k * Hx + fb] = e2;
+                if (pair) {
+                    if (oka) out_o[(int64_t)k * Hx + fa] = p1;
+                    if (okb) out_o[(int64_t)k * Hx + fb] = p2;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Free-space z pass of the field kernel's three components, two CTA roles
+// (blockIdx.y): role 0 transforms components 0 (even along z) and 2 (odd)
+// together, four lines per FFT; role 1 component 1 (even), two lines per
+// FFT through the same code.  Column pairs fa, fb = fa + kColW of the ncols
+// columns: input sample d >= 0 of component c at in + c*cs_in + col +
+// d*as_in (d < nh), output k <= L/2 of the kept part (E for the even, P for
+// the odd component) at out + c*cs_out + col + k*as_out.  Lines summed into
+// one FFT keep the precision of the larger: component 2 lacks the factor
+// gamma of components 0 and 1, so it enters multiplied by s2 (a power of two
+// near gamma) and leaves divided by it, both exact.
+template <int L, typename Tr>
+__global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k4_green_col(const Tr* __restrict__ in,
+                                                                           Tr* __restrict__ out, int ncols, int nh,
+                                                                           int64_t as_in, int64_t cs_in,
+                                                                           int64_t as_out, int64_t cs_out, Tr s2,
+                                                                           const typename Cplx<Tr>::T2* __restrict__ tw) {
+    using E = F2<L>;
+    using T2 = typename Cplx<Tr>::T2;
+    __shared__ T2 swt[L];
+    stage_twiddles<L>(swt, tw);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    T2* xb = reinterpret_cast<T2*>(smraw);
+    const bool pair = blockIdx.y == 0;
+    const Tr* ie = in + (pair ? 0 : 1) * cs_in;
+    const Tr* io = in + 2 * cs_in;
+    Tr* oe = out + (pair ? 0 : 1) * cs_out;
+    Tr* oo = out + 2 * cs_out;
+    const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
+    const int64_t fa = (int64_t)blockIdx.x * (2 * kColW) + c, fb = fa + kColW;
+    const bool oka = fa < ncols, okb = fb < ncols;
+    T2* col = xb + c * E::S;
+    T2 v[16];
+    if (t < E::R2) {
+#pragma unroll
+        for (int s = 0; s < E::R1; ++s) {
+            const int n = t + E::R2 * s;
+            const int d = n < nh ? n : (n > L - nh ? n - L : L);
+            Tr e1 = 0, e2 = 0, o1 = 0, o2 = 0;
+            if (d != L) {
+                const int64_t o = (int64_t)(d < 0 ? -d : d) * as_in;
+                if (oka) e1 = __ldg(ie + fa + o);
+                if (okb) e2 = __ldg(ie + fb + o);
+                // an odd line vanishes at d = 0 (the stored sample there is rounding)
+                if (pair && d != 0) {
+                    if (oka) o1 = s2 * __ldg(io + fa + o);
+                    if (okb) o2 = s2 * __ldg(io + fb + o);
+                    if (d < 0) o1 = -o1, o2 = -o2;
+                }
+            }
+            v[s] = Cplx<Tr>::make(e1 + o1, e2 + o2);
+        }
+    }
+    E::template fwd<false>(v, col, t, swt);
+    if (t < E::R1) {
+#pragma unroll
+        for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+    }
+    __syncthreads();
+    const Tr inv2 = Tr(1) / s2;
+    for (int k = t; k <= L / 2; k += E::NT) {
+        Tr e1, e2, p1, p2;
+        unpack4(col[xsw(k)], col[xsw((L - k) & (L - 1))], e1, e2, p1, p2);
+        if (oka) oe[fa + k * as_out] = e1;
+        if (okb) oe[fb + k * as_out] = e2;
+        if (pair) {
+            if (oka) oo[fa + k * as_out] = p1 * inv2;
+            if (okb) oo[fb + k * as_out] = p2 * inv2;
+        }
+    }
+}
+
 // Launch helpers: run the two-step kernel when L <= 256, report false
 // otherwise (the caller falls back to the Stockham kernels).
 #define SC_L_SWITCH(logL, MACRO) \
@@ -1163,6 +1391,58 @@ static bool launch3_green_col(bool img, int logL, const Tr* in, void* out, int n
     }
     SC_L_SWITCH(logL, SC_K3GC)
 #undef SC_K3GC
+    return true;
+}
+
+// x and y passes of the field kernel's three components in one launch of
+// k4_green_xy (256 threads, or 512 when the two slices need more than
+// 100 KB of shared memory).  Returns false (nothing launched) where they do
+// not fit; the caller then runs launch3_green_xy or the separate passes.
+template <typename Tr>
+static bool launch_green_xy_field(int logLx, int logLy, const Tr* G, Tr* T2, int nx, int ny, int zc, int Hx,
+                                  int64_t gcs, int64_t t2cs, const typename Cplx<Tr>::T2* tw, cudaStream_t s) {
+    using C2 = typename Cplx<Tr>::T2;
+    if (logLx != logLy) return false;
+    const size_t planes = 2 * sizeof(Tr) * (size_t)ny * Hx;
+    bool ok = false;
+#define SC_K4XY(LL)                                                                                              \
+    {                                                                                                            \
+        const size_t s256 = sizeof(C2) * (size_t)(256 / F2<LL>::NT) * F2<LL>::S + planes;                        \
+        const size_t s512 = sizeof(C2) * (size_t)(512 / F2<LL>::NT) * F2<LL>::S + planes;                        \
+        if (s256 <= 100 * 1024) {                                                                                \
+            if (set_smem(k4_green_xy<LL, Tr, 256>, s256) != SC_OK) return false;                                 \
+            launch_pdl(k4_green_xy<LL, Tr, 256>, dim3(zc, 2), 256, s256, s, G, T2, nx, ny, Hx, gcs, t2cs, tw);   \
+            ok = true;                                                                                           \
+        } else if (s512 <= 220 * 1024) {                                                                         \
+            if (set_smem(k4_green_xy<LL, Tr, 512>, s512) != SC_OK) return false;                                 \
+            launch_pdl(k4_green_xy<LL, Tr, 512>, dim3(zc, 2), 512, s512, s, G, T2, nx, ny, Hx, gcs, t2cs, tw);   \
+            ok = true;                                                                                           \
+        }                                                                                                        \
+    }
+    SC_L_SWITCH(logLx, SC_K4XY)
+#undef SC_K4XY
+    return ok;
+}
+
+// Free-space z pass of the field kernel's three components in one launch
+// of k4_green_col.  Columns at in + c*cs_in + col + d*as_in, out + c*cs_out
+// + col + k*as_out.
+template <typename Tr>
+static bool launch_green_z_field(int logL, const Tr* in, Tr* out, int ncols, int nh, int64_t as_in, int64_t cs_in,
+                                 int64_t as_out, int64_t cs_out, double gamma, const typename Cplx<Tr>::T2* tw,
+                                 cudaStream_t s) {
+    using T2 = typename Cplx<Tr>::T2;
+    const Tr s2 = (Tr)exp2(rint(log2(gamma > 1.0 ? gamma : 1.0)));  // a power of two: exact scaling
+    const dim3 grid((unsigned)(((int64_t)ncols + 2 * kColW - 1) / (2 * kColW)), 2);
+#define SC_K4GC(LL)                                                                                         \
+    {                                                                                                       \
+        const size_t smem = sizeof(T2) * kColW * F2<LL>::S;                                                 \
+        if (set_smem(k4_green_col<LL, Tr>, smem) != SC_OK) return false;                                    \
+        launch_pdl(k4_green_col<LL, Tr>, grid, kColW * F2<LL>::NT, smem, s, in, out, ncols, nh, as_in, cs_in, \
+                   as_out, cs_out, s2, tw);                                                                 \
+    }
+    SC_L_SWITCH(logL, SC_K4GC)
+#undef SC_K4GC
     return true;
 }
 
