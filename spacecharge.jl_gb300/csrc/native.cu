@@ -834,12 +834,54 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
     const int near_blocks = (int)((nterm + 63) / 64);
     k_igf_split<<<(unsigned)(near_blocks + (cells + 63) / 64), 64, 0, s>>>((float*)goct, fnear, g, near_blocks);
     SC_LAUNCH_CHECK("k_igf_split");
+    // the near cells' differences: inside the paired x+y pass where that
+    // runs, else their own launch before the transform
+    GreenNear gn{};
+    if (has_near) {
+        gn.T = fnear;
+        gn.nx = nx;
+        gn.ny = ny;
+        gn.nz = nz;
+        gn.image = g.image;
+        gn.nbx = g.nbx;
+        gn.nby = g.nby;
+        gn.bz0 = g.bz0;
+        gn.bz1 = g.bz1;
+        gn.ux = g.ux;
+        gn.uy = g.uy;
+        gn.uz = g.uz;
+        gn.uoff = g.uoff;
+        gn.ratio = (float)kNearRatio;
+        gn.fz = 1.0 / (g.dx * g.dy * g.dz);
+        gn.fxy = g.gamma / (g.dx * g.dy * g.dz);
+        gn.scale = g.scale;
+    }
+    const bool two_step = fft_engine() == 0 && w.log2L[0] <= 8 && w.log2L[1] <= 8 && w.log2L[2] <= 8;
+    if (two_step && SC_PAIRED_GREEN && has_near) {
+        const int64_t t1max = (int64_t)Hx * ny * (2 * nz - 1), t2max = (int64_t)Hx * Hy * (2 * nz - 1);
+        if (!gtmp) SC_CUDA(dev_alloc(&gtmp, sizeof(float) * 3 * (t1max + t2max)));
+        float* T2p = (float*)gtmp + 3 * t1max;
+        const int64_t t2cs = (int64_t)Hx * Hy * zc;
+        const int64_t plane = (int64_t)Hx * Hy;
+        if (launch_green_xy_field(w.log2L[0], w.log2L[1], (float*)goct, T2p, nx, ny, zc, Hx, gcs, t2cs, tw, s, gn)) {
+            SC_LAUNCH_CHECK("k4_green_xy");
+            const bool zok = image ? launch3_green_col(true, w.log2L[2], T2p, w.gimg, (int)plane, 1, nz, 2, plane, 0,
+                                                       t2cs, plane, 0, plane * Hz, tw, s)
+                                   : launch_green_z_field(w.log2L[2], (const float*)T2p, (float*)w.gfree, (int)plane,
+                                                          nz, plane, t2cs, plane, plane * Hz, m->gamma, tw, s);
+            if (!zok) return fail(SC_ERR_UNSUPPORTED, "Green z pass: transform length out of range");
+            SC_LAUNCH_CHECK("green z pass");
+            if (image) w.img_half = true;
+            m->launches += 3;
+            return SC_OK;
+        }
+    }
     if (has_near) {
         const int64_t box = (int64_t)g.nbx * g.nby * (g.bz1 - g.bz0);
         launch_pdl(k_igf_near_cells, (unsigned)((3 * box + 63) / 64), 64, 0, s, (float*)goct, (const double*)fnear, g);
         SC_LAUNCH_CHECK("k_igf_near_cells");
     }
-    if (fft_engine() == 0 && w.log2L[0] <= 8 && w.log2L[1] <= 8 && w.log2L[2] <= 8) {
+    if (two_step) {
         // parity-reduced transform: real octant lines only (pipeline2.cuh)
         const int64_t t1max = (int64_t)Hx * ny * (2 * nz - 1), t2max = (int64_t)Hx * Hy * (2 * nz - 1);
         if (!gtmp) SC_CUDA(dev_alloc(&gtmp, sizeof(float) * 3 * (t1max + t2max)));
@@ -852,7 +894,7 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
         bool xy = false;
         int nl = 0;
         if (SC_PAIRED_GREEN &&
-            launch_green_xy_field(w.log2L[0], w.log2L[1], (const float*)goct, T2, nx, ny, zc, Hx, gcs, t2cs, tw, s)) {
+            launch_green_xy_field(w.log2L[0], w.log2L[1], (float*)goct, T2, nx, ny, zc, Hx, gcs, t2cs, tw, s)) {
             xy = true;
             nl = 1;
         } else if (SC_FUSED_GREEN_XY &&

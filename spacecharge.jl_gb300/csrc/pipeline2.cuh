@@ -972,6 +972,47 @@ __device__ __forceinline__ void unpack4(T2 Zk, T2 Zm, Tr& e1, Tr& e2, Tr& p1, Tr
     p1 = Tr(0.5) * (Zk.y - Zm.y);
 }
 
+// The FP32 Green build's near cells, for k4_green_xy to fill in: the FP64
+// antiderivative terms T[term][comp][corner] on the corners of the near box
+// (ix < nbx, iy < nby, bz0 <= dz < bz1), and what the near test and the
+// 8-point difference need.  T null: no near cells to fill (the FP64 build).
+struct GreenNear {
+    const double* T;
+    int nx, ny, nz, image;
+    int nbx, nby, bz0, bz1;
+    float ux, uy, uz, uoff, ratio;  // the cell test: |centre| / hmax < ratio
+    double fxy, fz;                 // gamma / (dx dy dz), 1 / (dx dy dz)
+    double scale;                   // FPEI / (Lx Ly Lz)
+};
+
+// Whether the stored cell (ix, iy, dz) takes the FP64 corner difference: the
+// test the far-cell quadrature skipped it by (native.cu oct_cell).
+__device__ __forceinline__ bool green_near_cell(const GreenNear& g, int ix, int iy, int dz) {
+    const float px = (float)ix * g.ux, py = (float)iy * g.uy, pz = fmaf((float)dz, g.uz, g.uoff);
+    const float r = sqrtf(fmaf(px, px, fmaf(py, py, pz * pz)));
+    return r < g.ratio && ix < g.nbx && iy < g.nby && dz >= g.bz0 && dz < g.bz1;
+}
+
+// The 8-point difference (green_functions.jl:108-111) of near cell (ix, iy,
+// dz), component c, from the corner terms F = (T0 - T1 + T2) * factor_c.
+__device__ __forceinline__ float green_near_value(const GreenNear& g, int c, int ix, int iy, int dz) {
+    const int cx = g.nbx + 1, cy = g.nby + 1, cz = g.bz1 - g.bz0 + 1;
+    const int64_t per = (int64_t)cx * cy * cz;
+    const int64_t sy = cx, sz = (int64_t)cx * cy;
+    const double fc = c == 2 ? g.fz : g.fxy;
+    const double* t0 = g.T + c * per + ix + sy * iy + sz * (dz - g.bz0);
+    const double* t1 = t0 + 3 * per;
+    const double* t2 = t1 + 3 * per;
+    double F[8];  // corner (a, b, e) at a + 2b + 4e
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int64_t q = (k & 1) + sy * ((k >> 1) & 1) + sz * (k >> 2);
+        F[k] = (__ldg(t0 + q) - __ldg(t1 + q) + __ldg(t2 + q)) * fc;
+    }
+    const double G3 = F[7] - F[6] - F[5] - F[3] - F[0] + F[4] + F[2] + F[1];
+    return (float)(G3 * g.scale);
+}
+
 // x and y passes of the field kernel's three components, Lx = Ly = L, NTH
 // threads, one stored z slice per blockIdx.x and two CTA roles
 // (blockIdx.y): role 0 transforms components 0 (odd along x, even along y)
@@ -979,9 +1020,13 @@ __device__ __forceinline__ void unpack4(T2 Zk, T2 Zm, Tr& e1, Tr& e2, Tr& p1, Tr
 // transforms component 2 (even along both) with two lines per FFT through
 // the same code, its odd partner zero.  The rows go along x into shared
 // memory, then the columns along y into T2out[comp][iz][ky][kx].
+// With near.T set (the FP32 build), a CTA whose slice meets the near box
+// first writes that slice's near cells of its components into G (the far
+// cells come from the preceding launch), so the near cells take no launch
+// of their own; G is then read through L2 (__ldcg), which sees those writes.
 template <int L, typename Tr, int NTH>
-__global__ void __launch_bounds__(NTH, 1) k4_green_xy(const Tr* __restrict__ G, Tr* __restrict__ T2out, int nx,
-                                                      int ny, int Hx, int64_t gcs, int64_t t2cs,
+__global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2out, int nx,
+                                                      int ny, int Hx, int64_t gcs, int64_t t2cs, GreenNear near,
                                                       const typename Cplx<Tr>::T2* __restrict__ tw) {
     using E = F2<L>;
     using T2 = typename Cplx<Tr>::T2;
@@ -994,6 +1039,20 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(const Tr* __restrict__ G, 
     Tr* ts1 = ts0 + (int64_t)ny * Hx;                 // the lines odd along y (role 0)
     const int iz = blockIdx.x;
     const bool pair = blockIdx.y == 0;
+    if (near.T) {
+        const int dz = near.image ? iz - (near.nz - 1) : iz;
+        if (dz >= near.bz0 && dz < near.bz1) {
+            const int box = near.nbx * near.nby;
+            for (int e = threadIdx.x; e < (pair ? 2 : 1) * box; e += NTH) {
+                const int c = pair ? e / box : 2;
+                const int r = e - (pair ? c : 0) * box;
+                const int ix = r % near.nbx, iy = r / near.nbx;
+                if (green_near_cell(near, ix, iy, dz))
+                    G[c * gcs + ix + (int64_t)nx * (iy + (int64_t)ny * iz)] = (Tr)green_near_value(near, c, ix, iy, dz);
+            }
+            __syncthreads();
+        }
+    }
     T2 v[16];
     {
         const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
@@ -1013,12 +1072,12 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(const Tr* __restrict__ G, 
                     Tr e1 = 0, e2 = 0, o1 = 0, o2 = 0;
                     if (dx != L) {
                         const int ax = dx < 0 ? -dx : dx;
-                        if (ok0) e1 = __ldg(ge + (int64_t)nx * y0 + ax);
-                        if (ok1) e2 = __ldg(ge + (int64_t)nx * y1 + ax);
+                        if (ok0) e1 = __ldcg(ge + (int64_t)nx * y0 + ax);
+                        if (ok1) e2 = __ldcg(ge + (int64_t)nx * y1 + ax);
                         // an odd line vanishes at d = 0 (the stored sample there is rounding)
                         if (pair && dx != 0) {
-                            if (ok0) o1 = __ldg(go + (int64_t)nx * y0 + ax);
-                            if (ok1) o2 = __ldg(go + (int64_t)nx * y1 + ax);
+                            if (ok0) o1 = __ldcg(go + (int64_t)nx * y0 + ax);
+                            if (ok1) o2 = __ldcg(go + (int64_t)nx * y1 + ax);
                             if (dx < 0) o1 = -o1, o2 = -o2;
                         }
                     }
@@ -1399,8 +1458,9 @@ static bool launch3_green_col(bool img, int logL, const Tr* in, void* out, int n
 // 100 KB of shared memory).  Returns false (nothing launched) where they do
 // not fit; the caller then runs launch3_green_xy or the separate passes.
 template <typename Tr>
-static bool launch_green_xy_field(int logLx, int logLy, const Tr* G, Tr* T2, int nx, int ny, int zc, int Hx,
-                                  int64_t gcs, int64_t t2cs, const typename Cplx<Tr>::T2* tw, cudaStream_t s) {
+static bool launch_green_xy_field(int logLx, int logLy, Tr* G, Tr* T2, int nx, int ny, int zc, int Hx,
+                                  int64_t gcs, int64_t t2cs, const typename Cplx<Tr>::T2* tw, cudaStream_t s,
+                                  const GreenNear& near = GreenNear{}) {
     using C2 = typename Cplx<Tr>::T2;
     if (logLx != logLy) return false;
     const size_t planes = 2 * sizeof(Tr) * (size_t)ny * Hx;
@@ -1411,11 +1471,11 @@ static bool launch_green_xy_field(int logLx, int logLy, const Tr* G, Tr* T2, int
         const size_t s512 = sizeof(C2) * (size_t)(512 / F2<LL>::NT) * F2<LL>::S + planes;                        \
         if (s256 <= 100 * 1024) {                                                                                \
             if (set_smem(k4_green_xy<LL, Tr, 256>, s256) != SC_OK) return false;                                 \
-            launch_pdl(k4_green_xy<LL, Tr, 256>, dim3(zc, 2), 256, s256, s, G, T2, nx, ny, Hx, gcs, t2cs, tw);   \
+            launch_pdl(k4_green_xy<LL, Tr, 256>, dim3(zc, 2), 256, s256, s, G, T2, nx, ny, Hx, gcs, t2cs, near, tw);   \
             ok = true;                                                                                           \
         } else if (s512 <= 220 * 1024) {                                                                         \
             if (set_smem(k4_green_xy<LL, Tr, 512>, s512) != SC_OK) return false;                                 \
-            launch_pdl(k4_green_xy<LL, Tr, 512>, dim3(zc, 2), 512, s512, s, G, T2, nx, ny, Hx, gcs, t2cs, tw);   \
+            launch_pdl(k4_green_xy<LL, Tr, 512>, dim3(zc, 2), 512, s512, s, G, T2, nx, ny, Hx, gcs, t2cs, near, tw);   \
             ok = true;                                                                                           \
         }                                                                                                        \
     }
