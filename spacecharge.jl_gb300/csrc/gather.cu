@@ -206,8 +206,10 @@ __global__ void __launch_bounds__(256, SC_GATH_MINB) gather_packed(const P* __re
 }
 
 // Staged batch kick (batch.cuh): the gather of a group of bunches in one launch.
+// (three CTAs per SM, as the single-mesh gather's 80 registers allow; the
+// table lookup would otherwise push it to 128 and two)
 template <typename P>
-__global__ void __launch_bounds__(256, SC_GATH_MINB) kb_gather(const BunchDesc* __restrict__ tab,
+__global__ void __launch_bounds__(256, 3) kb_gather(const BunchDesc* __restrict__ tab,
                                                                const CtaRef* __restrict__ map) {
     const CtaRef r = map[blockIdx.x];
     const BunchDesc& b = tab[r.item];
