@@ -608,7 +608,7 @@ def main():
     # kernels and algorithmic bytes per launch of each stage on the caller's stream
     stages = {
         "deposit": ("memset + deposit_vector<double> + k_corner_sum", NP * 32 + N * 4),
-        "zpass": ("k2_zpass<256>", Hx * Ly * nz * 8 + 3 * Hx * Ly * nz * 8),
+        "zpass": ("k2_zpass<256, true>", Hx * Ly * nz * 8 + 3 * Hx * Ly * nz * 8),
         "gather": ("gather_packed<double,float>", NP * (24 + 24) + N * 16),
         "fwd_x": ("k2_fwd_x<128>", N * 4 + Hx * ny * nz * 8),
         "fwd_y": ("k2_col<128,fwd>", Hx * ny * nz * 8 + Hx * Ly * nz * 8),

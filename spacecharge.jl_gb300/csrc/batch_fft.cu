@@ -74,7 +74,10 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) kb_zpass(con
     const int Hx = b.Hx, Ly = b.Ly, nz = b.nz;
     stage_twiddles<L>(swt, tw);
     extern __shared__ __align__(16) unsigned char smraw[];
-    zpass_body<L>(B, C, Hx, Ly, nz, gv, r.local, swt, smraw);
+    if (2 * nz == L)
+        zpass_body<L, true>(B, C, Hx, Ly, nz, gv, r.local, swt, smraw);
+    else
+        zpass_body<L, false>(B, C, Hx, Ly, nz, gv, r.local, swt, smraw);
 }
 
 // CTA local index = 3 * z + component

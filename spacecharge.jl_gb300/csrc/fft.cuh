@@ -7,6 +7,8 @@
 // FP32 transform uses correctly rounded roots of unity.
 #pragma once
 
+#include <type_traits>
+
 #include "sc_internal.cuh"
 
 namespace sc {
@@ -24,17 +26,28 @@ struct Cplx<double> {
     __device__ __forceinline__ static double2 make(double a, double b) { return make_double2(a, b); }
 };
 
+// Complex add and subtract.  FP32 pairs use the paired FP32 instructions of
+// sm_100 and later (one instruction for both lanes of a float2, each lane
+// rounded as the scalar operation); a - b is the exact fma(b, -1, a).
 template <typename T2>
 __device__ __forceinline__ T2 cadd(T2 a, T2 b) {
-    a.x += b.x;
-    a.y += b.y;
-    return a;
+    if constexpr (std::is_same<T2, float2>::value) {
+        return __fadd2_rn(a, b);
+    } else {
+        a.x += b.x;
+        a.y += b.y;
+        return a;
+    }
 }
 template <typename T2>
 __device__ __forceinline__ T2 csub(T2 a, T2 b) {
-    a.x -= b.x;
-    a.y -= b.y;
-    return a;
+    if constexpr (std::is_same<T2, float2>::value) {
+        return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+    } else {
+        a.x -= b.x;
+        a.y -= b.y;
+        return a;
+    }
 }
 template <typename T2>
 __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
@@ -103,11 +116,21 @@ __device__ __forceinline__ void dft2(T2& a, T2& b) {
 template <bool INV, typename T2>
 __device__ __forceinline__ void dft4(T2& v0, T2& v1, T2& v2, T2& v3) {
     const T2 a0 = cadd(v0, v2), a1 = csub(v0, v2);
-    const T2 a2 = cadd(v1, v3), a3 = rot<INV>(csub(v1, v3));
+    const T2 a2 = cadd(v1, v3);
     v0 = cadd(a0, a2);
     v2 = csub(a0, a2);
-    v1 = cadd(a1, a3);
-    v3 = csub(a1, a3);
+    if constexpr (std::is_same<T2, float2>::value) {
+        // a1 +- rot(d) lane by lane: the rotation swaps the lanes, which a
+        // paired instruction cannot do without moves
+        const T2 d = csub(v1, v3);
+        const float dy = INV ? -d.y : d.y, dx = INV ? -d.x : d.x;
+        v1 = make_float2(a1.x + dy, a1.y - dx);
+        v3 = make_float2(a1.x - dy, a1.y + dx);
+    } else {
+        const T2 a3 = rot<INV>(csub(v1, v3));
+        v1 = cadd(a1, a3);
+        v3 = csub(a1, a3);
+    }
 }
 template <bool INV, typename T2>
 __device__ __forceinline__ void dft8(T2* v) {

@@ -28,6 +28,17 @@ struct XS {
     static constexpr int value = (raw & 1) ? raw : raw + 1;
 };
 __device__ __forceinline__ int xsw(int idx) { return idx + (idx >> 4); }
+// The two access patterns of the exchange, with the swizzle split into a
+// per-thread base and a compile-time offset (R divides 16, so a run of R
+// consecutive indices starting at a multiple of R never crosses a multiple
+// of 16, and t + R*r with t < R carries nothing into bit 4):
+//   xsw(t * R + k) = xrow<R>(t) + k          for k < R
+//   xsw(t + R * r) = t + xoff(R * r)         for t < R
+__host__ __device__ constexpr int xoff(int i) { return i + (i >> 4); }
+template <int R>
+__device__ __forceinline__ int xrow(int t) {
+    return t * R + ((t * R) >> 4);
+}
 
 template <int L>
 struct Split;  // (R1, R2) for each length
@@ -62,18 +73,21 @@ struct F2 {
     // A -> B.  v holds R1 (data) values on entry when t < R2; on exit R2
     // (spectrum) values when t < R1.  `col` is this column's exchange buffer,
     // `sw` the staged twiddles w_L^j.
+    // `active` as in inv().
     template <bool INV, typename T2>
-    __device__ __forceinline__ static void fwd(T2 (&v)[16], T2* col, int t, const T2* sw) {
-        if (t < R2) {
+    __device__ __forceinline__ static void fwd(T2 (&v)[16], T2* col, int t, const T2* sw, bool active = true) {
+        if (active && t < R2) {
             dft<R1, INV>(v);
+            T2* cw = col + xrow<R1>(t);
 #pragma unroll
-            for (int k = 0; k < R1; ++k) col[xsw(t * R1 + k)] = v[k];
+            for (int k = 0; k < R1; ++k) cw[k] = v[k];
         }
         __syncthreads();
-        if (t < R1) {
+        if (active && t < R1) {
+            const T2* cr = col + t;
 #pragma unroll
             for (int r = 0; r < R2; ++r) {
-                T2 a = col[xsw(t + R1 * r)];
+                T2 a = cr[xoff(R1 * r)];
                 if (r > 0) {
                     const T2 w = sw[r * t];
                     a = INV ? cmulc(a, w) : cmul(a, w);
@@ -86,11 +100,14 @@ struct F2 {
     }
 
     // B -> A (unnormalised inverse when INV).  v holds R2 spectrum values on
-    // entry when t < R1; on exit R1 data values when t < R2.
+    // entry when t < R1; on exit R1 data values when t < R2.  `active` false
+    // (uniform over each warp) skips the arithmetic but keeps the two
+    // barriers, so warps without a column cost almost no issue slots.
     template <bool INV, typename T2>
-    __device__ __forceinline__ static void inv(T2 (&v)[16], T2* col, int t, const T2* sw) {
-        if (t < R1) {
+    __device__ __forceinline__ static void inv(T2 (&v)[16], T2* col, int t, const T2* sw, bool active = true) {
+        if (active && t < R1) {
             dft<R2, INV>(v);
+            T2* cw = col + xrow<R2>(t);
 #pragma unroll
             for (int n1 = 0; n1 < R2; ++n1) {
                 T2 a = v[n1];
@@ -98,13 +115,14 @@ struct F2 {
                     const T2 w = sw[n1 * t];
                     a = INV ? cmulc(a, w) : cmul(a, w);
                 }
-                col[xsw(t * R2 + n1)] = a;
+                cw[n1] = a;
             }
         }
         __syncthreads();
-        if (t < R2) {
+        if (active && t < R2) {
+            const T2* cr = col + t;
 #pragma unroll
-            for (int j = 0; j < R1; ++j) v[j] = col[xsw(j * R2 + t)];
+            for (int j = 0; j < R1; ++j) v[j] = cr[xoff(j * R2)];
             dft<R1, INV>(v);
         }
         __syncthreads();

@@ -112,24 +112,46 @@ __device__ __forceinline__ void inv_yx_body(const float2* __restrict__ Cp, float
     float2* xb = reinterpret_cast<float2*>(smraw);  // W exchange columns
     float2* ds = xb + W * E::S;                     // [ny][Hx]: the plane after inverse y
     float2 v[16];
-    // phase 1: inverse y of the Hx columns (column-fastest thread map)
+    // phase 1: inverse y of the Hx columns: rounds of W whole columns
+    // (column-fastest thread map, coalesced loads), then the Hx mod W left
+    // over (the Nyquist column of a power-of-two plane) with NT consecutive
+    // threads per column, so that warps holding none of them skip the math
+    const int full = Hx - Hx % W;
     {
         const int c = threadIdx.x % W, t = threadIdx.x / W;
         float2* col = xb + c * E::S;
-        for (int k0 = 0; k0 < Hx; k0 += W) {
+        for (int k0 = 0; k0 < full; k0 += W) {
             const int kx = k0 + c;
-            const bool ok = kx < Hx;
             if (t < E::R1) {
 #pragma unroll
-                for (int r = 0; r < E::R2; ++r) v[r] = ok ? Cp[kx + (int64_t)Hx * (t + E::R1 * r)] : make_float2(0.f, 0.f);
+                for (int r = 0; r < E::R2; ++r) v[r] = Cp[kx + (int64_t)Hx * (t + E::R1 * r)];
             }
             E::template inv<true>(v, col, t, swt);
-            if (t < E::R2 && ok) {
+            if (t < E::R2) {
 #pragma unroll
                 for (int s = 0; s < E::R1; ++s) {
                     const int y = t + E::R2 * s;
                     if (y < ny) ds[y * Hx + kx] = v[s];
                 }
+            }
+        }
+    }
+    if (full < Hx) {
+        const int c = threadIdx.x / E::NT, t = threadIdx.x % E::NT;
+        const int kx = full + c;
+        const bool ok = kx < Hx;
+        const bool busy = full + (int)((threadIdx.x & ~31u) / E::NT) < Hx;  // uniform per warp
+        float2* col = xb + c * E::S;
+        if (busy && t < E::R1) {
+#pragma unroll
+            for (int r = 0; r < E::R2; ++r) v[r] = ok ? Cp[kx + (int64_t)Hx * (t + E::R1 * r)] : make_float2(0.f, 0.f);
+        }
+        E::template inv<true>(v, col, t, swt, busy);
+        if (t < E::R2 && ok) {
+#pragma unroll
+            for (int s = 0; s < E::R1; ++s) {
+                const int y = t + E::R2 * s;
+                if (y < ny) ds[y * Hx + kx] = v[s];
             }
         }
     }
@@ -212,7 +234,7 @@ __device__ __forceinline__ void fwd_x_body(const float* __restrict__ rho, float2
     E::template fwd<false>(v, col, t, swt);
     if (t < E::R1) {
 #pragma unroll
-        for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+        for (int r = 0; r < E::R2; ++r) col[t + xoff(E::R1 * r)] = v[r];
     }
     __syncthreads();
     if (r0 < rows) {
@@ -271,7 +293,7 @@ __device__ __forceinline__ void fwd_xy_body(const float* __restrict__ rz, float2
             E::template fwd<false>(v, col, t, swt);
             if (t < E::R1) {
 #pragma unroll
-                for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+                for (int r = 0; r < E::R2; ++r) col[t + xoff(E::R1 * r)] = v[r];
             }
             __syncthreads();
             if (y0 < ny) {
@@ -285,25 +307,47 @@ __device__ __forceinline__ void fwd_xy_body(const float* __restrict__ rz, float2
             __syncthreads();
         }
     }
-    // y pass: the Hx columns (column-fastest thread map), zero beyond y = ny
+    // y pass: the Hx columns, zero beyond y = ny: rounds of W whole columns
+    // (column-fastest thread map), then the Hx mod W left over (the Nyquist
+    // column of a power-of-two plane) with NT consecutive threads per column,
+    // so that warps holding none of them skip the math
+    const int full = Hx - Hx % W;
     {
         const int c = threadIdx.x % W, t = threadIdx.x / W;
         float2* col = xb + c * E::S;
-        for (int k0 = 0; k0 < Hx; k0 += W) {
+        for (int k0 = 0; k0 < full; k0 += W) {
             const int kx = k0 + c;
-            const bool ok = kx < Hx;
             if (t < E::R2) {
 #pragma unroll
                 for (int s = 0; s < E::R1; ++s) {
                     const int n = t + E::R2 * s;
-                    v[s] = (ok && n < ny) ? ds[n * Hx + kx] : make_float2(0.f, 0.f);
+                    v[s] = n < ny ? ds[n * Hx + kx] : make_float2(0.f, 0.f);
                 }
             }
             E::template fwd<false>(v, col, t, swt);
-            if (t < E::R1 && ok) {
+            if (t < E::R1) {
 #pragma unroll
                 for (int r = 0; r < E::R2; ++r) Bz[kx + (int64_t)Hx * (t + E::R1 * r)] = v[r];
             }
+        }
+    }
+    if (full < Hx) {
+        const int c = threadIdx.x / E::NT, t = threadIdx.x % E::NT;
+        const int kx = full + c;
+        const bool ok = kx < Hx;
+        const bool busy = full + (int)((threadIdx.x & ~31u) / E::NT) < Hx;  // uniform per warp
+        float2* col = xb + c * E::S;
+        if (busy && t < E::R2) {
+#pragma unroll
+            for (int s = 0; s < E::R1; ++s) {
+                const int n = t + E::R2 * s;
+                v[s] = (ok && n < ny) ? ds[n * Hx + kx] : make_float2(0.f, 0.f);
+            }
+        }
+        E::template fwd<false>(v, col, t, swt, busy);
+        if (t < E::R1 && ok) {
+#pragma unroll
+            for (int r = 0; r < E::R2; ++r) Bz[kx + (int64_t)Hx * (t + E::R1 * r)] = v[r];
         }
     }
 }
@@ -451,12 +495,16 @@ __device__ __forceinline__ float2 img_smem_at(const float2* gim, int kz, int c, 
 // (L/2+1) x kColW floats) are copied to shared memory asynchronously at the
 // start, so their L2 latency overlaps the forward transform.
 // Body of one CTA: `tile` is the CTA's column tile (kColW consecutive
-// columns of the flattened (kx, ky) plane).
-template <int L>
+// columns of the flattened (kx, ky) plane).  HALF: nz = L/2 (every
+// power-of-two axis), so which z rows exist is known at compile time.
+// Columns past the plane (the last tile only) load the plane's last column
+// and store nothing, so no branch inside the unrolled loops tests them.
+template <int L, bool HALF>
 __device__ __forceinline__ void zpass_body(const float2* __restrict__ B, float2* __restrict__ C, int Hx, int Ly,
                                            int nz, const GreenView& gv, int tile, const float2* swt,
                                            unsigned char* smraw) {
     using E = F2<L>;
+    constexpr int RL = E::R1;
     float2* xb = reinterpret_cast<float2*>(smraw);
     float2* spec = xb + kColW * E::S;  // natural-order spectrum of this tile's columns
     constexpr int HZ = L / 2 + 1;
@@ -473,22 +521,27 @@ __device__ __forceinline__ void zpass_body(const float2* __restrict__ B, float2*
     const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
     const int f = tile * kColW + c;
     const bool cok = f < plane;
-    const int ky = cok ? f / Hx : 0;
-    const int kx = f - ky * Hx;
+    const int fl = cok ? f : (int)plane - 1;
+    const int ky = fl / Hx;
+    const int kx = fl - ky * Hx;
     float2* col = xb + c * E::S;
     float2* sc = spec + c * E::S;
     float2 v[16];
     if (t < E::R2) {
+        const float2* Bc = B + fl;
 #pragma unroll
         for (int s = 0; s < E::R1; ++s) {
             const int z = t + E::R2 * s;
-            v[s] = (cok && z < nz) ? B[f + plane * z] : make_float2(0.f, 0.f);
+            if constexpr (HALF)
+                v[s] = E::R2 * s < L / 2 ? Bc[plane * z] : make_float2(0.f, 0.f);
+            else
+                v[s] = z < nz ? Bc[plane * z] : make_float2(0.f, 0.f);
         }
     }
     E::template fwd<false>(v, col, t, swt);
     if (t < E::R1) {
 #pragma unroll
-        for (int r = 0; r < E::R2; ++r) sc[xsw(t + E::R1 * r)] = v[r];
+        for (int r = 0; r < E::R2; ++r) sc[t + xoff(E::R1 * r)] = v[r];
     }
     cp_async_wait_all();
     __syncthreads();
@@ -500,30 +553,43 @@ __device__ __forceinline__ void zpass_body(const float2* __restrict__ B, float2*
             __syncthreads();
         }
         if (t < E::R1) {
+            // kz = t + RL*r: below L/2 for RL*r < L/2 (folded index kz), at
+            // or above it otherwise (folded index L - kz).  Signs: component
+            // 1 is odd along y, component 2 odd along z (kz > L/2).
+            const float sy = comp == 1 ? ysign : 1.f;
+            const float su = comp == 2 ? -sy : sy;
+            const float sm = t > 0 ? su : sy;  // kz = L/2 + t
             const float* gfc = gsm + comp * HZ * kColW + c;
-            const float2* gic = reinterpret_cast<const float2*>(gv.gimg) + comp * gv.cs_img + kx + gv.Hx * kyf;
+            const float* glo = gfc + t * kColW;
+            const float* ghi = gfc + (L - t) * kColW;
+            const float2* sct = sc + t;
+            if (!gv.image) {
 #pragma unroll
-            for (int r = 0; r < E::R2; ++r) {
-                const int kz = t + E::R1 * r;
-                float2 out = make_float2(0.f, 0.f);
-                if (cok) {
-                    const int kzf = kz <= L / 2 ? kz : L - kz;
-                    float sg = 1.f;
-                    if (comp == 1) sg = ysign;
-                    if (comp == 2 && kz > L / 2) sg = -1.f;
-                    const float g = sg * gfc[kzf * kColW];
-                    const float2 X = sc[xsw(kz)];
-                    out = make_float2(-X.y * g, X.x * g);  // X * (i g)
-                    if (gv.image) {
-                        float2 gc = img_smem ? img_smem_at<L>(gim, kz, c, comp) : img_at(gic, gstep, kz, gv, comp);
-                        if (comp == 1) {
-                            gc.x *= ysign;
-                            gc.y *= ysign;
-                        }
-                        out = cadd(out, cmul(sc[xsw((L - kz) & (L - 1))], gc));
-                    }
+                for (int r = 0; r < E::R2; ++r) {
+                    const float g = RL * r < L / 2    ? glo[RL * r * kColW] * sy
+                                    : RL * r == L / 2 ? ghi[-RL * r * kColW] * sm
+                                                      : ghi[-RL * r * kColW] * su;
+                    const float2 X = sct[xoff(RL * r)];
+                    v[r] = make_float2(-X.y * g, X.x * g);  // X * (i g)
                 }
-                v[r] = out;
+            } else {
+                const float2* gic =
+                    reinterpret_cast<const float2*>(gv.gimg) + comp * gv.cs_img + kx + gv.Hx * kyf;
+#pragma unroll
+                for (int r = 0; r < E::R2; ++r) {
+                    const int kz = t + RL * r;
+                    const float g = RL * r < L / 2    ? glo[RL * r * kColW] * sy
+                                    : RL * r == L / 2 ? ghi[-RL * r * kColW] * sm
+                                                      : ghi[-RL * r * kColW] * su;
+                    const float2 X = sct[xoff(RL * r)];
+                    float2 out = make_float2(-X.y * g, X.x * g);  // X * (i g)
+                    float2 gc = img_smem ? img_smem_at<L>(gim, kz, c, comp) : img_at(gic, gstep, kz, gv, comp);
+                    if (comp == 1) {
+                        gc.x *= ysign;
+                        gc.y *= ysign;
+                    }
+                    v[r] = cadd(out, cmul(sc[xsw((L - kz) & (L - 1))], gc));
+                }
             }
         }
         if (img_smem && comp < 2) {
@@ -536,20 +602,20 @@ __device__ __forceinline__ void zpass_body(const float2* __restrict__ B, float2*
 #pragma unroll
             for (int s = 0; s < E::R1; ++s) {
                 const int z = t + E::R2 * s;
-                if (z < nz) Cc[plane * z] = v[s];
+                if (HALF ? E::R2 * s < L / 2 : z < nz) Cc[plane * z] = v[s];
             }
         }
     }
 }
 
-template <int L>
+template <int L, bool HALF>
 __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(const float2* __restrict__ B,
                                                                  float2* __restrict__ C, int Hx, int Ly, int nz,
                                                                  GreenView gv, const float2* __restrict__ tw) {
     __shared__ float2 swt[L];
     stage_twiddles<L>(swt, tw);
     extern __shared__ __align__(16) unsigned char smraw[];
-    zpass_body<L>(B, C, Hx, Ly, nz, gv, blockIdx.x, swt, smraw);
+    zpass_body<L, HALF>(B, C, Hx, Ly, nz, gv, blockIdx.x, swt, smraw);
 }
 
 // Adjoint z pass: three forward z transforms of Ebar_c, correlation with the
@@ -594,7 +660,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass
         if (gv.image) {
             if (t < E::R1) {
 #pragma unroll
-                for (int r = 0; r < E::R2; ++r) sc[xsw(t + E::R1 * r)] = v[r];
+                for (int r = 0; r < E::R2; ++r) sc[t + xoff(E::R1 * r)] = v[r];
             }
         }
         if (comp == 0) cp_async_wait_all();
@@ -733,7 +799,7 @@ __global__ void __launch_bounds__(256) k3_green_x(const Tr* __restrict__ G, Tr* 
     E::template fwd<false>(v, col, t, swt);
     if (t < E::R1) {
 #pragma unroll
-        for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+        for (int r = 0; r < E::R2; ++r) col[t + xoff(E::R1 * r)] = v[r];
     }
     __syncthreads();
     if (ok0) {
@@ -802,7 +868,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(c
     E::template fwd<false>(v, col, t, swt);
     if (t < E::R1) {
 #pragma unroll
-        for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+        for (int r = 0; r < E::R2; ++r) col[t + xoff(E::R1 * r)] = v[r];
     }
     __syncthreads();
     for (int k = t; k <= L / 2; k += E::NT) {
@@ -881,7 +947,7 @@ __global__ void __launch_bounds__(256, sizeof(Tr) == 4 ? 3 : 1) k3_green_xy(cons
             E::template fwd<false>(v, col, t, swt);
             if (t < E::R1) {
 #pragma unroll
-                for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+                for (int r = 0; r < E::R2; ++r) col[t + xoff(E::R1 * r)] = v[r];
             }
             __syncthreads();
             if (ok0) {
@@ -940,7 +1006,7 @@ __global__ void __launch_bounds__(256, sizeof(Tr) == 4 ? 3 : 1) k3_green_xy(cons
             E::template fwd<false>(v, col, t, swt);
             if (t < E::R1) {
 #pragma unroll
-                for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+                for (int r = 0; r < E::R2; ++r) col[t + xoff(E::R1 * r)] = v[r];
             }
             __syncthreads();
             for (int k = t; k <= L / 2; k += E::NT) {
@@ -1087,7 +1153,7 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
             E::template fwd<false>(v, col, t, swt);
             if (t < E::R1) {
 #pragma unroll
-                for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+                for (int r = 0; r < E::R2; ++r) col[t + xoff(E::R1 * r)] = v[r];
             }
             __syncthreads();
             if (ok0) {
@@ -1152,7 +1218,7 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
             E::template fwd<false>(v, col, t, swt);
             if (t < E::R1) {
 #pragma unroll
-                for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+                for (int r = 0; r < E::R2; ++r) col[t + xoff(E::R1 * r)] = v[r];
             }
             __syncthreads();
             for (int k = t; k <= L / 2; k += E::NT) {
@@ -1225,7 +1291,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k4_green_col(c
     E::template fwd<false>(v, col, t, swt);
     if (t < E::R1) {
 #pragma unroll
-        for (int r = 0; r < E::R2; ++r) col[xsw(t + E::R1 * r)] = v[r];
+        for (int r = 0; r < E::R2; ++r) col[t + xoff(E::R1 * r)] = v[r];
     }
     __syncthreads();
     const Tr inv2 = Tr(1) / s2;
@@ -1349,9 +1415,15 @@ static bool launch2_zpass(int logL, const float2* B, float2* C, int Hx, int Ly, 
         const size_t smem = sizeof(float2) * kColW * F2<LL>::S * 2 +                        \
                             sizeof(float) * 3 * (LL / 2 + 1) * kColW +                          \
                             (gv.image && gv.img_half ? sizeof(float2) * (LL / 2 + 1) * kColW : 0); \
-        if (set_smem(k2_zpass<LL>, smem) != SC_OK) return false;                            \
         const int64_t ncol = (int64_t)Hx * Ly;                                              \
-        launch_pdl(k2_zpass<LL>, (unsigned)((ncol + kColW - 1) / kColW), kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz, gv, tw); \
+        const unsigned grid = (unsigned)((ncol + kColW - 1) / kColW);                       \
+        if (2 * nz == LL) {                                                                 \
+            if (set_smem(k2_zpass<LL, true>, smem) != SC_OK) return false;                  \
+            launch_pdl(k2_zpass<LL, true>, grid, kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz, gv, tw); \
+        } else {                                                                            \
+            if (set_smem(k2_zpass<LL, false>, smem) != SC_OK) return false;                 \
+            launch_pdl(k2_zpass<LL, false>, grid, kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz, gv, tw); \
+        }                                                                                   \
     }
     SC_L_SWITCH(logL, SC_K2Z)
 #undef SC_K2Z
