@@ -431,6 +431,10 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
@@ -1090,10 +1094,13 @@ __device__ __forceinline__ float green_near_value(const GreenNear& g, int c, int
 // first writes that slice's near cells of its components into G (the far
 // cells come from the preceding launch), so the near cells take no launch
 // of their own; G is then read through L2 (__ldcg), which sees those writes.
-template <int L, typename Tr, int NTH>
+// STG: the CTA first copies its slice of G (its components, nx*ny each) to
+// shared memory with cp.async (16-byte chunks when g16), writes the near
+// cells there, and the x pass reads shared memory instead of L2.
+template <int L, typename Tr, int NTH, bool STG>
 __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2out, int nx,
                                                       int ny, int Hx, int64_t gcs, int64_t t2cs, GreenNear near,
-                                                      const typename Cplx<Tr>::T2* __restrict__ tw) {
+                                                      int g16, const typename Cplx<Tr>::T2* __restrict__ tw) {
     using E = F2<L>;
     using T2 = typename Cplx<Tr>::T2;
     constexpr int W = NTH / E::NT;  // row pairs (x pass) or column pairs (y pass) per round
@@ -1103,8 +1110,33 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
     T2* xb = reinterpret_cast<T2*>(smraw);             // W exchange columns
     Tr* ts0 = reinterpret_cast<Tr*>(xb + W * E::S);  // [ny][Hx]: the lines even along y, after the x pass
     Tr* ts1 = ts0 + (int64_t)ny * Hx;                 // the lines odd along y (role 0)
+    // staged slice, 16-byte aligned: [slot][ny][nx], slot 0 the component
+    // odd along x (0; role 1: component 2), slot 1 component 1
+    Tr* gs = reinterpret_cast<Tr*>(smraw + ((W * E::S * sizeof(T2) + 2 * sizeof(Tr) * ny * Hx + 15) & ~(size_t)15));
     const int iz = blockIdx.x;
     const bool pair = blockIdx.y == 0;
+    const int per = nx * ny;
+    if constexpr (STG) {
+        const Tr* src0 = G + (pair ? 0 : 2) * gcs + (int64_t)per * iz;
+        for (int sl = 0; sl < (pair ? 2 : 1); ++sl) {
+            const Tr* src = src0 + sl * gcs;
+            Tr* dst = gs + sl * per;
+            if (g16) {
+                constexpr int K = 16 / sizeof(Tr);
+                for (int i = threadIdx.x; i < per / K; i += NTH) cp_async16(dst + i * K, src + i * K);
+            } else {
+                for (int i = threadIdx.x; i < per; i += NTH) {
+                    if constexpr (sizeof(Tr) == 4)
+                        cp_async4(dst + i, src + i);
+                    else
+                        cp_async8(dst + i, src + i);
+                }
+            }
+        }
+        cp_async_commit();
+        cp_async_wait_all();
+        __syncthreads();
+    }
     if (near.T) {
         const int dz = near.image ? iz - (near.nz - 1) : iz;
         if (dz >= near.bz0 && dz < near.bz1) {
@@ -1113,8 +1145,13 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
                 const int c = pair ? e / box : 2;
                 const int r = e - (pair ? c : 0) * box;
                 const int ix = r % near.nbx, iy = r / near.nbx;
-                if (green_near_cell(near, ix, iy, dz))
-                    G[c * gcs + ix + (int64_t)nx * (iy + (int64_t)ny * iz)] = (Tr)green_near_value(near, c, ix, iy, dz);
+                if (green_near_cell(near, ix, iy, dz)) {
+                    const Tr val = (Tr)green_near_value(near, c, ix, iy, dz);
+                    if constexpr (STG)
+                        gs[(pair ? c : 0) * per + ix + nx * iy] = val;
+                    else
+                        G[c * gcs + ix + (int64_t)nx * (iy + (int64_t)ny * iz)] = val;
+                }
             }
             __syncthreads();
         }
@@ -1124,8 +1161,8 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
         const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
         T2* col = xb + p * E::S;
         // even along x: component 1 (role 0) or 2 (role 1); odd: component 0
-        const Tr* ge = G + (pair ? 1 : 2) * gcs + (int64_t)nx * ny * iz;
-        const Tr* go = G + (int64_t)nx * ny * iz;
+        const Tr* ge = STG ? gs + (pair ? per : 0) : G + (pair ? 1 : 2) * gcs + (int64_t)per * iz;
+        const Tr* go = STG ? gs : G + (int64_t)per * iz;
         Tr* dst_e = pair ? ts1 : ts0;
         for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
             const int y0 = 2 * (q0 + p), y1 = y0 + 1;
@@ -1138,12 +1175,22 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
                     Tr e1 = 0, e2 = 0, o1 = 0, o2 = 0;
                     if (dx != L) {
                         const int ax = dx < 0 ? -dx : dx;
-                        if (ok0) e1 = __ldcg(ge + (int64_t)nx * y0 + ax);
-                        if (ok1) e2 = __ldcg(ge + (int64_t)nx * y1 + ax);
+                        if constexpr (STG) {
+                            if (ok0) e1 = ge[nx * y0 + ax];
+                            if (ok1) e2 = ge[nx * y1 + ax];
+                        } else {
+                            if (ok0) e1 = __ldcg(ge + (int64_t)nx * y0 + ax);
+                            if (ok1) e2 = __ldcg(ge + (int64_t)nx * y1 + ax);
+                        }
                         // an odd line vanishes at d = 0 (the stored sample there is rounding)
                         if (pair && dx != 0) {
-                            if (ok0) o1 = __ldcg(go + (int64_t)nx * y0 + ax);
-                            if (ok1) o2 = __ldcg(go + (int64_t)nx * y1 + ax);
+                            if constexpr (STG) {
+                                if (ok0) o1 = go[nx * y0 + ax];
+                                if (ok1) o2 = go[nx * y1 + ax];
+                            } else {
+                                if (ok0) o1 = __ldcg(go + (int64_t)nx * y0 + ax);
+                                if (ok1) o2 = __ldcg(go + (int64_t)nx * y1 + ax);
+                            }
                             if (dx < 0) o1 = -o1, o2 = -o2;
                         }
                     }
@@ -1179,19 +1226,25 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
         Tr* out_o = T2out + t2cs + (int64_t)Hx * (L / 2 + 1) * iz;
         // the Nyquist column kx = L/2 by direct sums:
         // X(k) = sum_d x(d) w^(k d), d = -(ny-1)..ny-1
+        // (four partial sums, so the loads of one step overlap the next)
         for (int k = threadIdx.x; k <= L / 2; k += NTH) {
-            Tr re = 0, im = 0;
-            for (int d = 0; d < ny; ++d) {
-                const T2 wp = swt[(k * d) & (L - 1)];
-                if (d == 0) {
-                    re += ts0[L / 2];
-                } else {
-                    re += Tr(2) * ts0[d * Hx + L / 2] * wp.x;                   // even: 2 x(d) Re w^kd
-                    if (pair) im += Tr(2) * ts1[d * Hx + L / 2] * wp.y;        // odd: 2i x(d) Im w^kd
+            Tr re[4] = {0, 0, 0, 0}, im[4] = {0, 0, 0, 0};
+            int d = 1;
+            for (; d + 3 < ny; d += 4) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const T2 wp = swt[(k * (d + u)) & (L - 1)];
+                    re[u] += Tr(2) * ts0[(d + u) * Hx + L / 2] * wp.x;             // even: 2 x(d) Re w^kd
+                    if (pair) im[u] += Tr(2) * ts1[(d + u) * Hx + L / 2] * wp.y;  // odd: 2i x(d) Im w^kd
                 }
             }
-            out_e[(int64_t)k * Hx + L / 2] = re;
-            if (pair) out_o[(int64_t)k * Hx + L / 2] = im;
+            for (; d < ny; ++d) {
+                const T2 wp = swt[(k * d) & (L - 1)];
+                re[0] += Tr(2) * ts0[d * Hx + L / 2] * wp.x;
+                if (pair) im[0] += Tr(2) * ts1[d * Hx + L / 2] * wp.y;
+            }
+            out_e[(int64_t)k * Hx + L / 2] = ts0[L / 2] + ((re[0] + re[1]) + (re[2] + re[3]));
+            if (pair) out_o[(int64_t)k * Hx + L / 2] = (im[0] + im[1]) + (im[2] + im[3]);
         }
         for (int k0 = 0; k0 < L / 2; k0 += 2 * W) {
             const int fa = k0 + c, fb = fa + W;
@@ -1536,18 +1589,28 @@ static bool launch_green_xy_field(int logLx, int logLy, Tr* G, Tr* T2, int nx, i
     using C2 = typename Cplx<Tr>::T2;
     if (logLx != logLy) return false;
     const size_t planes = 2 * sizeof(Tr) * (size_t)ny * Hx;
+    const size_t slice = 2 * sizeof(Tr) * (size_t)nx * ny + 16;  // the staged slice, with its alignment slack
+    const int g16 = ((uintptr_t)G % 16 == 0 && (sizeof(Tr) * (size_t)nx * ny) % 16 == 0 &&
+                     (sizeof(Tr) * (size_t)gcs) % 16 == 0) ? 1 : 0;
     bool ok = false;
 #define SC_K4XY(LL)                                                                                              \
     {                                                                                                            \
         const size_t s256 = sizeof(C2) * (size_t)(256 / F2<LL>::NT) * F2<LL>::S + planes;                        \
         const size_t s512 = sizeof(C2) * (size_t)(512 / F2<LL>::NT) * F2<LL>::S + planes;                        \
-        if (s256 <= 100 * 1024) {                                                                                \
-            if (set_smem(k4_green_xy<LL, Tr, 256>, s256) != SC_OK) return false;                                 \
-            launch_pdl(k4_green_xy<LL, Tr, 256>, dim3(zc, 2), 256, s256, s, G, T2, nx, ny, Hx, gcs, t2cs, near, tw);   \
+        if (s256 + slice <= 100 * 1024) {                                                                        \
+            if (set_smem(k4_green_xy<LL, Tr, 256, true>, s256 + slice) != SC_OK) return false;                   \
+            launch_pdl(k4_green_xy<LL, Tr, 256, true>, dim3(zc, 2), 256, s256 + slice, s, G, T2, nx, ny, Hx, gcs, \
+                       t2cs, near, g16, tw);                                                                      \
+            ok = true;                                                                                           \
+        } else if (s256 <= 100 * 1024) {                                                                         \
+            if (set_smem(k4_green_xy<LL, Tr, 256, false>, s256) != SC_OK) return false;                          \
+            launch_pdl(k4_green_xy<LL, Tr, 256, false>, dim3(zc, 2), 256, s256, s, G, T2, nx, ny, Hx, gcs, t2cs, \
+                       near, g16, tw);                                                                            \
             ok = true;                                                                                           \
         } else if (s512 <= 220 * 1024) {                                                                         \
-            if (set_smem(k4_green_xy<LL, Tr, 512>, s512) != SC_OK) return false;                                 \
-            launch_pdl(k4_green_xy<LL, Tr, 512>, dim3(zc, 2), 512, s512, s, G, T2, nx, ny, Hx, gcs, t2cs, near, tw);   \
+            if (set_smem(k4_green_xy<LL, Tr, 512, false>, s512) != SC_OK) return false;                          \
+            launch_pdl(k4_green_xy<LL, Tr, 512, false>, dim3(zc, 2), 512, s512, s, G, T2, nx, ny, Hx, gcs, t2cs, \
+                       near, g16, tw);                                                                            \
             ok = true;                                                                                           \
         }                                                                                                        \
     }
