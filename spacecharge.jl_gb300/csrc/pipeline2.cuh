@@ -1097,7 +1097,9 @@ __device__ __forceinline__ float green_near_value(const GreenNear& g, int c, int
 // STG: the CTA first copies its slice of G (its components, nx*ny each) to
 // shared memory with cp.async (16-byte chunks when g16), writes the near
 // cells there, and the x pass reads shared memory instead of L2.
-template <int L, typename Tr, int NTH, bool STG>
+// HALF: nx = ny = L/2 and Hx = L/2 + 1 (power-of-two meshes), so every
+// sample and output index is a per-thread base plus a constant.
+template <int L, typename Tr, int NTH, bool STG, bool HALF>
 __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2out, int nx,
                                                       int ny, int Hx, int64_t gcs, int64_t t2cs, GreenNear near,
                                                       int g16, const typename Cplx<Tr>::T2* __restrict__ tw) {
@@ -1167,7 +1169,29 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
         for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
             const int y0 = 2 * (q0 + p), y1 = y0 + 1;
             const bool ok0 = y0 < ny, ok1 = y1 < ny;
-            if (t < E::R2) {
+            if (HALF && t < E::R2) {
+                // x = t + R2*s: d = x below L/2, d = x - L above, nothing at
+                // x = L/2; |d| from a per-thread base and a constant offset
+                const Tr* ep0 = ge + nx * y0;
+                const Tr* op0 = go + nx * y0;
+#pragma unroll
+                for (int s = 0; s < E::R1; ++s) {
+                    const bool lower = E::R2 * s < L / 2;
+                    const bool here = lower || E::R2 * s > L / 2 || t > 0;
+                    const int ax = lower ? t + E::R2 * s : L - t - E::R2 * s;
+                    Tr e1 = 0, e2 = 0, o1 = 0, o2 = 0;
+                    if (here) {
+                        if (ok0) e1 = STG ? ep0[ax] : __ldcg(ep0 + ax);
+                        if (ok1) e2 = STG ? ep0[nx + ax] : __ldcg(ep0 + nx + ax);
+                        if (pair && (s > 0 || t > 0)) {  // odd: nothing at d = 0
+                            if (ok0) o1 = STG ? op0[ax] : __ldcg(op0 + ax);
+                            if (ok1) o2 = STG ? op0[nx + ax] : __ldcg(op0 + nx + ax);
+                            if (!lower) o1 = -o1, o2 = -o2;
+                        }
+                    }
+                    v[s] = Cplx<Tr>::make(e1 + o1, e2 + o2);
+                }
+            } else if (t < E::R2) {
 #pragma unroll
                 for (int s = 0; s < E::R1; ++s) {
                     const int x = t + E::R2 * s;
@@ -1203,7 +1227,24 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
                 for (int r = 0; r < E::R2; ++r) col[t + xoff(E::R1 * r)] = v[r];
             }
             __syncthreads();
-            if (ok0) {
+            if (HALF && ok0) {
+                constexpr int HX = L / 2 + 1, NT = E::NT;
+                const int tm = t == 0 ? 0 : NT - t;  // the mirror L - k = tm + constant
+#pragma unroll
+                for (int i = 0; i <= L / (2 * NT); ++i) {
+                    if (i == L / (2 * NT) && t > 0) break;  // k = L/2 only at t = 0
+                    const int k = t + NT * i;
+                    const int km = t == 0 ? xoff((L - NT * i) & (L - 1)) : tm + xoff(L - NT * (i + 1));
+                    Tr e1, e2, p1, p2;
+                    unpack4(col[t + xoff(NT * i)], col[km], e1, e2, p1, p2);
+                    dst_e[y0 * HX + k] = e1;
+                    if (ok1) dst_e[y1 * HX + k] = e2;
+                    if (pair) {
+                        ts0[y0 * HX + k] = p1;
+                        if (ok1) ts0[y1 * HX + k] = p2;
+                    }
+                }
+            } else if (ok0) {
                 for (int k = t; k <= L / 2; k += E::NT) {
                     Tr e1, e2, p1, p2;
                     unpack4(col[xsw(k)], col[xsw((L - k) & (L - 1))], e1, e2, p1, p2);
@@ -1249,7 +1290,32 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
         for (int k0 = 0; k0 < L / 2; k0 += 2 * W) {
             const int fa = k0 + c, fb = fa + W;
             const bool oka = fa < L / 2, okb = fb < L / 2;
-            if (t < E::R2) {
+            if (HALF && t < E::R2) {
+                // as the x pass, along y: rows of ts0 / ts1 (HX floats)
+                constexpr int HX = L / 2 + 1;
+                const Tr* lo0 = ts0 + t * HX;
+                const Tr* hi0 = ts0 + (L - t) * HX;
+                const Tr* lo1 = ts1 + t * HX;
+                const Tr* hi1 = ts1 + (L - t) * HX;
+#pragma unroll
+                for (int s = 0; s < E::R1; ++s) {
+                    const bool lower = E::R2 * s < L / 2;
+                    const bool here = lower || E::R2 * s > L / 2 || t > 0;
+                    const Tr* r0 = lower ? lo0 + E::R2 * s * HX : hi0 - E::R2 * s * HX;
+                    const Tr* r1 = lower ? lo1 + E::R2 * s * HX : hi1 - E::R2 * s * HX;
+                    Tr e1 = 0, e2 = 0, o1 = 0, o2 = 0;
+                    if (here) {
+                        if (oka) e1 = r0[fa];
+                        if (okb) e2 = r0[fb];
+                        if (pair && (s > 0 || t > 0)) {
+                            if (oka) o1 = r1[fa];
+                            if (okb) o2 = r1[fb];
+                            if (!lower) o1 = -o1, o2 = -o2;
+                        }
+                    }
+                    v[s] = Cplx<Tr>::make(e1 + o1, e2 + o2);
+                }
+            } else if (t < E::R2) {
 #pragma unroll
                 for (int s = 0; s < E::R1; ++s) {
                     const int n = t + E::R2 * s;
@@ -1274,14 +1340,34 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
                 for (int r = 0; r < E::R2; ++r) col[t + xoff(E::R1 * r)] = v[r];
             }
             __syncthreads();
-            for (int k = t; k <= L / 2; k += E::NT) {
-                Tr e1, e2, p1, p2;
-                unpack4(col[xsw(k)], col[xsw((L - k) & (L - 1))], e1, e2, p1, p2);
-                if (oka) out_e[(int64_t)k * Hx + fa] = e1;
-                if (okb) out_e[(int64_t)k * Hx + fb] = e2;
-                if (pair) {
-                    if (oka) out_o[(int64_t)k * Hx + fa] = p1;
-                    if (okb) out_o[(int64_t)k * Hx + fb] = p2;
+            if constexpr (HALF) {
+                constexpr int HX = L / 2 + 1, NT = E::NT;
+                const int tm = t == 0 ? 0 : NT - t;
+                Tr* oe = out_e + (int64_t)t * HX;
+                Tr* oo = out_o + (int64_t)t * HX;
+#pragma unroll
+                for (int i = 0; i <= L / (2 * NT); ++i) {
+                    if (i == L / (2 * NT) && t > 0) break;  // k = L/2 only at t = 0
+                    const int km = t == 0 ? xoff((L - NT * i) & (L - 1)) : tm + xoff(L - NT * (i + 1));
+                    Tr e1, e2, p1, p2;
+                    unpack4(col[t + xoff(NT * i)], col[km], e1, e2, p1, p2);
+                    if (oka) oe[NT * i * HX + fa] = e1;
+                    if (okb) oe[NT * i * HX + fb] = e2;
+                    if (pair) {
+                        if (oka) oo[NT * i * HX + fa] = p1;
+                        if (okb) oo[NT * i * HX + fb] = p2;
+                    }
+                }
+            } else {
+                for (int k = t; k <= L / 2; k += E::NT) {
+                    Tr e1, e2, p1, p2;
+                    unpack4(col[xsw(k)], col[xsw((L - k) & (L - 1))], e1, e2, p1, p2);
+                    if (oka) out_e[(int64_t)k * Hx + fa] = e1;
+                    if (okb) out_e[(int64_t)k * Hx + fb] = e2;
+                    if (pair) {
+                        if (oka) out_o[(int64_t)k * Hx + fa] = p1;
+                        if (okb) out_o[(int64_t)k * Hx + fb] = p2;
+                    }
                 }
             }
             __syncthreads();
@@ -1593,29 +1679,34 @@ static bool launch_green_xy_field(int logLx, int logLy, Tr* G, Tr* T2, int nx, i
     const int g16 = ((uintptr_t)G % 16 == 0 && (sizeof(Tr) * (size_t)nx * ny) % 16 == 0 &&
                      (sizeof(Tr) * (size_t)gcs) % 16 == 0) ? 1 : 0;
     bool ok = false;
-#define SC_K4XY(LL)                                                                                              \
-    {                                                                                                            \
-        const size_t s256 = sizeof(C2) * (size_t)(256 / F2<LL>::NT) * F2<LL>::S + planes;                        \
-        const size_t s512 = sizeof(C2) * (size_t)(512 / F2<LL>::NT) * F2<LL>::S + planes;                        \
-        if (s256 + slice <= 100 * 1024) {                                                                        \
-            if (set_smem(k4_green_xy<LL, Tr, 256, true>, s256 + slice) != SC_OK) return false;                   \
-            launch_pdl(k4_green_xy<LL, Tr, 256, true>, dim3(zc, 2), 256, s256 + slice, s, G, T2, nx, ny, Hx, gcs, \
-                       t2cs, near, g16, tw);                                                                      \
-            ok = true;                                                                                           \
-        } else if (s256 <= 100 * 1024) {                                                                         \
-            if (set_smem(k4_green_xy<LL, Tr, 256, false>, s256) != SC_OK) return false;                          \
-            launch_pdl(k4_green_xy<LL, Tr, 256, false>, dim3(zc, 2), 256, s256, s, G, T2, nx, ny, Hx, gcs, t2cs, \
-                       near, g16, tw);                                                                            \
-            ok = true;                                                                                           \
-        } else if (s512 <= 220 * 1024) {                                                                         \
-            if (set_smem(k4_green_xy<LL, Tr, 512, false>, s512) != SC_OK) return false;                          \
-            launch_pdl(k4_green_xy<LL, Tr, 512, false>, dim3(zc, 2), 512, s512, s, G, T2, nx, ny, Hx, gcs, t2cs, \
-                       near, g16, tw);                                                                            \
-            ok = true;                                                                                           \
-        }                                                                                                        \
+#define SC_K4XY_GO(LL, NTH, STG, SM)                                                                        \
+    {                                                                                                        \
+        if (half) {                                                                                          \
+            if (set_smem(k4_green_xy<LL, Tr, NTH, STG, true>, SM) != SC_OK) return false;                    \
+            launch_pdl(k4_green_xy<LL, Tr, NTH, STG, true>, dim3(zc, 2), NTH, SM, s, G, T2, nx, ny, Hx, gcs,  \
+                       t2cs, near, g16, tw);                                                                  \
+        } else {                                                                                             \
+            if (set_smem(k4_green_xy<LL, Tr, NTH, STG, false>, SM) != SC_OK) return false;                   \
+            launch_pdl(k4_green_xy<LL, Tr, NTH, STG, false>, dim3(zc, 2), NTH, SM, s, G, T2, nx, ny, Hx, gcs, \
+                       t2cs, near, g16, tw);                                                                  \
+        }                                                                                                    \
+        ok = true;                                                                                           \
+    }
+#define SC_K4XY(LL)                                                                                          \
+    {                                                                                                        \
+        const size_t s256 = sizeof(C2) * (size_t)(256 / F2<LL>::NT) * F2<LL>::S + planes;                    \
+        const size_t s512 = sizeof(C2) * (size_t)(512 / F2<LL>::NT) * F2<LL>::S + planes;                    \
+        const bool half = 2 * nx == LL && 2 * ny == LL && 2 * (Hx - 1) == LL;                               \
+        if (s256 + slice <= 100 * 1024)                                                                      \
+            SC_K4XY_GO(LL, 256, true, s256 + slice)                                                          \
+        else if (s256 <= 100 * 1024)                                                                         \
+            SC_K4XY_GO(LL, 256, false, s256)                                                                 \
+        else if (s512 <= 220 * 1024)                                                                         \
+            SC_K4XY_GO(LL, 512, false, s512)                                                                 \
     }
     SC_L_SWITCH(logLx, SC_K4XY)
 #undef SC_K4XY
+#undef SC_K4XY_GO
     return ok;
 }
 
