@@ -453,9 +453,12 @@ __device__ __forceinline__ void prefetch_green(float* gsm, const GreenView& gv, 
         const int kyy = ff / Hx, kxx = ff - kyy * Hx;
         const int kyf = kyy <= Ly / 2 ? kyy : Ly - kyy;
         const float* src = reinterpret_cast<const float*>(gv.gfree) + kxx + (int64_t)gv.Hx * kyf;
-        for (int row = threadIdx.x / kColW; row < 3 * HZ; row += blockDim.x / kColW) {
-            const int comp = row / HZ, kzf = row - comp * HZ;
-            cp_async4(gsm + row * kColW + cc, src + comp * gv.cs_free + gstep * kzf);
+        const int k0 = threadIdx.x / kColW, kstep = blockDim.x / kColW;
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp) {
+            const float* sc = src + comp * gv.cs_free + gstep * k0;
+            float* dc = gsm + (comp * HZ + k0) * kColW + cc;
+            for (int kzf = k0; kzf < HZ; kzf += kstep, sc += gstep * kstep, dc += kColW * kstep) cp_async4(dc, sc);
         }
     }
     cp_async_commit();
@@ -1385,7 +1388,7 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
 // one FFT keep the precision of the larger: component 2 lacks the factor
 // gamma of components 0 and 1, so it enters multiplied by s2 (a power of two
 // near gamma) and leaves divided by it, both exact.
-template <int L, typename Tr>
+template <int L, typename Tr, bool HALF>
 __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k4_green_col(const Tr* __restrict__ in,
                                                                            Tr* __restrict__ out, int ncols, int nh,
                                                                            int64_t as_in, int64_t cs_in,
@@ -1407,7 +1410,33 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k4_green_col(c
     const bool oka = fa < ncols, okb = fb < ncols;
     T2* col = xb + c * E::S;
     T2 v[16];
-    if (t < E::R2) {
+    if (HALF && t < E::R2) {
+        // nh = L/2: sample n = t + R2*s is d = n below L/2, d = n - L above,
+        // nothing at L/2; |d| * as_in from per-thread bases
+        const Tr* elo = ie + t * as_in;
+        const Tr* ehi = ie + (L - t) * as_in;
+        const Tr* olo = io + t * as_in;
+        const Tr* ohi = io + (L - t) * as_in;
+#pragma unroll
+        for (int s = 0; s < E::R1; ++s) {
+            const bool lower = E::R2 * s < L / 2;
+            const bool here = lower || E::R2 * s > L / 2 || t > 0;
+            const int64_t o = (int64_t)(E::R2 * s) * as_in;
+            const Tr* pe = lower ? elo + o : ehi - o;
+            const Tr* po = lower ? olo + o : ohi - o;
+            Tr e1 = 0, e2 = 0, o1 = 0, o2 = 0;
+            if (here) {
+                if (oka) e1 = __ldg(pe + fa);
+                if (okb) e2 = __ldg(pe + fb);
+                if (pair && (s > 0 || t > 0)) {
+                    if (oka) o1 = s2 * __ldg(po + fa);
+                    if (okb) o2 = s2 * __ldg(po + fb);
+                    if (!lower) o1 = -o1, o2 = -o2;
+                }
+            }
+            v[s] = Cplx<Tr>::make(e1 + o1, e2 + o2);
+        }
+    } else if (t < E::R2) {
 #pragma unroll
         for (int s = 0; s < E::R1; ++s) {
             const int n = t + E::R2 * s;
@@ -1434,14 +1463,35 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k4_green_col(c
     }
     __syncthreads();
     const Tr inv2 = Tr(1) / s2;
-    for (int k = t; k <= L / 2; k += E::NT) {
-        Tr e1, e2, p1, p2;
-        unpack4(col[xsw(k)], col[xsw((L - k) & (L - 1))], e1, e2, p1, p2);
-        if (oka) oe[fa + k * as_out] = e1;
-        if (okb) oe[fb + k * as_out] = e2;
-        if (pair) {
-            if (oka) oo[fa + k * as_out] = p1 * inv2;
-            if (okb) oo[fb + k * as_out] = p2 * inv2;
+    if constexpr (HALF) {
+        constexpr int NT = E::NT;
+        const int tm = t == 0 ? 0 : NT - t;
+        Tr* pe = oe + t * as_out;
+        Tr* po = oo + t * as_out;
+#pragma unroll
+        for (int i = 0; i <= L / (2 * NT); ++i) {
+            if (i == L / (2 * NT) && t > 0) break;  // k = L/2 only at t = 0
+            const int km = t == 0 ? xoff((L - NT * i) & (L - 1)) : tm + xoff(L - NT * (i + 1));
+            const int64_t o = (int64_t)(NT * i) * as_out;
+            Tr e1, e2, p1, p2;
+            unpack4(col[t + xoff(NT * i)], col[km], e1, e2, p1, p2);
+            if (oka) pe[o + fa] = e1;
+            if (okb) pe[o + fb] = e2;
+            if (pair) {
+                if (oka) po[o + fa] = p1 * inv2;
+                if (okb) po[o + fb] = p2 * inv2;
+            }
+        }
+    } else {
+        for (int k = t; k <= L / 2; k += E::NT) {
+            Tr e1, e2, p1, p2;
+            unpack4(col[xsw(k)], col[xsw((L - k) & (L - 1))], e1, e2, p1, p2);
+            if (oka) oe[fa + k * as_out] = e1;
+            if (okb) oe[fb + k * as_out] = e2;
+            if (pair) {
+                if (oka) oo[fa + k * as_out] = p1 * inv2;
+                if (okb) oo[fb + k * as_out] = p2 * inv2;
+            }
         }
     }
 }
@@ -1720,15 +1770,23 @@ static bool launch_green_z_field(int logL, const Tr* in, Tr* out, int ncols, int
     using T2 = typename Cplx<Tr>::T2;
     const Tr s2 = (Tr)exp2(rint(log2(gamma > 1.0 ? gamma : 1.0)));  // a power of two: exact scaling
     const dim3 grid((unsigned)(((int64_t)ncols + 2 * kColW - 1) / (2 * kColW)), 2);
-#define SC_K4GC(LL)                                                                                         \
-    {                                                                                                       \
-        const size_t smem = sizeof(T2) * kColW * F2<LL>::S;                                                 \
-        if (set_smem(k4_green_col<LL, Tr>, smem) != SC_OK) return false;                                    \
-        launch_pdl(k4_green_col<LL, Tr>, grid, kColW * F2<LL>::NT, smem, s, in, out, ncols, nh, as_in, cs_in, \
-                   as_out, cs_out, s2, tw);                                                                 \
+#define SC_K4GC_GO(LL, HALF)                                                                                  \
+    {                                                                                                         \
+        if (set_smem(k4_green_col<LL, Tr, HALF>, smem) != SC_OK) return false;                                \
+        launch_pdl(k4_green_col<LL, Tr, HALF>, grid, kColW * F2<LL>::NT, smem, s, in, out, ncols, nh, as_in,   \
+                   cs_in, as_out, cs_out, s2, tw);                                                             \
+    }
+#define SC_K4GC(LL)                                                                                           \
+    {                                                                                                         \
+        const size_t smem = sizeof(T2) * kColW * F2<LL>::S;                                                   \
+        if (2 * nh == LL)                                                                                     \
+            SC_K4GC_GO(LL, true)                                                                              \
+        else                                                                                                  \
+            SC_K4GC_GO(LL, false)                                                                             \
     }
     SC_L_SWITCH(logL, SC_K4GC)
 #undef SC_K4GC
+#undef SC_K4GC_GO
     return true;
 }
 
