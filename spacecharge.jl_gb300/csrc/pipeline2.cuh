@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(256) k2_fwd_xy(const float* __restrict__ rho, 
 
 // Inverse x pass of the three components, two rows per complex IFFT, packed
 // float4 output nodes.
-template <int L>
+template <int L, bool HALF>
 __global__ void __launch_bounds__(256) k2_inv_x(const float2* __restrict__ D, float4* __restrict__ E4, int nx,
                                                 int rows, int Hx, int64_t cs, const float2* __restrict__ tw) {
     using E = F2<L>;
@@ -377,7 +377,7 @@ __global__ void __launch_bounds__(256) k2_inv_x(const float2* __restrict__ D, fl
     constexpr int P = 256 / E::NT;
     extern __shared__ __align__(16) unsigned char smraw[];
     float2* xb = reinterpret_cast<float2*>(smraw);
-    float2* keep = xb + P * E::S;  // [2][P][L]: components 0, 1 until the float4 store
+    float2* keep = xb + P * E::S;  // [2][P][nx]: components 0, 1 until the float4 store
     const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
     const int r0 = 2 * (blockIdx.x * P + p), r1 = r0 + 1;
     float2* col = xb + p * E::S;
@@ -385,14 +385,19 @@ __global__ void __launch_bounds__(256) k2_inv_x(const float2* __restrict__ D, fl
     for (int comp = 0; comp < 3; ++comp) {
         const float2* Dc = D + comp * cs;
         if (t < E::R1) {
+            const float2* Da = Dc + (int64_t)r0 * Hx;
+            const float2* Db = Da + Hx;
 #pragma unroll
             for (int r = 0; r < E::R2; ++r) {
                 const int k = t + E::R1 * r;
-                const bool cj = k > L / 2;
-                const int kk = cj ? L - k : k;
+                // HALF (Hx = L/2 + 1): k below L/2 for R1*r < L/2, above
+                // for R1*r > L/2, and L/2 + t at R1*r = L/2
+                const bool cj = HALF ? (E::R1 * r > L / 2 || (E::R1 * r == L / 2 && t > 0)) : k > L / 2;
+                const int kk = HALF ? (E::R1 * r < L / 2 ? t + E::R1 * r : (cj ? L - t - E::R1 * r : L / 2))
+                                    : (cj ? L - k : k);
                 float2 xa = make_float2(0.f, 0.f), xbv = make_float2(0.f, 0.f);
-                if (r0 < rows) xa = Dc[(int64_t)r0 * Hx + kk];
-                if (r1 < rows) xbv = Dc[(int64_t)r1 * Hx + kk];
+                if (r0 < rows) xa = Da[kk];
+                if (r1 < rows) xbv = Db[kk];
                 if (cj) {
                     xa.y = -xa.y;
                     xbv.y = -xbv.y;
@@ -403,20 +408,25 @@ __global__ void __launch_bounds__(256) k2_inv_x(const float2* __restrict__ D, fl
         E::template inv<true>(v, col, t, swt);
         if (comp < 2) {
             if (t < E::R2) {
+                float2* kp = keep + (int64_t)(comp * P + p) * nx + t;
 #pragma unroll
-                for (int s = 0; s < E::R1; ++s) keep[(comp * P + p) * L + t + E::R2 * s] = v[s];
+                for (int s = 0; s < E::R1; ++s)
+                    if (HALF ? E::R2 * s < L / 2 : t + E::R2 * s < nx) kp[E::R2 * s] = v[s];
             }
         }
     }
     __syncthreads();
     if (t < E::R2) {
+        const float2* k0 = keep + (int64_t)p * nx + t;
+        const float2* k1 = keep + (int64_t)(P + p) * nx + t;
+        float4* o0 = E4 + (int64_t)r0 * nx + t;
+        float4* o1 = o0 + nx;
 #pragma unroll
         for (int s = 0; s < E::R1; ++s) {
-            const int x = t + E::R2 * s;
-            if (x >= nx) continue;
-            const float2 ex = keep[p * L + x], ey = keep[(P + p) * L + x], ez = v[s];
-            if (r0 < rows) E4[(int64_t)r0 * nx + x] = make_float4(ex.x, ey.x, ez.x, 0.f);
-            if (r1 < rows) E4[(int64_t)r1 * nx + x] = make_float4(ex.y, ey.y, ez.y, 0.f);
+            if (!(HALF ? E::R2 * s < L / 2 : t + E::R2 * s < nx)) continue;
+            const float2 ex = k0[E::R2 * s], ey = k1[E::R2 * s], ez = v[s];
+            if (r0 < rows) o0[E::R2 * s] = make_float4(ex.x, ey.x, ez.x, 0.f);
+            if (r1 < rows) o1[E::R2 * s] = make_float4(ex.y, ey.y, ez.y, 0.f);
         }
     }
 }
@@ -1584,16 +1594,24 @@ static bool launch2_inv_yx(int logLx, int logLy, const float2* C, float4* E4, in
 
 static bool launch2_inv_x(int logL, const float2* D, float4* E4, int nx, int rows, int Hx, int64_t cs,
                           const float2* tw, cudaStream_t s) {
-#define SC_K2IX(LL)                                                                         \
-    {                                                                                       \
-        constexpr int P = 256 / F2<LL>::NT;                                                 \
-        const size_t smem = sizeof(float2) * (P * F2<LL>::S + 2 * P * LL);                  \
-        if (set_smem(k2_inv_x<LL>, smem) != SC_OK) return false;                            \
-        const int pairs = (rows + 1) / 2;                                                   \
-        launch_pdl(k2_inv_x<LL>, (pairs + P - 1) / P, 256, smem, s, D, E4, nx, rows, Hx, cs, tw);   \
+#define SC_K2IX_GO(LL, HALF)                                                                          \
+    {                                                                                                 \
+        if (set_smem(k2_inv_x<LL, HALF>, smem) != SC_OK) return false;                                \
+        launch_pdl(k2_inv_x<LL, HALF>, (pairs + P - 1) / P, 256, smem, s, D, E4, nx, rows, Hx, cs, tw); \
+    }
+#define SC_K2IX(LL)                                                                                   \
+    {                                                                                                 \
+        constexpr int P = 256 / F2<LL>::NT;                                                           \
+        const size_t smem = sizeof(float2) * (P * F2<LL>::S + 2 * (size_t)P * nx);                    \
+        const int pairs = (rows + 1) / 2;                                                             \
+        if (2 * nx == LL && 2 * (Hx - 1) == LL)                                                       \
+            SC_K2IX_GO(LL, true)                                                                      \
+        else                                                                                          \
+            SC_K2IX_GO(LL, false)                                                                     \
     }
     SC_L_SWITCH(logL, SC_K2IX)
 #undef SC_K2IX
+#undef SC_K2IX_GO
     return true;
 }
 
