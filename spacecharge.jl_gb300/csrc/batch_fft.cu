@@ -94,8 +94,11 @@ __global__ void __launch_bounds__(256) kb_inv_yx(const BunchDesc* __restrict__ t
     extern __shared__ __align__(16) unsigned char smraw[];
     const int z = r.local / 3, comp = r.local - 3 * (r.local / 3);
     const int64_t plane = (int64_t)Hx * L;
-    inv_yx_body<L>(C + (int64_t)comp * plane * nz + plane * z, E4 + comp + 4 * (int64_t)nx * ny * z, nx, ny, Hx,
-                   swt, smraw);
+    float* o = E4 + comp + 4 * (int64_t)nx * ny * z;
+    if (2 * nx == L && 2 * ny == L && 2 * (Hx - 1) == L)
+        inv_yx_body<L, true>(C + (int64_t)comp * plane * nz + plane * z, o, nx, ny, Hx, swt, smraw);
+    else
+        inv_yx_body<L, false>(C + (int64_t)comp * plane * nz + plane * z, o, nx, ny, Hx, swt, smraw);
 }
 
 // Expands MACRO(L) for the transform length 2^logL; `fallback` otherwise.

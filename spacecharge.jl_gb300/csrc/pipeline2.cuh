@@ -104,11 +104,14 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k2_col(const f
 // global memory.
 // Body of one CTA: Cp is the (component, z plane) of C, `out` the plane's
 // first node lane to write (stride 4 floats per node).
-template <int L>
+template <int L, bool HALF>
 __device__ __forceinline__ void inv_yx_body(const float2* __restrict__ Cp, float* __restrict__ out, int nx, int ny,
-                                            int Hx, const float2* swt, unsigned char* smraw) {
+                                            int Hx_, const float2* swt, unsigned char* smraw) {
     using E = F2<L>;
     constexpr int W = 256 / E::NT;  // columns (phase 1) or row pairs (phase 2) per round
+    // HALF: nx = ny = L/2 and Hx = L/2 + 1 (power-of-two planes), so the
+    // strides and which samples exist are compile-time constants
+    const int Hx = HALF ? L / 2 + 1 : Hx_;
     float2* xb = reinterpret_cast<float2*>(smraw);  // W exchange columns
     float2* ds = xb + W * E::S;                     // [ny][Hx]: the plane after inverse y
     float2 v[16];
@@ -123,16 +126,16 @@ __device__ __forceinline__ void inv_yx_body(const float2* __restrict__ Cp, float
         for (int k0 = 0; k0 < full; k0 += W) {
             const int kx = k0 + c;
             if (t < E::R1) {
+                const float2* Ct = Cp + kx + (int64_t)Hx * t;
 #pragma unroll
-                for (int r = 0; r < E::R2; ++r) v[r] = Cp[kx + (int64_t)Hx * (t + E::R1 * r)];
+                for (int r = 0; r < E::R2; ++r) v[r] = Ct[(int64_t)Hx * E::R1 * r];
             }
             E::template inv<true>(v, col, t, swt);
             if (t < E::R2) {
+                float2* dt = ds + t * Hx + kx;
 #pragma unroll
-                for (int s = 0; s < E::R1; ++s) {
-                    const int y = t + E::R2 * s;
-                    if (y < ny) ds[y * Hx + kx] = v[s];
-                }
+                for (int s = 0; s < E::R1; ++s)
+                    if (HALF ? E::R2 * s < L / 2 : t + E::R2 * s < ny) dt[E::R2 * s * Hx] = v[s];
             }
         }
     }
@@ -151,7 +154,7 @@ __device__ __forceinline__ void inv_yx_body(const float2* __restrict__ Cp, float
 #pragma unroll
             for (int s = 0; s < E::R1; ++s) {
                 const int y = t + E::R2 * s;
-                if (y < ny) ds[y * Hx + kx] = v[s];
+                if (HALF ? E::R2 * s < L / 2 : y < ny) ds[y * Hx + kx] = v[s];
             }
         }
     }
@@ -163,14 +166,19 @@ __device__ __forceinline__ void inv_yx_body(const float2* __restrict__ Cp, float
         for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
             const int y0 = 2 * (q0 + p), y1 = y0 + 1;
             if (t < E::R1) {
+                const float2* da = ds + y0 * Hx;
+                const float2* db = da + Hx;
 #pragma unroll
                 for (int r = 0; r < E::R2; ++r) {
                     const int k = t + E::R1 * r;
-                    const bool cj = k > L / 2;
-                    const int kk = cj ? L - k : k;
+                    // HALF: k below L/2 for R1*r < L/2, above for R1*r >
+                    // L/2, and L/2 + t at R1*r = L/2
+                    const bool cj = HALF ? (E::R1 * r > L / 2 || (E::R1 * r == L / 2 && t > 0)) : k > L / 2;
+                    const int kk = HALF ? (E::R1 * r < L / 2 ? t + E::R1 * r : (cj ? L - t - E::R1 * r : L / 2))
+                                        : (cj ? L - k : k);
                     float2 xa = make_float2(0.f, 0.f), xbv = make_float2(0.f, 0.f);
-                    if (y0 < ny) xa = ds[y0 * Hx + kk];
-                    if (y1 < ny) xbv = ds[y1 * Hx + kk];
+                    if (y0 < ny) xa = da[kk];
+                    if (y1 < ny) xbv = db[kk];
                     if (cj) {
                         xa.y = -xa.y;
                         xbv.y = -xbv.y;
@@ -180,13 +188,12 @@ __device__ __forceinline__ void inv_yx_body(const float2* __restrict__ Cp, float
             }
             E::template inv<true>(v, col, t, swt);
             if (t < E::R2) {
+                float* o0 = out + 4 * ((int64_t)nx * y0 + t);
 #pragma unroll
                 for (int s = 0; s < E::R1; ++s) {
-                    const int x = t + E::R2 * s;
-                    if (x >= nx) continue;
-                    const int64_t node = x + (int64_t)nx * y0;
-                    if (y0 < ny) out[4 * node] = v[s].x;
-                    if (y1 < ny) out[4 * (node + nx)] = v[s].y;
+                    if (!(HALF ? E::R2 * s < L / 2 : t + E::R2 * s < nx)) continue;
+                    if (y0 < ny) o0[4 * E::R2 * s] = v[s].x;
+                    if (y1 < ny) o0[4 * (E::R2 * s + nx)] = v[s].y;
                 }
             }
         }
@@ -204,8 +211,11 @@ __global__ void __launch_bounds__(256) k2_inv_yx(const float2* __restrict__ C, f
     extern __shared__ __align__(16) unsigned char smraw[];
     const int z = blockIdx.x, comp = blockIdx.y;
     const int64_t plane = (int64_t)Hx * L;
-    inv_yx_body<L>(C + (int64_t)comp * plane * nz + plane * z, E4 + lane0 + comp + 4 * (int64_t)nx * ny * z, nx, ny,
-                   Hx, swt, smraw);
+    float* o = E4 + lane0 + comp + 4 * (int64_t)nx * ny * z;
+    if (2 * nx == L && 2 * ny == L && 2 * (Hx - 1) == L)
+        inv_yx_body<L, true>(C + (int64_t)comp * plane * nz + plane * z, o, nx, ny, Hx, swt, smraw);
+    else
+        inv_yx_body<L, false>(C + (int64_t)comp * plane * nz + plane * z, o, nx, ny, Hx, swt, smraw);
 }
 
 // x pass: two real rows per complex FFT -> their half spectra.
