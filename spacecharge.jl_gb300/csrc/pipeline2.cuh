@@ -1409,7 +1409,7 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
 // gamma of components 0 and 1, so it enters multiplied by s2 (a power of two
 // near gamma) and leaves divided by it, both exact.
 template <int L, typename Tr, bool HALF>
-__global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k4_green_col(const Tr* __restrict__ in,
+__global__ void __launch_bounds__(kColW * F2<L>::NT, sizeof(Tr) == 4 ? 3 : 1) k4_green_col(const Tr* __restrict__ in,
                                                                            Tr* __restrict__ out, int ncols, int nh,
                                                                            int64_t as_in, int64_t cs_in,
                                                                            int64_t as_out, int64_t cs_out, Tr s2,
