@@ -43,42 +43,47 @@ __device__ __forceinline__ void col_body(const float2* in, float2* out, int ncol
     // straddle two batches: two contiguous segments)
     const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
     const int64_t f = tile * kColW + c;
-    const bool cok = f < (int64_t)ncols * nbatch;
-    const int bb = cok ? (int)(f / ncols) : 0;
-    const int col = (int)(f - (int64_t)bb * ncols);
+    const int64_t total = (int64_t)ncols * nbatch;
+    const bool cok = f < total;
+    // columns past the end (the last tile only) read the last column and store nothing
+    const int64_t fl = cok ? f : total - 1;
+    const int bb = total < (int64_t)1 << 31 ? (int)((unsigned)fl / (unsigned)ncols) : (int)(fl / ncols);
+    const int col = (int)(fl - (int64_t)bb * ncols);
     const int b = bwrap_n > 0 ? wrap_row2(bb, bwrap_n, bwrap_L) : bb;
     const float2* src = in + b * bs_in + comp * cs_in + col;
     float2* dst = out + b * bs_out + comp * cs_out + col;
     float2 v[16];
     if (!INV) {
+        // n_valid = L/2 without wrap (power-of-two axes): sample s exists for R2*s < L/2
+        const bool half = 2 * n_valid == L && !wrap;
         if (t < E::R2) {
+            const float2* st = src + t * as_in;
 #pragma unroll
             for (int s = 0; s < E::R1; ++s) {
                 const int n = t + E::R2 * s;
-                const bool ok = n < n_valid || (wrap && n > L - n_valid);
-                v[s] = (cok && ok) ? src[n * as_in] : make_float2(0.f, 0.f);
+                const bool ok = half ? E::R2 * s < L / 2 : (n < n_valid || (wrap && n > L - n_valid));
+                v[s] = ok ? st[E::R2 * s * as_in] : make_float2(0.f, 0.f);
             }
         }
         E::template fwd<false>(v, xb + c * E::S, t, swt);
         if (t < E::R1 && cok) {
+            float2* dt = dst + t * as_out;
 #pragma unroll
-            for (int r = 0; r < E::R2; ++r) dst[(t + E::R1 * r) * as_out] = v[r];
+            for (int r = 0; r < E::R2; ++r) dt[E::R1 * r * as_out] = v[r];
         }
     } else {
         if (t < E::R1) {
+            const float2* st = src + t * as_in;
 #pragma unroll
-            for (int r = 0; r < E::R2; ++r) {
-                const int k = t + E::R1 * r;
-                v[r] = cok ? src[k * as_in] : make_float2(0.f, 0.f);
-            }
+            for (int r = 0; r < E::R2; ++r) v[r] = st[E::R1 * r * as_in];
         }
         E::template inv<true>(v, xb + c * E::S, t, swt);
         if (t < E::R2 && cok) {
+            const bool half = 2 * n_store == L;
+            float2* dt = dst + t * as_out;
 #pragma unroll
-            for (int s = 0; s < E::R1; ++s) {
-                const int n = t + E::R2 * s;
-                if (n < n_store) dst[n * as_out] = v[s];
-            }
+            for (int s = 0; s < E::R1; ++s)
+                if (half ? E::R2 * s < L / 2 : t + E::R2 * s < n_store) dt[E::R2 * s * as_out] = v[s];
         }
     }
 }
@@ -229,14 +234,19 @@ __device__ __forceinline__ void fwd_x_body(const float* __restrict__ rho, float2
     const int r0 = 2 * (blk * P + p), r1 = r0 + 1;
     float2* col = xb + p * E::S;
     float2 v[16];
+    // power-of-two rows (nx = L/2, Hx = L/2 + 1): sample s exists for
+    // R2*s < L/2, and the output indices are constants past a per-thread base
+    const bool half = 2 * nx == L && 2 * (Hx - 1) == L;
     if (t < E::R2) {
+        const float* ra = rho + (int64_t)r0 * nx + t;
+        const float* rb = ra + nx;
 #pragma unroll
         for (int s = 0; s < E::R1; ++s) {
             const int x = t + E::R2 * s;
             float re = 0.f, im = 0.f;
-            if (x < nx) {
-                if (r0 < rows) re = rho[(int64_t)r0 * nx + x];
-                if (r1 < rows) im = rho[(int64_t)r1 * nx + x];
+            if (half ? E::R2 * s < L / 2 : x < nx) {
+                if (r0 < rows) re = ra[E::R2 * s];
+                if (r1 < rows) im = rb[E::R2 * s];
             }
             v[s] = make_float2(re, im);
         }
@@ -248,11 +258,18 @@ __device__ __forceinline__ void fwd_x_body(const float* __restrict__ rho, float2
     }
     __syncthreads();
     if (r0 < rows) {
-        for (int k = t; k <= L / 2; k += E::NT) {
+        constexpr int NT = E::NT;
+        const int tm = t == 0 ? 0 : NT - t;  // the mirror L - k = tm + constant
+        float2* Aa = A + (int64_t)r0 * Hx + t;
+        float2* Ab = Aa + Hx;
+#pragma unroll
+        for (int i = 0; i <= L / (2 * NT); ++i) {
+            if (i == L / (2 * NT) && t > 0) break;  // k = t + NT*i <= L/2
+            const int km = t == 0 ? xoff((L - NT * i) & (L - 1)) : tm + xoff(L - NT * (i + 1));
             float2 xa, xbv;
-            split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
-            A[(int64_t)r0 * Hx + k] = xa;
-            if (r1 < rows) A[(int64_t)r1 * Hx + k] = xbv;
+            split_pair(col[t + xoff(NT * i)], col[km], xa, xbv);
+            Aa[NT * i] = xa;
+            if (r1 < rows) Ab[NT * i] = xbv;
         }
     }
 }
