@@ -201,9 +201,18 @@ __device__ __forceinline__ void corner_sum_body(const float* __restrict__ corner
                                                 float* __restrict__ rho, int assign, int64_t blk) {
     const int64_t node = blk * blockDim.x + threadIdx.x;
     if (node >= N) return;
-    const int i = (int)(node % nx);
-    const int64_t r = node / nx;
-    const int j = (int)(r % ny), k = (int)(r / ny);
+    int i, j, k;
+    if (N <= 0x7FFFFFFF) {  // 32-bit index arithmetic (every mesh that fits in memory)
+        const unsigned u = (unsigned)node, r = u / (unsigned)nx;
+        i = (int)(u - r * (unsigned)nx);
+        j = (int)(r % (unsigned)ny);
+        k = (int)(r / (unsigned)ny);
+    } else {
+        const int64_t r = node / nx;
+        i = (int)(node - r * nx);
+        j = (int)(r % ny);
+        k = (int)(r / ny);
+    }
     const int64_t sy = nx, sz = (int64_t)nx * ny;
     float s = 0.0f;
 #pragma unroll

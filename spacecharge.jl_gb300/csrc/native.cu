@@ -491,9 +491,17 @@ __global__ void __launch_bounds__(64) k_igf_split(float* __restrict__ G, double*
     const int64_t total = (int64_t)g.nx * g.ny * zc;
     const int64_t t = (blockIdx.x - near_blocks) * (int64_t)blockDim.x + threadIdx.x;
     if (t >= total) return;
-    const int ix = (int)(t % g.nx);
-    const int iy = (int)((t / g.nx) % g.ny);
-    const int iz = (int)(t / ((int64_t)g.nx * g.ny));
+    int ix, iy, iz;
+    if (total <= 0x7FFFFFFF) {  // 32-bit index arithmetic
+        const unsigned u = (unsigned)t, r = u / (unsigned)g.nx;
+        ix = (int)(u - r * (unsigned)g.nx);
+        iy = (int)(r % (unsigned)g.ny);
+        iz = (int)(r / (unsigned)g.ny);
+    } else {
+        ix = (int)(t % g.nx);
+        iy = (int)((t / g.nx) % g.ny);
+        iz = (int)(t / ((int64_t)g.nx * g.ny));
+    }
     const int dz = g.image ? iz - (g.nz - 1) : iz;
     const OctCell cell = oct_cell(g, ix, iy, dz);
     if (cell.near) return;
@@ -541,9 +549,17 @@ __global__ void __launch_bounds__(256) k_igf_octant(float* __restrict__ G, Octan
     const int64_t total = (int64_t)g.nx * g.ny * zc;
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= total) return;
-    const int ix = (int)(t % g.nx);
-    const int iy = (int)((t / g.nx) % g.ny);
-    const int iz = (int)(t / ((int64_t)g.nx * g.ny));
+    int ix, iy, iz;
+    if (total <= 0x7FFFFFFF) {  // 32-bit index arithmetic
+        const unsigned u = (unsigned)t, r = u / (unsigned)g.nx;
+        ix = (int)(u - r * (unsigned)g.nx);
+        iy = (int)(r % (unsigned)g.ny);
+        iz = (int)(r / (unsigned)g.ny);
+    } else {
+        ix = (int)(t % g.nx);
+        iy = (int)((t / g.nx) % g.ny);
+        iz = (int)(t / ((int64_t)g.nx * g.ny));
+    }
     const int dz = g.image ? iz - (g.nz - 1) : iz;
     const OctCell cell = oct_cell(g, ix, iy, dz);
     float out[3];
