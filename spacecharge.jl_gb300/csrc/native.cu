@@ -1144,6 +1144,9 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
     const int Lx = w.L[0], Ly = w.L[1], Lz = w.L[2], Hx = w.Hx;
     (void)Lx;
     // green_ready: the spectra are being built on another stream (native_green_async)
+#ifndef SC_FUSED_FWD_WITH_GREEN
+#define SC_FUSED_FWD_WITH_GREEN 0  // the fused forward x+y pass beside a concurrent Green build
+#endif
     if (!green_ready) SC_TRY(ensure_green_t<T>(m, at_cathode, s));
     m->launches += 5;
     T2* A = (T2*)w.A;
@@ -1162,7 +1165,8 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
     // from 6.10 to 6.43 ms; alone, the Green-cached kick went from 0.110 to
     // 0.108 ms and the tracking step from 0.134 to 0.131 ms.
     bool fwd_fused = false;
-    if (two && SC_FUSED_FWD_XY && (!green_ready || m->green_ahead) && !m->beside_others) {
+    if (two && SC_FUSED_FWD_XY && (!green_ready || m->green_ahead || SC_FUSED_FWD_WITH_GREEN) &&
+        !m->beside_others) {
         StageScope st(m->timer, SC_STAGE_FWD_X, s);
         fwd_fused = launch2_fwd_xy(w.log2L[0], w.log2L[1], (const float*)m->rho, (float2*)B, nx, ny, nz, Hx,
                                    (const float2*)tw, s, m->fused_smem_cap);

@@ -303,16 +303,20 @@ __device__ __forceinline__ void fwd_xy_body(const float* __restrict__ rz, float2
     {
         const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
         float2* col = xb + p * E::S;
+        // power-of-two rows (nx = L/2, Hx = L/2 + 1): constant sample and output offsets
+        const bool half = 2 * nx == L && 2 * (Hx - 1) == L;
         for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
             const int y0 = 2 * (q0 + p), y1 = y0 + 1;
             if (t < E::R2) {
+                const float* ra = rz + (int64_t)y0 * nx + t;
+                const float* rb = ra + nx;
 #pragma unroll
                 for (int s = 0; s < E::R1; ++s) {
                     const int x = t + E::R2 * s;
                     float re = 0.f, im = 0.f;
-                    if (x < nx) {
-                        if (y0 < ny) re = rz[(int64_t)y0 * nx + x];
-                        if (y1 < ny) im = rz[(int64_t)y1 * nx + x];
+                    if (half ? E::R2 * s < L / 2 : x < nx) {
+                        if (y0 < ny) re = ra[E::R2 * s];
+                        if (y1 < ny) im = rb[E::R2 * s];
                     }
                     v[s] = make_float2(re, im);
                 }
@@ -324,11 +328,18 @@ __device__ __forceinline__ void fwd_xy_body(const float* __restrict__ rz, float2
             }
             __syncthreads();
             if (y0 < ny) {
-                for (int k = t; k <= L / 2; k += E::NT) {
+                constexpr int NT = E::NT;
+                const int tm = t == 0 ? 0 : NT - t;  // the mirror L - k = tm + constant
+                float2* da = ds + y0 * Hx + t;
+                float2* db = da + Hx;
+#pragma unroll
+                for (int i = 0; i <= L / (2 * NT); ++i) {
+                    if (i == L / (2 * NT) && t > 0) break;  // k = t + NT*i <= L/2
+                    const int km = t == 0 ? xoff((L - NT * i) & (L - 1)) : tm + xoff(L - NT * (i + 1));
                     float2 xa, xbv;
-                    split_pair(col[xsw(k)], col[xsw((L - k) & (L - 1))], xa, xbv);
-                    ds[y0 * Hx + k] = xa;
-                    if (y1 < ny) ds[y1 * Hx + k] = xbv;
+                    split_pair(col[t + xoff(NT * i)], col[km], xa, xbv);
+                    da[NT * i] = xa;
+                    if (y1 < ny) db[NT * i] = xbv;
                 }
             }
             __syncthreads();
@@ -342,19 +353,22 @@ __device__ __forceinline__ void fwd_xy_body(const float* __restrict__ rz, float2
     {
         const int c = threadIdx.x % W, t = threadIdx.x / W;
         float2* col = xb + c * E::S;
+        const bool yhalf = 2 * ny == L;
         for (int k0 = 0; k0 < full; k0 += W) {
             const int kx = k0 + c;
             if (t < E::R2) {
+                const float2* dt = ds + t * Hx + kx;
 #pragma unroll
                 for (int s = 0; s < E::R1; ++s) {
                     const int n = t + E::R2 * s;
-                    v[s] = n < ny ? ds[n * Hx + kx] : make_float2(0.f, 0.f);
+                    v[s] = (yhalf ? E::R2 * s < L / 2 : n < ny) ? dt[E::R2 * s * Hx] : make_float2(0.f, 0.f);
                 }
             }
             E::template fwd<false>(v, col, t, swt);
             if (t < E::R1) {
+                float2* bt = Bz + kx + (int64_t)Hx * t;
 #pragma unroll
-                for (int r = 0; r < E::R2; ++r) Bz[kx + (int64_t)Hx * (t + E::R1 * r)] = v[r];
+                for (int r = 0; r < E::R2; ++r) bt[(int64_t)Hx * E::R1 * r] = v[r];
             }
         }
     }
