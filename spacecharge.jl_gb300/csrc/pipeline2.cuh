@@ -678,11 +678,14 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_zpass(con
 
 // Adjoint z pass: three forward z transforms of Ebar_c, correlation with the
 // conjugate Green spectra summed over components, one inverse transform.
-template <int L>
+template <int L, bool HALF>
 __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass(const float2* __restrict__ C,
                                                                      float2* __restrict__ B, int Hx, int Ly, int nz,
                                                                      GreenView gv, const float2* __restrict__ tw) {
+    // HALF: nz = L/2, so which z rows exist is known at compile time; the
+    // free-space Green values and signs at constant offsets as in zpass_body
     using E = F2<L>;
+    constexpr int RL = E::R1;
     __shared__ float2 swt[L];
     stage_twiddles<L>(swt, tw);
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -692,8 +695,9 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass
     const int64_t plane = (int64_t)Hx * Ly;
     const int f = blockIdx.x * kColW + c;
     const bool cok = f < plane;
-    const int ky = cok ? f / Hx : 0;
-    const int kx = f - ky * Hx;
+    const int fl = cok ? f : (int)plane - 1;  // columns past the plane load the last one, store nothing
+    const int ky = fl / Hx;
+    const int kx = fl - ky * Hx;
     float2* col = xb + c * E::S;
     float2* sc = spec + c * E::S;
     constexpr int HZ = L / 2 + 1;
@@ -706,12 +710,13 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass
 #pragma unroll
     for (int r = 0; r < 16; ++r) acc[r] = make_float2(0.f, 0.f);
     for (int comp = 0; comp < 3; ++comp) {
-        const float2* Cc = C + comp * (plane * nz) + f;
+        const float2* Cc = C + comp * (plane * nz) + fl;
         if (t < E::R2) {
 #pragma unroll
             for (int s = 0; s < E::R1; ++s) {
                 const int z = t + E::R2 * s;
-                v[s] = (cok && z < nz) ? Cc[plane * z] : make_float2(0.f, 0.f);
+                const bool ok = HALF ? E::R2 * s < L / 2 : z < nz;
+                v[s] = ok ? Cc[plane * z] : make_float2(0.f, 0.f);
             }
         }
         E::template fwd<false>(v, col, t, swt);
@@ -723,17 +728,20 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass
         }
         if (comp == 0) cp_async_wait_all();
         if (gv.image || comp == 0) __syncthreads();
-        if (t < E::R1 && cok) {
+        if (t < E::R1) {
+            const float sy = comp == 1 ? ysign : 1.f;
+            const float su = comp == 2 ? -sy : sy;
+            const float sm = t > 0 ? su : sy;  // kz = L/2 + t
             const float* gfc = gsm + comp * HZ * kColW + c;
+            const float* glo = gfc + t * kColW;
+            const float* ghi = gfc + (L - t) * kColW;
             const float2* gic = reinterpret_cast<const float2*>(gv.gimg) + comp * gv.cs_img + kx + gv.Hx * kyf;
 #pragma unroll
             for (int r = 0; r < E::R2; ++r) {
-                const int kz = t + E::R1 * r;
-                const int kzf = kz <= L / 2 ? kz : L - kz;
-                float sg = 1.f;
-                if (comp == 1) sg = ysign;
-                if (comp == 2 && kz > L / 2) sg = -1.f;
-                const float g = sg * gfc[kzf * kColW];
+                const int kz = t + RL * r;
+                const float g = RL * r < L / 2    ? glo[RL * r * kColW] * sy
+                                : RL * r == L / 2 ? ghi[-RL * r * kColW] * sm
+                                                  : ghi[-RL * r * kColW] * su;
                 // Ebar^ * conj(i g) = Ebar^ * (-i g)
                 acc[r].x += v[r].y * g;
                 acc[r].y -= v[r].x * g;
@@ -756,7 +764,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB) k2_adj_zpass
 #pragma unroll
         for (int s = 0; s < E::R1; ++s) {
             const int z = t + E::R2 * s;
-            if (z < nz) Bc[plane * z] = acc[s];
+            if (HALF ? E::R2 * s < L / 2 : z < nz) Bc[plane * z] = acc[s];
         }
     }
 }
@@ -1684,9 +1692,15 @@ static bool launch2_adj_zpass(int logL, const float2* C, float2* B, int Hx, int 
     {                                                                                       \
         const size_t smem = sizeof(float2) * kColW * F2<LL>::S * 2 +                        \
                             sizeof(float) * 3 * (LL / 2 + 1) * kColW;                           \
-        if (set_smem(k2_adj_zpass<LL>, smem) != SC_OK) return false;                        \
         const int64_t ncol = (int64_t)Hx * Ly;                                              \
-        launch_pdl(k2_adj_zpass<LL>, (unsigned)((ncol + kColW - 1) / kColW), kColW * F2<LL>::NT, smem, s, C, B, Hx, Ly, nz, gv, tw); \
+        const unsigned grid = (unsigned)((ncol + kColW - 1) / kColW);                       \
+        if (2 * nz == LL) {                                                                 \
+            if (set_smem(k2_adj_zpass<LL, true>, smem) != SC_OK) return false;              \
+            launch_pdl(k2_adj_zpass<LL, true>, grid, kColW * F2<LL>::NT, smem, s, C, B, Hx, Ly, nz, gv, tw); \
+        } else {                                                                            \
+            if (set_smem(k2_adj_zpass<LL, false>, smem) != SC_OK) return false;             \
+            launch_pdl(k2_adj_zpass<LL, false>, grid, kColW * F2<LL>::NT, smem, s, C, B, Hx, Ly, nz, gv, tw); \
+        }                                                                                   \
     }
     SC_L_SWITCH(logL, SC_K2AZ)
 #undef SC_K2AZ
