@@ -221,6 +221,115 @@ __global__ void __launch_bounds__(256) k_zpass_pot(const typename Cplx<T>::T2* _
     }
 }
 
+// The same z pass for FP32 and Lz <= 256 on the register two-step transform
+// (zpass_body's thread map: kColW columns of the flattened (kx, ky) plane per
+// CTA, F2<L>::NT threads per column).  The tile's free-space spectrum
+// (Lz/2 + 1 values per column) and, with the image, its half-stored image
+// spectrum are copied to shared memory with cp.async while the forward
+// transform runs; the forward spectrum stays in shared memory for the image
+// term at -kz.  HALF: nz = Lz/2.
+template <int L, bool HALF>
+__global__ void __launch_bounds__(kColW * F2<L>::NT, SC_ZPASS_MINB)
+    k2_zpass_pot(const float2* __restrict__ B, float2* __restrict__ C, int Hx, int Ly, int nz,
+                 const float* __restrict__ pf, const float2* __restrict__ pi, int image, int Hy,
+                 const float2* __restrict__ tw) {
+    using E = F2<L>;
+    constexpr int RL = E::R1, HZ = L / 2 + 1;
+    __shared__ float2 swt[L];
+    stage_twiddles<L>(swt, tw);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    float2* xb = reinterpret_cast<float2*>(smraw);
+    float2* spec = xb + kColW * E::S;
+    float2* gis = spec + kColW * E::S;                    // [HZ][kColW] image spectrum
+    float* gs = reinterpret_cast<float*>(gis + HZ * kColW);  // [HZ][kColW] free-space spectrum
+    const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
+    const int64_t plane = (int64_t)Hx * Ly;
+    const int f = blockIdx.x * kColW + c;
+    const bool cok = f < plane;
+    const int fl = cok ? f : (int)plane - 1;
+    const int ky = fl / Hx, kx = fl - ky * Hx;
+    const int kyf = ky <= Ly / 2 ? ky : Ly - ky;
+    const int64_t gstep = (int64_t)Hx * Hy;
+    {
+        const int64_t o = kx + (int64_t)Hx * kyf;
+        for (int kz = t; kz < HZ; kz += blockDim.x / kColW) {
+            cp_async4(gs + kz * kColW + c, pf + o + gstep * kz);
+            if (image) cp_async8(gis + kz * kColW + c, pi + o + gstep * kz);
+        }
+        cp_async_commit();
+    }
+    float2* col = xb + c * E::S;
+    float2* sc = spec + c * E::S;
+    float2 v[16];
+    if (t < E::R2) {
+        const float2* Bc = B + fl;
+#pragma unroll
+        for (int s = 0; s < E::R1; ++s) {
+            const int z = t + E::R2 * s;
+            v[s] = (HALF ? E::R2 * s < L / 2 : z < nz) ? Bc[plane * z] : make_float2(0.f, 0.f);
+        }
+    }
+    E::template fwd<false>(v, col, t, swt);
+    if (t < E::R1) {
+#pragma unroll
+        for (int r = 0; r < E::R2; ++r) sc[t + xoff(RL * r)] = v[r];
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (t < E::R1) {
+        // kz = t + RL*r: folded index kz below L/2, L - kz at or above it
+        const float* glo = gs + t * kColW + c;
+        const float* ghi = gs + (L - t) * kColW + c;
+#pragma unroll
+        for (int r = 0; r < E::R2; ++r) {
+            const int kz = t + RL * r;
+            const bool lower = RL * r < L / 2;
+            const float g = lower ? glo[RL * r * kColW] : ghi[-RL * r * kColW];
+            const float2 X = v[r];
+            float2 o = make_float2(X.x * g, X.y * g);
+            if (image) {
+                const int kzf = kz <= L / 2 ? kz : L - kz;
+                float2 gc = gis[kzf * kColW + c];
+                if (kz > L / 2) gc.y = -gc.y;  // S(L - kz) = conj S(kz)
+                o = cadd(o, cmul(sc[xsw((L - kz) & (L - 1))], gc));
+            }
+            v[r] = o;
+        }
+    }
+    E::template inv<true>(v, col, t, swt);
+    if (t < E::R2 && cok) {
+        float2* Cc = C + f;
+#pragma unroll
+        for (int s = 0; s < E::R1; ++s) {
+            const int z = t + E::R2 * s;
+            if (HALF ? E::R2 * s < L / 2 : z < nz) Cc[plane * z] = v[s];
+        }
+    }
+}
+
+static bool launch2_zpass_pot(int logLz, const float2* B, float2* C, int Hx, int Ly, int nz, const float* pf,
+                              const float2* pi, int image, int Hy, const float2* tw, cudaStream_t s) {
+#define SC_K2ZP_GO(LL, HALF)                                                                               \
+    {                                                                                                      \
+        if (set_smem(k2_zpass_pot<LL, HALF>, smem) != SC_OK) return false;                                 \
+        k2_zpass_pot<LL, HALF><<<grid, kColW * F2<LL>::NT, smem, s>>>(B, C, Hx, Ly, nz, pf, pi, image, Hy, tw); \
+    }
+#define SC_K2ZP(LL)                                                                                         \
+    {                                                                                                       \
+        const size_t smem = sizeof(float2) * kColW * F2<LL>::S * 2 + sizeof(float2) * (LL / 2 + 1) * kColW + \
+                            sizeof(float) * (LL / 2 + 1) * kColW;                                           \
+        const unsigned grid = (unsigned)(((int64_t)Hx * Ly + kColW - 1) / kColW);                          \
+        if (2 * nz == LL)                                                                                   \
+            SC_K2ZP_GO(LL, true)                                                                            \
+        else                                                                                                \
+            SC_K2ZP_GO(LL, false)                                                                           \
+    }
+    SC_L_SWITCH(logLz, SC_K2ZP)
+#undef SC_K2ZP
+#undef SC_K2ZP_GO
+    return true;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_lane3(const T* __restrict__ E4, T* __restrict__ phi, int64_t N) {
     pdl_wait();
@@ -352,7 +461,11 @@ static int potential_t(sc_mesh* m, int at_cathode, void* phi, cudaStream_t s) {
     const T2* tw = twiddles<T>(ctx);
     SC_TRY(native_forward(m, s));
     T2* C = (T2*)w.C;
-    {
+    const bool two_z = std::is_same<T, float>::value && (w.engine >= 0 ? w.engine : fft_engine()) == 0;
+    if (two_z && launch2_zpass_pot(w.log2L[2], (const float2*)w.B, (float2*)C, Hx, Ly, nz, (const float*)w.pfree,
+                                   (const float2*)w.pimg, at_cathode ? 1 : 0, Hy, (const float2*)tw, s)) {
+        SC_LAUNCH_CHECK("k2_zpass_pot");
+    } else {
         int lgW = pick_cols(w.log2L[2]);
         while (lgW > 0 && sizeof(T2) * 3 * ((size_t)1 << lgW) * Lz > 200 * 1024) --lgW;
         const int W = 1 << lgW;
