@@ -454,12 +454,23 @@ static int potential_t(sc_mesh* m, int at_cathode, void* phi, cudaStream_t s) {
     const int Lx = w.L[0], Ly = w.L[1], Lz = w.L[2], Hx = w.Hx;
     const int Hy = Ly / 2 + 1;
     (void)Lx;
-    SC_TRY(pot_green<T>(m, false, s));
-    if (at_cathode) SC_TRY(pot_green<T>(m, true, s));
+    // The Green spectra do not depend on rho: build them on the mesh's side
+    // stream beside the forward x and y transforms, join before the z pass.
+    if (!m->side) SC_CUDA(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
+    if (!m->ev_fork) SC_CUDA(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
+    if (!m->ev_join) SC_CUDA(cudaEventCreateWithFlags(&m->ev_join, cudaEventDisableTiming));
+    SC_CUDA(cudaEventRecord(m->ev_fork, s));
+    SC_CUDA(cudaStreamWaitEvent(m->side, m->ev_fork, 0));
+    int st = pot_green<T>(m, false, m->side);
+    if (st == SC_OK && at_cathode) st = pot_green<T>(m, true, m->side);
+    const cudaError_t ej = cudaEventRecord(m->ev_join, m->side);
+    if (st == SC_OK && ej != cudaSuccess) st = cuda_fail(ej, "cudaEventRecord");
+    if (st == SC_OK) st = native_forward(m, s);
+    cudaStreamWaitEvent(s, m->ev_join, 0);  // joined on every path
+    SC_TRY(st);
     DeviceCtx* ctx = nullptr;
     SC_TRY(device_ctx(&ctx));
     const T2* tw = twiddles<T>(ctx);
-    SC_TRY(native_forward(m, s));
     T2* C = (T2*)w.C;
     const bool two_z = std::is_same<T, float>::value && (w.engine >= 0 ? w.engine : fft_engine()) == 0;
     if (two_z && launch2_zpass_pot(w.log2L[2], (const float2*)w.B, (float2*)C, Hx, Ly, nz, (const float*)w.pfree,
