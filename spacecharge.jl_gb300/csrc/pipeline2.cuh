@@ -1164,7 +1164,8 @@ __device__ __forceinline__ float green_near_value(const GreenNear& g, int c, int
 template <int L, typename Tr, int NTH, bool STG, bool HALF>
 __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2out, int nx,
                                                       int ny, int Hx, int64_t gcs, int64_t t2cs, GreenNear near,
-                                                      int g16, const typename Cplx<Tr>::T2* __restrict__ tw) {
+                                                      int g16, int solo,
+                                                      const typename Cplx<Tr>::T2* __restrict__ tw) {
     using E = F2<L>;
     using T2 = typename Cplx<Tr>::T2;
     constexpr int W = NTH / E::NT;  // row pairs (x pass) or column pairs (y pass) per round
@@ -1178,10 +1179,13 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
     // odd along x (0; role 1: component 2), slot 1 component 1
     Tr* gs = reinterpret_cast<Tr*>(smraw + ((W * E::S * sizeof(T2) + 2 * sizeof(Tr) * ny * Hx + 15) & ~(size_t)15));
     const int iz = blockIdx.x;
-    const bool pair = blockIdx.y == 0;
+    // solo: one component (0), even along x and y (the potential kernel):
+    // every CTA takes role 1 with that component
+    const bool pair = !solo && blockIdx.y == 0;
+    const int c1 = solo ? 0 : 2;  // the component of role 1
     const int per = nx * ny;
     if constexpr (STG) {
-        const Tr* src0 = G + (pair ? 0 : 2) * gcs + (int64_t)per * iz;
+        const Tr* src0 = G + (pair ? 0 : c1) * gcs + (int64_t)per * iz;
         for (int sl = 0; sl < (pair ? 2 : 1); ++sl) {
             const Tr* src = src0 + sl * gcs;
             Tr* dst = gs + sl * per;
@@ -1206,7 +1210,7 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
         if (dz >= near.bz0 && dz < near.bz1) {
             const int box = near.nbx * near.nby;
             for (int e = threadIdx.x; e < (pair ? 2 : 1) * box; e += NTH) {
-                const int c = pair ? e / box : 2;
+                const int c = pair ? e / box : c1;
                 const int r = e - (pair ? c : 0) * box;
                 const int ix = r % near.nbx, iy = r / near.nbx;
                 if (green_near_cell(near, ix, iy, dz)) {
@@ -1225,7 +1229,7 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
         const int t = threadIdx.x % E::NT, p = threadIdx.x / E::NT;
         T2* col = xb + p * E::S;
         // even along x: component 1 (role 0) or 2 (role 1); odd: component 0
-        const Tr* ge = STG ? gs + (pair ? per : 0) : G + (pair ? 1 : 2) * gcs + (int64_t)per * iz;
+        const Tr* ge = STG ? gs + (pair ? per : 0) : G + (pair ? 1 : c1) * gcs + (int64_t)per * iz;
         const Tr* go = STG ? gs : G + (int64_t)per * iz;
         Tr* dst_e = pair ? ts1 : ts0;
         for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
@@ -1325,7 +1329,7 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
         const int c = threadIdx.x % W, t = threadIdx.x / W;
         T2* col = xb + c * E::S;
         // even along y: component 0 (role 0) or 2 (role 1); odd: component 1
-        Tr* out_e = T2out + (pair ? 0 : 2) * t2cs + (int64_t)Hx * (L / 2 + 1) * iz;
+        Tr* out_e = T2out + (pair ? 0 : c1) * t2cs + (int64_t)Hx * (L / 2 + 1) * iz;
         Tr* out_o = T2out + t2cs + (int64_t)Hx * (L / 2 + 1) * iz;
         // the Nyquist column kx = L/2 by direct sums:
         // X(k) = sum_d x(d) w^(k d), d = -(ny-1)..ny-1
@@ -1452,6 +1456,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, sizeof(Tr) == 4 ? 3 : 1) k4
                                                                            Tr* __restrict__ out, int ncols, int nh,
                                                                            int64_t as_in, int64_t cs_in,
                                                                            int64_t as_out, int64_t cs_out, Tr s2,
+                                                                           int solo,
                                                                            const typename Cplx<Tr>::T2* __restrict__ tw) {
     using E = F2<L>;
     using T2 = typename Cplx<Tr>::T2;
@@ -1459,10 +1464,13 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, sizeof(Tr) == 4 ? 3 : 1) k4
     stage_twiddles<L>(swt, tw);
     extern __shared__ __align__(16) unsigned char smraw[];
     T2* xb = reinterpret_cast<T2*>(smraw);
-    const bool pair = blockIdx.y == 0;
-    const Tr* ie = in + (pair ? 0 : 1) * cs_in;
+    // solo: one component (0), even along z (the potential kernel): every CTA
+    // takes role 1 with that component
+    const bool pair = !solo && blockIdx.y == 0;
+    const int c1 = solo ? 0 : 1;  // the component of role 1
+    const Tr* ie = in + (pair ? 0 : c1) * cs_in;
     const Tr* io = in + 2 * cs_in;
-    Tr* oe = out + (pair ? 0 : 1) * cs_out;
+    Tr* oe = out + (pair ? 0 : c1) * cs_out;
     Tr* oo = out + 2 * cs_out;
     const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
     const int64_t fa = (int64_t)blockIdx.x * (2 * kColW) + c, fb = fa + kColW;
@@ -1789,12 +1797,13 @@ static bool launch3_green_col(bool img, int logL, const Tr* in, void* out, int n
 
 // x and y passes of the field kernel's three components in one launch of
 // k4_green_xy (256 threads, or 512 when the two slices need more than
-// 100 KB of shared memory).  Returns false (nothing launched) where they do
+// 100 KB of shared memory); solo: the one component of the potential kernel
+// (even along x and y) at G and T2.  Returns false (nothing launched) where they do
 // not fit; the caller then runs launch3_green_xy or the separate passes.
 template <typename Tr>
 static bool launch_green_xy_field(int logLx, int logLy, Tr* G, Tr* T2, int nx, int ny, int zc, int Hx,
                                   int64_t gcs, int64_t t2cs, const typename Cplx<Tr>::T2* tw, cudaStream_t s,
-                                  const GreenNear& near = GreenNear{}) {
+                                  const GreenNear& near = GreenNear{}, int solo = 0) {
     using C2 = typename Cplx<Tr>::T2;
     if (logLx != logLy) return false;
     const size_t planes = 2 * sizeof(Tr) * (size_t)ny * Hx;
@@ -1806,12 +1815,12 @@ static bool launch_green_xy_field(int logLx, int logLy, Tr* G, Tr* T2, int nx, i
     {                                                                                                        \
         if (half) {                                                                                          \
             if (set_smem(k4_green_xy<LL, Tr, NTH, STG, true>, SM) != SC_OK) return false;                    \
-            launch_pdl(k4_green_xy<LL, Tr, NTH, STG, true>, dim3(zc, 2), NTH, SM, s, G, T2, nx, ny, Hx, gcs,  \
-                       t2cs, near, g16, tw);                                                                  \
+            launch_pdl(k4_green_xy<LL, Tr, NTH, STG, true>, dim3(zc, solo ? 1 : 2), NTH, SM, s, G, T2, nx, ny, \
+                       Hx, gcs, t2cs, near, g16, solo, tw);                                                   \
         } else {                                                                                             \
             if (set_smem(k4_green_xy<LL, Tr, NTH, STG, false>, SM) != SC_OK) return false;                   \
-            launch_pdl(k4_green_xy<LL, Tr, NTH, STG, false>, dim3(zc, 2), NTH, SM, s, G, T2, nx, ny, Hx, gcs, \
-                       t2cs, near, g16, tw);                                                                  \
+            launch_pdl(k4_green_xy<LL, Tr, NTH, STG, false>, dim3(zc, solo ? 1 : 2), NTH, SM, s, G, T2, nx,   \
+                       ny, Hx, gcs, t2cs, near, g16, solo, tw);                                               \
         }                                                                                                    \
         ok = true;                                                                                           \
     }
@@ -1834,20 +1843,21 @@ static bool launch_green_xy_field(int logLx, int logLy, Tr* G, Tr* T2, int nx, i
 }
 
 // Free-space z pass of the field kernel's three components in one launch
-// of k4_green_col.  Columns at in + c*cs_in + col + d*as_in, out + c*cs_out
+// of k4_green_col; solo: the one component of the potential kernel (even
+// along z).  Columns at in + c*cs_in + col + d*as_in, out + c*cs_out
 // + col + k*as_out.
 template <typename Tr>
 static bool launch_green_z_field(int logL, const Tr* in, Tr* out, int ncols, int nh, int64_t as_in, int64_t cs_in,
                                  int64_t as_out, int64_t cs_out, double gamma, const typename Cplx<Tr>::T2* tw,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, int solo = 0) {
     using T2 = typename Cplx<Tr>::T2;
     const Tr s2 = (Tr)exp2(rint(log2(gamma > 1.0 ? gamma : 1.0)));  // a power of two: exact scaling
-    const dim3 grid((unsigned)(((int64_t)ncols + 2 * kColW - 1) / (2 * kColW)), 2);
+    const dim3 grid((unsigned)(((int64_t)ncols + 2 * kColW - 1) / (2 * kColW)), solo ? 1 : 2);
 #define SC_K4GC_GO(LL, HALF)                                                                                  \
     {                                                                                                         \
         if (set_smem(k4_green_col<LL, Tr, HALF>, smem) != SC_OK) return false;                                \
         launch_pdl(k4_green_col<LL, Tr, HALF>, grid, kColW * F2<LL>::NT, smem, s, in, out, ncols, nh, as_in,   \
-                   cs_in, as_out, cs_out, s2, tw);                                                             \
+                   cs_in, as_out, cs_out, s2, solo, tw);                                                       \
     }
 #define SC_K4GC(LL)                                                                                           \
     {                                                                                                         \

@@ -424,14 +424,19 @@ static int pot_green(sc_mesh* m, bool image, cudaStream_t s) {
     }
     // parity-reduced transform, every axis even (pipeline2.cuh)
     const int64_t plane = (int64_t)Hx * Hy;
-    if (!launch3_green_xy<T>(w.log2L[0], w.log2L[1], G, Txy, nx, ny, zc, Hx, cells, t2n, tw, s, 1, -1, -1)) {
+    // the paired kernels' single-component mode where they apply (Lx = Ly):
+    // the slice staged in shared memory, constant offsets for power-of-two axes
+    if (!launch_green_xy_field<T>(w.log2L[0], w.log2L[1], G, Txy, nx, ny, zc, Hx, cells, t2n, tw, s, GreenNear{}, 1) &&
+        !launch3_green_xy<T>(w.log2L[0], w.log2L[1], G, Txy, nx, ny, zc, Hx, cells, t2n, tw, s, 1, -1, -1)) {
         if (!(launch3_green_x<T>(w.log2L[0], G, T1, nx, ny * zc, Hx, cells, t1n, tw, s, 1, -1) &&
               launch3_green_col<T>(false, w.log2L[1], T1, Txy, Hx, zc, ny, -1, Hx, (int64_t)Hx * ny, t1n, Hx, plane, t2n,
                                    tw, s, 1, 0)))
             return fail(SC_ERR_UNSUPPORTED, "potential Green x/y pass: transform length out of range");
     }
     SC_LAUNCH_CHECK("potential Green x/y");
-    if (!launch3_green_col<T>(image, w.log2L[2], Txy, dst, (int)plane, 1, nz, -1, plane, 0, t2n, plane, 0, plane * Hz,
+    if (!(!image && launch_green_z_field<T>(w.log2L[2], Txy, (T*)dst, (int)plane, nz, plane, t2n, plane, plane * Hz,
+                                            1.0, tw, s, 1)) &&
+        !launch3_green_col<T>(image, w.log2L[2], Txy, dst, (int)plane, 1, nz, -1, plane, 0, t2n, plane, 0, plane * Hz,
                               tw, s, 1, 0))
         return fail(SC_ERR_UNSUPPORTED, "potential Green z pass: transform length out of range");
     SC_LAUNCH_CHECK("potential Green z");
