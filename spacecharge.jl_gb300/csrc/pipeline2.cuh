@@ -1232,14 +1232,39 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
         const Tr* ge = STG ? gs + (pair ? per : 0) : G + (pair ? 1 : c1) * gcs + (int64_t)per * iz;
         const Tr* go = STG ? gs : G + (int64_t)per * iz;
         Tr* dst_e = pair ? ts1 : ts0;
+        // RS (a slice too large to stage whole: 256-point FP32 planes, two x
+        // rounds of 2W rows): each round's rows are copied with cp.async into
+        // the upper halves of ts0 (the even-along-x component) and ts1 (the
+        // odd one), which only the last round's output uses, one round ahead
+        // of the transform
+        constexpr bool RS = !STG && HALF && L / 4 == 2 * W && sizeof(Tr) == 4;
+        const bool rs = RS && g16;
+        Tr* re_ = ts0 + (ny / 2) * Hx;
+        Tr* ro_ = ts1 + (ny / 2) * Hx;
+        auto stage_rows = [&](int q) {  // rows 2q .. 2q + 2W - 1
+            constexpr int K = 16 / sizeof(Tr);
+            const int n16 = 2 * W * nx / K;
+            const Tr* se = ge + (int64_t)nx * 2 * q;
+            const Tr* so = go + (int64_t)nx * 2 * q;
+            for (int i = threadIdx.x; i < n16; i += NTH) {
+                cp_async16(re_ + i * K, se + i * K);
+                if (pair) cp_async16(ro_ + i * K, so + i * K);
+            }
+            cp_async_commit();
+        };
+        if (rs) stage_rows(0);
         for (int q0 = 0; q0 < (ny + 1) / 2; q0 += W) {
             const int y0 = 2 * (q0 + p), y1 = y0 + 1;
             const bool ok0 = y0 < ny, ok1 = y1 < ny;
+            if (rs) {
+                cp_async_wait_all();
+                __syncthreads();
+            }
             if (HALF && t < E::R2) {
                 // x = t + R2*s: d = x below L/2, d = x - L above, nothing at
                 // x = L/2; |d| from a per-thread base and a constant offset
-                const Tr* ep0 = ge + nx * y0;
-                const Tr* op0 = go + nx * y0;
+                const Tr* ep0 = rs ? re_ + nx * (y0 - 2 * q0) : ge + nx * y0;
+                const Tr* op0 = rs ? ro_ + nx * (y0 - 2 * q0) : go + nx * y0;
 #pragma unroll
                 for (int s = 0; s < E::R1; ++s) {
                     const bool lower = E::R2 * s < L / 2;
@@ -1247,11 +1272,11 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
                     const int ax = lower ? t + E::R2 * s : L - t - E::R2 * s;
                     Tr e1 = 0, e2 = 0, o1 = 0, o2 = 0;
                     if (here) {
-                        if (ok0) e1 = STG ? ep0[ax] : __ldcg(ep0 + ax);
-                        if (ok1) e2 = STG ? ep0[nx + ax] : __ldcg(ep0 + nx + ax);
+                        if (ok0) e1 = (STG || rs) ? ep0[ax] : __ldcg(ep0 + ax);
+                        if (ok1) e2 = (STG || rs) ? ep0[nx + ax] : __ldcg(ep0 + nx + ax);
                         if (pair && (s > 0 || t > 0)) {  // odd: nothing at d = 0
-                            if (ok0) o1 = STG ? op0[ax] : __ldcg(op0 + ax);
-                            if (ok1) o2 = STG ? op0[nx + ax] : __ldcg(op0 + nx + ax);
+                            if (ok0) o1 = (STG || rs) ? op0[ax] : __ldcg(op0 + ax);
+                            if (ok1) o2 = (STG || rs) ? op0[nx + ax] : __ldcg(op0 + nx + ax);
                             if (!lower) o1 = -o1, o2 = -o2;
                         }
                     }
@@ -1286,6 +1311,10 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
                     }
                     v[s] = Cplx<Tr>::make(e1 + o1, e2 + o2);
                 }
+            }
+            if (rs) {
+                __syncthreads();  // every thread has its samples: the staged rows are free
+                if (q0 + W < (ny + 1) / 2) stage_rows(q0 + W);
             }
             E::template fwd<false>(v, col, t, swt);
             if (t < E::R1) {

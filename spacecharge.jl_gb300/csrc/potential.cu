@@ -105,8 +105,19 @@ __global__ void __launch_bounds__(64) k_pot_split(float* __restrict__ G, double*
     }
     const int zc = g.image ? 2 * g.nz - 1 : g.nz;
     const int64_t t = (blockIdx.x - near_blocks) * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= (int64_t)g.nx * g.ny * zc) return;
-    const int ix = (int)(t % g.nx), iy = (int)((t / g.nx) % g.ny), iz = (int)(t / ((int64_t)g.nx * g.ny));
+    const int64_t total = (int64_t)g.nx * g.ny * zc;
+    if (t >= total) return;
+    int ix, iy, iz;
+    if (total <= 0x7FFFFFFF) {  // 32-bit index arithmetic
+        const unsigned u = (unsigned)t, r = u / (unsigned)g.nx;
+        ix = (int)(u - r * (unsigned)g.nx);
+        iy = (int)(r % (unsigned)g.ny);
+        iz = (int)(r / (unsigned)g.ny);
+    } else {
+        ix = (int)(t % g.nx);
+        iy = (int)((t / g.nx) % g.ny);
+        iz = (int)(t / ((int64_t)g.nx * g.ny));
+    }
     const int dz = g.image ? iz - (g.nz - 1) : iz;
     float px, py, pz;
     if (pot_near(g, ix, iy, dz, px, py, pz)) return;
