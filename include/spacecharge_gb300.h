@@ -297,8 +297,10 @@ int sc_solve_noalloc(const int32_t grid_size[3], const double delta[3], double g
  *  - Staged engine (default).  Bunches on SC_PREC_MIXED meshes with
  *    transforms of at most 256 points, Lx = Ly, and deposit mode
  *    SC_DEPOSIT_VECTOR or SC_DEPOSIT_ATOMIC are kicked stage by stage in
- *    groups (sc_batch_set_group_bytes): per group, on one internal stream,
- *    one launch clears its bunches' charge buffers, one deposits them, one
+ *    groups (sc_batch_set_group_bytes): per group, on one internal stream
+ *    (the first for every group when the call builds no Green spectrum;
+ *    group g on stream g % nstreams when it does), one launch clears its
+ *    bunches' charge buffers, one deposits them, one
  *    sums the corner slots, one or two run the forward x+y transforms
  *    (sc_batch_set_fused_forward), one the z pass with the Green multiply,
  *    one the inverse y+x pass and one the gather.  A vector-mode bunch with
