@@ -916,7 +916,26 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(c
     const bool odd = comp == odd_comp;
     T2* col = xb + c * E::S;
     T2 v[16];
-    if (t < E::R2) {
+    if (2 * nh == L && t < E::R2) {
+        // nh = L/2: sample n = t + R2*s is d = n below L/2, d = n - L above,
+        // nothing at L/2; its offset a per-thread base plus R2*s*as_in
+        const int64_t blo = (IMG ? t + nh - 1 : t) * as_in;
+        const int64_t bhi = (IMG ? t - nh - 1 : L - t) * as_in;
+#pragma unroll
+        for (int s = 0; s < E::R1; ++s) {
+            const bool lower = E::R2 * s < L / 2;
+            const bool here = lower || E::R2 * s > L / 2 || t > 0;
+            const int64_t step = (int64_t)(E::R2 * s) * as_in;
+            const int64_t o = lower ? blo + step : (IMG ? bhi + step : bhi - step);
+            Tr a = 0, b = 0;
+            if (here) {
+                if (oka) a = __ldg(sa + o);
+                if (okb) b = __ldg(sb + o);
+                if (!IMG && odd && !lower) a = -a, b = -b;
+            }
+            v[s] = Cplx<Tr>::make(a, b);
+        }
+    } else if (t < E::R2) {
 #pragma unroll
         for (int s = 0; s < E::R1; ++s) {
             const int n = t + E::R2 * s;
@@ -947,7 +966,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, SC_COL_MINB) k3_green_col(c
         } else {
             // the line is real, so X(L - k) = conj X(k): only k <= L/2 is
             // stored, and img_at rebuilds the rest
-            const T2 ph1 = tw[(int)(((int64_t)k * (nh - 1)) & (L - 1)) * (kMaxL / L)];
+            const T2 ph1 = swt[(k * (nh - 1)) & (L - 1)];  // w_L^(k (nh - 1)), staged in shared memory
             T2* o = reinterpret_cast<T2*>(out) + comp * cs_out;
             for (int w = 0; w < 2; ++w) {
                 const bool okw = w == 0 ? oka : okb;
