@@ -81,16 +81,22 @@ static int device_ctx_init(DeviceCtx* c, int dev) {
     // correctly rounded FP64 value.
     std::vector<float2> t32(kMaxL);
     std::vector<double2> t64(kMaxL);
+    std::vector<float4> tdd(kMaxL);  // double-FP32: hi (re, im), lo (re, im)
     for (int k = 0; k < kMaxL; ++k) {
         long double a = -2.0L * 3.141592653589793238462643383279502884L * (long double)k / (long double)kMaxL;
-        double c = (double)cosl(a), s = (double)sinl(a);
+        const long double cl = cosl(a), sl = sinl(a);
+        double c = (double)cl, s = (double)sl;
         t64[k] = make_double2(c, s);
         t32[k] = make_float2((float)c, (float)s);
+        const float ch = (float)cl, sh = (float)sl;
+        tdd[k] = make_float4(ch, sh, (float)(cl - (long double)ch), (float)(sl - (long double)sh));
     }
     SC_CUDA(dev_alloc(&c->tw32, sizeof(float2) * kMaxL));
     SC_CUDA(dev_alloc(&c->tw64, sizeof(double2) * kMaxL));
+    SC_CUDA(dev_alloc(&c->twdd, sizeof(float4) * kMaxL));
     SC_CUDA(cudaMemcpy(c->tw32, t32.data(), sizeof(float2) * kMaxL, cudaMemcpyHostToDevice));
     SC_CUDA(cudaMemcpy(c->tw64, t64.data(), sizeof(double2) * kMaxL, cudaMemcpyHostToDevice));
+    SC_CUDA(cudaMemcpy(c->twdd, tdd.data(), sizeof(float4) * kMaxL, cudaMemcpyHostToDevice));
     c->partial_blocks = 2 * c->sm_count;
     SC_CUDA(dev_alloc(&c->partials, sizeof(double) * 6 * (c->partial_blocks + 1)));
     SC_CUDA(cudaHostAlloc((void**)&c->ext_host, sizeof(double) * 8, cudaHostAllocMapped));
@@ -113,6 +119,7 @@ int device_ctx(DeviceCtx** out) {
     if (st != SC_OK) {
         cudaFree(c->tw32);
         cudaFree(c->tw64);
+        cudaFree(c->twdd);
         cudaFree(c->partials);
         if (c->ext_host) cudaFreeHost(c->ext_host);
         delete c;
@@ -319,6 +326,7 @@ struct KickGraph {
 
 void mesh_state_key(const sc_mesh* m, std::vector<int64_t>& k, bool with_epoch) {
     k.push_back(m->green_cache);
+    k.push_back(m->df32_transforms);
     k.push_back(m->kick_mode);
     k.push_back(fft_engine());
     k.push_back(m->nw.engine);
@@ -789,6 +797,15 @@ int sc_mesh_set_green_cache(sc_mesh* m, int enabled) {
         m->nw.key_free.valid = false;
         m->nw.key_img.valid = false;
     }
+    return SC_OK;
+}
+
+int sc_mesh_set_fp64_transforms(sc_mesh* m, int mode) {
+    SC_TRY(check_mesh(m));
+    if (m->precision != SC_PREC_FP64) return fail(SC_ERR_INVALID, "FP64 transform modes apply to SC_PREC_FP64 meshes");
+    if (mode != SC_FP64_TRANSFORMS_FP64 && mode != SC_FP64_TRANSFORMS_DF32)
+        return fail(SC_ERR_INVALID, "unknown FP64 transform mode %d", mode);
+    m->df32_transforms = mode == SC_FP64_TRANSFORMS_DF32;
     return SC_OK;
 }
 

@@ -9,6 +9,7 @@
 
 #include <type_traits>
 
+#include "dd.cuh"
 #include "sc_internal.cuh"
 
 namespace sc {
@@ -33,6 +34,8 @@ template <typename T2>
 __device__ __forceinline__ T2 cadd(T2 a, T2 b) {
     if constexpr (std::is_same<T2, float2>::value) {
         return __fadd2_rn(a, b);
+    } else if constexpr (std::is_same<T2, ddc>::value) {
+        return dd_add(a, b);
     } else {
         a.x += b.x;
         a.y += b.y;
@@ -43,6 +46,8 @@ template <typename T2>
 __device__ __forceinline__ T2 csub(T2 a, T2 b) {
     if constexpr (std::is_same<T2, float2>::value) {
         return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+    } else if constexpr (std::is_same<T2, ddc>::value) {
+        return dd_sub(a, b);
     } else {
         a.x -= b.x;
         a.y -= b.y;
@@ -51,31 +56,44 @@ __device__ __forceinline__ T2 csub(T2 a, T2 b) {
 }
 template <typename T2>
 __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
-    T2 r;
-    r.x = a.x * b.x - a.y * b.y;
-    r.y = a.x * b.y + a.y * b.x;
-    return r;
+    if constexpr (std::is_same<T2, ddc>::value) {
+        return dd_cmul(a, b);
+    } else {
+        T2 r;
+        r.x = a.x * b.x - a.y * b.y;
+        r.y = a.x * b.y + a.y * b.x;
+        return r;
+    }
 }
 // a * conj(b)
 template <typename T2>
 __device__ __forceinline__ T2 cmulc(T2 a, T2 b) {
-    T2 r;
-    r.x = a.x * b.x + a.y * b.y;
-    r.y = a.y * b.x - a.x * b.y;
-    return r;
+    if constexpr (std::is_same<T2, ddc>::value) {
+        return dd_cmulc(a, b);
+    } else {
+        T2 r;
+        r.x = a.x * b.x + a.y * b.y;
+        r.y = a.y * b.x - a.x * b.y;
+        return r;
+    }
 }
 // multiply by -i (forward) or +i (inverse)
 template <bool INV, typename T2>
 __device__ __forceinline__ T2 rot(T2 d) {
-    T2 r;
-    if (INV) {
-        r.x = -d.y;
-        r.y = d.x;
+    if constexpr (std::is_same<T2, ddc>::value) {
+        return INV ? ddc{make_float2(-d.h.y, d.h.x), make_float2(-d.l.y, d.l.x)}
+                   : ddc{make_float2(d.h.y, -d.h.x), make_float2(d.l.y, -d.l.x)};
     } else {
-        r.x = d.y;
-        r.y = -d.x;
+        T2 r;
+        if (INV) {
+            r.x = -d.y;
+            r.y = d.x;
+        } else {
+            r.x = d.y;
+            r.y = -d.x;
+        }
+        return r;
     }
-    return r;
 }
 
 // Twiddles of the in-register butterflies: cos/sin(2 pi k / 16), k < 8.
@@ -98,13 +116,21 @@ __device__ __forceinline__ T2 twc(T2 v) {
     constexpr int k16 = K * (16 / R);  // same angle on the 16-point circle
     if (k16 == 0) return v;
     if (k16 == 4) return rot<INV>(v);  // -+i
-    using T = decltype(v.x);
     constexpr double cd = c16(k16), sd = s16(k16);
-    const T c = (T)cd, s = INV ? (T)sd : -(T)sd;
-    T2 r;
-    r.x = v.x * c - v.y * s;
-    r.y = v.x * s + v.y * c;
-    return r;
+    if constexpr (std::is_same<T2, ddc>::value) {
+        // the constant (c, s) as double-FP32
+        constexpr double sdd = INV ? sd : -sd;
+        constexpr float ch = (float)cd, sh = (float)sdd;
+        constexpr float cl = (float)(cd - (double)ch), sl = (float)(sdd - (double)sh);
+        return dd_cmul(v, ddc{make_float2(ch, sh), make_float2(cl, sl)});
+    } else {
+        using T = decltype(v.x);
+        const T c = (T)cd, s = INV ? (T)sd : -(T)sd;
+        T2 r;
+        r.x = v.x * c - v.y * s;
+        r.y = v.x * s + v.y * c;
+        return r;
+    }
 }
 
 template <bool INV, typename T2>

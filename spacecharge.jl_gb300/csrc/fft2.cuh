@@ -59,7 +59,12 @@ __device__ __forceinline__ void stage_twiddles(T2* sw, const T2* __restrict__ tw
     // ahead of the wait for the preceding grid (programmatic launch).  Every
     // two-step kernel starts here, so the wait below orders all of its other
     // global-memory accesses after the grids it follows.
-    for (int j = threadIdx.x; j < L; j += blockDim.x) sw[j] = __ldg(tw + j * (kMaxL / L));
+    for (int j = threadIdx.x; j < L; j += blockDim.x) {
+        if constexpr (std::is_same<T2, ddc>::value)
+            sw[j] = tw[j * (kMaxL / L)];
+        else
+            sw[j] = __ldg(tw + j * (kMaxL / L));
+    }
     pdl_wait();
     __syncthreads();
 }

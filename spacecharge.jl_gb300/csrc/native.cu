@@ -1199,6 +1199,12 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
             SC_LAUNCH_CHECK("k2_zpass");
             goto zdone;
         }
+        // FP64 in free space, on request: the z pass in double-FP32
+        if (std::is_same<T, double>::value && m->df32_transforms && eng == 0 &&
+            launch2_dd_zpass(w.log2L[2], (const double2*)B, (double2*)C, Hx, Ly, nz, gv, (const ddc*)ctx->twdd, s)) {
+            SC_LAUNCH_CHECK("k2_dd_zpass");
+            goto zdone;
+        }
         {
         int lgW = w.lgW >= 0 ? w.lgW : pick_cols(w.log2L[2]);
         while (lgW > 0 && sizeof(T2) * 3 * ((size_t)1 << lgW) * Lz > 200 * 1024) --lgW;  // shared-memory cap

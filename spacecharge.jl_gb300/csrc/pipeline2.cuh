@@ -9,10 +9,9 @@
 
 #include "fft2.cuh"
 #include "pipeline.cuh"
+#include "zstage.cuh"
 
 namespace sc {
-
-constexpr int kColW = 16;  // columns per CTA of the column passes
 
 // CTAs per SM the register allocation of the z passes and the column passes
 // is sized for (the z pass's two shared buffers, 70 KB at L = 256, allow 3)
@@ -470,49 +469,6 @@ __global__ void __launch_bounds__(256) k2_inv_x(const float2* __restrict__ D, fl
             if (r1 < rows) o1[E::R2 * s] = make_float4(ex.y, ey.y, ez.y, 0.f);
         }
     }
-}
-
-// Asynchronous 4-byte global -> shared copies (cp.async, sm_80+), waited
-// for with cp_async_wait_all before a barrier.
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
-// Copies this CTA's free-space Green values, gsm[comp][kzf][column] for
-// kzf <= L/2 and the tile's kColW columns (kx, ky folded to ky <= Ly/2), to
-// shared memory asynchronously; cp_async_wait_all + a barrier before use.
-// blockDim.x is a multiple of kColW, so each thread keeps one column.
-template <int L>
-__device__ __forceinline__ void prefetch_green(float* gsm, const GreenView& gv, int Hx, int Ly, int tile) {
-    constexpr int HZ = L / 2 + 1;
-    const int64_t plane = (int64_t)Hx * Ly;
-    const int64_t gstep = (int64_t)gv.Hx * gv.Hy;
-    const int cc = threadIdx.x % kColW;
-    const int ff = tile * kColW + cc;
-    if (ff < plane) {
-        const int kyy = ff / Hx, kxx = ff - kyy * Hx;
-        const int kyf = kyy <= Ly / 2 ? kyy : Ly - kyy;
-        const float* src = reinterpret_cast<const float*>(gv.gfree) + kxx + (int64_t)gv.Hx * kyf;
-        const int k0 = threadIdx.x / kColW, kstep = blockDim.x / kColW;
-#pragma unroll
-        for (int comp = 0; comp < 3; ++comp) {
-            const float* sc = src + comp * gv.cs_free + gstep * k0;
-            float* dc = gsm + (comp * HZ + k0) * kColW + cc;
-            for (int kzf = k0; kzf < HZ; kzf += kstep, sc += gstep * kstep, dc += kColW * kstep) cp_async4(dc, sc);
-        }
-    }
-    cp_async_commit();
 }
 
 // Copies one component's half-stored image spectrum for this CTA's kColW
@@ -1613,17 +1569,6 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, sizeof(Tr) == 4 ? 3 : 1) k4
 
 // Launch helpers: run the two-step kernel when L <= 256, report false
 // otherwise (the caller falls back to the Stockham kernels).
-#define SC_L_SWITCH(logL, MACRO) \
-    switch (logL) {              \
-        case 2: MACRO(4); break; \
-        case 3: MACRO(8); break; \
-        case 4: MACRO(16); break; \
-        case 5: MACRO(32); break; \
-        case 6: MACRO(64); break; \
-        case 7: MACRO(128); break; \
-        case 8: MACRO(256); break; \
-        default: return false;   \
-    }
 
 static bool launch2_col(bool inv, int logL, const float2* in, float2* out, int ncols, int n_valid, int n_store,
                         int64_t as_in, int64_t bs_in, int64_t cs_in, int64_t as_out, int64_t bs_out, int64_t cs_out,
@@ -1741,6 +1686,11 @@ static bool launch2_zpass(int logL, const float2* B, float2* C, int Hx, int Ly, 
 #undef SC_K2Z
     return true;
 }
+
+// FP64 free-space z pass in double-FP32 (zpass_dd.cu); false where it does
+// not apply (the image, transforms above 256 points)
+bool launch2_dd_zpass(int logL, const double2* B, double2* C, int Hx, int Ly, int nz, const GreenView& gv,
+                      const ddc* tw, cudaStream_t s);
 
 static bool launch2_adj_zpass(int logL, const float2* C, float2* B, int Hx, int Ly, int nz, const GreenView& gv,
                               const float2* tw, cudaStream_t s) {

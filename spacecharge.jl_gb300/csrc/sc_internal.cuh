@@ -116,6 +116,7 @@ struct DeviceCtx {
     int device = -1;
     float2* tw32 = nullptr;   // exp(-2 pi i k / kMaxL), k < kMaxL, FP32
     double2* tw64 = nullptr;  // the same in FP64
+    void* twdd = nullptr;     // the same as double-FP32 pairs (ddc, dd.cuh): {hi re, hi im}, {lo re, lo im}
     double* partials = nullptr;  // bounds reduction partials
     int partial_blocks = 0;
     double* ext_host = nullptr;  // the reduction's 6 extrema: page-locked, mapped,
@@ -229,6 +230,7 @@ struct sc_mesh {
     int precision;
     int device;
     bool green_cache = true;
+    bool df32_transforms = false;  // FP64 meshes: the z pass in double-FP32
     void* rho = nullptr;     // T[N]
     void* efield = nullptr;  // planar T[3N] or packed T[4N]
     unsigned long long* oob = nullptr;  // device counter of skipped particles

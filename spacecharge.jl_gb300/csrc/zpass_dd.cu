@@ -1,0 +1,115 @@
+// FP64 meshes: the free-space z pass in double-FP32 (dd.cuh), a
+// translation unit of its own so that it compiles beside the others.
+#include "fft2.cuh"
+#include "pipeline.cuh"
+#include "zstage.cuh"
+
+namespace sc {
+
+// z pass of an FP64 mesh in free space, in double-FP32 (dd.cuh): the FP64
+// spectrum rho^(kx, ky, .) is split into FP32 pairs with integer operations,
+// transformed forward, multiplied by i g for the three FP64 Green spectra
+// (split the same way), transformed back and widened to FP64.  The FP64
+// pipe sees only the two additions per complex value of the widening.
+// Same column tiles, thread layout and compile-time z patterns as the FP32
+// zpass_body of pipeline2.cuh (free-space branch); the Green values are copied to shared
+// memory asynchronously during the forward transform.
+template <int L, bool HALF>
+__global__ void __launch_bounds__(kColW * F2<L>::NT, 1) k2_dd_zpass(const double2* __restrict__ B,
+                                                                   double2* __restrict__ C, int Hx, int Ly, int nz,
+                                                                   GreenView gv, const ddc* __restrict__ tw) {
+    using E = F2<L>;
+    constexpr int RL = E::R1;
+    constexpr int HZ = L / 2 + 1;
+    __shared__ ddc swt[L];
+    stage_twiddles<L>(swt, tw);
+    extern __shared__ __align__(16) unsigned char smraw[];
+    ddc* xb = reinterpret_cast<ddc*>(smraw);
+    ddc* spec = xb + kColW * E::S;
+    double* gsm = reinterpret_cast<double*>(spec + kColW * E::S);  // [3][HZ][kColW]
+    const int tile = blockIdx.x;
+    const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
+    const int64_t plane = (int64_t)Hx * Ly;
+    prefetch_green<L, double>(gsm, gv, Hx, Ly, tile);
+    const int f = tile * kColW + c;
+    const bool cok = f < plane;
+    const int fl = cok ? f : (int)plane - 1;
+    const int ky = fl / Hx;
+    ddc* col = xb + c * E::S;
+    ddc* sc = spec + c * E::S;
+    ddc v[16];
+    if (t < E::R2) {
+        const double2* Bc = B + fl;
+        const ddc zero{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+        for (int s = 0; s < E::R1; ++s) {
+            const int z = t + E::R2 * s;
+            const bool in = HALF ? E::R2 * s < L / 2 : z < nz;
+            v[s] = in ? dd_from(Bc[plane * z]) : zero;
+        }
+    }
+    E::template fwd<false>(v, col, t, swt);
+    // this thread's spectrum values, kept for the three components (read
+    // back by the same thread only)
+    if (t < E::R1) {
+#pragma unroll
+        for (int r = 0; r < E::R2; ++r) sc[t + xoff(E::R1 * r)] = v[r];
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const float ysign = ky <= Ly / 2 ? 1.f : -1.f;
+    for (int comp = 0; comp < 3; ++comp) {
+        if (t < E::R1) {
+            // signs as in zpass_body: component 1 odd along y, component 2
+            // odd along z (kz > L/2)
+            const float sy = comp == 1 ? ysign : 1.f;
+            const float su = comp == 2 ? -sy : sy;
+            const float sm = t > 0 ? su : sy;  // kz = L/2 + t
+            const double* gfc = gsm + comp * HZ * kColW + c;
+            const double* glo = gfc + t * kColW;
+            const double* ghi = gfc + (L - t) * kColW;
+            const ddc* sct = sc + t;
+#pragma unroll
+            for (int r = 0; r < E::R2; ++r) {
+                const double gd = RL * r < L / 2 ? glo[RL * r * kColW] : ghi[-RL * r * kColW];
+                const float sg = RL * r < L / 2 ? sy : RL * r == L / 2 ? sm : su;
+                float gh, gl;
+                dd_split(gd, gh, gl);
+                v[r] = rot<true>(dd_scale(sct[xoff(RL * r)], gh * sg, gl * sg));  // X * (i g)
+            }
+        }
+        E::template inv<true>(v, col, t, swt);
+        if (t < E::R2 && cok) {
+            double2* Cc = C + comp * (plane * nz) + f;
+#pragma unroll
+            for (int s = 0; s < E::R1; ++s) {
+                const int z = t + E::R2 * s;
+                if (HALF ? E::R2 * s < L / 2 : z < nz) Cc[plane * z] = dd_to(v[s]);
+            }
+        }
+    }
+}
+
+
+bool launch2_dd_zpass(int logL, const double2* B, double2* C, int Hx, int Ly, int nz, const GreenView& gv,
+                      const ddc* tw, cudaStream_t s) {
+    if (gv.image || logL > 8) return false;
+#define SC_KDZ(LL)                                                                          \
+    {                                                                                       \
+        const size_t smem = sizeof(ddc) * kColW * F2<LL>::S * 2 + sizeof(double) * 3 * (LL / 2 + 1) * kColW; \
+        const int64_t ncol = (int64_t)Hx * Ly;                                              \
+        const unsigned grid = (unsigned)((ncol + kColW - 1) / kColW);                       \
+        if (2 * nz == LL) {                                                                 \
+            if (set_smem(k2_dd_zpass<LL, true>, smem) != SC_OK) return false;               \
+            launch_pdl(k2_dd_zpass<LL, true>, grid, kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz, gv, tw); \
+        } else {                                                                            \
+            if (set_smem(k2_dd_zpass<LL, false>, smem) != SC_OK) return false;              \
+            launch_pdl(k2_dd_zpass<LL, false>, grid, kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz, gv, tw); \
+        }                                                                                   \
+    }
+    SC_L_SWITCH(logL, SC_KDZ)
+#undef SC_KDZ
+    return true;
+}
+
+}  // namespace sc

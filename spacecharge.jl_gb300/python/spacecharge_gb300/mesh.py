@@ -220,6 +220,15 @@ class Mesh3D:
     def set_green_cache(self, enabled: bool) -> None:
         L.call("sc_mesh_set_green_cache", self._h.ptr, 1 if enabled else 0)
 
+    def set_fp64_transforms(self, mode: str) -> None:
+        """precision="fp64" meshes: "fp64" (default) runs the free-space z
+        pass in FP64; "df32" in double-FP32 (48-bit significands, about
+        1e-14 of the field's maximum)."""
+        modes = {"fp64": L.SC_FP64_TRANSFORMS_FP64, "df32": L.SC_FP64_TRANSFORMS_DF32}
+        if mode not in modes:
+            raise ValueError(f"unknown FP64 transform mode {mode!r}")
+        L.call("sc_mesh_set_fp64_transforms", self._h.ptr, modes[mode])
+
     def out_of_range(self) -> int:
         """Particles skipped as outside the mesh since the last query."""
         n = C.c_int64()

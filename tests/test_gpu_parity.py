@@ -394,3 +394,45 @@ def test_fft_engines_agree(sc, cuda, grid, cath, first):
     finally:
         L.call("sc_set_fft_engine", L.SC_FFT_AUTO)
     assert relerr(out[L.SC_FFT_AUTO], out[L.SC_FFT_STOCKHAM]) < 2e-6
+
+
+@pytest.mark.parametrize("grid", [(64, 64, 128), (32, 32, 64), (12, 20, 33), (3, 5, 9), (8, 8, 128)])
+def test_fp64_df32_zpass(sc, cuda, grid):
+    """FP64 meshes in free space: the double-FP32 z pass against the FP64 z
+    pass on the same deposit, and against the oracle at the FP64 tolerance.
+    Double-FP32 carries 48-bit significands, so the fields agree to ~1e-14 of
+    their maximum; 1e-12 is asserted.  nz = L/2 (64x64x128, 32x32x64,
+    8x8x128) and nz < L/2 (12x20x33, 3x5x9) take the two compile-time z
+    patterns."""
+    n = 50_000
+    x, y, z = bunch(n, 17, sig=(1e-3, 1e-3, 0.3e-3))
+    q = np.full(n, 1e-9 / n)
+    m = sc.Mesh3D(grid, x, y, z, precision="fp64", gamma=4.0)
+    out = {}
+    for mode in ("fp64", "df32"):
+        m.set_fp64_transforms(mode)
+        sc.deposit(m, x, y, z, q, mode="deterministic")
+        sc.solve(m)
+        out[mode] = host(m.efield)
+    assert relerr(out["df32"], out["fp64"]) < 1e-12
+    om = O.mesh_auto(grid, x, y, z, gamma=4.0)
+    O.deposit(om, x, y, z, q)
+    O.solve(om)
+    assert relerr(out["df32"], om.efield) < TOL["fp64"]
+    m.set_fp64_transforms("fp64")
+    sc.solve(m)
+    assert np.array_equal(host(m.efield), out["fp64"])
+
+
+def test_fp64_transforms_mode_checks(sc, cuda):
+    """The double-FP32 switch exists for FP64 meshes only, with two modes."""
+    from spacecharge_gb300 import _lib as L
+
+    m = sc.Mesh3D((8, 8, 8), (-1e-3,) * 3, (1e-3,) * 3, precision="mixed")
+    with pytest.raises(Exception):
+        m.set_fp64_transforms("df32")
+    m64 = sc.Mesh3D((8, 8, 8), (-1e-3,) * 3, (1e-3,) * 3, precision="fp64")
+    with pytest.raises(ValueError):
+        m64.set_fp64_transforms("fp32")
+    with pytest.raises(Exception):
+        L.call("sc_mesh_set_fp64_transforms", m64._h.ptr, 7)
