@@ -159,15 +159,16 @@ int sc_mesh_efield(sc_mesh* mesh, void** dptr);
  * The reference rebuilds it on every solve! (free_space.jl:77-96). */
 int sc_mesh_set_green_cache(sc_mesh* mesh, int enabled);
 
-/* Arithmetic of the free-space z pass of an SC_PREC_FP64 mesh (no
+/* Arithmetic of the field solve's transforms on an SC_PREC_FP64 mesh (no
  * counterpart in the reference).  SC_FP64_TRANSFORMS_FP64 (default): FP64
- * throughout.  SC_FP64_TRANSFORMS_DF32: the forward z transform, the Green
- * products and the three inverse z transforms carry each value as the
- * unevaluated sum of two FP32 numbers (48-bit significands, FP32's exponent
- * range), with FP64 inputs and outputs; the field moves by about 1e-14 of its
- * maximum.  The GB300 runs FP64 at 1/64 of its FP32 rate, so this takes the
- * largest FP64 pass off the FP64 units.  Transforms above 256 points and the
- * cathode image stay FP64.  Other precisions: SC_ERR_INVALID. */
+ * throughout.  SC_FP64_TRANSFORMS_DF32: the z pass (forward z transform,
+ * Green products, three inverse z transforms; free space) and the inverse y
+ * and x passes carry each value as the unevaluated sum of two FP32 numbers
+ * (48-bit significands, FP32's exponent range), with FP64 inputs and
+ * outputs; the field moves by about 1e-15 of its maximum.  The GB300 runs
+ * FP64 at 1/64 of its FP32 rate, so this takes those passes off the FP64
+ * units.  Meshes with a transform above 256 points, and the z pass with the
+ * cathode image, stay FP64.  Other precisions: SC_ERR_INVALID. */
 #define SC_FP64_TRANSFORMS_FP64 0
 #define SC_FP64_TRANSFORMS_DF32 1
 int sc_mesh_set_fp64_transforms(sc_mesh* mesh, int mode);

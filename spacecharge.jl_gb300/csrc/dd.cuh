@@ -117,4 +117,12 @@ __device__ __forceinline__ double2 dd_to(ddc v) {
     return make_double2(f32_to_f64(v.h.x) + f32_to_f64(v.l.x), f32_to_f64(v.h.y) + f32_to_f64(v.l.y));
 }
 
+
+// loads and stores of a buffer between passes that holds FP64 (double2) or
+// double-FP32 (ddc) values
+__device__ __forceinline__ ddc dd_load(const double2* p) { return dd_from(*p); }
+__device__ __forceinline__ ddc dd_load(const ddc* p) { return *p; }
+__device__ __forceinline__ void dd_store(double2* p, ddc v) { *p = dd_to(v); }
+__device__ __forceinline__ void dd_store(ddc* p, ddc v) { *p = v; }
+
 }  // namespace sc

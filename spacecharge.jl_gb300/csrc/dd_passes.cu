@@ -1,23 +1,31 @@
-// FP64 meshes: the free-space z pass in double-FP32 (dd.cuh), a
-// translation unit of its own so that it compiles beside the others.
+// FP64 meshes: the free-space z pass in double-FP32 (dd.cuh), one of the
+// double-FP32 passes of the FP64 pipeline:
+//   k2_dd_zpass    forward z, Green products, three inverse z (free space)
+//   k2_dd_col_inv  inverse y of the three components (dd_inverse.cu)
+//   k2_dd_inv_x    inverse x, two rows per complex transform, packed nodes
+//                  (dd_inverse.cu)
+// Between the passes the spectra stay in double-FP32 (a ddc is 16 bytes, as
+// a double2, so the FP64 pipeline's buffers hold them); FP64 values enter
+// through an integer split and leave through one FP64 addition per part.
+// Translation units of their own, so that they compile beside the others.
 #include "fft2.cuh"
 #include "pipeline.cuh"
 #include "zstage.cuh"
 
 namespace sc {
 
-// z pass of an FP64 mesh in free space, in double-FP32 (dd.cuh): the FP64
-// spectrum rho^(kx, ky, .) is split into FP32 pairs with integer operations,
-// transformed forward, multiplied by i g for the three FP64 Green spectra
-// (split the same way), transformed back and widened to FP64.  The FP64
-// pipe sees only the two additions per complex value of the widening.
-// Same column tiles, thread layout and compile-time z patterns as the FP32
-// zpass_body of pipeline2.cuh (free-space branch); the Green values are copied to shared
-// memory asynchronously during the forward transform.
+// z pass of an FP64 mesh in free space: the FP64 spectrum rho^(kx, ky, .)
+// is split into FP32 pairs with integer operations, transformed forward,
+// multiplied by i g for the three FP64 Green spectra (split the same way)
+// and transformed back, the result kept in double-FP32 for the inverse
+// passes.  Same column tiles, thread layout and
+// compile-time z patterns as the FP32 zpass_body of pipeline2.cuh
+// (free-space branch); the Green values are copied to shared memory
+// asynchronously during the forward transform.
 template <int L, bool HALF>
-__global__ void __launch_bounds__(kColW * F2<L>::NT, 1) k2_dd_zpass(const double2* __restrict__ B,
-                                                                   double2* __restrict__ C, int Hx, int Ly, int nz,
-                                                                   GreenView gv, const ddc* __restrict__ tw) {
+__global__ void __launch_bounds__(kColW * F2<L>::NT, 1) k2_dd_zpass(const double2* __restrict__ B, ddc* __restrict__ C,
+                                                                   int Hx, int Ly, int nz, GreenView gv,
+                                                                   const ddc* __restrict__ tw) {
     using E = F2<L>;
     constexpr int RL = E::R1;
     constexpr int HZ = L / 2 + 1;
@@ -80,32 +88,31 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, 1) k2_dd_zpass(const double
         }
         E::template inv<true>(v, col, t, swt);
         if (t < E::R2 && cok) {
-            double2* Cc = C + comp * (plane * nz) + f;
+            ddc* Cc = C + comp * (plane * nz) + f;
 #pragma unroll
             for (int s = 0; s < E::R1; ++s) {
                 const int z = t + E::R2 * s;
-                if (HALF ? E::R2 * s < L / 2 : z < nz) Cc[plane * z] = dd_to(v[s]);
+                if (HALF ? E::R2 * s < L / 2 : z < nz) Cc[plane * z] = v[s];
             }
         }
     }
 }
 
-
-bool launch2_dd_zpass(int logL, const double2* B, double2* C, int Hx, int Ly, int nz, const GreenView& gv,
-                      const ddc* tw, cudaStream_t s) {
+bool launch2_dd_zpass(int logL, const double2* B, ddc* C, int Hx, int Ly, int nz, const GreenView& gv, const ddc* tw,
+                      cudaStream_t s) {
     if (gv.image || logL > 8) return false;
-#define SC_KDZ(LL)                                                                          \
-    {                                                                                       \
+#define SC_KDZ(LL)                                                                                          \
+    {                                                                                                       \
         const size_t smem = sizeof(ddc) * kColW * F2<LL>::S * 2 + sizeof(double) * 3 * (LL / 2 + 1) * kColW; \
-        const int64_t ncol = (int64_t)Hx * Ly;                                              \
-        const unsigned grid = (unsigned)((ncol + kColW - 1) / kColW);                       \
-        if (2 * nz == LL) {                                                                 \
-            if (set_smem(k2_dd_zpass<LL, true>, smem) != SC_OK) return false;               \
+        const int64_t ncol = (int64_t)Hx * Ly;                                                              \
+        const unsigned grid = (unsigned)((ncol + kColW - 1) / kColW);                                       \
+        if (2 * nz == LL) {                                                                                 \
+            if (set_smem(k2_dd_zpass<LL, true>, smem) != SC_OK) return false;                               \
             launch_pdl(k2_dd_zpass<LL, true>, grid, kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz, gv, tw); \
-        } else {                                                                            \
-            if (set_smem(k2_dd_zpass<LL, false>, smem) != SC_OK) return false;              \
+        } else {                                                                                            \
+            if (set_smem(k2_dd_zpass<LL, false>, smem) != SC_OK) return false;                              \
             launch_pdl(k2_dd_zpass<LL, false>, grid, kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz, gv, tw); \
-        }                                                                                   \
+        }                                                                                                   \
     }
     SC_L_SWITCH(logL, SC_KDZ)
 #undef SC_KDZ

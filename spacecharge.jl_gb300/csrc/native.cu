@@ -1190,6 +1190,13 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
                                      0, nz, 1, tw, s, lgWy));
         SC_LAUNCH_CHECK("fwd_y");
     }
+    // FP64 meshes with double-FP32 transforms: the inverse y and x passes in
+    // double-FP32 where both lengths fit the register kernels (D then holds
+    // double-FP32 values); c_dd: the z pass left C in double-FP32 too
+    const bool dd = std::is_same<T, double>::value && m->df32_transforms && eng == 0 && w.log2L[0] <= 8 &&
+                    w.log2L[1] <= 8;
+    const ddc* twdd = (const ddc*)ctx->twdd;
+    bool c_dd = false;
     // z + Green + inverse z
     {
         if (green_ready) SC_CUDA(cudaStreamWaitEvent(s, green_ready, 0));
@@ -1199,9 +1206,10 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
             SC_LAUNCH_CHECK("k2_zpass");
             goto zdone;
         }
-        // FP64 in free space, on request: the z pass in double-FP32
-        if (std::is_same<T, double>::value && m->df32_transforms && eng == 0 &&
-            launch2_dd_zpass(w.log2L[2], (const double2*)B, (double2*)C, Hx, Ly, nz, gv, (const ddc*)ctx->twdd, s)) {
+        // FP64 in free space, on request: the z pass in double-FP32, its
+        // output kept in double-FP32 for the inverse passes
+        if (dd && launch2_dd_zpass(w.log2L[2], (const double2*)B, (ddc*)C, Hx, Ly, nz, gv, twdd, s)) {
+            c_dd = true;
             SC_LAUNCH_CHECK("k2_dd_zpass");
             goto zdone;
         }
@@ -1227,7 +1235,16 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
             m->launches -= 1;  // one launch for the two passes
             return SC_OK;
         }
-        if (!(two && launch2_col(true, w.log2L[1], (const float2*)C, (float2*)D, Hx, Ly, ny, Hx, (int64_t)Hx * Ly,
+        if (dd) {
+            const bool ok = c_dd ? launch2_dd_col_inv(w.log2L[1], (const ddc*)C, (ddc*)D, Hx, nz, ny, Hx,
+                                                      (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, Hx, (int64_t)Hx * ny,
+                                                      (int64_t)Hx * ny * nz, twdd, s)
+                                 : launch2_dd_col_inv(w.log2L[1], (const double2*)C, (ddc*)D, Hx, nz, ny, Hx,
+                                                      (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, Hx, (int64_t)Hx * ny,
+                                                      (int64_t)Hx * ny * nz, twdd, s);
+            if (!ok) return fail(SC_ERR_CUDA, "double-FP32 inverse y pass did not launch");
+            SC_LAUNCH_CHECK("k2_dd_col_inv");
+        } else if (!(two && launch2_col(true, w.log2L[1], (const float2*)C, (float2*)D, Hx, Ly, ny, Hx, (int64_t)Hx * Ly,
                                  (int64_t)Hx * Ly * nz, Hx, (int64_t)Hx * ny, (int64_t)Hx * ny * nz, nz, 3,
                                  (const float2*)tw, s)))
             SC_TRY(run_col<true, T>(C, D, Hx, Ly, w.log2L[1], Ly, ny, Hx, (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, Hx,
@@ -1240,6 +1257,13 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
         if (two && launch2_inv_x(w.log2L[0], (const float2*)D, (float4*)m->efield, nx, rows, Hx, (int64_t)Hx * rows,
                                  (const float2*)tw, s)) {
             SC_LAUNCH_CHECK("k2_inv_x");
+            return SC_OK;
+        }
+        if (dd) {
+            if (!launch2_dd_inv_x(w.log2L[0], (const ddc*)D, (dnode4*)m->efield, nx, rows, Hx, (int64_t)Hx * rows, twdd,
+                                  s))
+                return fail(SC_ERR_CUDA, "double-FP32 inverse x pass did not launch");
+            SC_LAUNCH_CHECK("k2_dd_inv_x");
             return SC_OK;
         }
         const int lgP = pick_rows(w.log2L[0]);

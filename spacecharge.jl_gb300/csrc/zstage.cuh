@@ -1,6 +1,6 @@
 // Column tiles of the z passes and their asynchronous shared-memory
 // staging, shared by the FP32 kernels of pipeline2.cuh and the FP64
-// double-FP32 z pass (zpass_dd.cu).
+// double-FP32 z pass (dd_passes.cu).
 #pragma once
 
 #include "pipeline.cuh"

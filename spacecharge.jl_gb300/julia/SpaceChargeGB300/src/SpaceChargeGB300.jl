@@ -190,9 +190,10 @@ set_kick_mode!(mesh::Mesh3D, mode::Symbol) =
 """
     set_fp64_transforms!(mesh, mode::Symbol)
 
-`Float64` meshes: `:fp64` (the default) runs the free-space z pass in FP64,
-`:df32` in double-FP32 (pairs of `Float32`, 48-bit significands, about 1e-14
-of the field's maximum), off the GPU's FP64 units.
+`Float64` meshes: `:fp64` (the default) runs the field solve's transforms in
+FP64; `:df32` runs the free-space z pass and the inverse y and x passes in
+double-FP32 (pairs of `Float32`, 48-bit significands, about 1e-15 of the
+field's maximum), off the GPU's FP64 units.
 """
 set_fp64_transforms!(mesh::Mesh3D, mode::Symbol) =
     check(ccall((:sc_mesh_set_fp64_transforms, libsc), Cint, (Ptr{Cvoid}, Cint), mesh.ptr,

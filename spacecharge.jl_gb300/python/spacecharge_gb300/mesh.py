@@ -221,9 +221,10 @@ class Mesh3D:
         L.call("sc_mesh_set_green_cache", self._h.ptr, 1 if enabled else 0)
 
     def set_fp64_transforms(self, mode: str) -> None:
-        """precision="fp64" meshes: "fp64" (default) runs the free-space z
-        pass in FP64; "df32" in double-FP32 (48-bit significands, about
-        1e-14 of the field's maximum)."""
+        """precision="fp64" meshes: "fp64" (default) runs the field solve's
+        transforms in FP64; "df32" runs the free-space z pass and the inverse
+        y and x passes in double-FP32 (48-bit significands, about 1e-15 of the
+        field's maximum)."""
         modes = {"fp64": L.SC_FP64_TRANSFORMS_FP64, "df32": L.SC_FP64_TRANSFORMS_DF32}
         if mode not in modes:
             raise ValueError(f"unknown FP64 transform mode {mode!r}")

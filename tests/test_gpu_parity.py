@@ -396,31 +396,37 @@ def test_fft_engines_agree(sc, cuda, grid, cath, first):
     assert relerr(out[L.SC_FFT_AUTO], out[L.SC_FFT_STOCKHAM]) < 2e-6
 
 
-@pytest.mark.parametrize("grid", [(64, 64, 128), (32, 32, 64), (12, 20, 33), (3, 5, 9), (8, 8, 128)])
-def test_fp64_df32_zpass(sc, cuda, grid):
-    """FP64 meshes in free space: the double-FP32 z pass against the FP64 z
-    pass on the same deposit, and against the oracle at the FP64 tolerance.
-    Double-FP32 carries 48-bit significands, so the fields agree to ~1e-14 of
-    their maximum; 1e-12 is asserted.  nz = L/2 (64x64x128, 32x32x64,
-    8x8x128) and nz < L/2 (12x20x33, 3x5x9) take the two compile-time z
-    patterns."""
+@pytest.mark.parametrize("grid,cath", [((64, 64, 128), False), ((32, 32, 64), False), ((12, 20, 33), False),
+                                       ((3, 5, 9), False), ((8, 8, 128), False), ((12, 12, 16), True),
+                                       ((24, 12, 33), True)])
+def test_fp64_df32_transforms(sc, cuda, grid, cath):
+    """FP64 meshes with the double-FP32 transforms (the z pass in free space,
+    the inverse y and x passes) against the FP64 transforms on the same
+    deposit, and against the oracle at the FP64 tolerance.  Double-FP32
+    carries 48-bit significands, so the fields agree to ~1e-15 of their
+    maximum; 1e-12 is asserted.  nz = L/2 (64x64x128, 32x32x64, 8x8x128) and
+    nz < L/2 (12x20x33, 3x5x9) take the two compile-time z patterns; with the
+    cathode image the z pass stays FP64 and the inverse y pass reads its FP64
+    output."""
     n = 50_000
     x, y, z = bunch(n, 17, sig=(1e-3, 1e-3, 0.3e-3))
+    if cath:
+        z = np.abs(z) + 0.1e-3
     q = np.full(n, 1e-9 / n)
     m = sc.Mesh3D(grid, x, y, z, precision="fp64", gamma=4.0)
     out = {}
     for mode in ("fp64", "df32"):
         m.set_fp64_transforms(mode)
         sc.deposit(m, x, y, z, q, mode="deterministic")
-        sc.solve(m)
+        sc.solve(m, at_cathode=cath)
         out[mode] = host(m.efield)
     assert relerr(out["df32"], out["fp64"]) < 1e-12
     om = O.mesh_auto(grid, x, y, z, gamma=4.0)
     O.deposit(om, x, y, z, q)
-    O.solve(om)
+    O.solve(om, at_cathode=cath)
     assert relerr(out["df32"], om.efield) < TOL["fp64"]
     m.set_fp64_transforms("fp64")
-    sc.solve(m)
+    sc.solve(m, at_cathode=cath)
     assert np.array_equal(host(m.efield), out["fp64"])
 
 
