@@ -159,23 +159,25 @@ int sc_mesh_efield(sc_mesh* mesh, void** dptr);
  * The reference rebuilds it on every solve! (free_space.jl:77-96). */
 int sc_mesh_set_green_cache(sc_mesh* mesh, int enabled);
 
-/* Arithmetic of the field solve's transforms on an SC_PREC_FP64 mesh (no
- * counterpart in the reference).  SC_FP64_TRANSFORMS_FP64 (default): FP64
- * throughout.  SC_FP64_TRANSFORMS_DF32: the z pass (forward z transform,
- * Green products, three inverse z transforms; free space) and the inverse y
- * and x passes carry each value as the unevaluated sum of two FP32 numbers
- * (48-bit significands, FP32's exponent range), with FP64 inputs and
- * outputs; the field moves by about 1e-15 of its maximum.  The GB300 runs
+/* Arithmetic of an SC_PREC_FP64 mesh's kick (no counterpart in the
+ * reference).  SC_FP64_ARITH_FP64 (default): FP64 throughout.
+ * SC_FP64_ARITH_DF32: the atomic deposit's weights, the x and y transform
+ * passes, the z pass (forward z transform, Green products, three inverse z
+ * transforms; free space) and the trilinear interpolation carry each value
+ * as the unevaluated sum of two FP32 numbers (48-bit significands, FP32's
+ * exponent range, magnitudes from 2^-103 to 2^128), with FP64 inputs and
+ * outputs; fields move by about 1e-14 of their maximum.  The GB300 runs
  * FP64 at 1/64 of its FP32 rate, so this takes those passes off the FP64
- * units.  Meshes with a transform above 256 points, and the z pass with the
- * cathode image, stay FP64.  Other precisions: SC_ERR_INVALID. */
-#define SC_FP64_TRANSFORMS_FP64 0
-#define SC_FP64_TRANSFORMS_DF32 1
-int sc_mesh_set_fp64_transforms(sc_mesh* mesh, int mode);
+ * units.  The Green function stays FP64; meshes with a transform above 256
+ * points keep FP64 transforms, and the z pass with the cathode image stays
+ * FP64.  Other precisions: SC_ERR_INVALID. */
+#define SC_FP64_ARITH_FP64 0
+#define SC_FP64_ARITH_DF32 1
+int sc_mesh_set_fp64_arithmetic(sc_mesh* mesh, int mode);
 
 /* FFT kernels of the hand-written pipelines (process-wide).  SC_FFT_AUTO
  * (default): register-resident two-step transforms for FP32 lengths up to
- * 256 (and for the double-FP32 z pass, sc_mesh_set_fp64_transforms),
+ * 256 (and for the double-FP32 z pass, sc_mesh_set_fp64_arithmetic),
  * shared-memory Stockham transforms otherwise; SC_FFT_STOCKHAM: the Stockham
  * transforms everywhere.  Both give the same result to rounding. */
 #define SC_FFT_AUTO     0

@@ -326,7 +326,7 @@ struct KickGraph {
 
 void mesh_state_key(const sc_mesh* m, std::vector<int64_t>& k, bool with_epoch) {
     k.push_back(m->green_cache);
-    k.push_back(m->df32_transforms);
+    k.push_back(m->df32);
     k.push_back(m->kick_mode);
     k.push_back(fft_engine());
     k.push_back(m->nw.engine);
@@ -800,12 +800,12 @@ int sc_mesh_set_green_cache(sc_mesh* m, int enabled) {
     return SC_OK;
 }
 
-int sc_mesh_set_fp64_transforms(sc_mesh* m, int mode) {
+int sc_mesh_set_fp64_arithmetic(sc_mesh* m, int mode) {
     SC_TRY(check_mesh(m));
     if (m->precision != SC_PREC_FP64) return fail(SC_ERR_INVALID, "FP64 transform modes apply to SC_PREC_FP64 meshes");
-    if (mode != SC_FP64_TRANSFORMS_FP64 && mode != SC_FP64_TRANSFORMS_DF32)
+    if (mode != SC_FP64_ARITH_FP64 && mode != SC_FP64_ARITH_DF32)
         return fail(SC_ERR_INVALID, "unknown FP64 transform mode %d", mode);
-    m->df32_transforms = mode == SC_FP64_TRANSFORMS_DF32;
+    m->df32 = mode == SC_FP64_ARITH_DF32;
     return SC_OK;
 }
 

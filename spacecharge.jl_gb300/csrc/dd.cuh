@@ -85,24 +85,55 @@ __device__ __forceinline__ ddc dd_scale(ddc a, float gh, float gl) {
     return dd_renorm(p, e);
 }
 
-// A double split into hi + lo without FP64 instructions: hi keeps the top
-// 24 significand bits (truncated), lo is the remaining 29 bits rounded to
-// FP32, so hi + lo equals x to about 2^-47 relative.  Magnitudes outside
-// [2^-74, 2^100] (and zero, subnormal or non-finite values) take the FP64
-// conversion instead.
+// A double split into hi + lo with integer operations only (no FP64
+// instruction, not even in a branch the compiler could if-convert): hi keeps
+// the top 24 significand bits (truncated), lo is the remaining 29 bits
+// rounded to FP32, so hi + lo equals x to 2^-47 relative.  The FP32 range
+// bounds it: below |x| = 2^-103 lo flushes to zero (gradually from 2^-126
+// on), below 2^-126 hi too; from 2^128 on hi is +-inf (NaN stays NaN).
 __device__ __forceinline__ void dd_split(double x, float& hi, float& lo) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const int e = (int)((b >> 52) & 0x7FF);
-    if (e >= 1023 - 74 && e <= 1023 + 100) {
-        const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
-        hi = __uint_as_float(sgn | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)((b >> 29) & 0x7FFFFFu));
-        const unsigned rem = (unsigned)(b & ((1ull << 29) - 1));  // weight 2^(e - 1075)
-        const float pw = __uint_as_float((unsigned)(e - 1075 + 127) << 23);
-        lo = __uint_as_float(__float_as_uint((float)rem * pw) | sgn);
-        return;
+    const unsigned bh = (unsigned)(b >> 32), bl = (unsigned)b;
+    const int e = (int)((bh >> 20) & 0x7FF);
+    const unsigned sgn = bh & 0x80000000u;
+    const unsigned top = ((bh & 0xFFFFFu) << 3) | (bl >> 29);  // 23 fraction bits
+    unsigned hb;
+    if (e >= 897 && e <= 1150)
+        hb = sgn | ((unsigned)(e - 896) << 23) | top;
+    else if (e < 897)
+        hb = sgn;
+    else
+        hb = sgn | 0x7F800000u | ((e == 2047 && (top | (bl & 0x1FFFFFFFu))) ? 0x400000u : 0u);
+    hi = __uint_as_float(hb);
+    // lo = rem * 2^(e - 1075) = (rem * 2^-29) * 2^(e - 1046)
+    const int pe = e - 1046 + 127;
+    const float sc = (pe >= 1 && e <= 1150) ? __uint_as_float((unsigned)pe << 23) : 0.0f;
+    lo = __uint_as_float(__float_as_uint(__uint2float_rn(bl & 0x1FFFFFFFu) * 1.862645149230957e-09f * sc) | sgn);
+}
+
+__device__ __forceinline__ void dd_split(float x, float& hi, float& lo) {
+    hi = x;
+    lo = 0.0f;
+}
+
+// An FP32 value widened to FP64 exactly, with integer operations only
+// (zeros, subnormals, infinities and NaN included).
+__device__ __forceinline__ double dd_widen(float v) {
+    const unsigned u = __float_as_uint(v);
+    const unsigned e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+    const unsigned long long sg = (unsigned long long)(u & 0x80000000u) << 32;
+    unsigned long long b;
+    if (e != 0 && e != 0xFF) {
+        b = sg | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)m << 29);
+    } else if (e == 0xFF) {
+        b = sg | (0x7FFull << 52) | ((unsigned long long)m << 29);
+    } else if (m == 0) {
+        b = sg;
+    } else {  // subnormal: m * 2^-149, normalised
+        const int lz = __clz(m);
+        b = sg | ((unsigned long long)(905 - lz) << 52) | ((unsigned long long)((m << (lz - 8)) & 0x7FFFFFu) << 29);
     }
-    hi = (float)x;
-    lo = (float)(x - (double)hi);
+    return __longlong_as_double((long long)b);
 }
 
 __device__ __forceinline__ ddc dd_from(double2 v) {
@@ -114,9 +145,71 @@ __device__ __forceinline__ ddc dd_from(double2 v) {
 // back to FP64: the parts widened with integer operations, then one FP64
 // addition per part
 __device__ __forceinline__ double2 dd_to(ddc v) {
-    return make_double2(f32_to_f64(v.h.x) + f32_to_f64(v.l.x), f32_to_f64(v.h.y) + f32_to_f64(v.l.y));
+    return make_double2(dd_widen(v.h.x) + dd_widen(v.l.x), dd_widen(v.h.y) + dd_widen(v.l.y));
 }
 
+
+// real double-FP32 values as float2 {hi, lo}: a * b, and 1 - a for a in [0, 1]
+__device__ __forceinline__ float2 ddr_mul(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    const float e = fmaf(a.x, b.y, fmaf(a.y, b.x, fmaf(a.x, b.x, -p)));
+    const float h = p + e;
+    return make_float2(h, e - (h - p));
+}
+// 1 - (h + l) for h + l in [0, 1]
+__device__ __forceinline__ float2 ddr_one_minus(float2 a) {
+    const float s = 1.0f - a.x;
+    const float bb = s - 1.0f;
+    const float e = ((1.0f - (s - bb)) + (-a.x - bb)) - a.y;
+    const float h = s + e;
+    return make_float2(h, e - (h - s));
+}
+// a real double-FP32 value to FP64
+__device__ __forceinline__ double ddr_to(float2 v) { return dd_widen(v.x) + dd_widen(v.y); }
+
+__device__ __forceinline__ double dd_f64(double x) { return x; }
+__device__ __forceinline__ double dd_f64(float x) { return dd_widen(x); }
+
+// The reference's i (decided in FP32 as in cell_df32) and its in-cell
+// fraction f = (x - min)/delta - i in double-FP32, fh + fl: the cell's
+// lower face min + i*delta by one FP64 FMA, r = x - face by one FP64
+// subtraction (exact, or within 2^-53 of the cell, since x lies within a
+// cell of the face), r split and multiplied by the FP64 1/delta split into
+// ih + il.  f is then within about 2^-53 (i + 1) + 2^-47 f of the exact
+// quotient, as close as the reference's FP64 division.  Near a face the
+// exact FP64 division decides, and its f is split.
+template <typename P>
+__device__ __forceinline__ bool cell_dd(P x, const AxisP& a, int& i, float& fh, float& fl) {
+    float xh, xr;
+    dd_split(x, xh, xr);
+    const float s = xh - a.loh;
+    const float bb = s - xh;
+    const float t = (xh - (s - bb)) + (-a.loh - bb);
+    const float v = t + (xr - a.lol);
+    const float qf = (s + v) * a.invf;
+    const float fq = floorf(qf);
+    const float m = 4.0e-7f * fabsf(qf) + a.mabs * (fabsf(xh) + fabsf(a.loh)) + 1e-30f;
+    const float rq = qf - fq;
+    if (rq < m || rq > 1.0f - m || !(fabsf(qf) < 1.6e7f)) {
+        double fe;
+        if (!cell_exact(x, a, i, fe)) return false;
+        dd_split(fe, fh, fl);
+        return true;
+    }
+    if (!(fq >= 0.0f && fq <= (float)(a.n - 2))) return false;
+    i = (int)fq;
+    const double face = fma(dd_widen(fq), a.delta, a.lo);
+    float rh, rl;
+    dd_split(dd_f64(x) - face, rh, rl);
+    // (rh + rl) (ih + il)
+    float ih, il;
+    dd_split(a.inv, ih, il);
+    const float ph = rh * ih;
+    const float pl = fmaf(rh, il, fmaf(rl, ih, fmaf(rh, ih, -ph)));
+    fh = ph + pl;
+    fl = pl - (fh - ph);
+    return true;
+}
 
 // loads and stores of a buffer between passes that holds FP64 (double2) or
 // double-FP32 (ddc) values

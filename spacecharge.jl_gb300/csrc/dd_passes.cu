@@ -14,8 +14,8 @@
 
 namespace sc {
 
-// z pass of an FP64 mesh in free space: the FP64 spectrum rho^(kx, ky, .)
-// is split into FP32 pairs with integer operations, transformed forward,
+// z pass of an FP64 mesh in free space: the double-FP32 spectrum
+// rho^(kx, ky, .) of the forward x and y passes is transformed forward,
 // multiplied by i g for the three FP64 Green spectra (split the same way)
 // and transformed back, the result kept in double-FP32 for the inverse
 // passes.  Same column tiles, thread layout and
@@ -23,7 +23,7 @@ namespace sc {
 // (free-space branch); the Green values are copied to shared memory
 // asynchronously during the forward transform.
 template <int L, bool HALF>
-__global__ void __launch_bounds__(kColW * F2<L>::NT, 1) k2_dd_zpass(const double2* __restrict__ B, ddc* __restrict__ C,
+__global__ void __launch_bounds__(kColW * F2<L>::NT, 1) k2_dd_zpass(const ddc* __restrict__ B, ddc* __restrict__ C,
                                                                    int Hx, int Ly, int nz, GreenView gv,
                                                                    const ddc* __restrict__ tw) {
     using E = F2<L>;
@@ -47,13 +47,13 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, 1) k2_dd_zpass(const double
     ddc* sc = spec + c * E::S;
     ddc v[16];
     if (t < E::R2) {
-        const double2* Bc = B + fl;
+        const ddc* Bc = B + fl;
         const ddc zero{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll
         for (int s = 0; s < E::R1; ++s) {
             const int z = t + E::R2 * s;
             const bool in = HALF ? E::R2 * s < L / 2 : z < nz;
-            v[s] = in ? dd_from(Bc[plane * z]) : zero;
+            v[s] = in ? Bc[plane * z] : zero;
         }
     }
     E::template fwd<false>(v, col, t, swt);
@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, 1) k2_dd_zpass(const double
     }
 }
 
-bool launch2_dd_zpass(int logL, const double2* B, ddc* C, int Hx, int Ly, int nz, const GreenView& gv, const ddc* tw,
+bool launch2_dd_zpass(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz, const GreenView& gv, const ddc* tw,
                       cudaStream_t s) {
     if (gv.image || logL > 8) return false;
 #define SC_KDZ(LL)                                                                                          \

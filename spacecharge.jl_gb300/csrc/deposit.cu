@@ -10,6 +10,7 @@
 //   corner slots, then a pass that sums each node's 8 slots.
 #include "batch.cuh"
 #include "cells.cuh"
+#include "dd.cuh"
 #include "sc_internal.cuh"
 
 namespace sc {
@@ -128,6 +129,61 @@ __device__ __forceinline__ void deposit_atomic_body(const P* __restrict__ px, co
         atomicAdd(r + 1 + sz, q * fx * wy0 * fz);
         atomicAdd(r + sy + sz, q * wx0 * fy * fz);
         atomicAdd(r + 1 + sy + sz, q * fx * fy * fz);
+    }
+    if (skipped) atomicAdd(oob, (unsigned long long)skipped);
+}
+
+// FP64 meshes in double-FP32 mode (sc_mesh_set_fp64_arithmetic): the
+// atomic deposit with the cell fractions (cell_dd), the weights and the
+// charge products in double-FP32 (dd.cuh), in the reference's order
+// q*wx*wy*wz; each corner's charge is widened to FP64 (one FP64 addition)
+// for its FP64 atomic add, which the L2 performs.
+template <typename P>
+__global__ void __launch_bounds__(256) deposit_dd(const P* __restrict__ px, const P* __restrict__ py,
+                                                  const P* __restrict__ pz, const P* __restrict__ pq, int64_t n,
+                                                  Axes ax, double* __restrict__ rho,
+                                                  unsigned long long* __restrict__ oob) {
+    const int64_t base = blockIdx.x * (int64_t)(blockDim.x * kDepPerThread) + threadIdx.x;
+    P x[kDepPerThread], y[kDepPerThread], z[kDepPerThread], qq[kDepPerThread];
+#pragma unroll
+    for (int k = 0; k < kDepPerThread; ++k) {
+        const int64_t p = base + (int64_t)k * blockDim.x;
+        const bool in = p < n;
+        x[k] = in ? __ldg(px + p) : P(0);
+        y[k] = in ? __ldg(py + p) : P(0);
+        z[k] = in ? __ldg(pz + p) : P(0);
+        qq[k] = in ? __ldg(pq + p) : P(0);
+    }
+    const int nx = ax.a[0].n, ny = ax.a[1].n;
+    const int64_t sy = nx, sz = (int64_t)nx * ny;
+    unsigned skipped = 0;
+#pragma unroll
+    for (int k = 0; k < kDepPerThread; ++k) {
+        const int64_t p = base + (int64_t)k * blockDim.x;
+        if (p >= n) break;
+        int ix = 0, iy = 0, iz = 0;
+        float2 fx, fy, fz;
+        const bool ok = cell_dd(x[k], ax.a[0], ix, fx.x, fx.y) & cell_dd(y[k], ax.a[1], iy, fy.x, fy.y) &
+                        cell_dd(z[k], ax.a[2], iz, fz.x, fz.y);
+        if (!ok) {
+            ++skipped;
+            continue;
+        }
+        float2 q;
+        dd_split(qq[k], q.x, q.y);
+        const float2 wx0 = ddr_one_minus(fx), wy0 = ddr_one_minus(fy), wz0 = ddr_one_minus(fz);
+        const float2 qx0 = ddr_mul(q, wx0), qx1 = ddr_mul(q, fx);
+        const float2 q00 = ddr_mul(qx0, wy0), q10 = ddr_mul(qx1, wy0), q01 = ddr_mul(qx0, fy), q11 = ddr_mul(qx1, fy);
+        double* r = rho + (ix + sy * iy + sz * iz);
+        // deposition.jl:67-74 corner order
+        atomicAdd(r, ddr_to(ddr_mul(q00, wz0)));
+        atomicAdd(r + 1, ddr_to(ddr_mul(q10, wz0)));
+        atomicAdd(r + sy, ddr_to(ddr_mul(q01, wz0)));
+        atomicAdd(r + 1 + sy, ddr_to(ddr_mul(q11, wz0)));
+        atomicAdd(r + sz, ddr_to(ddr_mul(q00, fz)));
+        atomicAdd(r + 1 + sz, ddr_to(ddr_mul(q10, fz)));
+        atomicAdd(r + sy + sz, ddr_to(ddr_mul(q01, fz)));
+        atomicAdd(r + 1 + sy + sz, ddr_to(ddr_mul(q11, fz)));
     }
     if (skipped) atomicAdd(oob, (unsigned long long)skipped);
 }
@@ -390,6 +446,13 @@ int deposit_launch(sc_mesh* m, const void* x, const void* y, const void* z, cons
         else
             deposit_atomic<float, float><<<ablocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z,
                                                                (const float*)q, n, ax, (float*)m->rho, m->oob);
+    } else if (m->df32) {
+        if (dtype == SC_F64)
+            deposit_dd<double><<<ablocks, 256, 0, s>>>((const double*)x, (const double*)y, (const double*)z,
+                                                      (const double*)q, n, ax, (double*)m->rho, m->oob);
+        else
+            deposit_dd<float><<<ablocks, 256, 0, s>>>((const float*)x, (const float*)y, (const float*)z,
+                                                     (const float*)q, n, ax, (double*)m->rho, m->oob);
     } else {
         if (dtype == SC_F64)
             deposit_atomic<double, double><<<ablocks, 256, 0, s>>>((const double*)x, (const double*)y,

@@ -9,6 +9,7 @@
 // of bounds there).
 #include "batch.cuh"
 #include "cells.cuh"
+#include "dd.cuh"
 #include "sc_internal.cuh"
 
 namespace sc {
@@ -205,6 +206,113 @@ __global__ void __launch_bounds__(256, SC_GATH_MINB) gather_packed(const P* __re
     gather_packed_body<P, A>(px, py, pz, n, ax, ef, ex, ey, ez, oob, blockIdx.x, early != 0);
 }
 
+// FP64 meshes in double-FP32 mode (sc_mesh_set_fp64_arithmetic): the
+// packed gather with the cell fractions (cell_dd), the weights and the sums
+// in double-FP32 (dd.cuh), so that the FP64 units see only the output's one
+// addition per component.  The FP64 node values are split with integer
+// operations.  Ex and Ey of a corner share the paired FP32 instructions, and
+// so do Ez of two corners.
+template <typename P>
+__device__ __forceinline__ P dd_out(float h, float l);
+template <>
+__device__ __forceinline__ double dd_out<double>(float h, float l) {
+    return dd_widen(h) + dd_widen(l);
+}
+template <>
+__device__ __forceinline__ float dd_out<float>(float h, float l) {
+    return h + l;
+}
+
+// One particle per thread, two CTAs per SM: the double-FP32 sums are
+// longer dependent chains than gather_packed's, so more warps hide them.
+constexpr int kGathDdPerThread = 1;
+template <typename P>
+__global__ void __launch_bounds__(256, 2) gather_dd(const P* __restrict__ px, const P* __restrict__ py,
+                                                   const P* __restrict__ pz, int64_t n, Axes ax,
+                                                   const dnode4* __restrict__ ef, P* __restrict__ ex,
+                                                   P* __restrict__ ey, P* __restrict__ ez,
+                                                   unsigned long long* __restrict__ oob, int early) {
+    constexpr int K = kGathDdPerThread;
+    if (!early) pdl_wait();
+    const int64_t base = blockIdx.x * (int64_t)(blockDim.x * K) + threadIdx.x;
+    P x[K], y[K], z[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int64_t p = base + (int64_t)k * blockDim.x;
+        const bool in = p < n;
+        x[k] = in ? __ldg(px + p) : P(0);
+        y[k] = in ? __ldg(py + p) : P(0);
+        z[k] = in ? __ldg(pz + p) : P(0);
+    }
+    if (early) pdl_wait();
+    const int nx = ax.a[0].n, ny = ax.a[1].n;
+    const int64_t sy = nx, sz = (int64_t)nx * ny;
+    const int64_t off[8] = {0, 1, sy, 1 + sy, sz, 1 + sz, sy + sz, 1 + sy + sz};
+    float2 w[K][8];
+    dnode4 v[K][8];
+    bool ok[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int64_t p = base + (int64_t)k * blockDim.x;
+        int ix = 0, iy = 0, iz = 0;
+        float2 dx = make_float2(0.f, 0.f), dy = dx, dz = dx;
+        ok[k] = p < n && (cell_dd(x[k], ax.a[0], ix, dx.x, dx.y) & cell_dd(y[k], ax.a[1], iy, dy.x, dy.y) &
+                          cell_dd(z[k], ax.a[2], iz, dz.x, dz.y));
+        const float2 ux = ddr_one_minus(dx), uy = ddr_one_minus(dy), uz = ddr_one_minus(dz);
+        // interpolation.jl:46-53, as (x y) products times the z factor
+        const float2 q0 = ddr_mul(ux, uy), q1 = ddr_mul(dx, uy), q2 = ddr_mul(ux, dy), q3 = ddr_mul(dx, dy);
+        w[k][0] = ddr_mul(q0, uz);
+        w[k][1] = ddr_mul(q1, uz);
+        w[k][2] = ddr_mul(q2, uz);
+        w[k][3] = ddr_mul(q3, uz);
+        w[k][4] = ddr_mul(q0, dz);
+        w[k][5] = ddr_mul(q1, dz);
+        w[k][6] = ddr_mul(q2, dz);
+        w[k][7] = ddr_mul(q3, dz);
+        const dnode4* e = ef + (ok[k] ? (ix + sy * iy + sz * iz) : 0);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) v[k][c] = ok[k] ? ldg4(e + off[c]) : dnode4{};
+    }
+    unsigned skipped = 0;
+    const ddc zero{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const int64_t p = base + (int64_t)k * blockDim.x;
+        if (p >= n) break;
+        ddc axy = zero, az = zero;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            ddc e;
+            dd_split(v[k][c].x, e.h.x, e.l.x);
+            dd_split(v[k][c].y, e.h.y, e.l.y);
+            axy = dd_add(axy, dd_scale(e, w[k][c].x, w[k][c].y));
+        }
+#pragma unroll
+        for (int c = 0; c < 8; c += 2) {
+            ddc e;
+            dd_split(v[k][c].z, e.h.x, e.l.x);
+            dd_split(v[k][c + 1].z, e.h.y, e.l.y);
+            float2 pp, pe;
+            dd_prod2(e.h, e.l, make_float2(w[k][c].x, w[k][c + 1].x), make_float2(w[k][c].y, w[k][c + 1].y), pp, pe);
+            az = dd_add(az, dd_renorm(pp, pe));
+        }
+        // Ez: the two lanes' sums added
+        const float zs = az.h.x + az.h.y;
+        const float zb = zs - az.h.x;
+        const float ze = ((az.h.x - (zs - zb)) + (az.h.y - zb)) + (az.l.x + az.l.y);
+        const float zh = zs + ze, zl = ze - (zh - zs);
+        if (!ok[k]) {
+            ++skipped;
+            ex[p] = ey[p] = ez[p] = P(0);
+            continue;
+        }
+        ex[p] = dd_out<P>(axy.h.x, axy.l.x);
+        ey[p] = dd_out<P>(axy.h.y, axy.l.y);
+        ez[p] = dd_out<P>(zh, zl);
+    }
+    if (skipped) atomicAdd(oob, (unsigned long long)skipped);
+}
+
 // Staged batch kick (batch.cuh): the gather of a group of bunches in one launch.
 // (three CTAs per SM, as the single-mesh gather's 80 registers allow; the
 // table lookup would otherwise push it to 128 and two)
@@ -259,6 +367,16 @@ int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64
             launch_pdl(gather_packed<float, float>, (unsigned)gblocks, 256, 0, s, (const float*)x, (const float*)y, (const float*)z, n,
                                                               ax, (const float4*)m->efield, (float*)ex, (float*)ey,
                                                               (float*)ez, m->oob, e);
+    } else if (m->df32) {
+        const unsigned dblocks = (unsigned)((n + 256 * kGathDdPerThread - 1) / (256 * kGathDdPerThread));
+        if (dtype == SC_F64)
+            launch_pdl(gather_dd<double>, dblocks, 256, 0, s, (const double*)x, (const double*)y,
+                       (const double*)z, n, ax, (const dnode4*)m->efield, (double*)ex, (double*)ey, (double*)ez,
+                       m->oob, e);
+        else
+            launch_pdl(gather_dd<float>, dblocks, 256, 0, s, (const float*)x, (const float*)y,
+                       (const float*)z, n, ax, (const dnode4*)m->efield, (float*)ex, (float*)ey, (float*)ez, m->oob,
+                       e);
     } else {
         if (dtype == SC_F64)
             launch_pdl(gather_packed<double, double>, (unsigned)gblocks, 256, 0, s, (const double*)x, (const double*)y,

@@ -1158,6 +1158,12 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
     // (unless this mesh's autotuned or the process-wide choice says Stockham)
     const int eng = w.engine >= 0 ? w.engine : fft_engine();
     const bool two = std::is_same<T, float>::value && eng == 0;
+    // FP64 meshes in double-FP32 mode where all three lengths fit the
+    // register kernels: the x and y passes in double-FP32 (A, D and, in free
+    // space, B hold double-FP32 values), and the z pass too in free space
+    const bool dd = std::is_same<T, double>::value && m->df32 && eng == 0 && w.log2L[0] <= 8 &&
+                    w.log2L[1] <= 8 && w.log2L[2] <= 8;
+    const ddc* twdd = (const ddc*)ctx->twdd;
     const int lgWy = w.lgW >= 0 ? w.lgW : pick_cols(w.log2L[1]);
     // The fused forward pass runs one CTA per z plane, each a long chain of
     // FFT rounds: it pays only with the GPU to itself.  Beside a concurrent
@@ -1177,26 +1183,31 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
     }
     if (!fwd_fused) {
         StageScope st(m->timer, SC_STAGE_FWD_X, s);
-        if (!(two && launch2_fwd_x(w.log2L[0], (const float*)m->rho, (float2*)A, nx, rows, Hx, (const float2*)tw, s)))
+        if (dd) {
+            if (!launch2_dd_fwd_x(w.log2L[0], (const double*)m->rho, (ddc*)A, nx, rows, Hx, twdd, s))
+                return fail(SC_ERR_CUDA, "double-FP32 forward x pass did not launch");
+        } else if (!(two && launch2_fwd_x(w.log2L[0], (const float*)m->rho, (float2*)A, nx, rows, Hx, (const float2*)tw,
+                                          s)))
             SC_TRY(run_fwd_x<T>((const T*)m->rho, A, nx, rows, w, tw, s));
         SC_LAUNCH_CHECK("fwd_x");
     }
     if (!fwd_fused) {
         // y: A (Hx x ny x nz) -> B (Hx x Ly x nz)
         StageScope st(m->timer, SC_STAGE_FWD_Y, s);
-        if (!(two && launch2_col(false, w.log2L[1], (const float2*)A, (float2*)B, Hx, ny, Ly, Hx, (int64_t)Hx * ny,
+        if (dd) {
+            // with the image the z pass stays FP64: B widened to FP64
+            const bool ok = at_cathode ? launch2_dd_col<false>(w.log2L[1], (const ddc*)A, (double2*)B, Hx, nz, 1, ny, Ly,
+                                                               Hx, (int64_t)Hx * ny, 0, Hx, (int64_t)Hx * Ly, 0, twdd, s)
+                                       : launch2_dd_col<false>(w.log2L[1], (const ddc*)A, (ddc*)B, Hx, nz, 1, ny, Ly, Hx,
+                                                               (int64_t)Hx * ny, 0, Hx, (int64_t)Hx * Ly, 0, twdd, s);
+            if (!ok) return fail(SC_ERR_CUDA, "double-FP32 forward y pass did not launch");
+        } else if (!(two && launch2_col(false, w.log2L[1], (const float2*)A, (float2*)B, Hx, ny, Ly, Hx, (int64_t)Hx * ny,
                                  0, Hx, (int64_t)Hx * Ly, 0, nz, 1, (const float2*)tw, s)))
             SC_TRY(run_col<false, T>(A, B, Hx, Ly, w.log2L[1], ny, Ly, Hx, (int64_t)Hx * ny, 0, Hx, (int64_t)Hx * Ly,
                                      0, nz, 1, tw, s, lgWy));
         SC_LAUNCH_CHECK("fwd_y");
     }
-    // FP64 meshes with double-FP32 transforms: the inverse y and x passes in
-    // double-FP32 where both lengths fit the register kernels (D then holds
-    // double-FP32 values); c_dd: the z pass left C in double-FP32 too
-    const bool dd = std::is_same<T, double>::value && m->df32_transforms && eng == 0 && w.log2L[0] <= 8 &&
-                    w.log2L[1] <= 8;
-    const ddc* twdd = (const ddc*)ctx->twdd;
-    bool c_dd = false;
+    bool c_dd = false;  // the z pass left C in double-FP32
     // z + Green + inverse z
     {
         if (green_ready) SC_CUDA(cudaStreamWaitEvent(s, green_ready, 0));
@@ -1208,7 +1219,7 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
         }
         // FP64 in free space, on request: the z pass in double-FP32, its
         // output kept in double-FP32 for the inverse passes
-        if (dd && launch2_dd_zpass(w.log2L[2], (const double2*)B, (ddc*)C, Hx, Ly, nz, gv, twdd, s)) {
+        if (dd && launch2_dd_zpass(w.log2L[2], (const ddc*)B, (ddc*)C, Hx, Ly, nz, gv, twdd, s)) {
             c_dd = true;
             SC_LAUNCH_CHECK("k2_dd_zpass");
             goto zdone;
@@ -1236,14 +1247,14 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
             return SC_OK;
         }
         if (dd) {
-            const bool ok = c_dd ? launch2_dd_col_inv(w.log2L[1], (const ddc*)C, (ddc*)D, Hx, nz, ny, Hx,
-                                                      (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, Hx, (int64_t)Hx * ny,
-                                                      (int64_t)Hx * ny * nz, twdd, s)
-                                 : launch2_dd_col_inv(w.log2L[1], (const double2*)C, (ddc*)D, Hx, nz, ny, Hx,
-                                                      (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, Hx, (int64_t)Hx * ny,
-                                                      (int64_t)Hx * ny * nz, twdd, s);
+            const bool ok = c_dd ? launch2_dd_col<true>(w.log2L[1], (const ddc*)C, (ddc*)D, Hx, nz, 3, Ly, ny, Hx,
+                                                        (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, Hx, (int64_t)Hx * ny,
+                                                        (int64_t)Hx * ny * nz, twdd, s)
+                                 : launch2_dd_col<true>(w.log2L[1], (const double2*)C, (ddc*)D, Hx, nz, 3, Ly, ny, Hx,
+                                                        (int64_t)Hx * Ly, (int64_t)Hx * Ly * nz, Hx, (int64_t)Hx * ny,
+                                                        (int64_t)Hx * ny * nz, twdd, s);
             if (!ok) return fail(SC_ERR_CUDA, "double-FP32 inverse y pass did not launch");
-            SC_LAUNCH_CHECK("k2_dd_col_inv");
+            SC_LAUNCH_CHECK("k2_dd_col");
         } else if (!(two && launch2_col(true, w.log2L[1], (const float2*)C, (float2*)D, Hx, Ly, ny, Hx, (int64_t)Hx * Ly,
                                  (int64_t)Hx * Ly * nz, Hx, (int64_t)Hx * ny, (int64_t)Hx * ny * nz, nz, 3,
                                  (const float2*)tw, s)))

@@ -1687,16 +1687,17 @@ static bool launch2_zpass(int logL, const float2* B, float2* C, int Hx, int Ly, 
     return true;
 }
 
-// FP64 meshes, double-FP32 passes (dd_passes.cu, dd_inverse.cu); false
-// where they do not apply (the image for the z pass, transforms above 256
-// points).  TI: double2 (FP64 values) or ddc (double-FP32 values) in the
-// buffer the inverse y pass reads.
-bool launch2_dd_zpass(int logL, const double2* B, ddc* C, int Hx, int Ly, int nz, const GreenView& gv, const ddc* tw,
+// FP64 meshes, double-FP32 passes (dd_passes.cu, dd_xy.cu); false where
+// they do not apply (the image for the z pass, transforms above 256
+// points).  launch2_dd_col: column transforms (forward or inverse) of ncomp
+// components; TI / TO: double2 (FP64) or ddc (double-FP32) buffers.
+bool launch2_dd_fwd_x(int logL, const double* rho, ddc* A, int nx, int rows, int Hx, const ddc* tw, cudaStream_t s);
+template <bool INV, typename TI, typename TO>
+bool launch2_dd_col(int logL, const TI* in, TO* out, int ncols, int nbatch, int ncomp, int n_valid, int n_store,
+                    int64_t as_in, int64_t bs_in, int64_t cs_in, int64_t as_out, int64_t bs_out, int64_t cs_out,
+                    const ddc* tw, cudaStream_t s);
+bool launch2_dd_zpass(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz, const GreenView& gv, const ddc* tw,
                       cudaStream_t s);
-template <typename TI>
-bool launch2_dd_col_inv(int logL, const TI* in, ddc* out, int ncols, int nbatch, int n_store, int64_t as_in,
-                        int64_t bs_in, int64_t cs_in, int64_t as_out, int64_t bs_out, int64_t cs_out, const ddc* tw,
-                        cudaStream_t s);
 bool launch2_dd_inv_x(int logL, const ddc* D, dnode4* E4, int nx, int rows, int Hx, int64_t cs, const ddc* tw,
                       cudaStream_t s);
 

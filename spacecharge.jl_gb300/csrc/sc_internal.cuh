@@ -230,7 +230,7 @@ struct sc_mesh {
     int precision;
     int device;
     bool green_cache = true;
-    bool df32_transforms = false;  // FP64 meshes: the z pass in double-FP32
+    bool df32 = false;  // FP64 meshes: transforms and gather in double-FP32 (sc_mesh_set_fp64_arithmetic)
     void* rho = nullptr;     // T[N]
     void* efield = nullptr;  // planar T[3N] or packed T[4N]
     unsigned long long* oob = nullptr;  // device counter of skipped particles

@@ -15,7 +15,7 @@ using CUDA
 import ChainRulesCore
 
 export Mesh3D, deposit!, clear_mesh!, interpolate_field, solve!, kick, kick!, kick_host, track!, magnetic_field,
-       set_kick_mode!, set_fp64_transforms!, set_bounds!, refit!, solve_potential
+       set_kick_mode!, set_fp64_arithmetic!, set_bounds!, refit!, solve_potential
 
 const libsc = normpath(joinpath(@__DIR__, "..", "..", "..", "lib", "libspacecharge_gb300.so"))
 
@@ -188,15 +188,15 @@ set_kick_mode!(mesh::Mesh3D, mode::Symbol) =
     check(ccall((:sc_mesh_set_kick_mode, libsc), Cint, (Ptr{Cvoid}, Cint), mesh.ptr, deposit_mode_code(mode)))
 
 """
-    set_fp64_transforms!(mesh, mode::Symbol)
+    set_fp64_arithmetic!(mesh, mode::Symbol)
 
-`Float64` meshes: `:fp64` (the default) runs the field solve's transforms in
-FP64; `:df32` runs the free-space z pass and the inverse y and x passes in
-double-FP32 (pairs of `Float32`, 48-bit significands, about 1e-15 of the
-field's maximum), off the GPU's FP64 units.
+`Float64` meshes: `:fp64` (the default) runs the kick in FP64; `:df32` runs
+the atomic deposit's weights, the x, y and (free-space) z transform passes and
+the interpolation in double-FP32 (pairs of `Float32`, 48-bit significands,
+about 1e-14 of the fields' maximum), off the GPU's FP64 units.
 """
-set_fp64_transforms!(mesh::Mesh3D, mode::Symbol) =
-    check(ccall((:sc_mesh_set_fp64_transforms, libsc), Cint, (Ptr{Cvoid}, Cint), mesh.ptr,
+set_fp64_arithmetic!(mesh::Mesh3D, mode::Symbol) =
+    check(ccall((:sc_mesh_set_fp64_arithmetic, libsc), Cint, (Ptr{Cvoid}, Cint), mesh.ptr,
                 mode === :fp64 ? Cint(0) : mode === :df32 ? Cint(1) : throw(ArgumentError("mode: :fp64 or :df32"))))
 
 # solve!(mesh; at_cathode=false), src/solvers/free_space.jl:14-47

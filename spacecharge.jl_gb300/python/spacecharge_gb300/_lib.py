@@ -36,8 +36,8 @@ STAGES = ["deposit", "green", "fwd_x", "fwd_y", "zpass", "inv_y", "inv_x", "gath
 
 SC_FFT_AUTO = 0
 SC_FFT_STOCKHAM = 1
-SC_FP64_TRANSFORMS_FP64 = 0
-SC_FP64_TRANSFORMS_DF32 = 1
+SC_FP64_ARITH_FP64 = 0
+SC_FP64_ARITH_DF32 = 1
 
 SC_LAYOUT_PLANAR = 0
 SC_LAYOUT_PACKED = 1
@@ -89,7 +89,7 @@ SIGNATURES = {
     "sc_mesh_rho": [_vp, C.POINTER(_vp)],
     "sc_mesh_efield": [_vp, C.POINTER(_vp)],
     "sc_mesh_set_green_cache": [_vp, _int],
-    "sc_mesh_set_fp64_transforms": [_vp, _int],
+    "sc_mesh_set_fp64_arithmetic": [_vp, _int],
     "sc_mesh_set_kick_mode": [_vp, _int],
     "sc_mesh_set_kick_graph": [_vp, _int],
     "sc_set_fft_engine": [_int],

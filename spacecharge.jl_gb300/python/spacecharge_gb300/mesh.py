@@ -220,15 +220,15 @@ class Mesh3D:
     def set_green_cache(self, enabled: bool) -> None:
         L.call("sc_mesh_set_green_cache", self._h.ptr, 1 if enabled else 0)
 
-    def set_fp64_transforms(self, mode: str) -> None:
-        """precision="fp64" meshes: "fp64" (default) runs the field solve's
-        transforms in FP64; "df32" runs the free-space z pass and the inverse
-        y and x passes in double-FP32 (48-bit significands, about 1e-15 of the
-        field's maximum)."""
-        modes = {"fp64": L.SC_FP64_TRANSFORMS_FP64, "df32": L.SC_FP64_TRANSFORMS_DF32}
+    def set_fp64_arithmetic(self, mode: str) -> None:
+        """precision="fp64" meshes: "fp64" (default) runs the kick in FP64;
+        "df32" runs the atomic deposit's weights, the x, y and (free-space) z
+        transform passes and the interpolation in double-FP32 (48-bit
+        significands, about 1e-14 of the fields' maximum)."""
+        modes = {"fp64": L.SC_FP64_ARITH_FP64, "df32": L.SC_FP64_ARITH_DF32}
         if mode not in modes:
             raise ValueError(f"unknown FP64 transform mode {mode!r}")
-        L.call("sc_mesh_set_fp64_transforms", self._h.ptr, modes[mode])
+        L.call("sc_mesh_set_fp64_arithmetic", self._h.ptr, modes[mode])
 
     def out_of_range(self) -> int:
         """Particles skipped as outside the mesh since the last query."""

@@ -399,14 +399,14 @@ def test_fft_engines_agree(sc, cuda, grid, cath, first):
 @pytest.mark.parametrize("grid,cath", [((64, 64, 128), False), ((32, 32, 64), False), ((12, 20, 33), False),
                                        ((3, 5, 9), False), ((8, 8, 128), False), ((12, 12, 16), True),
                                        ((24, 12, 33), True)])
-def test_fp64_df32_transforms(sc, cuda, grid, cath):
-    """FP64 meshes with the double-FP32 transforms (the z pass in free space,
-    the inverse y and x passes) against the FP64 transforms on the same
-    deposit, and against the oracle at the FP64 tolerance.  Double-FP32
-    carries 48-bit significands, so the fields agree to ~1e-15 of their
-    maximum; 1e-12 is asserted.  nz = L/2 (64x64x128, 32x32x64, 8x8x128) and
-    nz < L/2 (12x20x33, 3x5x9) take the two compile-time z patterns; with the
-    cathode image the z pass stays FP64 and the inverse y pass reads its FP64
+def test_fp64_df32_arithmetic(sc, cuda, grid, cath):
+    """FP64 meshes in double-FP32 mode (the atomic deposit, the x and y
+    passes, the z pass in free space, the interpolation) against FP64 mode on
+    the same deposit, and against the oracle at the FP64 tolerance.
+    Double-FP32 carries 48-bit significands, so the fields agree to ~1e-14 of
+    their maximum; 1e-12 is asserted.  nz = L/2 (64x64x128, 32x32x64, 8x8x128) and nz < L/2
+    (12x20x33, 3x5x9) take the two compile-time z patterns; with the cathode
+    image the z pass stays FP64 and the inverse y pass reads its FP64
     output."""
     n = 50_000
     x, y, z = bunch(n, 17, sig=(1e-3, 1e-3, 0.3e-3))
@@ -414,31 +414,49 @@ def test_fp64_df32_transforms(sc, cuda, grid, cath):
         z = np.abs(z) + 0.1e-3
     q = np.full(n, 1e-9 / n)
     m = sc.Mesh3D(grid, x, y, z, precision="fp64", gamma=4.0)
-    out = {}
+    out, part, part32 = {}, {}, {}
+    x32, y32, z32 = (v.astype(np.float32) for v in (x, y, z))
     for mode in ("fp64", "df32"):
-        m.set_fp64_transforms(mode)
+        m.set_fp64_arithmetic(mode)
         sc.deposit(m, x, y, z, q, mode="deterministic")
         sc.solve(m, at_cathode=cath)
         out[mode] = host(m.efield)
+        part[mode] = sc.interpolate_field(m, x, y, z)
+        part32[mode] = sc.interpolate_field(m, x32, y32, z32)
     assert relerr(out["df32"], out["fp64"]) < 1e-12
+    for a, b in zip(part["df32"], part["fp64"]):
+        assert relerr(a, b) < 1e-12
+    for a, b in zip(part32["df32"], part32["fp64"]):
+        assert relerr(a, b) < 1e-6
     om = O.mesh_auto(grid, x, y, z, gamma=4.0)
     O.deposit(om, x, y, z, q)
     O.solve(om, at_cathode=cath)
     assert relerr(out["df32"], om.efield) < TOL["fp64"]
-    m.set_fp64_transforms("fp64")
+    for a, b in zip(part["df32"], O.interpolate_field(om, x, y, z)):
+        assert relerr(a, b) < TOL["fp64"]
+    # the atomic deposit (the kick's default on FP64 meshes)
+    rho = {}
+    for mode in ("fp64", "df32"):
+        m.set_fp64_arithmetic(mode)
+        sc.deposit(m, x, y, z, q, mode="atomic")
+        rho[mode] = host(m.rho)
+    assert relerr(rho["df32"], rho["fp64"]) < 1e-13
+    assert relerr(rho["df32"], om.rho) < RHO_TOL["fp64"]
+    m.set_fp64_arithmetic("fp64")
+    sc.deposit(m, x, y, z, q, mode="deterministic")
     sc.solve(m, at_cathode=cath)
     assert np.array_equal(host(m.efield), out["fp64"])
 
 
-def test_fp64_transforms_mode_checks(sc, cuda):
+def test_fp64_arithmetic_mode_checks(sc, cuda):
     """The double-FP32 switch exists for FP64 meshes only, with two modes."""
     from spacecharge_gb300 import _lib as L
 
     m = sc.Mesh3D((8, 8, 8), (-1e-3,) * 3, (1e-3,) * 3, precision="mixed")
     with pytest.raises(Exception):
-        m.set_fp64_transforms("df32")
+        m.set_fp64_arithmetic("df32")
     m64 = sc.Mesh3D((8, 8, 8), (-1e-3,) * 3, (1e-3,) * 3, precision="fp64")
     with pytest.raises(ValueError):
-        m64.set_fp64_transforms("fp32")
+        m64.set_fp64_arithmetic("fp32")
     with pytest.raises(Exception):
-        L.call("sc_mesh_set_fp64_transforms", m64._h.ptr, 7)
+        L.call("sc_mesh_set_fp64_arithmetic", m64._h.ptr, 7)
