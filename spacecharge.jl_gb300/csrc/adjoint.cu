@@ -257,7 +257,11 @@ static int adjoint_t(sc_mesh* m, const P* x, const P* y, const P* z, const P* q,
     // forward recompute: rho and E for these particles (a Green build, when
     // needed, overlaps the deposit on the mesh's side stream)
     cudaEvent_t ready = nullptr;
-    if (n > 0) SC_TRY(native_green_async(m, at_cathode, s, &ready));
+    // (the FP64 adjoint z pass reads an FP64 free-space spectrum)
+    if (n > 0)
+        SC_TRY(native_green_async(m, at_cathode, s, &ready, false));
+    else
+        SC_TRY(native_ensure_green(m, at_cathode, s, false));
     const int dmode = m->precision == SC_PREC_MIXED ? SC_DEPOSIT_VECTOR : SC_DEPOSIT_ATOMIC;
     const bool assign = deposit_assigns(m, dmode);
     int st = assign || cudaMemsetAsync(m->rho, 0, sizeof(T) * m->N, s) == cudaSuccess

@@ -136,6 +136,50 @@ __device__ __forceinline__ double dd_widen(float v) {
     return __longlong_as_double((long long)b);
 }
 
+// A real double-FP32 value, for kernels written over a real type (the Green
+// transform): the arithmetic of the complex pairs above, one lane.
+struct __align__(8) dreal {
+    float h, l;
+    dreal() = default;
+    __host__ __device__ constexpr dreal(float a, float b) : h(a), l(b) {}
+    __host__ __device__ constexpr dreal(int v) : h((float)v), l(0.0f) {}  // |v| < 2^24
+    __host__ __device__ constexpr dreal(float v) : h(v), l(0.0f) {}
+    __host__ __device__ dreal(double v) {
+#ifdef __CUDA_ARCH__
+        dd_split(v, h, l);
+#else
+        h = (float)v;
+        l = (float)(v - (double)h);
+#endif
+    }
+};
+__device__ __forceinline__ dreal dd_renorm1(float s, float e) {
+    const float h = s + e;
+    return dreal(h, e - (h - s));
+}
+__device__ __forceinline__ dreal operator+(dreal a, dreal b) {
+    const float s = a.h + b.h;
+    const float bb = s - a.h;
+    const float e = (a.h - (s - bb)) + (b.h - bb);
+    return dd_renorm1(s, e + (a.l + b.l));
+}
+__device__ __forceinline__ dreal operator-(dreal a) { return dreal(-a.h, -a.l); }
+__device__ __forceinline__ dreal operator-(dreal a, dreal b) { return a + (-b); }
+__device__ __forceinline__ dreal operator*(dreal a, dreal b) {
+    const float p = a.h * b.h;
+    return dd_renorm1(p, fmaf(a.h, b.l, fmaf(a.l, b.h, fmaf(a.h, b.h, -p))));
+}
+// a / b: the FP32 quotient, corrected by one step on the double-FP32 residual
+__device__ __forceinline__ dreal operator/(dreal a, dreal b) {
+    const float q1 = a.h / b.h;
+    const dreal r = a - b * dreal(q1);
+    return dd_renorm1(q1, r.h / b.h);
+}
+__device__ __forceinline__ dreal& operator+=(dreal& a, dreal b) {
+    a = a + b;
+    return a;
+}
+
 __device__ __forceinline__ ddc dd_from(double2 v) {
     ddc r;
     dd_split(v.x, r.h.x, r.l.x);

@@ -16,13 +16,13 @@ namespace sc {
 
 // z pass of an FP64 mesh in free space: the double-FP32 spectrum
 // rho^(kx, ky, .) of the forward x and y passes is transformed forward,
-// multiplied by i g for the three FP64 Green spectra (split the same way)
-// and transformed back, the result kept in double-FP32 for the inverse
-// passes.  Same column tiles, thread layout and
-// compile-time z patterns as the FP32 zpass_body of pipeline2.cuh
-// (free-space branch); the Green values are copied to shared memory
-// asynchronously during the forward transform.
-template <int L, bool HALF>
+// multiplied by i g for the three Green spectra (TG: double, split with
+// integer operations, or dreal from the double-FP32 Green transform) and
+// transformed back, the result kept in double-FP32 for the inverse passes.
+// Same column tiles, thread layout and compile-time z patterns as the FP32
+// zpass_body of pipeline2.cuh (free-space branch); the Green values are
+// copied to shared memory asynchronously during the forward transform.
+template <int L, bool HALF, typename TG>
 __global__ void __launch_bounds__(kColW * F2<L>::NT, 1) k2_dd_zpass(const ddc* __restrict__ B, ddc* __restrict__ C,
                                                                    int Hx, int Ly, int nz, GreenView gv,
                                                                    const ddc* __restrict__ tw) {
@@ -34,11 +34,11 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, 1) k2_dd_zpass(const ddc* _
     extern __shared__ __align__(16) unsigned char smraw[];
     ddc* xb = reinterpret_cast<ddc*>(smraw);
     ddc* spec = xb + kColW * E::S;
-    double* gsm = reinterpret_cast<double*>(spec + kColW * E::S);  // [3][HZ][kColW]
+    TG* gsm = reinterpret_cast<TG*>(spec + kColW * E::S);  // [3][HZ][kColW]
     const int tile = blockIdx.x;
     const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
     const int64_t plane = (int64_t)Hx * Ly;
-    prefetch_green<L, double>(gsm, gv, Hx, Ly, tile);
+    prefetch_green<L, TG>(gsm, gv, Hx, Ly, tile);
     const int f = tile * kColW + c;
     const bool cok = f < plane;
     const int fl = cok ? f : (int)plane - 1;
@@ -73,16 +73,21 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, 1) k2_dd_zpass(const ddc* _
             const float sy = comp == 1 ? ysign : 1.f;
             const float su = comp == 2 ? -sy : sy;
             const float sm = t > 0 ? su : sy;  // kz = L/2 + t
-            const double* gfc = gsm + comp * HZ * kColW + c;
-            const double* glo = gfc + t * kColW;
-            const double* ghi = gfc + (L - t) * kColW;
+            const TG* gfc = gsm + comp * HZ * kColW + c;
+            const TG* glo = gfc + t * kColW;
+            const TG* ghi = gfc + (L - t) * kColW;
             const ddc* sct = sc + t;
 #pragma unroll
             for (int r = 0; r < E::R2; ++r) {
-                const double gd = RL * r < L / 2 ? glo[RL * r * kColW] : ghi[-RL * r * kColW];
+                const TG gd = RL * r < L / 2 ? glo[RL * r * kColW] : ghi[-RL * r * kColW];
                 const float sg = RL * r < L / 2 ? sy : RL * r == L / 2 ? sm : su;
                 float gh, gl;
-                dd_split(gd, gh, gl);
+                if constexpr (std::is_same<TG, dreal>::value) {
+                    gh = gd.h;
+                    gl = gd.l;
+                } else {
+                    dd_split(gd, gh, gl);
+                }
                 v[r] = rot<true>(dd_scale(sct[xoff(RL * r)], gh * sg, gl * sg));  // X * (i g)
             }
         }
@@ -98,24 +103,34 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, 1) k2_dd_zpass(const ddc* _
     }
 }
 
-bool launch2_dd_zpass(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz, const GreenView& gv, const ddc* tw,
-                      cudaStream_t s) {
+bool launch2_dd_zpass(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz, const GreenView& gv, int gfmt,
+                      const ddc* tw, cudaStream_t s) {
     if (gv.image || logL > 8) return false;
-#define SC_KDZ(LL)                                                                                          \
+#define SC_KDZ_GO(LL, HALF, TG)                                                                             \
     {                                                                                                       \
-        const size_t smem = sizeof(ddc) * kColW * F2<LL>::S * 2 + sizeof(double) * 3 * (LL / 2 + 1) * kColW; \
+        const size_t smem = sizeof(ddc) * kColW * F2<LL>::S * 2 + sizeof(TG) * 3 * (LL / 2 + 1) * kColW;    \
         const int64_t ncol = (int64_t)Hx * Ly;                                                              \
         const unsigned grid = (unsigned)((ncol + kColW - 1) / kColW);                                       \
+        if (set_smem(k2_dd_zpass<LL, HALF, TG>, smem) != SC_OK) return false;                               \
+        launch_pdl(k2_dd_zpass<LL, HALF, TG>, grid, kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz, gv, tw); \
+    }
+#define SC_KDZ(LL)                                                                                          \
+    {                                                                                                       \
         if (2 * nz == LL) {                                                                                 \
-            if (set_smem(k2_dd_zpass<LL, true>, smem) != SC_OK) return false;                               \
-            launch_pdl(k2_dd_zpass<LL, true>, grid, kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz, gv, tw); \
+            if (gfmt)                                                                                       \
+                SC_KDZ_GO(LL, true, dreal)                                                                  \
+            else                                                                                            \
+                SC_KDZ_GO(LL, true, double)                                                                 \
         } else {                                                                                            \
-            if (set_smem(k2_dd_zpass<LL, false>, smem) != SC_OK) return false;                              \
-            launch_pdl(k2_dd_zpass<LL, false>, grid, kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz, gv, tw); \
+            if (gfmt)                                                                                       \
+                SC_KDZ_GO(LL, false, dreal)                                                                 \
+            else                                                                                            \
+                SC_KDZ_GO(LL, false, double)                                                                \
         }                                                                                                   \
     }
     SC_L_SWITCH(logL, SC_KDZ)
 #undef SC_KDZ
+#undef SC_KDZ_GO
     return true;
 }
 

@@ -26,6 +26,40 @@ struct Cplx<double> {
     using T2 = double2;
     __device__ __forceinline__ static double2 make(double a, double b) { return make_double2(a, b); }
 };
+template <>
+struct Cplx<dreal> {
+    using T2 = ddc;
+    __device__ __forceinline__ static ddc make(dreal a, dreal b) {
+        return ddc{make_float2(a.h, b.h), make_float2(a.l, b.l)};
+    }
+};
+
+// Real and imaginary parts, and loads of a real value, for kernels written
+// over the real type (float, double or dreal)
+__device__ __forceinline__ float c_re(float2 v) { return v.x; }
+__device__ __forceinline__ float c_im(float2 v) { return v.y; }
+__device__ __forceinline__ double c_re(double2 v) { return v.x; }
+__device__ __forceinline__ double c_im(double2 v) { return v.y; }
+__device__ __forceinline__ dreal c_re(ddc v) { return dreal(v.h.x, v.l.x); }
+__device__ __forceinline__ dreal c_im(ddc v) { return dreal(v.h.y, v.l.y); }
+template <typename T>
+__device__ __forceinline__ T ldg_r(const T* p) {
+    return __ldg(p);
+}
+template <>
+__device__ __forceinline__ dreal ldg_r<dreal>(const dreal* p) {
+    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    return dreal(v.x, v.y);
+}
+template <typename T>
+__device__ __forceinline__ T ldcg_r(const T* p) {
+    return __ldcg(p);
+}
+template <>
+__device__ __forceinline__ dreal ldcg_r<dreal>(const dreal* p) {
+    const float2 v = __ldcg(reinterpret_cast<const float2*>(p));
+    return dreal(v.x, v.y);
+}
 
 // Complex add and subtract.  FP32 pairs use the paired FP32 instructions of
 // sm_100 and later (one instruction for both lanes of a float2, each lane

@@ -232,7 +232,8 @@ __global__ void __launch_bounds__(128) k_igf_corners3(double* __restrict__ F, in
 // 8-point difference (green_functions.jl:108-111) of every stored cell of
 // the three components, scaled by FPEI/(Lx Ly Lz), into the octant array
 // G[c][dz - ez0][dy][dx] that the parity-reduced transform reads.
-__global__ void __launch_bounds__(128) k_igf_place_oct(const double* __restrict__ F, double* __restrict__ G, int nx,
+template <typename OT>  // double, or dreal (double-FP32) for the double-FP32 transform
+__global__ void __launch_bounds__(128) k_igf_place_oct(const double* __restrict__ F, OT* __restrict__ G, int nx,
                                                        int ny, int nz, int ez0, double scale) {
     const int cx = nx + 1, cy = ny + 1, cz = nz + 1 - ez0;
     const int64_t per = (int64_t)cx * cy * cz;
@@ -250,7 +251,7 @@ __global__ void __launch_bounds__(128) k_igf_place_oct(const double* __restrict_
     auto Fv = [&](int a, int b, int d) { return f[a + sy * b + sz * d]; };
     const double g = Fv(1, 1, 1) - Fv(0, 1, 1) - Fv(1, 0, 1) - Fv(1, 1, 0) - Fv(0, 0, 0) + Fv(0, 0, 1) +
                      Fv(0, 1, 0) + Fv(1, 0, 0);
-    G[t] = g * scale;
+    G[t] = OT(g * scale);
 }
 
 // 8-point difference (green_functions.jl:108-111) for displacements
@@ -986,9 +987,10 @@ static int build_green_mixed(sc_mesh* m, bool image, double offz, cudaStream_t s
 }
 
 template <typename T>
-static int build_green_any(sc_mesh* m, bool image, double offz, cudaStream_t s);
+static int build_green_any(sc_mesh* m, bool image, double offz, cudaStream_t s, bool dd, int* fmt);
 template <>
-int build_green_any<float>(sc_mesh* m, bool image, double offz, cudaStream_t s) {
+int build_green_any<float>(sc_mesh* m, bool image, double offz, cudaStream_t s, bool, int* fmt) {
+    *fmt = 0;
     return build_green_mixed(m, image, offz, s);
 }
 // FP64 pipeline: the reference's FP64 corner differences on the stored
@@ -997,8 +999,12 @@ int build_green_any<float>(sc_mesh* m, bool image, double offz, cudaStream_t s) 
 // per complex FFT, about 8x less transform work than the full L grid).
 // Returns false (nothing issued) where that transform does not apply
 // (transform lengths above 256).
-static int build_green_fp64_reduced(sc_mesh* m, bool image, double offz, cudaStream_t s, bool* done) {
+// dd (free space only): the x+y and z transforms in double-FP32 (k4_*<L,
+// dreal>), the spectrum stored as dreal; *fmt reports the format written.
+static int build_green_fp64_reduced(sc_mesh* m, bool image, double offz, cudaStream_t s, bool* done, bool dd,
+                                    int* fmt) {
     *done = false;
+    *fmt = 0;
     NativeWork& w = m->nw;
     // (the process-wide Stockham-only setting keeps the full-grid build too)
     if (fft_engine() != 0 || w.log2L[0] > 8 || w.log2L[1] > 8 || w.log2L[2] > 8) return SC_OK;
@@ -1030,12 +1036,28 @@ static int build_green_fp64_reduced(sc_mesh* m, bool image, double offz, cudaStr
     k_igf_corners3<<<(unsigned)((3 * ncorner + 127) / 128), 128, 0, s>>>(F, nx, ny, nz, ez0, m->delta[0], m->delta[1],
                                                                         m->delta[2], m->gamma, image ? offz : 0.0);
     SC_LAUNCH_CHECK("k_igf_corners3");
-    launch_pdl(k_igf_place_oct, (unsigned)((3 * gcs + 127) / 128), 128, 0, s, (const double*)F, G, nx, ny, nz, ez0,
-               kFpei / ((double)Lx * Ly * Lz));
-    SC_LAUNCH_CHECK("k_igf_place_oct");
     const int64_t t1cs = (int64_t)Hx * ny * zc, t2cs = (int64_t)Hx * Hy * zc;
     const int64_t plane = (int64_t)Hx * Hy;
     void* dst = image ? w.gimg : w.gfree;
+    if (dd && !image && SC_PAIRED_GREEN && dd_green_applies(w.log2L[0], w.log2L[1], w.log2L[2], nx, ny, nz)) {
+        // double-FP32: the octant split as it is placed, then the paired
+        // transforms on the FP32 units (dreal buffers: 8 bytes, as double)
+        dreal* Gd = reinterpret_cast<dreal*>(G);
+        launch_pdl(k_igf_place_oct<dreal>, (unsigned)((3 * gcs + 127) / 128), 128, 0, s, (const double*)F, Gd, nx, ny,
+                   nz, ez0, kFpei / ((double)Lx * Ly * Lz));
+        SC_LAUNCH_CHECK("k_igf_place_oct");
+        if (!launch_dd_green(w.log2L[0], w.log2L[2], Gd, reinterpret_cast<dreal*>(T2), (dreal*)dst, nx, ny, nz, Hx,
+                             gcs, t2cs, m->gamma, (const ddc*)ctx->twdd, s))
+            return fail(SC_ERR_CUDA, "double-FP32 Green transform did not launch");
+        SC_LAUNCH_CHECK("double-FP32 Green transform");
+        m->launches += 3;
+        *fmt = 1;
+        *done = true;
+        return SC_OK;
+    }
+    launch_pdl(k_igf_place_oct<double>, (unsigned)((3 * gcs + 127) / 128), 128, 0, s, (const double*)F, G, nx, ny, nz,
+               ez0, kFpei / ((double)Lx * Ly * Lz));
+    SC_LAUNCH_CHECK("k_igf_place_oct");
     bool ok = SC_PAIRED_GREEN &&
               launch_green_xy_field<double>(w.log2L[0], w.log2L[1], G, T2, nx, ny, zc, Hx, gcs, t2cs, tw, s);
     if (ok) {
@@ -1065,63 +1087,81 @@ static int build_green_fp64_reduced(sc_mesh* m, bool image, double offz, cudaStr
 }
 
 template <>
-int build_green_any<double>(sc_mesh* m, bool image, double offz, cudaStream_t s) {
+int build_green_any<double>(sc_mesh* m, bool image, double offz, cudaStream_t s, bool dd, int* fmt) {
     bool done = false;
-    SC_TRY(build_green_fp64_reduced(m, image, offz, s, &done));
+    SC_TRY(build_green_fp64_reduced(m, image, offz, s, &done, dd, fmt));
     if (done) return SC_OK;
     SC_TRY(build_green<double>(m, image, offz, s));
     m->launches += 18;
     return SC_OK;
 }
 
-static bool key_matches(const GreenKey& k, const sc_mesh* m, double offz) {
+// fmt < 0: either format
+static bool key_matches(const GreenKey& k, const sc_mesh* m, double offz, int fmt = -1) {
     return k.valid && k.delta[0] == m->delta[0] && k.delta[1] == m->delta[1] && k.delta[2] == m->delta[2] &&
-           k.gamma == m->gamma && k.offset_z == offz;
+           k.gamma == m->gamma && k.offset_z == offz && (fmt < 0 || k.fmt == fmt);
 }
-static void set_key(GreenKey& k, const sc_mesh* m, double offz) {
+static void set_key(GreenKey& k, const sc_mesh* m, double offz, int fmt) {
     for (int d = 0; d < 3; ++d) k.delta[d] = m->delta[d];
     k.gamma = m->gamma;
     k.offset_z = offz;
+    k.fmt = fmt;
     k.valid = true;
+}
+
+// Whether the free-space spectrum is wanted in double-FP32: FP64 meshes in
+// double-FP32 mode, solves in free space (the FP64 image z pass reads the
+// FP64 one), every length within the register kernels, the caller's z pass
+// able to take it (dd_ok).
+static bool green_dd_wanted(const sc_mesh* m, int at_cathode, bool dd_ok) {
+    if (!dd_ok || at_cathode || m->precision != SC_PREC_FP64 || !m->df32) return false;
+    const NativeWork& w = m->nw;
+    const int eng = w.engine >= 0 ? w.engine : fft_engine();
+    return eng == 0 && w.log2L[0] > 0 && w.log2L[0] <= 8 && w.log2L[1] <= 8 && w.log2L[2] <= 8;
 }
 
 // Build (or reuse) the compressed Green spectra the solve needs.
 // Builds the free-space (image = false) or image spectrum unless the cached
 // one matches the geometry.
+// dd: build the free-space spectrum in double-FP32 (green_dd_wanted); the
+// double-FP32 z pass takes a cached FP64 one as well, the FP64 z passes
+// only that
 template <typename T>
-static int ensure_green_part(sc_mesh* m, bool image, cudaStream_t s) {
+static int ensure_green_part(sc_mesh* m, bool image, cudaStream_t s, bool dd = false) {
     NativeWork& w = m->nw;
     const double offz = image ? 2 * m->lo[2] + (m->hi[2] - m->lo[2]) : 0.0;  // free_space.jl:39
     GreenKey& key = image ? w.key_img : w.key_free;
-    if (m->green_cache && key_matches(key, m, offz)) return SC_OK;
+    if (m->green_cache && key_matches(key, m, offz, dd && !image ? -1 : 0)) return SC_OK;
     StageScope st(m->timer, SC_STAGE_GREEN, s);
-    SC_TRY(build_green_any<T>(m, image, offz, s));
-    set_key(key, m, offz);
+    int fmt = 0;
+    SC_TRY(build_green_any<T>(m, image, offz, s, dd && !image, &fmt));
+    set_key(key, m, offz, fmt);
     m->green_epoch++;
     return SC_OK;
 }
 
 template <typename T>
-static int ensure_green_t(sc_mesh* m, int at_cathode, cudaStream_t s) {
-    SC_TRY(ensure_green_part<T>(m, false, s));
+static int ensure_green_t(sc_mesh* m, int at_cathode, cudaStream_t s, bool dd_ok = true) {
+    SC_TRY(ensure_green_part<T>(m, false, s, green_dd_wanted(m, at_cathode, dd_ok)));
     if (at_cathode) SC_TRY(ensure_green_part<T>(m, true, s));
     return SC_OK;
 }
 
-bool native_green_stale(const sc_mesh* m, int at_cathode) {
+bool native_green_stale(const sc_mesh* m, int at_cathode, bool dd_ok) {
     const NativeWork& w = m->nw;
     const double offz = 2 * m->lo[2] + (m->hi[2] - m->lo[2]);  // free_space.jl:39
-    if (!(m->green_cache && key_matches(w.key_free, m, 0.0))) return true;
+    const int need = green_dd_wanted(m, at_cathode, dd_ok) ? -1 : 0;
+    if (!(m->green_cache && key_matches(w.key_free, m, 0.0, need))) return true;
     return at_cathode && !(m->green_cache && key_matches(w.key_img, m, offz));
 }
 
-int native_ensure_green(sc_mesh* m, int at_cathode, cudaStream_t s) {
+int native_ensure_green(sc_mesh* m, int at_cathode, cudaStream_t s, bool dd_ok) {
     if (m->precision == SC_PREC_MIXED) {
         SC_TRY(alloc_work<float>(m));
         return ensure_green_t<float>(m, at_cathode, s);
     }
     SC_TRY(alloc_work<double>(m));
-    return ensure_green_t<double>(m, at_cathode, s);
+    return ensure_green_t<double>(m, at_cathode, s, dd_ok);
 }
 
 // inverse y and x as one pass (k2_inv_yx) where it applies
@@ -1219,7 +1259,7 @@ static int solve_t(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green
         }
         // FP64 in free space, on request: the z pass in double-FP32, its
         // output kept in double-FP32 for the inverse passes
-        if (dd && launch2_dd_zpass(w.log2L[2], (const ddc*)B, (ddc*)C, Hx, Ly, nz, gv, twdd, s)) {
+        if (dd && launch2_dd_zpass(w.log2L[2], (const ddc*)B, (ddc*)C, Hx, Ly, nz, gv, w.key_free.fmt, twdd, s)) {
             c_dd = true;
             SC_LAUNCH_CHECK("k2_dd_zpass");
             goto zdone;
@@ -1427,9 +1467,9 @@ int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green_r
     return solve_t<double>(m, at_cathode, s, green_ready);
 }
 
-int native_green_async(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t* ready) {
+int native_green_async(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t* ready, bool dd_ok) {
     *ready = nullptr;
-    if (!native_green_stale(m, at_cathode)) return SC_OK;
+    if (!native_green_stale(m, at_cathode, dd_ok)) return SC_OK;
     // highest priority: the z pass waits for these builds, the deposit on
     // the caller's stream does not
     int least = 0, greatest = 0;
@@ -1456,7 +1496,7 @@ int native_green_async(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t* 
         if (st == SC_OK && e2 != cudaSuccess) st = cuda_fail(e2, "cudaEventRecord");
         cudaStreamWaitEvent(m->side, m->ev_join2, 0);
     } else {
-        st = native_ensure_green(m, at_cathode, m->side);
+        st = native_ensure_green(m, at_cathode, m->side, dd_ok);
     }
     const cudaError_t e = cudaEventRecord(m->ev_join, m->side);
     if (st != SC_OK || e != cudaSuccess) {

@@ -1073,10 +1073,10 @@ __global__ void __launch_bounds__(256, sizeof(Tr) == 4 ? 3 : 1) k3_green_xy(cons
 // k3_green_col; the remaining component runs through those kernels alone.
 template <typename T2, typename Tr>
 __device__ __forceinline__ void unpack4(T2 Zk, T2 Zm, Tr& e1, Tr& e2, Tr& p1, Tr& p2) {
-    e1 = Tr(0.5) * (Zk.x + Zm.x);
-    p2 = Tr(0.5) * (Zm.x - Zk.x);
-    e2 = Tr(0.5) * (Zk.y + Zm.y);
-    p1 = Tr(0.5) * (Zk.y - Zm.y);
+    e1 = Tr(0.5f) * (c_re(Zk) + c_re(Zm));
+    p2 = Tr(0.5f) * (c_re(Zm) - c_re(Zk));
+    e2 = Tr(0.5f) * (c_im(Zk) + c_im(Zm));
+    p1 = Tr(0.5f) * (c_im(Zk) - c_im(Zm));
 }
 
 // The FP32 Green build's near cells, for k4_green_xy to fill in: the FP64
@@ -1247,11 +1247,11 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
                     const int ax = lower ? t + E::R2 * s : L - t - E::R2 * s;
                     Tr e1 = 0, e2 = 0, o1 = 0, o2 = 0;
                     if (here) {
-                        if (ok0) e1 = (STG || rs) ? ep0[ax] : __ldcg(ep0 + ax);
-                        if (ok1) e2 = (STG || rs) ? ep0[nx + ax] : __ldcg(ep0 + nx + ax);
+                        if (ok0) e1 = (STG || rs) ? ep0[ax] : ldcg_r(ep0 + ax);
+                        if (ok1) e2 = (STG || rs) ? ep0[nx + ax] : ldcg_r(ep0 + nx + ax);
                         if (pair && (s > 0 || t > 0)) {  // odd: nothing at d = 0
-                            if (ok0) o1 = (STG || rs) ? op0[ax] : __ldcg(op0 + ax);
-                            if (ok1) o2 = (STG || rs) ? op0[nx + ax] : __ldcg(op0 + nx + ax);
+                            if (ok0) o1 = (STG || rs) ? op0[ax] : ldcg_r(op0 + ax);
+                            if (ok1) o2 = (STG || rs) ? op0[nx + ax] : ldcg_r(op0 + nx + ax);
                             if (!lower) o1 = -o1, o2 = -o2;
                         }
                     }
@@ -1269,8 +1269,8 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
                             if (ok0) e1 = ge[nx * y0 + ax];
                             if (ok1) e2 = ge[nx * y1 + ax];
                         } else {
-                            if (ok0) e1 = __ldcg(ge + (int64_t)nx * y0 + ax);
-                            if (ok1) e2 = __ldcg(ge + (int64_t)nx * y1 + ax);
+                            if (ok0) e1 = ldcg_r(ge + (int64_t)nx * y0 + ax);
+                            if (ok1) e2 = ldcg_r(ge + (int64_t)nx * y1 + ax);
                         }
                         // an odd line vanishes at d = 0 (the stored sample there is rounding)
                         if (pair && dx != 0) {
@@ -1278,8 +1278,8 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
                                 if (ok0) o1 = go[nx * y0 + ax];
                                 if (ok1) o2 = go[nx * y1 + ax];
                             } else {
-                                if (ok0) o1 = __ldcg(go + (int64_t)nx * y0 + ax);
-                                if (ok1) o2 = __ldcg(go + (int64_t)nx * y1 + ax);
+                                if (ok0) o1 = ldcg_r(go + (int64_t)nx * y0 + ax);
+                                if (ok1) o2 = ldcg_r(go + (int64_t)nx * y1 + ax);
                             }
                             if (dx < 0) o1 = -o1, o2 = -o2;
                         }
@@ -1345,14 +1345,14 @@ __global__ void __launch_bounds__(NTH, 1) k4_green_xy(Tr* G, Tr* __restrict__ T2
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const T2 wp = swt[(k * (d + u)) & (L - 1)];
-                    re[u] += Tr(2) * ts0[(d + u) * Hx + L / 2] * wp.x;             // even: 2 x(d) Re w^kd
-                    if (pair) im[u] += Tr(2) * ts1[(d + u) * Hx + L / 2] * wp.y;  // odd: 2i x(d) Im w^kd
+                    re[u] += Tr(2) * ts0[(d + u) * Hx + L / 2] * c_re(wp);             // even: 2 x(d) Re w^kd
+                    if (pair) im[u] += Tr(2) * ts1[(d + u) * Hx + L / 2] * c_im(wp);  // odd: 2i x(d) Im w^kd
                 }
             }
             for (; d < ny; ++d) {
                 const T2 wp = swt[(k * d) & (L - 1)];
-                re[0] += Tr(2) * ts0[d * Hx + L / 2] * wp.x;
-                if (pair) im[0] += Tr(2) * ts1[d * Hx + L / 2] * wp.y;
+                re[0] += Tr(2) * ts0[d * Hx + L / 2] * c_re(wp);
+                if (pair) im[0] += Tr(2) * ts1[d * Hx + L / 2] * c_im(wp);
             }
             out_e[(int64_t)k * Hx + L / 2] = ts0[L / 2] + ((re[0] + re[1]) + (re[2] + re[3]));
             if (pair) out_o[(int64_t)k * Hx + L / 2] = (im[0] + im[1]) + (im[2] + im[3]);
@@ -1497,11 +1497,11 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, sizeof(Tr) == 4 ? 3 : 1) k4
             const Tr* po = lower ? olo + o : ohi - o;
             Tr e1 = 0, e2 = 0, o1 = 0, o2 = 0;
             if (here) {
-                if (oka) e1 = __ldg(pe + fa);
-                if (okb) e2 = __ldg(pe + fb);
+                if (oka) e1 = ldg_r(pe + fa);
+                if (okb) e2 = ldg_r(pe + fb);
                 if (pair && (s > 0 || t > 0)) {
-                    if (oka) o1 = s2 * __ldg(po + fa);
-                    if (okb) o2 = s2 * __ldg(po + fb);
+                    if (oka) o1 = s2 * ldg_r(po + fa);
+                    if (okb) o2 = s2 * ldg_r(po + fb);
                     if (!lower) o1 = -o1, o2 = -o2;
                 }
             }
@@ -1515,12 +1515,12 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, sizeof(Tr) == 4 ? 3 : 1) k4
             Tr e1 = 0, e2 = 0, o1 = 0, o2 = 0;
             if (d != L) {
                 const int64_t o = (int64_t)(d < 0 ? -d : d) * as_in;
-                if (oka) e1 = __ldg(ie + fa + o);
-                if (okb) e2 = __ldg(ie + fb + o);
+                if (oka) e1 = ldg_r(ie + fa + o);
+                if (okb) e2 = ldg_r(ie + fb + o);
                 // an odd line vanishes at d = 0 (the stored sample there is rounding)
                 if (pair && d != 0) {
-                    if (oka) o1 = s2 * __ldg(io + fa + o);
-                    if (okb) o2 = s2 * __ldg(io + fb + o);
+                    if (oka) o1 = s2 * ldg_r(io + fa + o);
+                    if (okb) o2 = s2 * ldg_r(io + fb + o);
                     if (d < 0) o1 = -o1, o2 = -o2;
                 }
             }
@@ -1696,8 +1696,17 @@ template <bool INV, typename TI, typename TO>
 bool launch2_dd_col(int logL, const TI* in, TO* out, int ncols, int nbatch, int ncomp, int n_valid, int n_store,
                     int64_t as_in, int64_t bs_in, int64_t cs_in, int64_t as_out, int64_t bs_out, int64_t cs_out,
                     const ddc* tw, cudaStream_t s);
-bool launch2_dd_zpass(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz, const GreenView& gv, const ddc* tw,
-                      cudaStream_t s);
+// The FP64 free-space Green transform in double-FP32 (dd_green.cu): the
+// paired x+y and z passes of the field kernel with dreal values, from the
+// octant G to the spectrum `out` (the layout of the FP64 build).  Applies to
+// power-of-two meshes (n = L/2 on every axis) with Lx = Ly in {64, 128} and
+// Lz in {64, 128, 256}; dd_green_applies says whether.
+bool dd_green_applies(int logLx, int logLy, int logLz, int nx, int ny, int nz);
+bool launch_dd_green(int logLxy, int logLz, dreal* G, dreal* T2, dreal* out, int nx, int ny, int nz, int Hx,
+                     int64_t gcs, int64_t t2cs, double gamma, const ddc* tw, cudaStream_t s);
+// gfmt: the free-space Green spectrum is double-FP32 (dreal) rather than FP64
+bool launch2_dd_zpass(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz, const GreenView& gv, int gfmt,
+                      const ddc* tw, cudaStream_t s);
 bool launch2_dd_inv_x(int logL, const ddc* D, dnode4* E4, int nx, int rows, int Hx, int64_t cs, const ddc* tw,
                       cudaStream_t s);
 

@@ -134,6 +134,7 @@ struct GreenKey {
     double delta[3];
     double gamma;
     double offset_z;
+    int fmt = 0;  // 0: the mesh's real type; 1: double-FP32 (dreal), for the double-FP32 z pass
     bool valid = false;
 };
 
@@ -327,7 +328,9 @@ void host_pipe_release(sc_mesh* m);
 // change through their keys
 int mesh_set_geometry(sc_mesh* m, const double lo[3], const double hi[3], const double delta[3]);
 // true when the next solve would (re)build a Green spectrum
-bool native_green_stale(const sc_mesh* m, int at_cathode);
+// dd_ok: the caller's z pass takes a double-FP32 free-space spectrum (every
+// forward solve; not the FP64 adjoint's z pass)
+bool native_green_stale(const sc_mesh* m, int at_cathode, bool dd_ok = true);
 // early: load the positions before waiting for the preceding grid (only
 // where no preceding grid writes them: the kick, after its own passes)
 int gather_launch(sc_mesh* m, const void* x, const void* y, const void* z, int64_t n,
@@ -355,8 +358,8 @@ int native_solve(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t green_r
 // mesh's side stream (forked from s) and returns in *ready the event that
 // marks its end; otherwise *ready = nullptr.  The spectra do not depend on
 // rho, so the caller's deposit overlaps the build.
-int native_green_async(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t* ready);
-int native_ensure_green(sc_mesh* m, int at_cathode, cudaStream_t s);
+int native_green_async(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t* ready, bool dd_ok = true);
+int native_ensure_green(sc_mesh* m, int at_cathode, cudaStream_t s, bool dd_ok = true);
 int native_autotune(sc_mesh* m, cudaStream_t s, int* choice);
 int native_solve_noalloc(const int32_t* grid, const double* delta, double gamma, const float* rho, float* efield,
                          cudaStream_t s);

@@ -61,6 +61,28 @@ def test_adjoint_vs_torch_autograd(sc, cuda, at_cathode, n, grid):
             assert err < tol, f"{prec} d/d{name}: {err:.3e}"
 
 
+@pytest.mark.parametrize("grid", [(32, 32, 64), (12, 10, 14)])
+def test_adjoint_fp64_df32_mode(sc, cuda, grid):
+    """An FP64 mesh in double-FP32 mode gives the FP64 mode's adjoint: its
+    forward recompute runs in double-FP32, and its adjoint z pass in FP64 on
+    the FP64 Green spectrum, rebuilt where the forward kick left the
+    double-FP32 one cached (32x32x64)."""
+    n = 5000
+    x, y, z = bunch(n, 5)
+    q = np.full(n, 1e-9 / n)
+    lo, hi = (-5e-3,) * 3, (5e-3,) * 3
+    g, gg = loss_and_upstream(n, grid, 6)
+    out = {}
+    for mode in ("fp64", "df32"):
+        m = sc.Mesh3D(grid, lo, hi, precision="fp64", gamma=2.0)
+        m.set_fp64_arithmetic(mode)
+        sc.kick(m, x, y, z, q)  # leaves this mode's Green spectrum cached
+        out[mode] = [t.cpu().numpy() for t in sc.kick_adjoint(m, x, y, z, q, g[0], g[1], g[2], gEgrid=gg)]
+    for name, a, b in zip("xyzq", out["df32"], out["fp64"]):
+        err = rel(a, b)
+        assert err < 1e-11, f"d/d{name}: {err:.3e}"
+
+
 def test_adjoint_vs_finite_differences(sc, cuda):
     """FP64 central differences of L = sum_i g.E(x_i) + sum_n G.E_n on 32
     random particles whose perturbation stays inside their cell."""

@@ -401,10 +401,13 @@ def test_fft_engines_agree(sc, cuda, grid, cath, first):
                                        ((24, 12, 33), True)])
 def test_fp64_df32_arithmetic(sc, cuda, grid, cath):
     """FP64 meshes in double-FP32 mode (the atomic deposit, the x and y
-    passes, the z pass in free space, the interpolation) against FP64 mode on
-    the same deposit, and against the oracle at the FP64 tolerance.
-    Double-FP32 carries 48-bit significands, so the fields agree to ~1e-14 of
-    their maximum; 1e-12 is asserted.  nz = L/2 (64x64x128, 32x32x64, 8x8x128) and nz < L/2
+    passes, the z pass and the Green transform in free space, the
+    interpolation) against FP64 mode on the same deposit, and against the
+    oracle at the FP64 tolerance.  Double-FP32 carries 48-bit significands,
+    so the fields agree to ~1e-14 of their maximum; 1e-12 is asserted.  The
+    Green spectrum is rebuilt on every solve, so the double-FP32 solves take
+    the double-FP32 Green transform where it applies (64x64x128,
+    32x32x64).  nz = L/2 (64x64x128, 32x32x64, 8x8x128) and nz < L/2
     (12x20x33, 3x5x9) take the two compile-time z patterns; with the cathode
     image the z pass stays FP64 and the inverse y pass reads its FP64
     output."""
@@ -414,6 +417,7 @@ def test_fp64_df32_arithmetic(sc, cuda, grid, cath):
         z = np.abs(z) + 0.1e-3
     q = np.full(n, 1e-9 / n)
     m = sc.Mesh3D(grid, x, y, z, precision="fp64", gamma=4.0)
+    m.set_green_cache(False)
     out, part, part32 = {}, {}, {}
     x32, y32, z32 = (v.astype(np.float32) for v in (x, y, z))
     for mode in ("fp64", "df32"):
