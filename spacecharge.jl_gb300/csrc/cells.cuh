@@ -51,63 +51,79 @@ inline AxisP make_axis(double lo, double delta, int n) {
 }
 
 // ------------------------------------------------ FP64 <-> FP32 with INT ops
+// These issue no FP64 instruction on any path: the GB300's FP64 pipe is
+// slow enough that even a conversion in a rarely taken branch, once the
+// compiler turns the branch into predicated code, is paid on every call.
+//
 // x = h + r exactly up to the rounding of r: h is x truncated to 24
-// significant bits, r the remainder rounded to FP32.  Inputs outside the
-// FP32 normal range give h = x rounded by the hardware path (rare).
+// significant bits, r the remainder rounded to FP32.  Outside the FP32
+// normal range h is +-0 (|x| < 2^-126) or +-inf (|x| >= 2^128; NaN stays
+// NaN), with r = 0; below |x| ~ 2^-104 r flushes to zero.
 __device__ __forceinline__ void split_f64(double x, float& h, float& r) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
     const int e = (int)((hi >> 20) & 0x7FF);
     const unsigned sgn = hi & 0x80000000u;
-    if (e >= 1023 - 126 && e <= 1023 + 127) {
-        h = __uint_as_float(sgn | ((unsigned)(e - 1023 + 127) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29));
-        // remainder: (lo & (2^29-1)) * 2^(e-1075), formed as (m * 2^-29) *
-        // 2^(e-1046); below |x| ~ 2^-104 the remainder flushes to zero.
-        const unsigned m = lo & 0x1FFFFFFFu;
-        const float mf = __uint2float_rn(m) * 1.862645149230957e-09f;  // m * 2^-29
-        const int pe = e - 1075 + 29 + 127;  // biased exponent of 2^(e-1046)
-        const float scale = pe > 0 ? __uint_as_float((unsigned)pe << 23) : 0.0f;
-        r = __uint_as_float(__float_as_uint(mf * scale) | sgn);
-    } else if (e == 0) {
-        h = __uint_as_float(sgn);  // +-0 (FP64 subnormals flush to 0)
-        r = 0.0f;
-    } else {
-        h = (float)x;  // far outside any mesh: the bounds test rejects it
-        r = 0.0f;
-    }
+    const unsigned top = ((hi & 0xFFFFFu) << 3) | (lo >> 29);  // 23 fraction bits
+    unsigned hb;
+    if (e >= 1023 - 126 && e <= 1023 + 127)
+        hb = sgn | ((unsigned)(e - 1023 + 127) << 23) | top;
+    else if (e < 1023 - 126)
+        hb = sgn;
+    else
+        hb = sgn | 0x7F800000u | ((e == 2047 && (top | (lo & 0x1FFFFFFFu))) ? 0x400000u : 0u);
+    h = __uint_as_float(hb);
+    // remainder: (lo & (2^29-1)) * 2^(e-1075), formed as (m * 2^-29) *
+    // 2^(e-1046)
+    const unsigned m = lo & 0x1FFFFFFFu;
+    const float mf = __uint2float_rn(m) * 1.862645149230957e-09f;  // m * 2^-29
+    const int pe = e - 1075 + 29 + 127;                             // biased exponent of 2^(e-1046)
+    const float scale = (pe > 0 && e <= 1023 + 127) ? __uint_as_float((unsigned)pe << 23) : 0.0f;
+    r = __uint_as_float(__float_as_uint(mf * scale) | sgn);
 }
 __device__ __forceinline__ void split_f64(float x, float& h, float& r) {
     h = x;
     r = 0.0f;
 }
 
-// Round an FP64 value to FP32 (nearest, ties away) with integer ops only.
+// Round an FP64 value to FP32 (nearest, ties away) with integer ops only;
+// below the FP32 normal range +-0, from 2^128 on +-inf (NaN stays NaN).
 __device__ __forceinline__ float f64_to_f32(double x) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
     const int e = (int)((hi >> 20) & 0x7FF);
-    if (e >= 1023 - 126 && e <= 1023 + 126) {
-        const unsigned sgn = hi & 0x80000000u;
-        unsigned f = ((unsigned)(e - 1023 + 127) << 23) | ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-        f += (lo >> 28) & 1u;  // round half away from zero (carry may bump the exponent)
-        return __uint_as_float(sgn | f);
-    }
-    if (e == 0) return __uint_as_float(hi & 0x80000000u);
-    return (float)x;
+    const unsigned sgn = hi & 0x80000000u;
+    const unsigned top = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    unsigned f;
+    if (e >= 1023 - 126 && e <= 1023 + 127)
+        f = (((unsigned)(e - 1023 + 127) << 23) | top) + ((lo >> 28) & 1u);  // round half away; a carry
+                                                                            // may bump the exponent (to inf)
+    else if (e < 1023 - 126)
+        f = 0u;
+    else
+        f = 0x7F800000u | ((e == 2047 && (top | (lo & 0x1FFFFFFFu))) ? 0x400000u : 0u);
+    return __uint_as_float(sgn | f);
 }
 __device__ __forceinline__ float f64_to_f32(float x) { return x; }
 
-// Widen an FP32 value to FP64 exactly with integer ops only.
+// Widen an FP32 value to FP64 exactly with integer ops only (zeros,
+// subnormals, infinities and NaN included).
 __device__ __forceinline__ double f32_to_f64(float v) {
     const unsigned u = __float_as_uint(v);
-    const unsigned e = (u >> 23) & 0xFF;
+    const unsigned e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+    const unsigned long long sg = (unsigned long long)(u & 0x80000000u) << 32;
+    unsigned long long b;
     if (e != 0 && e != 0xFF) {
-        const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
-                                     ((unsigned long long)(e + 896) << 52) |
-                                     ((unsigned long long)(u & 0x7FFFFFu) << 29);
-        return __longlong_as_double((long long)b);
+        b = sg | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)m << 29);
+    } else if (e == 0xFF) {
+        b = sg | (0x7FFull << 52) | ((unsigned long long)m << 29);
+    } else if (m == 0) {
+        b = sg;
+    } else {  // subnormal: m * 2^-149, normalised
+        const int lz = __clz(m);
+        b = sg | ((unsigned long long)(905 - lz) << 52) | ((unsigned long long)((m << (lz - 8)) & 0x7FFFFFu) << 29);
     }
-    return (double)v;  // zero, subnormal, inf, nan
+    return __longlong_as_double((long long)b);
 }
 
 template <typename P>

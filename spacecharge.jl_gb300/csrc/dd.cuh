@@ -85,56 +85,20 @@ __device__ __forceinline__ ddc dd_scale(ddc a, float gh, float gl) {
     return dd_renorm(p, e);
 }
 
-// A double split into hi + lo with integer operations only (no FP64
-// instruction, not even in a branch the compiler could if-convert): hi keeps
-// the top 24 significand bits (truncated), lo is the remaining 29 bits
-// rounded to FP32, so hi + lo equals x to 2^-47 relative.  The FP32 range
-// bounds it: below |x| = 2^-103 lo flushes to zero (gradually from 2^-126
-// on), below 2^-126 hi too; from 2^128 on hi is +-inf (NaN stays NaN).
-__device__ __forceinline__ void dd_split(double x, float& hi, float& lo) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned bh = (unsigned)(b >> 32), bl = (unsigned)b;
-    const int e = (int)((bh >> 20) & 0x7FF);
-    const unsigned sgn = bh & 0x80000000u;
-    const unsigned top = ((bh & 0xFFFFFu) << 3) | (bl >> 29);  // 23 fraction bits
-    unsigned hb;
-    if (e >= 897 && e <= 1150)
-        hb = sgn | ((unsigned)(e - 896) << 23) | top;
-    else if (e < 897)
-        hb = sgn;
-    else
-        hb = sgn | 0x7F800000u | ((e == 2047 && (top | (bl & 0x1FFFFFFFu))) ? 0x400000u : 0u);
-    hi = __uint_as_float(hb);
-    // lo = rem * 2^(e - 1075) = (rem * 2^-29) * 2^(e - 1046)
-    const int pe = e - 1046 + 127;
-    const float sc = (pe >= 1 && e <= 1150) ? __uint_as_float((unsigned)pe << 23) : 0.0f;
-    lo = __uint_as_float(__float_as_uint(__uint2float_rn(bl & 0x1FFFFFFFu) * 1.862645149230957e-09f * sc) | sgn);
-}
-
+// A double split into hi + lo with integer operations only (split_f64 of
+// cells.cuh: no FP64 instruction, not even in a branch the compiler could
+// if-convert): hi keeps the top 24 significand bits (truncated), lo the
+// remaining 29 rounded to FP32, so hi + lo equals x to 2^-47 relative
+// within FP32's range (lo flushes below |x| ~ 2^-104, hi below 2^-126;
+// +-inf from 2^128 on).
+__device__ __forceinline__ void dd_split(double x, float& hi, float& lo) { split_f64(x, hi, lo); }
 __device__ __forceinline__ void dd_split(float x, float& hi, float& lo) {
     hi = x;
     lo = 0.0f;
 }
 
 // An FP32 value widened to FP64 exactly, with integer operations only
-// (zeros, subnormals, infinities and NaN included).
-__device__ __forceinline__ double dd_widen(float v) {
-    const unsigned u = __float_as_uint(v);
-    const unsigned e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
-    const unsigned long long sg = (unsigned long long)(u & 0x80000000u) << 32;
-    unsigned long long b;
-    if (e != 0 && e != 0xFF) {
-        b = sg | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)m << 29);
-    } else if (e == 0xFF) {
-        b = sg | (0x7FFull << 52) | ((unsigned long long)m << 29);
-    } else if (m == 0) {
-        b = sg;
-    } else {  // subnormal: m * 2^-149, normalised
-        const int lz = __clz(m);
-        b = sg | ((unsigned long long)(905 - lz) << 52) | ((unsigned long long)((m << (lz - 8)) & 0x7FFFFFu) << 29);
-    }
-    return __longlong_as_double((long long)b);
-}
+__device__ __forceinline__ double dd_widen(float v) { return f32_to_f64(v); }
 
 // A real double-FP32 value, for kernels written over a real type (the Green
 // transform): the arithmetic of the complex pairs above, one lane.
