@@ -163,14 +163,15 @@ int sc_mesh_set_green_cache(sc_mesh* mesh, int enabled);
  * reference).  SC_FP64_ARITH_FP64 (default): FP64 throughout.
  * SC_FP64_ARITH_DF32: the atomic deposit's weights, the x and y transform
  * passes, the z pass (forward z transform, Green products, three inverse z
- * transforms; free space) and the trilinear interpolation carry each value
- * as the unevaluated sum of two FP32 numbers (48-bit significands, FP32's
- * exponent range, magnitudes from 2^-103 to 2^128), with FP64 inputs and
- * outputs; fields move by about 1e-14 of their maximum.  The GB300 runs
- * FP64 at 1/64 of its FP32 rate, so this takes those passes off the FP64
- * units.  The Green function stays FP64; meshes with a transform above 256
- * points keep FP64 transforms, and the z pass with the cathode image stays
- * FP64.  Other precisions: SC_ERR_INVALID. */
+ * transforms; free space), the trilinear interpolation and the free-space
+ * Green function's transform carry each value as the unevaluated sum of two
+ * FP32 numbers (48-bit significands, FP32's exponent range, magnitudes from
+ * 2^-103 to 2^128), with FP64 inputs and outputs; fields move by about
+ * 1e-14 of their maximum.  The GB300 runs FP64 at 1/64 of its FP32 rate, so
+ * this takes those passes off the FP64 units.  The Green function's corner
+ * antiderivative stays FP64; meshes with a transform above 256 points keep
+ * FP64 transforms, and the z pass with the cathode image stays FP64.  Other
+ * precisions: SC_ERR_INVALID. */
 #define SC_FP64_ARITH_FP64 0
 #define SC_FP64_ARITH_DF32 1
 int sc_mesh_set_fp64_arithmetic(sc_mesh* mesh, int mode);
