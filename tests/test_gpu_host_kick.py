@@ -18,15 +18,18 @@ def bunch(n, seed):
 
 
 @pytest.mark.parametrize("prec,mode", [("mixed", "vector"), ("mixed", "atomic"), ("mixed", "sorted"),
-                                       ("fp64", "atomic"), ("plain64", "atomic")])
+                                       ("fp64", "atomic"), ("df32", "atomic"), ("plain64", "atomic")])
 @pytest.mark.parametrize("cath", [False, True])
 def test_kick_host_matches_device_kick(sc, cuda, prec, mode, cath):
+    """df32: an FP64 mesh in double-FP32 mode."""
     import torch
 
     n = 300_001  # not a multiple of the chunk count
     x, y, z = bunch(n, 5)
     q = np.full(n, 1e-9 / n)
-    m = sc.Mesh3D((24, 20, 40), x, y, z, precision=prec, gamma=3.0)
+    m = sc.Mesh3D((24, 20, 40), x, y, z, precision="fp64" if prec == "df32" else prec, gamma=3.0)
+    if prec == "df32":
+        m.set_fp64_arithmetic("df32")
     if prec != "plain64":
         m.set_kick_mode(mode)
     hx, hy, hz, hq = (torch.from_numpy(a).pin_memory() for a in (x, y, z, q))

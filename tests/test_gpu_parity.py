@@ -446,6 +446,16 @@ def test_fp64_df32_arithmetic(sc, cuda, grid, cath):
         rho[mode] = host(m.rho)
     assert relerr(rho["df32"], rho["fp64"]) < 1e-13
     assert relerr(rho["df32"], om.rho) < RHO_TOL["fp64"]
+    # the kick, replayed as a captured graph with the same arrays
+    import torch
+
+    m.set_fp64_arithmetic("df32")
+    dev = [torch.from_numpy(v).cuda() for v in (x, y, z, q)]
+    outs = [torch.empty(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    for _ in range(3):
+        sc.kick(m, *dev, at_cathode=cath, out=outs)
+        for a, b in zip(outs, part["fp64"]):
+            assert relerr(host(a), b) < 1e-12
     m.set_fp64_arithmetic("fp64")
     sc.deposit(m, x, y, z, q, mode="deterministic")
     sc.solve(m, at_cathode=cath)
