@@ -283,10 +283,14 @@ def bench_batch_graph(sc, torch, flush, stream, steps, warmup):
 
 def bench_potential(sc, torch, dev, flush, stream, steps, warmup):
     """Scalar potential of the headline bunch's charge (sc_solve_potential),
-    mixed and FP64 meshes, the potential Green function rebuilt every solve."""
+    mixed and FP64 meshes (FP64 mode and double-FP32 mode), the potential
+    Green function rebuilt every solve."""
     res = {"workload": WORKLOAD + ", scalar potential of the deposited charge", "green": "rebuilt every solve"}
-    for prec in ("mixed", "fp64", "plain64"):
-        m = sc.Mesh3D(GRID, *BOUNDS, precision=prec, gamma=GAMMA, total_charge=QTOT)
+    for prec in ("mixed", "fp64", "fp64_df32", "plain64"):
+        m = sc.Mesh3D(GRID, *BOUNDS, precision="fp64" if prec == "fp64_df32" else prec, gamma=GAMMA,
+                      total_charge=QTOT)
+        if prec == "fp64_df32":
+            m.set_fp64_arithmetic("df32")
         sc.deposit(m, *dev)
         m.set_green_cache(False)
         for _ in range(warmup):

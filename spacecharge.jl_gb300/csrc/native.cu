@@ -1507,8 +1507,10 @@ int native_green_async(sc_mesh* m, int at_cathode, cudaStream_t s, cudaEvent_t* 
     return SC_OK;
 }
 
+// dd: the FP64 mesh's forward passes in double-FP32 (B then holds
+// double-FP32 values); the caller checks native_dd_applies
 template <typename T>
-static int forward_t(sc_mesh* m, cudaStream_t s) {
+static int forward_t(sc_mesh* m, cudaStream_t s, bool dd) {
     using T2 = typename Cplx<T>::T2;
     DeviceCtx* ctx = nullptr;
     SC_TRY(device_ctx(&ctx));
@@ -1521,6 +1523,16 @@ static int forward_t(sc_mesh* m, cudaStream_t s) {
     const int eng = w.engine >= 0 ? w.engine : fft_engine();
     const bool two = std::is_same<T, float>::value && eng == 0;
     const int lgWy = w.lgW >= 0 ? w.lgW : pick_cols(w.log2L[1]);
+    if (std::is_same<T, double>::value && dd) {
+        const ddc* twdd = (const ddc*)ctx->twdd;
+        if (!launch2_dd_fwd_x(w.log2L[0], (const double*)m->rho, (ddc*)w.A, nx, rows, Hx, twdd, s) ||
+            !launch2_dd_col<false>(w.log2L[1], (const ddc*)w.A, (ddc*)w.B, Hx, nz, 1, ny, Ly, Hx, (int64_t)Hx * ny, 0,
+                                   Hx, (int64_t)Hx * Ly, 0, twdd, s))
+            return fail(SC_ERR_CUDA, "double-FP32 forward passes did not launch");
+        SC_LAUNCH_CHECK("double-FP32 forward x, y");
+        m->launches += 2;
+        return SC_OK;
+    }
     if (two && SC_FUSED_FWD_XY &&
         launch2_fwd_xy(w.log2L[0], w.log2L[1], (const float*)m->rho, (float2*)w.B, nx, ny, nz, Hx, (const float2*)tw,
                        s, m->fused_smem_cap)) {
@@ -1541,9 +1553,16 @@ static int forward_t(sc_mesh* m, cudaStream_t s) {
     return SC_OK;
 }
 
-int native_forward(sc_mesh* m, cudaStream_t s) {
-    if (m->precision == SC_PREC_MIXED) return forward_t<float>(m, s);
-    return forward_t<double>(m, s);
+bool native_dd_applies(const sc_mesh* m) {
+    if (m->precision != SC_PREC_FP64 || !m->df32) return false;
+    const NativeWork& w = m->nw;
+    const int eng = w.engine >= 0 ? w.engine : fft_engine();
+    return eng == 0 && w.log2L[0] > 0 && w.log2L[0] <= 8 && w.log2L[1] <= 8 && w.log2L[2] <= 8;
+}
+
+int native_forward(sc_mesh* m, cudaStream_t s, bool dd) {
+    if (m->precision == SC_PREC_MIXED) return forward_t<float>(m, s, false);
+    return forward_t<double>(m, s, dd);
 }
 
 int native_release(sc_mesh* m) {

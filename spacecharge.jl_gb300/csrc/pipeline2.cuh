@@ -1709,6 +1709,10 @@ bool launch2_dd_zpass(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz, co
                       const ddc* tw, cudaStream_t s);
 bool launch2_dd_inv_x(int logL, const ddc* D, dnode4* E4, int nx, int rows, int Hx, int64_t cs, const ddc* tw,
                       cudaStream_t s);
+// the scalar potential's z pass and inverse x pass (dd_pot.cu)
+bool launch2_dd_zpass_pot(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz, const double* pf, const double2* pi,
+                          int image, int Hy, const ddc* tw, cudaStream_t s);
+bool launch2_dd_inv_x1(int logL, const ddc* D, dnode4* E4, int nx, int rows, int Hx, const ddc* tw, cudaStream_t s);
 
 static bool launch2_adj_zpass(int logL, const float2* C, float2* B, int Hx, int Ly, int nz, const GreenView& gv,
                               const float2* tw, cudaStream_t s) {

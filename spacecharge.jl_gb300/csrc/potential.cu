@@ -481,13 +481,32 @@ static int potential_t(sc_mesh* m, int at_cathode, void* phi, cudaStream_t s) {
     if (st == SC_OK && at_cathode) st = pot_green<T>(m, true, m->side);
     const cudaError_t ej = cudaEventRecord(m->ev_join, m->side);
     if (st == SC_OK && ej != cudaSuccess) st = cuda_fail(ej, "cudaEventRecord");
-    if (st == SC_OK) st = native_forward(m, s);
+    // FP64 meshes in double-FP32 mode: every pass but the Green build in
+    // double-FP32 (dd_xy.cu, dd_pot.cu)
+    const bool dd = native_dd_applies(m);
+    if (st == SC_OK) st = native_forward(m, s, dd);
     cudaStreamWaitEvent(s, m->ev_join, 0);  // joined on every path
     SC_TRY(st);
     DeviceCtx* ctx = nullptr;
     SC_TRY(device_ctx(&ctx));
     const T2* tw = twiddles<T>(ctx);
     T2* C = (T2*)w.C;
+    if (dd) {
+        const ddc* twdd = (const ddc*)ctx->twdd;
+        const int rows = ny * nz;
+        if (!launch2_dd_zpass_pot(w.log2L[2], (const ddc*)w.B, (ddc*)C, Hx, Ly, nz, (const double*)w.pfree,
+                                  (const double2*)w.pimg, at_cathode ? 1 : 0, Hy, twdd, s) ||
+            !launch2_dd_col<true>(w.log2L[1], (const ddc*)C, (ddc*)w.A, Hx, nz, 1, Ly, ny, Hx, (int64_t)Hx * Ly, 0, Hx,
+                                  (int64_t)Hx * ny, 0, twdd, s) ||
+            !launch2_dd_inv_x1(w.log2L[0], (const ddc*)w.A, (dnode4*)m->efield, nx, rows, Hx, twdd, s))
+            return fail(SC_ERR_CUDA, "double-FP32 potential passes did not launch");
+        SC_LAUNCH_CHECK("double-FP32 potential z, y, x");
+        m->launches += 3;
+        launch_pdl(k_lane3<T>, (unsigned)((m->N + 255) / 256), 256, 0, s, (const T*)m->efield, (T*)phi, m->N);
+        SC_LAUNCH_CHECK("k_lane3");
+        m->launches += 1;
+        return SC_OK;
+    }
     const bool two_z = std::is_same<T, float>::value && (w.engine >= 0 ? w.engine : fft_engine()) == 0;
     if (two_z && launch2_zpass_pot(w.log2L[2], (const float2*)w.B, (float2*)C, Hx, Ly, nz, (const float*)w.pfree,
                                    (const float2*)w.pimg, at_cathode ? 1 : 0, Hy, (const float2*)tw, s)) {

@@ -369,7 +369,10 @@ int adjoint_launch(sc_mesh* m, const void* x, const void* y, const void* z, cons
 int native_release(sc_mesh* m);
 // the forward x and y transforms of the mesh's rho into the workspace's B
 // (the field solve's, alone on the GPU: fused where the plane fits)
-int native_forward(sc_mesh* m, cudaStream_t s);
+// dd: FP64 meshes, the forward passes in double-FP32 (native_dd_applies)
+int native_forward(sc_mesh* m, cudaStream_t s, bool dd = false);
+// FP64 mesh in double-FP32 mode whose lengths fit the double-FP32 passes
+bool native_dd_applies(const sc_mesh* m);
 // scalar potential of the mesh's rho on the hand-written pipeline (T phi[N],
 // x fastest); SC_ERR_UNSUPPORTED where a transform is longer than 256
 int native_potential(sc_mesh* m, int at_cathode, void* phi, cudaStream_t s);

@@ -15,9 +15,10 @@ def rel(a, b):
     return np.abs(a - b).max() / np.abs(b).max()
 
 
-@pytest.mark.parametrize("prec,tol", [("plain64", 1e-10), ("fp64", 1e-10), ("mixed", 1e-5)])
+@pytest.mark.parametrize("prec,tol", [("plain64", 1e-10), ("fp64", 1e-10), ("df32", 1e-10), ("mixed", 1e-5)])
 @pytest.mark.parametrize("cath,gamma", [(False, 1.0), (False, 5.0), (True, 1.5)])
 def test_potential_matches_oracle(sc, cuda, prec, tol, cath, gamma):
+    """df32: an FP64 mesh in double-FP32 mode."""
     rng = np.random.default_rng(3)
     n = 30_000
     x, y, z = rng.standard_normal((3, n)).clip(-4.5, 4.5) * np.array([[1e-3], [1.5e-3], [0.4e-3]])
@@ -28,11 +29,16 @@ def test_potential_matches_oracle(sc, cuda, prec, tol, cath, gamma):
     om = O.mesh_auto(grid, x, y, z, gamma=gamma)
     O.deposit(om, x, y, z, q)
     ref = O.solve_potential(om, at_cathode=cath)
-    m = sc.Mesh3D(grid, x, y, z, precision=prec, gamma=gamma)
+    m = sc.Mesh3D(grid, x, y, z, precision="fp64" if prec == "df32" else prec, gamma=gamma)
+    if prec == "df32":
+        m.set_fp64_arithmetic("df32")
     sc.deposit(m, x, y, z, q)
     phi = sc.solve_potential(m, at_cathode=cath)
     assert tuple(phi.shape) == grid
     assert rel(phi.cpu().numpy(), ref) < tol
+    if prec == "df32":  # against FP64 mode on the same deposit
+        m.set_fp64_arithmetic("fp64")
+        assert rel(phi.cpu().numpy(), sc.solve_potential(m, at_cathode=cath).cpu().numpy()) < 1e-12
 
 
 def test_minus_grad_phi_is_e(sc, cuda):
@@ -54,7 +60,7 @@ def test_minus_grad_phi_is_e(sc, cuda):
     assert np.abs(ex[7:23, 7:23, 7:23] - core).max() < 0.03 * np.abs(core).max()
 
 
-@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("mixed", 1e-5)])
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("df32", 1e-10), ("mixed", 1e-5)])
 @pytest.mark.parametrize("grid,gamma,cath", [((40, 36, 64), 10.0, False), ((32, 32, 48), 3.0, True),
                                              ((12, 10, 150), 2.0, False)])
 def test_potential_larger_grids(sc, cuda, prec, tol, grid, gamma, cath):
@@ -70,7 +76,9 @@ def test_potential_larger_grids(sc, cuda, prec, tol, grid, gamma, cath):
     om = O.mesh_auto(grid, x, y, z, gamma=gamma)
     O.deposit(om, x, y, z, q)
     ref = O.solve_potential(om, at_cathode=cath)
-    m = sc.Mesh3D(grid, x, y, z, precision=prec, gamma=gamma)
+    m = sc.Mesh3D(grid, x, y, z, precision="fp64" if prec == "df32" else prec, gamma=gamma)
+    if prec == "df32":
+        m.set_fp64_arithmetic("df32")
     sc.deposit(m, x, y, z, q)
     phi = sc.solve_potential(m, at_cathode=cath)
     assert rel(phi.cpu().numpy(), ref) < tol
