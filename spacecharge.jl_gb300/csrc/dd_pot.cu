@@ -16,10 +16,10 @@ namespace sc {
 // spectra are copied to shared memory with cp.async during the forward
 // transform; the forward spectrum stays in shared memory for the image
 // term.  HALF: nz = L/2.
-template <int L, bool HALF>
+template <int L, bool HALF, typename TG>
 __global__ void __launch_bounds__(kColW * F2<L>::NT, 1)
     k2_dd_zpass_pot(const ddc* __restrict__ B, ddc* __restrict__ C, int Hx, int Ly, int nz,
-                    const double* __restrict__ pf, const double2* __restrict__ pi, int image, int Hy,
+                    const TG* __restrict__ pf, const double2* __restrict__ pi, int image, int Hy,
                     const ddc* __restrict__ tw) {
     using E = F2<L>;
     constexpr int RL = E::R1, HZ = L / 2 + 1;
@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, 1)
     ddc* xb = reinterpret_cast<ddc*>(smraw);
     ddc* spec = xb + kColW * E::S;
     double2* gis = reinterpret_cast<double2*>(spec + kColW * E::S);  // [HZ][kColW] image spectrum
-    double* gs = reinterpret_cast<double*>(gis + HZ * kColW);         // [HZ][kColW] free-space spectrum
+    TG* gs = reinterpret_cast<TG*>(gis + HZ * kColW);                 // [HZ][kColW] free-space spectrum
     const int c = threadIdx.x % kColW, t = threadIdx.x / kColW;
     const int64_t plane = (int64_t)Hx * Ly;
     const int f = blockIdx.x * kColW + c;
@@ -67,14 +67,20 @@ __global__ void __launch_bounds__(kColW * F2<L>::NT, 1)
     __syncthreads();
     if (t < E::R1) {
         // kz = t + RL*r: folded index kz below L/2, L - kz at or above it
-        const double* glo = gs + t * kColW + c;
-        const double* ghi = gs + (L - t) * kColW + c;
+        const TG* glo = gs + t * kColW + c;
+        const TG* ghi = gs + (L - t) * kColW + c;
 #pragma unroll
         for (int r = 0; r < E::R2; ++r) {
             const int kz = t + RL * r;
             const bool lower = RL * r < L / 2;
+            const TG gv = lower ? glo[RL * r * kColW] : ghi[-RL * r * kColW];
             float gh, gl;
-            dd_split(lower ? glo[RL * r * kColW] : ghi[-RL * r * kColW], gh, gl);
+            if constexpr (std::is_same<TG, dreal>::value) {
+                gh = gv.h;
+                gl = gv.l;
+            } else {
+                dd_split(gv, gh, gl);
+            }
             ddc o = dd_scale(v[r], gh, gl);
             if (image) {
                 const int kzf = kz <= L / 2 ? kz : L - kz;
@@ -147,14 +153,23 @@ __global__ void __launch_bounds__(256, 1) k2_dd_inv_x1(const ddc* __restrict__ D
     }
 }
 
-bool launch2_dd_zpass_pot(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz, const double* pf, const double2* pi,
-                          int image, int Hy, const ddc* tw, cudaStream_t s) {
+bool launch2_dd_zpass_pot(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz, const void* pf, int pfmt,
+                          const double2* pi, int image, int Hy, const ddc* tw, cudaStream_t s) {
+#define SC_KDZP_GT(LL, HALF, TG)                                                                            \
+    {                                                                                                       \
+        if (set_smem(k2_dd_zpass_pot<LL, HALF, TG>, smem) != SC_OK) return false;                           \
+        launch_pdl(k2_dd_zpass_pot<LL, HALF, TG>, grid, kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz,       \
+                   (const TG*)pf, pi, image, Hy, tw);                                                       \
+    }
 #define SC_KDZP_GO(LL, HALF)                                                                                \
     {                                                                                                       \
-        if (set_smem(k2_dd_zpass_pot<LL, HALF>, smem) != SC_OK) return false;                               \
-        launch_pdl(k2_dd_zpass_pot<LL, HALF>, grid, kColW * F2<LL>::NT, smem, s, B, C, Hx, Ly, nz, pf, pi,   \
-                   image, Hy, tw);                                                                          \
+        if (pfmt)                                                                                           \
+            SC_KDZP_GT(LL, HALF, dreal)                                                                     \
+        else                                                                                                \
+            SC_KDZP_GT(LL, HALF, double)                                                                    \
     }
+// (a dreal spectrum comes from the double-FP32 Green build, which takes
+// power-of-two meshes only: nz = L/2)
 #define SC_KDZP(LL)                                                                                         \
     {                                                                                                       \
         const size_t smem = sizeof(ddc) * kColW * F2<LL>::S * 2 +                                           \
@@ -162,12 +177,15 @@ bool launch2_dd_zpass_pot(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz
         const unsigned grid = (unsigned)(((int64_t)Hx * Ly + kColW - 1) / kColW);                           \
         if (2 * nz == LL)                                                                                   \
             SC_KDZP_GO(LL, true)                                                                            \
+        else if (pfmt)                                                                                      \
+            return false;                                                                                   \
         else                                                                                                \
-            SC_KDZP_GO(LL, false)                                                                           \
+            SC_KDZP_GT(LL, false, double)                                                                   \
     }
     SC_L_SWITCH(logL, SC_KDZP)
 #undef SC_KDZP
 #undef SC_KDZP_GO
+#undef SC_KDZP_GT
     return true;
 }
 

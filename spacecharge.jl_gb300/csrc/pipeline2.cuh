@@ -1697,21 +1697,23 @@ bool launch2_dd_col(int logL, const TI* in, TO* out, int ncols, int nbatch, int 
                     int64_t as_in, int64_t bs_in, int64_t cs_in, int64_t as_out, int64_t bs_out, int64_t cs_out,
                     const ddc* tw, cudaStream_t s);
 // The FP64 free-space Green transform in double-FP32 (dd_green.cu): the
-// paired x+y and z passes of the field kernel with dreal values, from the
-// octant G to the spectrum `out` (the layout of the FP64 build).  Applies to
+// paired x+y and z passes of the field kernel (solo: the potential kernel,
+// one component even along every axis) with dreal values, from the octant G
+// to the spectrum `out` (the layout of the FP64 build).  Applies to
 // power-of-two meshes (n = L/2 on every axis) with Lx = Ly in {64, 128} and
 // Lz in {64, 128, 256}; dd_green_applies says whether.
 bool dd_green_applies(int logLx, int logLy, int logLz, int nx, int ny, int nz);
 bool launch_dd_green(int logLxy, int logLz, dreal* G, dreal* T2, dreal* out, int nx, int ny, int nz, int Hx,
-                     int64_t gcs, int64_t t2cs, double gamma, const ddc* tw, cudaStream_t s);
+                     int64_t gcs, int64_t t2cs, double gamma, const ddc* tw, cudaStream_t s, int solo = 0);
 // gfmt: the free-space Green spectrum is double-FP32 (dreal) rather than FP64
 bool launch2_dd_zpass(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz, const GreenView& gv, int gfmt,
                       const ddc* tw, cudaStream_t s);
 bool launch2_dd_inv_x(int logL, const ddc* D, dnode4* E4, int nx, int rows, int Hx, int64_t cs, const ddc* tw,
                       cudaStream_t s);
 // the scalar potential's z pass and inverse x pass (dd_pot.cu)
-bool launch2_dd_zpass_pot(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz, const double* pf, const double2* pi,
-                          int image, int Hy, const ddc* tw, cudaStream_t s);
+// pf: the free-space spectrum, FP64 (pfmt 0) or dreal (pfmt 1)
+bool launch2_dd_zpass_pot(int logL, const ddc* B, ddc* C, int Hx, int Ly, int nz, const void* pf, int pfmt,
+                          const double2* pi, int image, int Hy, const ddc* tw, cudaStream_t s);
 bool launch2_dd_inv_x1(int logL, const ddc* D, dnode4* E4, int nx, int rows, int Hx, const ddc* tw, cudaStream_t s);
 
 static bool launch2_adj_zpass(int logL, const float2* C, float2* B, int Hx, int Ly, int nz, const GreenView& gv,

@@ -154,7 +154,8 @@ __global__ void __launch_bounds__(128) k_pot_corners(double* __restrict__ F, Pot
     F[t] = pot_corner(g, ex, ey, ez);
 }
 
-__global__ void __launch_bounds__(128) k_pot_place(const double* __restrict__ F, double* __restrict__ G, PotGeom g,
+template <typename OT>  // double, or dreal for the double-FP32 transform
+__global__ void __launch_bounds__(128) k_pot_place(const double* __restrict__ F, OT* __restrict__ G, PotGeom g,
                                                    int ez0) {
     pdl_wait();  // the corners come from the preceding k_pot_corners
     const int cx = g.nx + 1, cy = g.ny + 1;
@@ -166,7 +167,7 @@ __global__ void __launch_bounds__(128) k_pot_place(const double* __restrict__ F,
     auto Fv = [&](int a, int b, int e) { return f[a + sy * b + sz * e]; };
     const double d = Fv(1, 1, 1) - Fv(0, 1, 1) - Fv(1, 0, 1) - Fv(1, 1, 0) - Fv(0, 0, 0) + Fv(0, 0, 1) +
                      Fv(0, 1, 0) + Fv(1, 0, 0);
-    G[t] = d * g.scale;
+    G[t] = OT(d * g.scale);
 }
 
 // z pass of the potential: forward z transform of rho^(kx, ky, .), times
@@ -348,20 +349,23 @@ __global__ void __launch_bounds__(256) k_lane3(const T* __restrict__ E4, T* __re
     if (i < N) phi[i] = E4[4 * i + 3];
 }
 
-static bool pot_key_matches(const GreenKey& k, const sc_mesh* m, double offz) {
+// fmt < 0: either format (the double-FP32 z pass reads both)
+static bool pot_key_matches(const GreenKey& k, const sc_mesh* m, double offz, int fmt = -1) {
     return k.valid && k.delta[0] == m->delta[0] && k.delta[1] == m->delta[1] && k.delta[2] == m->delta[2] &&
-           k.gamma == m->gamma && k.offset_z == offz;
+           k.gamma == m->gamma && k.offset_z == offz && (fmt < 0 || k.fmt == fmt);
 }
 
 // Builds the compressed potential spectrum (free space, or the image at
-// offset offz) unless the cached one matches the geometry.
+// offset offz) unless the cached one matches the geometry.  dd (FP64 meshes
+// in double-FP32 mode): the free-space spectrum's transform in double-FP32
+// where it applies, stored as dreal; a cached FP64 one serves too.
 template <typename T>
-static int pot_green(sc_mesh* m, bool image, cudaStream_t s) {
+static int pot_green(sc_mesh* m, bool image, cudaStream_t s, bool dd = false) {
     using T2 = typename Cplx<T>::T2;
     NativeWork& w = m->nw;
     const double offz = image ? 2 * m->lo[2] + (m->hi[2] - m->lo[2]) : 0.0;  // free_space.jl:39
     GreenKey& key = image ? w.key_pimg : w.key_pfree;
-    if (m->green_cache && pot_key_matches(key, m, offz)) return SC_OK;
+    if (m->green_cache && pot_key_matches(key, m, offz, dd && !image ? -1 : 0)) return SC_OK;
     DeviceCtx* ctx = nullptr;
     SC_TRY(device_ctx(&ctx));
     const T2* tw = twiddles<T>(ctx);
@@ -430,7 +434,28 @@ static int pot_green(sc_mesh* m, bool image, cudaStream_t s) {
     } else {
         k_pot_corners<<<(unsigned)((corners + 127) / 128), 128, 0, s>>>(F, g, ez0);
         SC_LAUNCH_CHECK("k_pot_corners");
-        launch_pdl(k_pot_place, (unsigned)((cells + 127) / 128), 128, 0, s, (const double*)F, (double*)G, g, ez0);
+        if (dd && !image && dd_green_applies(w.log2L[0], w.log2L[1], w.log2L[2], nx, ny, nz)) {
+            // double-FP32: the octant split as it is placed, then the paired
+            // kernels' single-component mode with dreal values
+            launch_pdl(k_pot_place<dreal>, (unsigned)((cells + 127) / 128), 128, 0, s, (const double*)F, (dreal*)G, g,
+                       ez0);
+            SC_LAUNCH_CHECK("k_pot_place");
+            if (!launch_dd_green(w.log2L[0], w.log2L[2], (dreal*)G, (dreal*)Txy, (dreal*)dst, nx, ny, nz, Hx, cells,
+                                 t2n, 1.0, (const ddc*)ctx->twdd, s, 1))
+                return fail(SC_ERR_CUDA, "double-FP32 potential Green transform did not launch");
+            SC_LAUNCH_CHECK("double-FP32 potential Green transform");
+            m->launches += 3;
+            key.delta[0] = m->delta[0];
+            key.delta[1] = m->delta[1];
+            key.delta[2] = m->delta[2];
+            key.gamma = m->gamma;
+            key.offset_z = offz;
+            key.fmt = 1;
+            key.valid = true;
+            return SC_OK;
+        }
+        launch_pdl(k_pot_place<double>, (unsigned)((cells + 127) / 128), 128, 0, s, (const double*)F, (double*)G, g,
+                   ez0);
         SC_LAUNCH_CHECK("k_pot_place");
     }
     // parity-reduced transform, every axis even (pipeline2.cuh)
@@ -457,6 +482,7 @@ static int pot_green(sc_mesh* m, bool image, cudaStream_t s) {
     key.delta[2] = m->delta[2];
     key.gamma = m->gamma;
     key.offset_z = offz;
+    key.fmt = 0;
     key.valid = true;
     return SC_OK;
 }
@@ -477,13 +503,13 @@ static int potential_t(sc_mesh* m, int at_cathode, void* phi, cudaStream_t s) {
     if (!m->ev_join) SC_CUDA(cudaEventCreateWithFlags(&m->ev_join, cudaEventDisableTiming));
     SC_CUDA(cudaEventRecord(m->ev_fork, s));
     SC_CUDA(cudaStreamWaitEvent(m->side, m->ev_fork, 0));
-    int st = pot_green<T>(m, false, m->side);
+    // FP64 meshes in double-FP32 mode: every pass but the Green function's
+    // antiderivative in double-FP32 (dd_xy.cu, dd_pot.cu, dd_green.cu)
+    const bool dd = native_dd_applies(m);
+    int st = pot_green<T>(m, false, m->side, dd);
     if (st == SC_OK && at_cathode) st = pot_green<T>(m, true, m->side);
     const cudaError_t ej = cudaEventRecord(m->ev_join, m->side);
     if (st == SC_OK && ej != cudaSuccess) st = cuda_fail(ej, "cudaEventRecord");
-    // FP64 meshes in double-FP32 mode: every pass but the Green build in
-    // double-FP32 (dd_xy.cu, dd_pot.cu)
-    const bool dd = native_dd_applies(m);
     if (st == SC_OK) st = native_forward(m, s, dd);
     cudaStreamWaitEvent(s, m->ev_join, 0);  // joined on every path
     SC_TRY(st);
@@ -494,7 +520,7 @@ static int potential_t(sc_mesh* m, int at_cathode, void* phi, cudaStream_t s) {
     if (dd) {
         const ddc* twdd = (const ddc*)ctx->twdd;
         const int rows = ny * nz;
-        if (!launch2_dd_zpass_pot(w.log2L[2], (const ddc*)w.B, (ddc*)C, Hx, Ly, nz, (const double*)w.pfree,
+        if (!launch2_dd_zpass_pot(w.log2L[2], (const ddc*)w.B, (ddc*)C, Hx, Ly, nz, w.pfree, w.key_pfree.fmt,
                                   (const double2*)w.pimg, at_cathode ? 1 : 0, Hy, twdd, s) ||
             !launch2_dd_col<true>(w.log2L[1], (const ddc*)C, (ddc*)w.A, Hx, nz, 1, Ly, ny, Hx, (int64_t)Hx * Ly, 0, Hx,
                                   (int64_t)Hx * ny, 0, twdd, s) ||

@@ -62,11 +62,13 @@ def test_minus_grad_phi_is_e(sc, cuda):
 
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("df32", 1e-10), ("mixed", 1e-5)])
 @pytest.mark.parametrize("grid,gamma,cath", [((40, 36, 64), 10.0, False), ((32, 32, 48), 3.0, True),
+                                             ((32, 32, 64), 4.0, False), ((32, 32, 64), 4.0, True),
                                              ((12, 10, 150), 2.0, False)])
 def test_potential_larger_grids(sc, cuda, prec, tol, grid, gamma, cath):
     """Grids where most cells are far from the origin (the mixed build's
-    quadrature), boosted cells, the image, and an axis of 150 nodes (a
-    512-point transform: the cuFFT schedule)."""
+    quadrature), boosted cells, the image, a power-of-two grid (32x32x64:
+    in double-FP32 mode the Green transform runs in double-FP32 too), and an
+    axis of 150 nodes (a 512-point transform: the cuFFT schedule)."""
     rng = np.random.default_rng(8)
     n = 40_000
     x, y, z = rng.standard_normal((3, n)).clip(-4.5, 4.5) * np.array([[1e-3], [0.8e-3], [0.3e-3]])
@@ -85,3 +87,6 @@ def test_potential_larger_grids(sc, cuda, prec, tol, grid, gamma, cath):
     # a second solve reuses the cached potential spectrum
     phi2 = sc.solve_potential(m, at_cathode=cath)
     assert rel(phi2.cpu().numpy(), ref) < tol
+    if prec == "df32":  # against FP64 mode (which rebuilds an FP64 spectrum)
+        m.set_fp64_arithmetic("fp64")
+        assert rel(phi.cpu().numpy(), sc.solve_potential(m, at_cathode=cath).cpu().numpy()) < 1e-12
