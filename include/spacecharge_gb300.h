@@ -172,7 +172,8 @@ int sc_mesh_set_green_cache(sc_mesh* mesh, int enabled);
  * antiderivative stays FP64; meshes with a transform above 256 points keep
  * FP64 transforms, and the field's z pass with the cathode image stays FP64.
  * sc_solve_potential follows the mode too (its forward, z and inverse
- * passes; its Green build stays FP64).  Other precisions: SC_ERR_INVALID. */
+ * passes, and its Green transform; the antiderivative stays FP64).  Other
+ * precisions: SC_ERR_INVALID. */
 #define SC_FP64_ARITH_FP64 0
 #define SC_FP64_ARITH_DF32 1
 int sc_mesh_set_fp64_arithmetic(sc_mesh* mesh, int mode);
