@@ -51,6 +51,23 @@ def test_julia_binding_calls_declared_symbols():
     assert jl == modes
 
 
+def test_python_constants_match_header():
+    """Every integer constant the Python binding defines has the header's
+    value (status codes, precisions, dtypes, deposit modes, FFT engines,
+    FP64 arithmetic modes)."""
+    hdr = open(os.path.join(ROOT, "include", "spacecharge_gb300.h")).read()
+    defs = {k: int(v) for k, v in re.findall(r"#define (SC_[A-Z0-9_]+)\s+(-?\d+)\b", hdr)}
+    src = open(os.path.join(ROOT, "spacecharge.jl_gb300", "python", "spacecharge_gb300", "_lib.py")).read()
+    py = {k: int(v) for k, v in re.findall(r"^(SC_[A-Z0-9_]+) = (-?\d+)\s*$", src, re.M)}
+    assert py and all(k in defs for k in py), set(py) - set(defs)
+    assert {k: defs[k] for k in py} == py
+    # the Julia wrapper's FP64 arithmetic modes
+    jl = open(os.path.join(ROOT, "spacecharge.jl_gb300", "julia", "SpaceChargeGB300", "src",
+                           "SpaceChargeGB300.jl")).read()
+    m = re.search(r"mode === :fp64 \? Cint\((\d+)\) : mode === :df32 \? Cint\((\d+)\)", jl)
+    assert m and (int(m.group(1)), int(m.group(2))) == (defs["SC_FP64_ARITH_FP64"], defs["SC_FP64_ARITH_DF32"])
+
+
 def test_version(lib):
     assert lib.sc_version() >= 10000
 
