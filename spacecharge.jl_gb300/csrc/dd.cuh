@@ -1,9 +1,11 @@
-// Double-FP32 complex arithmetic for the FP64 meshes' transforms.
+// Double-FP32 arithmetic for the FP64 meshes' double-FP32 mode
+// (sc_mesh_set_fp64_arithmetic).
 //
-// The GB300 issues FP64 at about 1/68 of its FP32 rate, so the FP64 mesh's
-// z pass and inverse passes carry each complex value as an unevaluated sum
-// of two FP32 complex numbers, hi + lo with |lo| <= ulp(hi)/2 per part
-// (48 significant bits).  Sums use Knuth's two-sum on the high parts, the
+// The GB300 issues FP64 at about 1/68 of its FP32 rate, so in that mode the
+// FP64 mesh's transforms, deposit weights and gather carry each value as an
+// unevaluated sum of two FP32 numbers, hi + lo with |lo| <= ulp(hi)/2 (48
+// significant bits): complex values as ddc, real ones as dreal or a float2
+// {hi, lo}.  Sums use Knuth's two-sum on the high parts, the
 // low parts added to its error and one renormalising fast two-sum (the
 // "sloppy" double-word addition: its error is bounded by a few 2^-48 of
 // |a| + |b|, which is the norm-wise bound a Fourier transform needs);
